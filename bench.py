@@ -1,0 +1,318 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 CVF engine: site-updates/ns on the L=256 checkerboard workload.
+
+Workload (one "step"): one cube (eta) move, one NPT volume move and one checkerboard Metropolis
+sweep of an L=256 lattice (16,777,216 cells, one uint32 per cell = 64 MB), ordered start,
+T=0.70, P=0.45, Metropolis only -- the bandwidth-bound single-lattice configuration.
+site-updates/ns counts a cell (all six sigma arms attempted) as one site update.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+                  [--workload l256|batch64]
+
+Timing: W untimed warm-up steps, then K steps each bracketed by CUDA events on the engine's own
+stream; the 64 MB lattice fits in the 129 MB L2, so a 256 MB buffer is written on the same
+stream before every timed step (outside the events). Under torchrun every rank steps its own
+replica (independent lattices, no collective); rank 0 prints the whole-job line.
+--impl reference times the CPU oracle (the reference's CPU path does not compile, so the
+restatement in oracle/ stands in) on all host cores, rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L_BENCH, T_BENCH, P_BENCH, SEED = 256, 0.70, 0.45, 44648604
+ALG_BYTES_PER_CELL_SWEEP = 8  # read + write one packed uint32 per cell per sweep
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-over-ranks on a CPU (gloo) group; a no-op for one process."""
+
+    def __init__(self, world):
+        self.world = world
+        if world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": float(np.median([r[0] for r in rows])), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(name):
+    """DRAM bytes per launch from a committed ncu summary under profiles/, if there is one."""
+    p = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(p):
+        return None
+    try:
+        return json.load(open(p)).get("dram_bytes_per_launch")
+    except (ValueError, OSError):
+        return None
+
+
+def cpu_baseline_oracle(steps_cap=3, budget_s=30.0):
+    """The CPU oracle on all host cores over a bounded sample of the same workload."""
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    o = O.Oracle(L_BENCH, T_BENCH, P_BENCH, SEED, 6.0, 0, 2, threads=threads)
+    o.step(1, 0)  # warm-up
+    t0 = time.perf_counter()
+    n = 0
+    while n < steps_cap and (time.perf_counter() - t0) < budget_s:
+        o.step(1, 0)
+        n += 1
+    dt = time.perf_counter() - t0
+    o.close()
+    val = L_BENCH ** 3 * n / dt / 1e9
+    return {"value": round(val, 6), "unit": "site-updates/ns", "cores": threads, "kind": "port",
+            "sample": f"{n} full MC steps (cube + volume + sweep) of the L=256 lattice on {threads} "
+                      f"OpenMP threads ({dt:.1f} s)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    cap = max(1, min(args.steps, 20))
+    base = cpu_baseline_oracle(steps_cap=cap, budget_s=90.0)
+    line = {"impl": "reference", "metric": "site-updates/ns at L=256", "value": base["value"],
+            "unit": "site-updates/ns", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (ordered start, Philox seed 44648604)",
+            "config": {"workload": "L=256 ordered start, T=0.70, P=0.45, Metropolis only; "
+                                   "1 cube + 1 volume move + 1 checkerboard sweep per step", "L": 256},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": "site-updates/ns", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_engine(args):
+    rank, world, local = dist_env()
+    dist = Dist(world)
+    import torch
+    from cvfbulkwater_gb300 import build
+    build.build()
+    import ctypes as C
+    from cvfbulkwater_gb300 import abi
+    from cvfbulkwater_gb300.engine import Lattice, Params
+
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        base = cpu_baseline_oracle()
+
+    torch.cuda.set_device(local)
+    L = L_BENCH
+    N = L ** 3
+    lat = Lattice(Params(L=L, T=T_BENCH, P=P_BENCH, seed=SEED + rank, start=2, replica=rank, device=local))
+    sp = C.c_void_p()
+    abi.check(abi.lib().cvf_get_stream(lat._h, C.byref(sp)))
+    stream = torch.cuda.ExternalStream(sp.value, device=local)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    lat.run(args.warmup, 1, 0)
+    lat.synchronize()
+    # roofline of the dominant kernel (the sweep), two launches per profiled sweep
+    nprof = max(4, min(args.steps, 50))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nprof)]
+    with torch.cuda.stream(stream):
+        for i in range(nprof):
+            flush.fill_(i & 255)
+            ev[i][0].record(stream)
+            abi.check(abi.lib().cvf_profile_launch(lat._h, 0, 1))
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    sweep_ms = sum(a.elapsed_time(b) for a, b in ev) / nprof
+    launch_s = sweep_ms / 2 / 1e3
+    alg_bytes_launch = ALG_BYTES_PER_CELL_SWEEP * N / 2
+
+    # timed region: K steps, L2 flushed before each
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for i in range(args.steps):
+            flush.fill_(i & 255)
+            ev[i][0].record(stream)
+            lat.run(1, 1, 0)
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    total_ms = sum(a.elapsed_time(b) for a, b in ev)
+    total_ms = dist.max(total_ms)
+    ms_per_step = total_ms / args.steps
+    value = world * N * args.steps / (total_ms * 1e6)
+
+    # L2-resident reference figure: the same K steps back to back, no flush
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        lat.run(args.steps, 1, 0)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    resident = N * args.steps / (e0.elapsed_time(e1) * 1e6)
+
+    # end to end through the C ABI with host buffers: upload a host configuration, then per step
+    # one run call and one observables read (device -> host), finally download the lattice
+    host_cfg = lat.get_config()
+    lat2 = Lattice(Params(L=L, T=T_BENCH, P=P_BENCH, seed=SEED + 7 + rank, start=1, replica=rank, device=local))
+    lat2.set_config(host_cfg)
+    lat2.run(2, 1, 0)
+    lat2.observables()
+    dist.barrier()
+    t0 = time.perf_counter()
+    lat2.set_config(host_cfg)
+    for _ in range(args.steps):
+        lat2.run(1, 1, 0)
+        lat2.observables()
+    out_cfg = lat2.get_config()
+    t1 = time.perf_counter()
+    e2e_s = dist.max(t1 - t0)
+    packed = 4 * N + 2 * (L // 2) ** 3
+    e2e = {"value": round(world * N * args.steps / (e2e_s * 1e9), 4), "unit": "site-updates/ns",
+           "h2d_bytes_per_step": int(round(packed / args.steps)),
+           "d2h_bytes_per_step": int(round(packed / args.steps)) + 320,
+           "note": "per step: cvf_run_steps(1 step) + cvf_observables (sync + counts D2H); "
+                   "lattice upload (cvf_set_config) and download (cvf_get_config) amortised over "
+                   "the K steps; cells12 host packing included"}
+    del out_cfg
+
+    peak, peak_kind = peaks()
+    achieved = alg_bytes_launch / launch_s / 1e9
+    traffic = ncu_traffic("sweep_l256_traffic.json")
+    line = {
+        "metric": "site-updates/ns at L=256", "value": round(value, 4), "unit": "site-updates/ns",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (ordered start, Philox seed 44648604 + rank)",
+        "config": {"workload": "L=256 ordered start, T=0.70, P=0.45, Metropolis only; 1 cube move + "
+                               "1 volume move + 1 checkerboard sweep per step", "L": L, "cells": N,
+                   "l2": "64 MB lattice < 129 MB L2: a 256 MB buffer is written before every timed step",
+                   "replicas": world},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic,
+                     "kernel": "k_sweep<4> (one colour of the checkerboard sweep)",
+                     "algorithmic_bytes_per_launch": int(alg_bytes_launch),
+                     "launch_us": round(launch_s * 1e6, 3), "peak_source": f"{peak_kind} hbm_gbs"},
+        "cpu_baseline": base,
+        "e2e": e2e,
+        "gpu_launches": 4 * args.steps,
+        "clocks": clk,
+        "l2_resident_value": round(resident, 4),
+        "arm_updates_per_ns": round(6 * value, 4),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    lat.close()
+    lat2.close()
+    dist.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_engine(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

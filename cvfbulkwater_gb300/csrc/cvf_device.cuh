@@ -1,0 +1,98 @@
+// Device-side data structures of the GB300 CVF engine and the launch entry points that the
+// host engine (cvf_engine.cpp) calls. One ReplicaDesc per lattice (a plain run is a batch of
+// one replica); kernels map blocks to replicas through a prefix table of block counts.
+//
+// HBM layout of one replica with edge L (N = L^3, H = L/2):
+//   cells[c]  : uint32[H*L*L]  colour-c cells ((x+y+z)&1 == c), word (x>>1) + H*(y + L*z),
+//                              bits 3a..3a+2 = sigma_a
+//   cubes[0]  : uint8[H^3]     states of the cubes with all-even origins (2a,2b,2c),
+//                              index a + H*(b + H*c)
+//   cubes[1]  : uint8[H^3]     states of the cubes with all-odd origins (2a+1,2b+1,2c+1)
+//   label     : int32[6N]      Swendsen-Wang site labels, site = arm*N + x + L*(y + L*z)
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cvf {
+
+struct ReplicaDesc {
+  uint32_t* cells[2];
+  uint8_t* cubes[2];
+  // Swendsen-Wang work arrays (null until the first SW step)
+  int32_t* label;     // 6N parents / labels
+  uint8_t* hbmask;    // N: bits 0..2 = active x+, y+, z+ cluster bonds
+  uint8_t* shift;     // 6N: cluster shift of each root
+  int32_t* csize;     // 6N: cluster sizes by root
+  int32_t* cand;      // 6N: percolation candidate id by root (-1 none)
+  uint32_t* cover;    // max_cand * 3 * W: coordinate coverage bitmaps
+  int max_cand;       // capacity of cover
+  // vdW shells (device copies)
+  const float* dist;
+  const int* freq;
+  int n_shells;
+  int L, H;
+  int start;          // Flag_config of the replica (0 disordered, 1 from file, 2 ordered)
+  uint32_t key0, key1, replica;
+  float T, P, Rc;
+  double beta, Jeff;
+  unsigned long long thr_sweep[33];  // U < T, T in [0, 2^32]; index (dN_hb+1)*11 + dN_s+5
+  unsigned long long thr_cube[9];    // index dN_hb+4
+  unsigned long long thr_sw[2];      // hydrogen-bond link, intra-cell link
+};
+
+// One measurement: exact integer counts plus the volume degree of freedom.
+struct SampleRec {
+  long long n_hb2;    // sum over bonds of delta*(eta_i + eta_j) = 2 N_hb
+  long long n_sigma;  // sum over cells of sum_{a<b} delta(sigma_a, sigma_b)
+  double r_cell;
+  double volume;
+};
+
+// Cluster statistics of the last SW labelling (GW:2677-2780), exact integers.
+struct CStatsRec {
+  long long largest, second, n_percolating, n_clusters;
+  long long sum_size, sum_size2, sum_size2_wrap32;
+};
+
+struct ReplicaState {
+  double r_cell, volume, e_vdw;
+  uint32_t ctr[4];  // next move counters: sweep, cube, volume, SW
+  uint32_t cur[4];  // counters used by the moves of the current step
+  unsigned long long acc_hb2, acc_ns;
+  unsigned long long top2[2];
+  unsigned long long ncl, sum2, sum2w, nperc;
+  int ncand;
+  int err;  // nonzero: a bounded loop gave up (1 SW union, 2 candidate overflow)
+  uint32_t n_samples, n_cstats;
+  uint32_t cap_samples, cap_cstats;
+  SampleRec* samples;   // device sample stream
+  CStatsRec* cstats;    // device cluster-statistics stream
+  SampleRec last;
+  CStatsRec last_cstats;
+};
+
+// ------------------------------------------------------------- launch entry points
+struct BatchDev {
+  ReplicaDesc* reps;    // device array [nrep]
+  ReplicaState* st;     // device array [nrep]
+  int nrep;
+  int vec;              // cells per thread in the sweep (1, 2 or 4; divides every H)
+  int* blk_sweep;       // device prefix tables (nrep+1) of blocks per replica
+  int* blk_cube;
+  int* blk_cell;        // one thread per cell
+  int* blk_site;        // one thread per arm site (6N)
+  int nblk_sweep, nblk_cube, nblk_cell, nblk_site;
+};
+
+constexpr int kThreads = 256;
+
+void launch_init_lattice(const BatchDev& b, cudaStream_t s);
+void init_device_tables();
+void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, cudaStream_t s);
+void launch_cube_move(const BatchDev& b, cudaStream_t s);
+void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s);
+void launch_measure(const BatchDev& b, int record, cudaStream_t s);
+void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s);
+void launch_cluster_stats_impl(const BatchDev& b, unsigned long long* blocktop, int record, cudaStream_t s);
+
+}  // namespace cvf

@@ -1,0 +1,613 @@
+// Host engine behind the C ABI of include/cvf.h: owns device memory, builds the per-replica
+// descriptors, captures Monte Carlo steps into CUDA graphs and replays them.
+// There is no CPU fallback: every Monte Carlo move runs in the kernels of cvf_mc.cu / cvf_sw.cu.
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/cvf.h"
+#include "cvf_device.cuh"
+#include "cvf_host.h"
+#include "cvf_spec.cuh"
+
+using namespace cvf;
+
+static thread_local std::string g_err;
+
+namespace cvf {
+void set_last_error(const std::string& m) { g_err = m; }
+}  // namespace cvf
+
+static int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(call)                                                                               \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess) return fail(CVF_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct ReplicaHost {
+  cvf_params p;
+  int L, H;
+  long long N;
+  std::vector<float> dist;
+  std::vector<int> freq;
+  Thresholds thr;
+  ReplicaDesc desc;
+};
+
+struct cvf_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<ReplicaHost> reps;
+  BatchDev b{};
+  std::vector<void*> allocs;
+  bool sw_alloc = false;
+  bool sw_done = false;
+  unsigned long long* blocktop = nullptr;
+  std::map<std::tuple<int, int, int, int>, cudaGraphExec_t> graphs;
+};
+
+static int dev_alloc(cvf_handle* h, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+  if (e != cudaSuccess) return fail(CVF_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  h->allocs.push_back(*p);
+  return 0;
+}
+
+static int upload_descs(cvf_handle* h) {
+  std::vector<ReplicaDesc> d;
+  for (auto& r : h->reps) d.push_back(r.desc);
+  CK(cudaMemcpy(h->b.reps, d.data(), d.size() * sizeof(ReplicaDesc), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+static int build_tables(cvf_handle* h) {
+  const int n = (int)h->reps.size();
+  int vec = 4;
+  for (auto& r : h->reps) {
+    while (vec > 1 && r.H % vec) vec >>= 1;
+  }
+  h->b.vec = vec;
+  std::vector<int> ts(n + 1), tc(n + 1), tl(n + 1), tsi(n + 1);
+  ts[0] = tc[0] = tl[0] = tsi[0] = 0;
+  auto blocks = [](long long threads) { return (int)((threads + kThreads - 1) / kThreads); };
+  for (int i = 0; i < n; ++i) {
+    const auto& r = h->reps[i];
+    long long L = r.L, H = r.H;
+    ts[i + 1] = ts[i] + blocks((H / vec) * L * L);
+    tc[i + 1] = tc[i] + blocks(2 * H * H * H);
+    tl[i + 1] = tl[i] + blocks(r.N);
+    tsi[i + 1] = tsi[i] + blocks(6 * r.N);
+  }
+  int* d;
+  if (int rc = dev_alloc(h, (void**)&d, sizeof(int) * 4 * (n + 1))) return rc;
+  std::vector<int> all;
+  all.insert(all.end(), ts.begin(), ts.end());
+  all.insert(all.end(), tc.begin(), tc.end());
+  all.insert(all.end(), tl.begin(), tl.end());
+  all.insert(all.end(), tsi.begin(), tsi.end());
+  CK(cudaMemcpy(d, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
+  h->b.blk_sweep = d;
+  h->b.blk_cube = d + (n + 1);
+  h->b.blk_cell = d + 2 * (n + 1);
+  h->b.blk_site = d + 3 * (n + 1);
+  h->b.nblk_sweep = ts[n];
+  h->b.nblk_cube = tc[n];
+  h->b.nblk_cell = tl[n];
+  h->b.nblk_site = tsi[n];
+  return 0;
+}
+
+static int ensure_sw(cvf_handle* h) {
+  if (h->sw_alloc) return 0;
+  for (auto& r : h->reps) {
+    size_t NS = (size_t)(6 * r.N);
+    int W = (r.L + 31) / 32;
+    r.desc.max_cand = 3 * r.L * r.L;  // at most 6N / 2L clusters of size >= 2L
+    if (int rc = dev_alloc(h, (void**)&r.desc.label, NS * sizeof(int32_t))) return rc;
+    if (int rc = dev_alloc(h, (void**)&r.desc.hbmask, (size_t)r.N)) return rc;
+    if (int rc = dev_alloc(h, (void**)&r.desc.shift, NS)) return rc;
+    if (int rc = dev_alloc(h, (void**)&r.desc.csize, NS * sizeof(int32_t))) return rc;
+    if (int rc = dev_alloc(h, (void**)&r.desc.cand, NS * sizeof(int32_t))) return rc;
+    if (int rc = dev_alloc(h, (void**)&r.desc.cover, (size_t)r.desc.max_cand * 3 * W * sizeof(uint32_t))) return rc;
+    CK(cudaMemset(r.desc.label, 0, NS * sizeof(int32_t)));
+  }
+  if (int rc = dev_alloc(h, (void**)&h->blocktop, (size_t)h->b.nblk_site * 2 * sizeof(unsigned long long))) return rc;
+  h->sw_alloc = true;
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+  h->graphs.clear();
+  return upload_descs(h);
+}
+
+static void enqueue_step(cvf_handle* h, int nmet, int ncl) {
+  launch_step_begin(h->b, nmet, ncl, 1, h->stream);
+  launch_cube_move(h->b, h->stream);
+  for (int j = 0; j < nmet; ++j) {
+    launch_sweep(h->b, 0, j, h->stream);
+    launch_sweep(h->b, 1, j, h->stream);
+  }
+  for (int j = 0; j < ncl; ++j) launch_sw_step(h->b, j, h->stream);
+}
+
+static void enqueue_cstats(cvf_handle* h, int record) {
+  for (auto& r : h->reps) {
+    cudaMemsetAsync(r.desc.csize, 0, (size_t)(6 * r.N) * sizeof(int32_t), h->stream);
+    int W = (r.L + 31) / 32;
+    cudaMemsetAsync(r.desc.cover, 0, (size_t)r.desc.max_cand * 3 * W * sizeof(uint32_t), h->stream);
+  }
+  launch_cluster_stats_impl(h->b, h->blocktop, record, h->stream);
+}
+
+// Graph of `steps` MC steps; when record is set, the first step is followed by a recorded
+// measurement (and cluster statistics when ncl > 0).
+static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cudaGraphExec_t* out) {
+  auto key = std::make_tuple(steps, nmet, ncl, record);
+  auto it = h->graphs.find(key);
+  if (it != h->graphs.end()) {
+    *out = it->second;
+    return 0;
+  }
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  for (int i = 0; i < steps; ++i) {
+    enqueue_step(h, nmet, ncl);
+    if (i == 0 && record) {
+      launch_measure(h->b, 1, h->stream);
+      if (ncl > 0) enqueue_cstats(h, 1);
+    }
+  }
+  CK(cudaStreamEndCapture(h->stream, &g));
+  cudaGraphExec_t ex;
+  cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(CVF_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+  h->graphs[key] = ex;
+  *out = ex;
+  return 0;
+}
+
+static int check_rep(const cvf_handle* h, int r) {
+  if (!h) return fail(CVF_EINVAL, "null handle");
+  if (r < 0 || r >= (int)h->reps.size()) return fail(CVF_EINVAL, "replica index out of range");
+  return 0;
+}
+
+static int read_state(cvf_handle* h, int r, ReplicaState* out) {
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(out, h->b.st + r, sizeof(ReplicaState), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+static int check_err(cvf_handle* h) {
+  CK(cudaStreamSynchronize(h->stream));
+  for (int r = 0; r < (int)h->reps.size(); ++r) {
+    int err = 0;
+    CK(cudaMemcpy(&err, (char*)(h->b.st + r) + offsetof(ReplicaState, err), sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return fail(CVF_ELIMIT, "device loop limit reached (code " + std::to_string(err) + ") in replica " + std::to_string(r));
+  }
+  return 0;
+}
+
+extern "C" {
+
+const char* cvf_last_error_string(void) { return g_err.c_str(); }
+const char* cvf_version(void) { return "cvfbulkwater_gb300 0.1 (sm_103a)"; }
+
+int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
+  if (!params || !out || n < 1) return fail(CVF_EINVAL, "null params/out or n_replicas < 1");
+  *out = nullptr;
+  for (int i = 0; i < n; ++i) {
+    const cvf_params& p = params[i];
+    if (p.L < 4 || (p.L & 1)) return fail(CVF_EINVAL, "L must be even and >= 4");
+    if ((long long)p.L * p.L * p.L * 6 >= (1LL << 31)) return fail(CVF_EINVAL, "L too large (6 L^3 must fit int32)");
+    if (p.flag_chessboard != 1)
+      return fail(CVF_EINVAL, "Flag_chessboard=0 (nhb<=4 mode) is not supported; use Flag_chessboard=1");
+    if (!(p.T > 0.0f)) return fail(CVF_EINVAL, "T must be > 0");
+    if (!(p.R_cutoff > 0.0f)) return fail(CVF_EINVAL, "R_cutoff must be > 0");
+    if (p.start < 0 || p.start > 2) return fail(CVF_EINVAL, "Flag_config must be 0, 1 or 2");
+    if (p.device != params[0].device) return fail(CVF_EINVAL, "all replicas of a handle share one device");
+  }
+  int ndev = 0;
+  CK(cudaGetDeviceCount(&ndev));
+  if (params[0].device < 0 || params[0].device >= ndev)
+    return fail(CVF_EINVAL, "Device_ID " + std::to_string(params[0].device) + " out of range (" + std::to_string(ndev) + " devices)");
+  CK(cudaSetDevice(params[0].device));
+  init_device_tables();
+  cvf_handle* h = new cvf_handle();
+  h->device = params[0].device;
+  auto bail = [&](int rc) {
+    cvf_destroy(h);
+    return rc;
+  };
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(CVF_ECUDA, "cudaStreamCreate failed"));
+  h->reps.resize(n);
+  std::vector<ReplicaState> st(n);
+  for (int i = 0; i < n; ++i) {
+    ReplicaHost& r = h->reps[i];
+    r.p = params[i];
+    r.L = r.p.L;
+    r.H = r.L / 2;
+    r.N = (long long)r.L * r.L * r.L;
+    compute_shells(r.L, r.p.R_cutoff, r.dist, r.freq);
+    if ((int)r.dist.size() > kMaxShells) return bail(fail(CVF_EINVAL, "too many vdW shells"));
+    r.thr = make_thresholds(r.p.T, r.p.P);
+    ReplicaDesc& d = r.desc;
+    memset(&d, 0, sizeof(d));
+    size_t half_cells = (size_t)(r.N / 2), ncubes = (size_t)r.H * r.H * r.H;
+    int rc;
+    if ((rc = dev_alloc(h, (void**)&d.cells[0], half_cells * 4)) || (rc = dev_alloc(h, (void**)&d.cells[1], half_cells * 4)) ||
+        (rc = dev_alloc(h, (void**)&d.cubes[0], ncubes)) || (rc = dev_alloc(h, (void**)&d.cubes[1], ncubes)))
+      return bail(rc);
+    float* dd;
+    int* df;
+    if ((rc = dev_alloc(h, (void**)&dd, kMaxShells * sizeof(float))) || (rc = dev_alloc(h, (void**)&df, kMaxShells * sizeof(int))))
+      return bail(rc);
+    cudaMemcpy(dd, r.dist.data(), r.dist.size() * sizeof(float), cudaMemcpyHostToDevice);
+    cudaMemcpy(df, r.freq.data(), r.freq.size() * sizeof(int), cudaMemcpyHostToDevice);
+    d.dist = dd;
+    d.freq = df;
+    d.n_shells = (int)r.dist.size();
+    d.L = r.L;
+    d.H = r.H;
+    d.start = r.p.start;
+    d.key0 = (uint32_t)((unsigned long long)r.p.seed & 0xffffffffu);
+    d.key1 = (uint32_t)((unsigned long long)r.p.seed >> 32);
+    d.replica = r.p.replica;
+    d.T = r.p.T;
+    d.P = r.p.P;
+    d.Rc = r.p.R_cutoff;
+    d.beta = r.thr.beta;
+    d.Jeff = r.thr.Jeff;
+    memcpy(d.thr_sweep, r.thr.sweep, sizeof(d.thr_sweep));
+    memcpy(d.thr_cube, r.thr.cube, sizeof(d.thr_cube));
+    memcpy(d.thr_sw, r.thr.sw, sizeof(d.thr_sw));
+    ReplicaState& s = st[i];
+    memset(&s, 0, sizeof(s));
+    s.r_cell = kRcell0;
+    s.volume = (double)r.N * s.r_cell * s.r_cell * s.r_cell;  // GW:481
+    s.e_vdw = host_evdw(s.r_cell, r.dist, r.freq, r.p.R_cutoff);
+    s.cap_samples = (uint32_t)(r.p.sample_capacity > 0 ? r.p.sample_capacity : 65536);
+    s.cap_cstats = s.cap_samples;
+    if ((rc = dev_alloc(h, (void**)&s.samples, s.cap_samples * sizeof(SampleRec))) ||
+        (rc = dev_alloc(h, (void**)&s.cstats, s.cap_cstats * sizeof(CStatsRec))))
+      return bail(rc);
+  }
+  h->b.nrep = n;
+  int rc;
+  if ((rc = dev_alloc(h, (void**)&h->b.reps, n * sizeof(ReplicaDesc))) ||
+      (rc = dev_alloc(h, (void**)&h->b.st, n * sizeof(ReplicaState))))
+    return bail(rc);
+  if (cudaMemcpy(h->b.st, st.data(), n * sizeof(ReplicaState), cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(fail(CVF_ECUDA, "state upload failed"));
+  if ((rc = upload_descs(h)) || (rc = build_tables(h))) return bail(rc);
+  // start 1 leaves sigma at zero until cvf_set_config; cubes always start random (GW:700-708)
+  launch_init_lattice(h->b, h->stream);
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) return bail(fail(CVF_ECUDA, std::string("init: ") + cudaGetErrorString(e)));
+  *out = h;
+  return 0;
+}
+
+int cvf_create(const cvf_params* params, cvf_handle** out) { return cvf_batch_create(params, 1, out); }
+
+int cvf_destroy(cvf_handle* h) {
+  if (!h) return 0;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+  for (void* p : h->allocs) cudaFree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return 0;
+}
+
+int cvf_num_replicas(const cvf_handle* h) { return h ? (int)h->reps.size() : 0; }
+
+int cvf_set_config(cvf_handle* h, int r, const int* c12, long long n_cells) {
+  if (int rc = check_rep(h, r)) return rc;
+  ReplicaHost& R = h->reps[r];
+  if (!c12 || n_cells != R.N) return fail(CVF_EINVAL, "cells12 must hold 12 ints for each of the N cells");
+  std::vector<uint32_t> c0, c1;
+  std::vector<uint8_t> ce, co;
+  std::string err;
+  if (!pack_config(R.L, c12, c0, c1, ce, co, err)) return fail(CVF_ECONFIG, err);
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(R.desc.cells[0], c0.data(), c0.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(R.desc.cells[1], c1.data(), c1.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(R.desc.cubes[0], ce.data(), ce.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(R.desc.cubes[1], co.data(), co.size(), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int cvf_get_config(cvf_handle* h, int r, int* c12, long long n_cells) {
+  if (int rc = check_rep(h, r)) return rc;
+  ReplicaHost& R = h->reps[r];
+  if (!c12 || n_cells != R.N) return fail(CVF_EINVAL, "cells12 must hold 12 ints for each of the N cells");
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  std::vector<uint32_t> c0((size_t)(R.N / 2)), c1((size_t)(R.N / 2));
+  std::vector<uint8_t> ce((size_t)R.H * R.H * R.H), co(ce.size());
+  CK(cudaMemcpy(c0.data(), R.desc.cells[0], c0.size() * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(c1.data(), R.desc.cells[1], c1.size() * 4, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(ce.data(), R.desc.cubes[0], ce.size(), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(co.data(), R.desc.cubes[1], co.size(), cudaMemcpyDeviceToHost));
+  unpack_config(R.L, c0, c1, ce, co, c12);
+  return 0;
+}
+
+int cvf_set_distances(cvf_handle* h, int r, const float* dist, const int* freq, int n) {
+  if (int rc = check_rep(h, r)) return rc;
+  if (!dist || !freq || n < 0 || n > kMaxShells) return fail(CVF_EINVAL, "bad distances table");
+  ReplicaHost& R = h->reps[r];
+  R.dist.assign(dist, dist + n);
+  R.freq.assign(freq, freq + n);
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy((void*)R.desc.dist, dist, n * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy((void*)R.desc.freq, freq, n * sizeof(int), cudaMemcpyHostToDevice));
+  R.desc.n_shells = n;
+  if (int rc = upload_descs(h)) return rc;
+  // E_vdW follows the new table (GW:1128 computes it after the table is read)
+  ReplicaState s;
+  if (int rc = read_state(h, r, &s)) return rc;
+  s.e_vdw = host_evdw(s.r_cell, R.dist, R.freq, R.p.R_cutoff);
+  CK(cudaMemcpy((char*)(h->b.st + r) + offsetof(ReplicaState, e_vdw), &s.e_vdw, sizeof(double), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int cvf_get_distances(const cvf_handle* h, int r, float* dist, int* freq, int cap, int* n) {
+  if (int rc = check_rep(h, r)) return rc;
+  const ReplicaHost& R = h->reps[r];
+  int k = (int)R.dist.size();
+  if (n) *n = k;
+  if (cap < k || !dist || !freq) return fail(CVF_EINVAL, "capacity too small");
+  std::copy(R.dist.begin(), R.dist.end(), dist);
+  std::copy(R.freq.begin(), R.freq.end(), freq);
+  return 0;
+}
+
+static int run_impl(cvf_handle* h, int n_steps, int nmet, int ncl, int interval) {
+  if (!h) return fail(CVF_EINVAL, "null handle");
+  if (n_steps < 0 || nmet < 0 || ncl < 0) return fail(CVF_EINVAL, "negative step counts");
+  CK(cudaSetDevice(h->device));
+  if (ncl > 0) {
+    if (int rc = ensure_sw(h)) return rc;
+  }
+  if (n_steps == 0) return 0;
+  const int chunk_plain = 32;
+  if (interval <= 0) {
+    int full = n_steps / chunk_plain, rem = n_steps % chunk_plain;
+    cudaGraphExec_t g;
+    if (full) {
+      if (int rc = get_graph(h, chunk_plain, nmet, ncl, 0, &g)) return rc;
+      for (int i = 0; i < full; ++i) CK(cudaGraphLaunch(g, h->stream));
+    }
+    if (rem) {
+      if (int rc = get_graph(h, rem, nmet, ncl, 0, &g)) return rc;
+      CK(cudaGraphLaunch(g, h->stream));
+    }
+  } else {
+    int full = n_steps / interval, rem = n_steps % interval;
+    cudaGraphExec_t g;
+    if (full) {
+      if (int rc = get_graph(h, interval, nmet, ncl, 1, &g)) return rc;
+      for (int i = 0; i < full; ++i) CK(cudaGraphLaunch(g, h->stream));
+    }
+    if (rem) {
+      if (int rc = get_graph(h, rem, nmet, ncl, 1, &g)) return rc;
+      CK(cudaGraphLaunch(g, h->stream));
+    }
+  }
+  if (ncl > 0) h->sw_done = true;
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int cvf_run_steps(cvf_handle* h, int n_steps, int nmet, int ncl) { return run_impl(h, n_steps, nmet, ncl, 0); }
+
+int cvf_run_sampled(cvf_handle* h, int n_steps, int nmet, int ncl, int interval) {
+  if (interval < 1) return fail(CVF_EINVAL, "interval must be >= 1");
+  return run_impl(h, n_steps, nmet, ncl, interval);
+}
+
+int cvf_synchronize(cvf_handle* h) {
+  if (!h) return fail(CVF_EINVAL, "null handle");
+  CK(cudaSetDevice(h->device));
+  return check_err(h);
+}
+
+int cvf_observables(cvf_handle* h, int r, cvf_obs* out) {
+  if (int rc = check_rep(h, r)) return rc;
+  if (!out) return fail(CVF_EINVAL, "null out");
+  CK(cudaSetDevice(h->device));
+  launch_measure(h->b, 0, h->stream);
+  ReplicaState s;
+  if (int rc = read_state(h, r, &s)) return rc;
+  const ReplicaHost& R = h->reps[r];
+  fill_obs(out, s.last.n_hb2, s.last.n_sigma, s.r_cell, s.volume, host_evdw(s.r_cell, R.dist, R.freq, R.p.R_cutoff),
+           R.N, R.p.P);
+  return 0;
+}
+
+static void degenerate_cstats(const ReplicaHost& R, cvf_cstats* c) {
+  long long NS = 6 * R.N;
+  c->largest = NS;
+  c->second = 0;
+  c->n_percolating = 1;
+  c->n_clusters = 1;
+  c->sum_size = NS;
+  c->sum_size2 = NS * NS;
+  c->sum_size2_wrap32 = (long long)(int32_t)(uint32_t)((unsigned long long)NS * (unsigned long long)NS);
+  fill_cstats(c);
+}
+
+static void from_rec(const CStatsRec& x, cvf_cstats* c) {
+  c->largest = x.largest;
+  c->second = x.second;
+  c->n_percolating = x.n_percolating;
+  c->n_clusters = x.n_clusters;
+  c->sum_size = x.sum_size;
+  c->sum_size2 = x.sum_size2;
+  c->sum_size2_wrap32 = x.sum_size2_wrap32;
+  fill_cstats(c);
+}
+
+int cvf_cluster_stats(cvf_handle* h, int r, cvf_cstats* out) {
+  if (int rc = check_rep(h, r)) return rc;
+  if (!out) return fail(CVF_EINVAL, "null out");
+  if (!h->sw_done) {
+    degenerate_cstats(h->reps[r], out);
+    return 0;
+  }
+  CK(cudaSetDevice(h->device));
+  enqueue_cstats(h, 0);
+  if (int rc = check_err(h)) return rc;
+  ReplicaState s;
+  if (int rc = read_state(h, r, &s)) return rc;
+  from_rec(s.last_cstats, out);
+  return 0;
+}
+
+int cvf_get_labels(cvf_handle* h, int r, int* labels, long long n) {
+  if (int rc = check_rep(h, r)) return rc;
+  const ReplicaHost& R = h->reps[r];
+  if (!labels || n != 6 * R.N) return fail(CVF_EINVAL, "labels must hold 6N ints");
+  if (!h->sw_alloc) {
+    memset(labels, 0, (size_t)n * sizeof(int));
+    return 0;
+  }
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(labels, R.desc.label, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int cvf_sample_count(cvf_handle* h, int r, long long* count) {
+  if (int rc = check_rep(h, r)) return rc;
+  CK(cudaSetDevice(h->device));
+  ReplicaState s;
+  if (int rc = read_state(h, r, &s)) return rc;
+  *count = s.n_samples;
+  return 0;
+}
+
+int cvf_get_samples(cvf_handle* h, int r, cvf_sample* out, long long max, long long* n_out) {
+  if (int rc = check_rep(h, r)) return rc;
+  CK(cudaSetDevice(h->device));
+  ReplicaState s;
+  if (int rc = read_state(h, r, &s)) return rc;
+  long long n = std::min<long long>(std::min<long long>(s.n_samples, s.cap_samples), max);
+  static_assert(sizeof(cvf_sample) == sizeof(SampleRec), "sample layout");
+  if (n > 0) CK(cudaMemcpy(out, s.samples, (size_t)n * sizeof(SampleRec), cudaMemcpyDeviceToHost));
+  if (n_out) *n_out = n;
+  if (s.n_samples > s.cap_samples) return fail(CVF_ELIMIT, "sample stream overflowed its capacity");
+  return 0;
+}
+
+int cvf_get_cstats_stream(cvf_handle* h, int r, cvf_cstats* out, long long max, long long* n_out) {
+  if (int rc = check_rep(h, r)) return rc;
+  CK(cudaSetDevice(h->device));
+  ReplicaState s;
+  if (int rc = read_state(h, r, &s)) return rc;
+  long long n = std::min<long long>(std::min<long long>(s.n_cstats, s.cap_cstats), max);
+  std::vector<CStatsRec> tmp((size_t)std::max<long long>(n, 0));
+  if (n > 0) CK(cudaMemcpy(tmp.data(), s.cstats, (size_t)n * sizeof(CStatsRec), cudaMemcpyDeviceToHost));
+  for (long long i = 0; i < n; ++i) from_rec(tmp[(size_t)i], out + i);
+  if (n_out) *n_out = n;
+  return 0;
+}
+
+int cvf_clear_samples(cvf_handle* h) {
+  if (!h) return fail(CVF_EINVAL, "null handle");
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  uint32_t zero = 0;
+  for (int r = 0; r < (int)h->reps.size(); ++r) {
+    CK(cudaMemcpy((char*)(h->b.st + r) + offsetof(ReplicaState, n_samples), &zero, 4, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy((char*)(h->b.st + r) + offsetof(ReplicaState, n_cstats), &zero, 4, cudaMemcpyHostToDevice));
+  }
+  return 0;
+}
+
+int cvf_sample_observables(const cvf_handle* h, int r, const cvf_sample* s, cvf_obs* out) {
+  if (int rc = check_rep(h, r)) return rc;
+  const ReplicaHost& R = h->reps[r];
+  fill_obs(out, s->n_hb2, s->n_sigma, s->r_cell, s->volume, host_evdw(s->r_cell, R.dist, R.freq, R.p.R_cutoff), R.N,
+           R.p.P);
+  return 0;
+}
+
+int cvf_get_state(cvf_handle* h, int r, cvf_state* out) {
+  if (int rc = check_rep(h, r)) return rc;
+  CK(cudaSetDevice(h->device));
+  ReplicaState s;
+  if (int rc = read_state(h, r, &s)) return rc;
+  out->r_cell = s.r_cell;
+  out->volume = s.volume;
+  out->e_vdw = s.e_vdw;
+  for (int i = 0; i < 4; ++i) out->counters[i] = s.ctr[i];
+  return 0;
+}
+
+int cvf_set_state(cvf_handle* h, int r, const cvf_state* in) {
+  if (int rc = check_rep(h, r)) return rc;
+  CK(cudaSetDevice(h->device));
+  ReplicaState s;
+  if (int rc = read_state(h, r, &s)) return rc;
+  const ReplicaHost& R = h->reps[r];
+  s.r_cell = in->r_cell;
+  s.volume = in->volume;
+  s.e_vdw = host_evdw(in->r_cell, R.dist, R.freq, R.p.R_cutoff);
+  for (int i = 0; i < 4; ++i) s.ctr[i] = in->counters[i];
+  CK(cudaMemcpy(h->b.st + r, &s, sizeof(ReplicaState), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int cvf_get_stream(cvf_handle* h, void** stream) {
+  if (!h || !stream) return fail(CVF_EINVAL, "null handle/out");
+  *stream = (void*)h->stream;
+  return 0;
+}
+
+int cvf_profile_launch(cvf_handle* h, int kind, int n) {
+  if (!h || n < 0 || kind < 0 || kind > 3) return fail(CVF_EINVAL, "bad profile request");
+  CK(cudaSetDevice(h->device));
+  for (int i = 0; i < n; ++i) {
+    switch (kind) {
+      case 0:
+        launch_sweep(h->b, 0, i, h->stream);
+        launch_sweep(h->b, 1, i, h->stream);
+        break;
+      case 1:
+        launch_step_begin(h->b, 0, 0, 1, h->stream);
+        launch_cube_move(h->b, h->stream);
+        break;
+      case 2: launch_step_begin(h->b, 0, 0, 0, h->stream); break;
+      default: launch_measure(h->b, 0, h->stream); break;
+    }
+  }
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int cvf_get_thresholds(const cvf_handle* h, int r, unsigned long long* out) {
+  if (int rc = check_rep(h, r)) return rc;
+  const Thresholds& t = h->reps[r].thr;
+  memcpy(out, t.sweep, sizeof(t.sweep));
+  memcpy(out + 33, t.cube, sizeof(t.cube));
+  memcpy(out + 42, t.sw, sizeof(t.sw));
+  return 0;
+}
+
+}  // extern "C"

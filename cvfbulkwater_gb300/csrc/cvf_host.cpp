@@ -1,0 +1,171 @@
+// Host-side helpers of the engine (no GPU). Compiled with -ffp-contract=off: the acceptance
+// tables and FP64 observables must round the same way as the CPU oracle.
+#include "cvf_host.h"
+
+#include <math.h>
+
+#include "cvf_spec.cuh"
+
+namespace cvf {
+
+void compute_shells(int L, float Rc, std::vector<float>& dist, std::vector<int>& freq) {
+  dist.clear();
+  freq.clear();
+  const long long N = (long long)L * L * L;
+  for (long long j = 1; j < N; ++j) {
+    int dx = (int)(j % L), dy = (int)((j / L) % L), dz = (int)(j / ((long long)L * L));
+    if (dx > L / 2) dx = L - dx;
+    if (dy > L / 2) dy = L - dy;
+    if (dz > L / 2) dz = L - dz;
+    float d = (float)sqrt((double)(dx * dx + dy * dy + dz * dz));
+    if (!(d < Rc)) continue;
+    size_t k = 0;
+    for (; k < dist.size(); ++k)
+      if (dist[k] == d) break;
+    if (k == dist.size()) {
+      dist.push_back(d);
+      freq.push_back(1);
+    } else {
+      freq[k]++;
+    }
+  }
+  for (size_t k = 0; k < freq.size(); ++k) freq[k] = (freq[k] / 2) * (int)N;
+}
+
+Thresholds make_thresholds(float T, float P) {
+  Thresholds t;
+  t.beta = 1. / T;
+  float jeff_f = kJhbF - P * kVhbF;
+  t.Jeff = (double)jeff_f;
+  const double Js = (double)kJsigF;
+  for (int dhb = -1; dhb <= 1; ++dhb)
+    for (int dns = -5; dns <= 5; ++dns) {
+      double dE = -t.Jeff * (double)dhb - Js * (double)dns;
+      t.sweep[(dhb + 1) * 11 + dns + 5] = threshold_from_p(exp(-t.beta * dE));
+    }
+  for (int dhb = -4; dhb <= 4; ++dhb) {
+    double dE = -t.Jeff * (double)dhb - Js * 0.0;
+    t.cube[dhb + 4] = threshold_from_p(exp(-t.beta * dE));
+  }
+  // GW:992-993
+  t.sw[0] = threshold_from_p(1.0 - exp(-t.beta * fabs(t.Jeff)));
+  t.sw[1] = threshold_from_p(1.0 - exp(-t.beta * fabs(Js)));
+  return t;
+}
+
+double host_evdw(double r, const std::vector<float>& dist, const std::vector<int>& freq, float Rc) {
+  return evdw(r, dist.data(), freq.data(), (int)dist.size(), Rc);
+}
+
+void fill_obs(cvf_obs* o, long long n_hb2, long long n_sigma, double r_cell, double volume, double e_vdw,
+              long long N, float P) {
+  o->n_hb2 = n_hb2;
+  o->n_sigma = n_sigma;
+  o->r_cell = r_cell;
+  o->volume = volume;
+  o->e_vdw = e_vdw;
+  o->n_hb = 0.5 * (double)n_hb2;
+  o->energy = (e_vdw + (-(double)kJhbF) * o->n_hb) + (-(double)kJsigF) * (double)n_sigma;
+  o->v_total = (double)N * r_cell * r_cell * r_cell + (double)kVhbF * o->n_hb;
+  o->enthalpy = o->energy + (double)P * o->v_total;
+  o->m = (double)n_sigma / ((double)N * 15.0);
+}
+
+void fill_cstats(cvf_cstats* c) {
+  if (c->n_clusters > 0) {
+    c->mean = (double)c->sum_size / (double)c->n_clusters;
+    c->variance = (double)c->sum_size2 / (double)c->n_clusters - c->mean * c->mean;
+    float n = (float)c->n_clusters;
+    float avg = (float)c->sum_size / n;
+    float avg2 = (float)c->sum_size2_wrap32 / n;
+    avg2 -= avg * avg;
+    c->mean_ref = avg;
+    c->variance_ref = avg2;
+  } else {
+    c->mean = c->variance = 0.0;
+    c->mean_ref = c->variance_ref = 0.0f;
+  }
+}
+
+static inline size_t word_index(int L, int x, int y, int z) {
+  const int H = L / 2;
+  return (size_t)(x >> 1) + (size_t)H * ((size_t)y + (size_t)L * z);
+}
+
+bool pack_config(int L, const int* c12, std::vector<uint32_t>& cells0, std::vector<uint32_t>& cells1,
+                 std::vector<uint8_t>& ce, std::vector<uint8_t>& co, std::string& err) {
+  const int H = L / 2;
+  const long long N = (long long)L * L * L;
+  cells0.assign((size_t)(N / 2), 0);
+  cells1.assign((size_t)(N / 2), 0);
+  ce.assign((size_t)H * H * H, 0);
+  co.assign((size_t)H * H * H, 0);
+  for (long long c = 0; c < N; ++c) {
+    int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
+    uint32_t w = 0;
+    for (int a = 0; a < 6; ++a) {
+      int s = c12[c * 12 + a], e = c12[c * 12 + 6 + a];
+      if (s < 0 || s > 5) {
+        err = "Unexpected value for spin (" + std::to_string(s) + ") appeared in line " + std::to_string(c);
+        return false;
+      }
+      if (e < 0 || e > 1) {
+        err = "Unexpected value for active_bond (" + std::to_string(e) + ") appeared in line " + std::to_string(c);
+        return false;
+      }
+      w |= (uint32_t)s << (3 * a);
+    }
+    ((x + y + z) & 1 ? cells1 : cells0)[word_index(L, x, y, z)] = w;
+  }
+  auto eta = [&](int arm, int x, int y, int z) -> int {
+    return c12[((long long)x + (long long)L * (y + (long long)L * z)) * 12 + 6 + arm];
+  };
+  for (int par = 0; par < 2; ++par)
+    for (int c = 0; c < H; ++c)
+      for (int b = 0; b < H; ++b)
+        for (int a = 0; a < H; ++a) {
+          int x = 2 * a + par, y = 2 * b + par, z = 2 * c + par;
+          int xp = (x + 1) % L, yp = (y + 1) % L, zp = (z + 1) % L;
+          // vertices v1 (x,y,z), v2 x+1, v3 y+1, v6 y+1,z+1, v7 x+1,z+1, v8 x+1,y+1 (GW:3330-3337)
+          int st;
+          if (eta(0, x, y, z) == 0) {
+            if (eta(0, x, yp, zp) == 0) st = 2;
+            else if (eta(4, x, yp, z) == 0) st = 3;
+            else st = 8;
+          } else if (eta(2, x, y, z) == 0) {
+            if (eta(4, xp, y, z) == 0) st = 4;
+            else if (eta(2, xp, y, zp) == 0) st = 5;
+            else st = 7;
+          } else {
+            if (eta(0, x, yp, z) == 0) st = 0;
+            else if (eta(4, xp, yp, z) == 0) st = 1;
+            else st = 6;
+          }
+          (par ? co : ce)[(size_t)a + (size_t)H * ((size_t)b + (size_t)H * c)] = (uint8_t)st;
+        }
+  return true;
+}
+
+void unpack_config(int L, const std::vector<uint32_t>& cells0, const std::vector<uint32_t>& cells1,
+                   const std::vector<uint8_t>& ce, const std::vector<uint8_t>& co, int* c12) {
+  const int H = L / 2;
+  const long long N = (long long)L * L * L;
+  uint8_t tab[72];
+  for (int s = 0; s < 9; ++s)
+    for (int p = 0; p < 8; ++p) tab[s * 8 + p] = (uint8_t)cube_eta_bits(s, p);
+  for (long long c = 0; c < N; ++c) {
+    int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
+    uint32_t w = ((x + y + z) & 1 ? cells1 : cells0)[word_index(L, x, y, z)];
+    int xo = (x & 1) ? x : (x + L - 1) % L, yo = (y & 1) ? y : (y + L - 1) % L, zo = (z & 1) ? z : (z + L - 1) % L;
+    int p = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+    uint32_t se = ce[(size_t)(x >> 1) + (size_t)H * ((size_t)(y >> 1) + (size_t)H * (z >> 1))];
+    uint32_t so = co[(size_t)(xo >> 1) + (size_t)H * ((size_t)(yo >> 1) + (size_t)H * (zo >> 1))];
+    uint32_t eta = (uint32_t)tab[se * 8 + p] | (uint32_t)tab[so * 8 + (p ^ 7)];
+    for (int a = 0; a < 6; ++a) {
+      c12[c * 12 + a] = (int)((w >> (3 * a)) & 7u);
+      c12[c * 12 + 6 + a] = (int)((eta >> a) & 1u);
+    }
+  }
+}
+
+}  // namespace cvf

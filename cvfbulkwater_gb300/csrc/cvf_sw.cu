@@ -1,0 +1,424 @@
+// Swendsen-Wang cluster step and cluster statistics of the GB300 CVF engine.
+//
+// Reference: SOURCE/gpu_water3D.cu ("GW") GW:2365-2542 (bond activation, min-label scans until
+// nothing changes, cluster shift) and GW:2677-2780 (cluster statistics on the host).
+// Here the labelling is a lock-free union-find over the 6N arm sites (site = arm*N + cell):
+// parents only ever point to smaller site ids, roots are hooked under smaller roots with
+// atomicMin, so each component's root is its minimum site id -- the same canonical label the
+// reference's min-label propagation converges to, independent of thread scheduling.
+#include "cvf_device.cuh"
+#include "cvf_spec.cuh"
+
+namespace cvf {
+
+// eta table of this translation unit ([state*8 + vertex offset] -> 6-bit eta mask); constant
+// memory is per translation unit without relocatable device code.
+static __constant__ uint8_t c_eta_table[72];
+
+void init_sw_device_tables() {
+  uint8_t eta[72];
+  for (int s = 0; s < 9; ++s)
+    for (int p = 0; p < 8; ++p) eta[s * 8 + p] = (uint8_t)cube_eta_bits(s, p);
+  cudaMemcpyToSymbol(c_eta_table, eta, sizeof(eta));
+}
+
+__device__ __forceinline__ int find_replica_sw(const int* __restrict__ blk, int nrep, int b) {
+  int lo = 0, hi = nrep - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(blk + mid) <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ uint32_t word_at(const ReplicaDesc& R, int x, int y, int z) {
+  return R.cells[(x + y + z) & 1][(uint32_t)(x >> 1) + (uint32_t)R.H * ((uint32_t)y + (uint32_t)R.L * (uint32_t)z)];
+}
+
+__device__ __forceinline__ uint32_t eta_of_cell(const ReplicaDesc& R, int x, int y, int z) {
+  const int L = R.L, H = R.H;
+  const int xo = (x & 1) ? x : (x == 0 ? L - 1 : x - 1);
+  const int yo = (y & 1) ? y : (y == 0 ? L - 1 : y - 1);
+  const int zo = (z & 1) ? z : (z == 0 ? L - 1 : z - 1);
+  const int p = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+  uint32_t se = R.cubes[0][(size_t)(x >> 1) + (size_t)H * ((size_t)(y >> 1) + (size_t)H * (z >> 1))];
+  uint32_t so = R.cubes[1][(size_t)(xo >> 1) + (size_t)H * ((size_t)(yo >> 1) + (size_t)H * (zo >> 1))];
+  return (uint32_t)c_eta_table[se * 8 + p] | (uint32_t)c_eta_table[so * 8 + (p ^ 7)];
+}
+
+// ---------------------------------------------------------------- bonds + in-cell components
+// GW:2383-2438: links 0..2 are the x+, y+, z+ hydrogen-bond links of the cell, links 3..17 the
+// intra-cell pairs (a<b) in row-major order. Each link draws word l of the cell's 20-word block.
+__global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __restrict__ reps,
+                                                       const ReplicaState* __restrict__ st,
+                                                       const int* __restrict__ blk, int nrep, int jsw) {
+  const int r = find_replica_sw(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  const int L = R.L;
+  const long long N = (long long)L * L * L;
+  long long c = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  const int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
+  const uint32_t t = st[r].cur[3] + (uint32_t)jsw;
+  const uint32_t w = word_at(R, x, y, z);
+  uint32_t rw[20];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    U4 q = philox((uint32_t)c, t, kStSwBond + j, R.replica, R.key0, R.key1);
+    rw[4 * j] = q.x;
+    rw[4 * j + 1] = q.y;
+    rw[4 * j + 2] = q.z;
+    rw[4 * j + 3] = q.w;
+  }
+  const unsigned long long thb = R.thr_sw[0], ts = R.thr_sw[1];
+  uint32_t hb = 0;
+  if (R.Jeff != 0.0) {
+    const uint32_t eta = eta_of_cell(R, x, y, z);
+    const int xn = x + 1 == L ? 0 : x + 1, yn = y + 1 == L ? 0 : y + 1, zn = z + 1 == L ? 0 : z + 1;
+    const uint32_t wn[3] = {word_at(R, xn, y, z), word_at(R, x, yn, z), word_at(R, x, y, zn)};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      uint32_t sa = (w >> (6 * d)) & 7u, sb = (wn[d] >> (6 * d + 3)) & 7u;
+      bool b;
+      if (R.Jeff > 0.0) b = ((eta >> (2 * d)) & 1u) && sa == sb && (unsigned long long)rw[d] < thb;
+      else b = sa != sb && (unsigned long long)rw[d] < thb;
+      hb |= (uint32_t)b << d;
+    }
+  }
+  R.hbmask[c] = (uint8_t)hb;
+  uint32_t adj[6] = {0, 0, 0, 0, 0, 0};
+  int l = 3;
+#pragma unroll
+  for (int a = 0; a < 5; ++a)
+#pragma unroll
+    for (int b = a + 1; b < 6; ++b, ++l) {
+      bool bond = ((w >> (3 * a)) & 7u) == ((w >> (3 * b)) & 7u) && (unsigned long long)rw[l] < ts;
+      if (bond) {
+        adj[a] |= 1u << b;
+        adj[b] |= 1u << a;
+      }
+    }
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    uint32_t m = 1u << a;
+#pragma unroll
+    for (int it = 0; it < 5; ++it) {
+      uint32_t nm = m;
+#pragma unroll
+      for (int b = 0; b < 6; ++b)
+        if ((m >> b) & 1u) nm |= adj[b];
+      m = nm;
+    }
+    int root = __ffs(m) - 1;
+    R.label[(long long)a * N + c] = (int32_t)((long long)root * N + c);
+  }
+}
+
+// ---------------------------------------------------------------- union-find
+__device__ __forceinline__ int32_t uf_find(int32_t* p, int32_t x) {
+  // Path halving. Parents only decrease and stay inside the component, so stale reads only
+  // cost extra iterations; the walk ends at the root (at most x steps).
+  for (int it = 0; it < (1 << 30); ++it) {
+    int32_t px = __ldcg(p + x);
+    if (px == x) return x;
+    int32_t ppx = __ldcg(p + px);
+    if (ppx != px) p[x] = ppx;
+    x = ppx;
+  }
+  return x;
+}
+
+__device__ __forceinline__ bool uf_unite(int32_t* p, int32_t a, int32_t b) {
+  for (int it = 0; it < (1 << 24); ++it) {
+    a = uf_find(p, a);
+    b = uf_find(p, b);
+    if (a == b) return true;
+    if (a > b) {
+      int32_t tmp = a;
+      a = b;
+      b = tmp;
+    }
+    int32_t old = atomicMin(p + b, a);
+    if (old == b) return true;
+    b = old;
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __restrict__ reps,
+                                                       ReplicaState* __restrict__ st,
+                                                       const int* __restrict__ blk, int nrep) {
+  const int r = find_replica_sw(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  const int L = R.L;
+  const long long N = (long long)L * L * L;
+  long long c = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  uint32_t hb = R.hbmask[c];
+  if (!hb) return;
+  const int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
+  const long long nb[3] = {(long long)(x + 1 == L ? 0 : x + 1) + (long long)L * (y + (long long)L * z),
+                           (long long)x + (long long)L * ((y + 1 == L ? 0 : y + 1) + (long long)L * z),
+                           (long long)x + (long long)L * (y + (long long)L * (z + 1 == L ? 0 : z + 1))};
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if ((hb >> d) & 1u)
+      if (!uf_unite(R.label, (int32_t)((long long)(2 * d) * N + c), (int32_t)((long long)(2 * d + 1) * N + nb[d])))
+        st[r].err = 1;
+}
+
+__global__ void __launch_bounds__(kThreads) k_sw_compress(const ReplicaDesc* __restrict__ reps,
+                                                          const int* __restrict__ blk, int nrep) {
+  const int r = find_replica_sw(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  const long long NS = 6LL * R.L * R.L * R.L;
+  long long s = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  if (s >= NS) return;
+  int32_t x = (int32_t)s;
+  for (int it = 0; it < (1 << 30); ++it) {
+    int32_t px = __ldcg(R.label + x);
+    if (px == x) break;
+    x = px;
+  }
+  R.label[s] = x;
+}
+
+// GW:2531-2542: every cluster gets one uniform shift in 0..5, drawn from its root's stream.
+__global__ void __launch_bounds__(kThreads) k_sw_roots(const ReplicaDesc* __restrict__ reps,
+                                                       const ReplicaState* __restrict__ st,
+                                                       const int* __restrict__ blk, int nrep, int jsw) {
+  const int r = find_replica_sw(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  const long long NS = 6LL * R.L * R.L * R.L;
+  long long s = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  if (s >= NS) return;
+  if (R.label[s] != (int32_t)s) return;
+  const uint32_t t = st[r].cur[3] + (uint32_t)jsw;
+  U4 q = philox((uint32_t)s, t, kStSwFlip, R.replica, R.key0, R.key1);
+  uint32_t k;
+  if (!lemire_try(q.x, 6, k) && !lemire_try(q.y, 6, k) && !lemire_try(q.z, 6, k) && !lemire_try(q.w, 6, k))
+    k = lemire_retry(6, (uint32_t)s, t, kStSwFlip, R.replica, R.key0, R.key1);
+  R.shift[s] = (uint8_t)k;
+}
+
+__global__ void __launch_bounds__(kThreads) k_sw_apply(const ReplicaDesc* __restrict__ reps,
+                                                       const int* __restrict__ blk, int nrep) {
+  const int r = find_replica_sw(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  const int L = R.L;
+  const long long N = (long long)L * L * L;
+  long long c = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  const int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
+  uint32_t* wp = R.cells[(x + y + z) & 1] + (uint32_t)(x >> 1) + (uint32_t)R.H * ((uint32_t)y + (uint32_t)L * (uint32_t)z);
+  uint32_t w = *wp, out = 0;
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    uint32_t sh = R.shift[R.label[(long long)a * N + c]];
+    uint32_t v = ((w >> (3 * a)) & 7u) + sh;
+    if (v >= 6u) v -= 6u;
+    out |= v << (3 * a);
+  }
+  *wp = out;
+}
+
+// ---------------------------------------------------------------- cluster statistics
+__global__ void __launch_bounds__(kThreads) k_cs_count(const ReplicaDesc* __restrict__ reps,
+                                                       const int* __restrict__ blk, int nrep) {
+  const int r = find_replica_sw(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  const long long NS = 6LL * R.L * R.L * R.L;
+  long long s = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  if (s >= NS) return;
+  int32_t lab = R.label[s];
+  unsigned peers = __match_any_sync(__activemask(), lab);
+  if ((threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1)) atomicAdd(R.csize + lab, __popc(peers));
+}
+
+__device__ __forceinline__ void top2_merge(unsigned long long& a1, unsigned long long& a2, unsigned long long b1,
+                                           unsigned long long b2) {
+  if (b1 > a1) {
+    a2 = a1 > b2 ? a1 : b2;
+    a1 = b1;
+  } else {
+    a2 = a2 > b1 ? a2 : b1;
+  }
+}
+
+// Per label slot: cluster count, sums of s and s^2 (exact and with the reference's 32-bit wrap of
+// s*s, GW:2697), block top-2 sizes into blocktop, percolation candidates (size >= 2L, GW:2702).
+__global__ void __launch_bounds__(kThreads) k_cs_reduce(const ReplicaDesc* __restrict__ reps,
+                                                        ReplicaState* __restrict__ st,
+                                                        const int* __restrict__ blk, int nrep,
+                                                        unsigned long long* __restrict__ blocktop) {
+  __shared__ unsigned long long s_red[3];
+  __shared__ unsigned long long s_top[kThreads / 32][2];
+  const int r = find_replica_sw(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  const int L = R.L;
+  const long long NS = 6LL * L * L * L;
+  long long s = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  if (threadIdx.x < 3) s_red[threadIdx.x] = 0;
+  __syncthreads();
+  unsigned long long ncl = 0, sum2 = 0, sum2w = 0, t1 = 0, t2 = 0;
+  if (s < NS) {
+    long long sz = R.csize[s];
+    if (sz > 0) {
+      ncl = 1;
+      sum2 = (unsigned long long)(sz * sz);
+      sum2w = (unsigned long long)(long long)(int32_t)(uint32_t)((unsigned long long)sz * (unsigned long long)sz);
+      t1 = (unsigned long long)sz;
+      int k = -1;
+      if (sz >= 2LL * L) {
+        k = atomicAdd(&st[r].ncand, 1);
+        if (k >= R.max_cand) {
+          k = -1;
+          st[r].err = 2;
+        }
+      }
+      R.cand[s] = k;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ncl += __shfl_xor_sync(0xffffffffu, ncl, o);
+    sum2 += __shfl_xor_sync(0xffffffffu, sum2, o);
+    sum2w += __shfl_xor_sync(0xffffffffu, sum2w, o);
+    unsigned long long b1 = __shfl_xor_sync(0xffffffffu, t1, o), b2 = __shfl_xor_sync(0xffffffffu, t2, o);
+    top2_merge(t1, t2, b1, b2);
+  }
+  const int warp = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&s_red[0], ncl);
+    atomicAdd(&s_red[1], sum2);
+    atomicAdd(&s_red[2], sum2w);
+    s_top[warp][0] = t1;
+    s_top[warp][1] = t2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long a1 = 0, a2 = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) top2_merge(a1, a2, s_top[w][0], s_top[w][1]);
+    blocktop[2 * (long long)blockIdx.x] = a1;
+    blocktop[2 * (long long)blockIdx.x + 1] = a2;
+    atomicAdd(&st[r].ncl, s_red[0]);
+    atomicAdd(&st[r].sum2, s_red[1]);
+    atomicAdd(&st[r].sum2w, s_red[2]);
+  }
+}
+
+// Coordinate coverage of candidate clusters (GW:2723-2780): bit x of axis 0, y of axis 1,
+// z of axis 2, OR-reduced across lanes that hit the same word before the atomic.
+__global__ void __launch_bounds__(kThreads) k_cs_cover(const ReplicaDesc* __restrict__ reps,
+                                                       const int* __restrict__ blk, int nrep) {
+  const int r = find_replica_sw(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  const int L = R.L;
+  const long long N = (long long)L * L * L;
+  long long s = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  int k = -1;
+  int coord[3] = {0, 0, 0};
+  if (s < 6 * N) {
+    k = R.cand[R.label[s]];
+    long long c = s % N;
+    coord[0] = (int)(c % L);
+    coord[1] = (int)((c / L) % L);
+    coord[2] = (int)(c / ((long long)L * L));
+  }
+  const unsigned active = __ballot_sync(0xffffffffu, k >= 0);
+  if (k < 0) return;
+  const int W = (L + 31) >> 5;
+#pragma unroll
+  for (int ax = 0; ax < 3; ++ax) {
+    long long word = ((long long)k * 3 + ax) * W + (coord[ax] >> 5);
+    unsigned grp = __match_any_sync(active, word);
+    unsigned bits = __reduce_or_sync(grp, 1u << (coord[ax] & 31));
+    if ((threadIdx.x & 31) == (unsigned)(__ffs(grp) - 1)) atomicOr(R.cover + word, bits);
+  }
+}
+
+// One block per replica: merge the block top-2 values, count candidates that cover every x,
+// every y or every z coordinate, and emit the statistics record.
+__global__ void __launch_bounds__(kThreads) k_cs_final(const ReplicaDesc* __restrict__ reps,
+                                                       ReplicaState* __restrict__ st,
+                                                       const int* __restrict__ blk, int nrep,
+                                                       const unsigned long long* __restrict__ blocktop,
+                                                       int record) {
+  __shared__ unsigned long long s_top[kThreads][2];
+  __shared__ unsigned long long s_perc;
+  const int r = blockIdx.x;
+  if (r >= nrep) return;
+  const ReplicaDesc& R = reps[r];
+  ReplicaState& S = st[r];
+  const int L = R.L;
+  const int W = (L + 31) >> 5;
+  unsigned long long a1 = 0, a2 = 0;
+  for (int b = blk[r] + threadIdx.x; b < blk[r + 1]; b += blockDim.x)
+    top2_merge(a1, a2, blocktop[2 * (long long)b], blocktop[2 * (long long)b + 1]);
+  s_top[threadIdx.x][0] = a1;
+  s_top[threadIdx.x][1] = a2;
+  if (threadIdx.x == 0) s_perc = 0;
+  __syncthreads();
+  int ncand = S.ncand < R.max_cand ? S.ncand : R.max_cand;
+  unsigned long long perc = 0;
+  for (int k = threadIdx.x; k < ncand; k += blockDim.x) {
+    bool any = false;
+    for (int ax = 0; ax < 3 && !any; ++ax) {
+      bool full = true;
+      for (int j = 0; j < W && full; ++j) {
+        int bits = L - 32 * j;
+        uint32_t want = bits >= 32 ? 0xffffffffu : ((1u << bits) - 1u);
+        full = (R.cover[((long long)k * 3 + ax) * W + j] & want) == want;
+      }
+      any = full;
+    }
+    perc += any;
+  }
+  atomicAdd(&s_perc, perc);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long m1 = 0, m2 = 0;
+    for (int i = 0; i < (int)blockDim.x; ++i) top2_merge(m1, m2, s_top[i][0], s_top[i][1]);
+    CStatsRec rec;
+    rec.largest = (long long)m1;
+    rec.second = (long long)m2;
+    rec.n_percolating = (long long)s_perc;
+    rec.n_clusters = (long long)S.ncl;
+    rec.sum_size = 6LL * L * L * L;
+    rec.sum_size2 = (long long)S.sum2;
+    rec.sum_size2_wrap32 = (long long)S.sum2w;
+    S.last_cstats = rec;
+    if (record && S.cstats && S.n_cstats < S.cap_cstats) S.cstats[S.n_cstats] = rec;
+    if (record) S.n_cstats++;
+  }
+}
+
+__global__ void k_cs_begin(ReplicaState* __restrict__ st, int nrep) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrep) return;
+  st[r].ncl = 0;
+  st[r].sum2 = 0;
+  st[r].sum2w = 0;
+  st[r].ncand = 0;
+}
+
+// ---------------------------------------------------------------- launchers
+void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s) {
+  k_sw_local<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.st, b.blk_cell, b.nrep, jsw);
+  k_sw_union<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.st, b.blk_cell, b.nrep);
+  k_sw_compress<<<b.nblk_site, kThreads, 0, s>>>(b.reps, b.blk_site, b.nrep);
+  k_sw_roots<<<b.nblk_site, kThreads, 0, s>>>(b.reps, b.st, b.blk_site, b.nrep, jsw);
+  k_sw_apply<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.blk_cell, b.nrep);
+}
+
+// Needs csize zeroed and cover zeroed by the caller (memset nodes); blocktop sized 2*nblk_site.
+void launch_cluster_stats_impl(const BatchDev& b, unsigned long long* blocktop, int record, cudaStream_t s) {
+  k_cs_begin<<<(b.nrep + kThreads - 1) / kThreads, kThreads, 0, s>>>(b.st, b.nrep);
+  k_cs_count<<<b.nblk_site, kThreads, 0, s>>>(b.reps, b.blk_site, b.nrep);
+  k_cs_reduce<<<b.nblk_site, kThreads, 0, s>>>(b.reps, b.st, b.blk_site, b.nrep, blocktop);
+  k_cs_cover<<<b.nblk_site, kThreads, 0, s>>>(b.reps, b.blk_site, b.nrep);
+  k_cs_final<<<b.nrep, kThreads, 0, s>>>(b.reps, b.st, b.blk_site, b.nrep, blocktop, record);
+}
+
+}  // namespace cvf

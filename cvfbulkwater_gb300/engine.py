@@ -1,0 +1,166 @@
+"""Python face of the engine: one handle of one or more replicas behind the C ABI.
+
+Mirrors the calls a reference user makes through gpu_water3D: load a configuration
+(input_config), run Monte Carlo steps (MonteCarlo_Step, GW:1346-1733), measure (measure,
+GW:2014-2160) and read cluster statistics (print_cluster_statistics, GW:2677-2721).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi
+from .abi import check, lib
+
+
+@dataclass
+class Params:
+    L: int
+    T: float
+    P: float
+    seed: int
+    R_cutoff: float = 6.0
+    start: int = 0            # Flag_config: 0 disordered, 1 from set_config, 2 ordered
+    flag_chessboard: int = 1
+    replica: int = 0
+    device: int = 0
+    sample_capacity: int = 0
+
+    def to_c(self) -> abi.Params:
+        return abi.Params(self.L, self.T, self.P, self.seed, self.R_cutoff, self.start,
+                          self.flag_chessboard, self.replica, self.device, self.sample_capacity)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Lattice:
+    """A handle of n >= 1 replicas on one GPU."""
+
+    def __init__(self, params):
+        if isinstance(params, Params):
+            params = [params]
+        arr = (abi.Params * len(params))(*[p.to_c() for p in params])
+        h = C.c_void_p()
+        if len(params) == 1:
+            check(lib().cvf_create(arr, C.byref(h)))
+        else:
+            check(lib().cvf_batch_create(arr, len(params), C.byref(h)))
+        self._h = h
+        self.params = list(params)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().cvf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def n_replicas(self) -> int:
+        return lib().cvf_num_replicas(self._h)
+
+    def N(self, r=0) -> int:
+        return self.params[r].L ** 3
+
+    # -- configuration
+    def set_config(self, cells12: np.ndarray, r: int = 0):
+        a = np.ascontiguousarray(cells12, dtype=np.int32)
+        check(lib().cvf_set_config(self._h, r, _ptr(a), a.size // 12))
+
+    def get_config(self, r: int = 0) -> np.ndarray:
+        a = np.zeros((self.N(r), 12), dtype=np.int32)
+        check(lib().cvf_get_config(self._h, r, _ptr(a), self.N(r)))
+        return a
+
+    def set_distances(self, dist, freq, r: int = 0):
+        d = np.ascontiguousarray(dist, dtype=np.float32)
+        f = np.ascontiguousarray(freq, dtype=np.int32)
+        check(lib().cvf_set_distances(self._h, r, _ptr(d), _ptr(f), d.size))
+
+    def get_distances(self, r: int = 0):
+        d = np.zeros(512, dtype=np.float32)
+        f = np.zeros(512, dtype=np.int32)
+        n = C.c_int()
+        check(lib().cvf_get_distances(self._h, r, _ptr(d), _ptr(f), 512, C.byref(n)))
+        return d[: n.value].copy(), f[: n.value].copy()
+
+    # -- running
+    def run(self, n_steps: int, n_metropolis: int = 1, n_cluster: int = 0):
+        check(lib().cvf_run_steps(self._h, n_steps, n_metropolis, n_cluster))
+
+    def run_sampled(self, n_steps: int, n_metropolis: int, n_cluster: int, interval: int):
+        check(lib().cvf_run_sampled(self._h, n_steps, n_metropolis, n_cluster, interval))
+
+    def synchronize(self):
+        check(lib().cvf_synchronize(self._h))
+
+    # -- measurement
+    def observables(self, r: int = 0) -> abi.Obs:
+        o = abi.Obs()
+        check(lib().cvf_observables(self._h, r, C.byref(o)))
+        return o
+
+    def cluster_stats(self, r: int = 0) -> abi.CStats:
+        s = abi.CStats()
+        check(lib().cvf_cluster_stats(self._h, r, C.byref(s)))
+        return s
+
+    def labels(self, r: int = 0) -> np.ndarray:
+        a = np.zeros(6 * self.N(r), dtype=np.int32)
+        check(lib().cvf_get_labels(self._h, r, _ptr(a), a.size))
+        return a
+
+    def samples(self, r: int = 0) -> np.ndarray:
+        n = C.c_longlong()
+        check(lib().cvf_sample_count(self._h, r, C.byref(n)))
+        buf = (abi.Sample * max(n.value, 1))()
+        got = C.c_longlong()
+        check(lib().cvf_get_samples(self._h, r, buf, n.value, C.byref(got)))
+        dt = np.dtype([("n_hb2", np.int64), ("n_sigma", np.int64), ("r_cell", np.float64),
+                       ("volume", np.float64)])
+        return np.frombuffer(bytes(buf), dtype=dt, count=got.value).copy()
+
+    def cstats_stream(self, r: int = 0):
+        n = C.c_longlong()
+        check(lib().cvf_sample_count(self._h, r, C.byref(n)))
+        buf = (abi.CStats * max(n.value, 1))()
+        got = C.c_longlong()
+        check(lib().cvf_get_cstats_stream(self._h, r, buf, n.value, C.byref(got)))
+        return [buf[i] for i in range(got.value)]
+
+    def clear_samples(self):
+        check(lib().cvf_clear_samples(self._h))
+
+    def sample_observables(self, s, r: int = 0) -> abi.Obs:
+        smp = abi.Sample(int(s["n_hb2"]), int(s["n_sigma"]), float(s["r_cell"]), float(s["volume"]))
+        o = abi.Obs()
+        check(lib().cvf_sample_observables(self._h, r, C.byref(smp), C.byref(o)))
+        return o
+
+    def state(self, r: int = 0):
+        s = abi.State()
+        check(lib().cvf_get_state(self._h, r, C.byref(s)))
+        return s.r_cell, s.volume, s.e_vdw, np.array(list(s.counters), dtype=np.uint32)
+
+    def set_state(self, r_cell: float, volume: float, counters, r: int = 0):
+        s = abi.State(r_cell, volume, 0.0, (C.c_uint * 4)(*[int(c) for c in counters]))
+        check(lib().cvf_set_state(self._h, r, C.byref(s)))
+
+    def thresholds(self, r: int = 0):
+        a = np.zeros(44, dtype=np.uint64)
+        check(lib().cvf_get_thresholds(self._h, r, _ptr(a)))
+        return a[:33], a[33:42], a[42:44]

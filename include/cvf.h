@@ -1,0 +1,189 @@
+/*
+ * cvf.h -- C ABI of the GB300 engine for the Coronas-Vilanova-Franzese (CVF) bulk-water
+ * lattice model (NPT Monte Carlo), a drop-in for the hot path of SOURCE/gpu_water3D.cu of
+ * lcoronas/CVFBulkWater ("GW" below).
+ *
+ * The reference has no library API: its boundary is the executable contract of gpu_water3D
+ * (input_data / input_config / distances in, data.out / cluster.out / config.out / water3D.log
+ * out) and, inside it, the seam MonteCarlo_Step() (GW:52-53, GW:1346-1733). Each entry point
+ * below names the reference code it replaces. Plain C types only; the library allocates and
+ * owns all device memory; callers pass host buffers with explicit sizes.
+ *
+ * Conventions
+ *  - Every function returns 0 on success or a negative CVF_E* code; cvf_last_error_string()
+ *    describes the last failure of the calling thread.
+ *  - A handle holds one or more replicas (independent lattices) on one GPU and one CUDA stream.
+ *    A handle is not thread-safe; different handles may be used concurrently.
+ *  - Cells are numbered cell = x + L*(y + L*z); arms a = 0..5 are x+, x-, y+, y-, z+, z-
+ *    (GW:1936-1962). Arm sites for cluster labels are site = a*N + cell.
+ *  - "cells12" arrays hold 12 ints per cell in config.out order: sigma_0..sigma_5 then
+ *    eta_0..eta_5 (GW:1296-1305).
+ */
+#ifndef CVF_H
+#define CVF_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CVF_OK 0
+#define CVF_EINVAL -1     /* invalid argument (sizes, ranges, unsupported flag) */
+#define CVF_ECUDA -2      /* CUDA runtime error */
+#define CVF_ELIMIT -3     /* a bounded device loop gave up (error word set by a kernel) */
+#define CVF_ENOMEM -4     /* device allocation failed */
+#define CVF_ECONFIG -5    /* malformed configuration (cells12 values out of range) */
+
+typedef struct cvf_handle cvf_handle;
+
+/* Run parameters of one replica. Mirrors the 14 lines of input_data (GW:293-386) that the
+ * hot path consumes, plus the lattice edge that the reference fixes at compile time (GW:35-37). */
+typedef struct cvf_params {
+  int L;                 /* lattice edge: even, >= 4 */
+  float T;               /* temperature, internal units (read as float, GW:304) */
+  float P;               /* pressure, internal units (read as float, GW:298) */
+  long long seed;        /* Philox key (GW:310 reads it as %ld) */
+  float R_cutoff;        /* vdW cut-off radius in lattice units (GW:352) */
+  int start;             /* Flag_config: 0 disordered, 1 caller loads cells12, 2 ordered (GW:730-833) */
+  int flag_chessboard;   /* must be 1: eta moves by 2x2x2 cubes (GW:639-724); 0 is rejected */
+  unsigned int replica;  /* replica id, counter word 3 of every Philox draw */
+  int device;            /* CUDA device ordinal (Device_ID, GW:457-468) */
+  int sample_capacity;   /* samples kept on the device per replica; 0 selects 65536 */
+} cvf_params;
+
+/* One measurement (GW:2014-2160). Integer counts are exact. */
+typedef struct cvf_obs {
+  long long n_hb2;       /* sum over bonds of delta*(eta_i+eta_j) = 2*N_hb */
+  long long n_sigma;     /* sum over cells of sum_{a<b} delta(sigma_a, sigma_b) */
+  double r_cell;         /* lattice spacing */
+  double volume;         /* N r^3 tracked by the volume move */
+  double e_vdw;          /* vdW lattice energy at r_cell */
+  double n_hb;           /* n_hb2 / 2 (data.out column 5) */
+  double energy;         /* e = E_vdW - J_hb N_hb - J_sigma N_sigma (column 2) */
+  double enthalpy;       /* h = e + P v (column 3) */
+  double v_total;        /* v = N r^3 + v_hb N_hb (column 4) */
+  double m;              /* N_sigma / (15 N) (column 6) */
+} cvf_obs;
+
+/* Cluster statistics of the last Swendsen-Wang labelling (GW:2677-2780). */
+typedef struct cvf_cstats {
+  long long largest, second, n_percolating, n_clusters;
+  long long sum_size;          /* always 6N */
+  long long sum_size2;         /* exact sum of s^2 */
+  long long sum_size2_wrap32;  /* sum of s*s wrapped to int32 as in GW:2697 */
+  double mean;                 /* sum_size / n_clusters */
+  double variance;             /* exact sum_size2/n - mean^2 */
+  float mean_ref;              /* cluster.out column 5, the reference's float formula */
+  float variance_ref;          /* cluster.out column 6, incl. the int32 wrap of s*s */
+} cvf_cstats;
+
+/* One recorded sample of the device sample stream. */
+typedef struct cvf_sample {
+  long long n_hb2, n_sigma;
+  double r_cell, volume;
+} cvf_sample;
+
+/* Mutable scalar state (for exact checkpoint/resume; the reference restarts r_cell at
+ * 1.0001 and loses its RNG state, GW:150). counters: sweep, cube, volume, SW moves done. */
+typedef struct cvf_state {
+  double r_cell, volume, e_vdw;
+  unsigned int counters[4];
+} cvf_state;
+
+const char* cvf_last_error_string(void);
+const char* cvf_version(void);
+
+/* Replaces main()'s set-up GW:440-1170 for one lattice. */
+int cvf_create(const cvf_params* params, cvf_handle** out);
+/* n independent replicas (own L, T, P, seed, replica id) stepped together in one set of
+ * launches captured in a CUDA graph. No reference counterpart: the reference runs one lattice
+ * per process. */
+int cvf_batch_create(const cvf_params* params, int n_replicas, cvf_handle** out);
+int cvf_destroy(cvf_handle* h);
+int cvf_num_replicas(const cvf_handle* h);
+
+/* Replaces the input_config reader GW:730-811 and gpu_Chessboard_set_state GW:3314-3371:
+ * cube states are inferred from eta with the reference's decision tree and every eta is
+ * rewritten from them (what the reference's first cube move does). */
+int cvf_set_config(cvf_handle* h, int replica, const int* cells12, long long n_cells);
+/* Replaces the config.out writer GW:1296-1305. */
+int cvf_get_config(cvf_handle* h, int replica, int* cells12, long long n_cells);
+
+/* vdW shell table (GW:865-989). The library computes it at create (Flag_distances=0);
+ * set_distances loads a table read from a distances file (Flag_distances=1). */
+int cvf_set_distances(cvf_handle* h, int replica, const float* dist, const int* freq, int n);
+int cvf_get_distances(const cvf_handle* h, int replica, float* dist, int* freq, int cap, int* n);
+
+/* Replaces n_steps calls of MonteCarlo_Step (GW:1346-1733) for every replica: one cube move,
+ * one volume move, n_metropolis checkerboard sweeps, n_cluster Swendsen-Wang steps per step. */
+int cvf_run_steps(cvf_handle* h, int n_steps, int n_metropolis, int n_cluster);
+/* The production loop GW:1204-1244: after step i (0-based within the call) with
+ * i % interval == 0, a sample (and, when n_cluster > 0, a cluster-statistics record) is
+ * appended on the device. No host synchronisation inside. */
+int cvf_run_sampled(cvf_handle* h, int n_steps, int n_metropolis, int n_cluster, int interval);
+int cvf_synchronize(cvf_handle* h);
+
+/* Replaces measure() GW:2014-2160 for the current configuration. */
+int cvf_observables(cvf_handle* h, int replica, cvf_obs* out);
+/* Replaces print_cluster_statistics() GW:2677-2721 for the current labels. Before any SW step
+ * the labels are all zero (one cluster of 6N sites), as in the reference's cluster.out. */
+int cvf_cluster_stats(cvf_handle* h, int replica, cvf_cstats* out);
+/* 6N canonical labels (minimum site id of the cluster), site = arm*N + cell (GW:2365-2529). */
+int cvf_get_labels(cvf_handle* h, int replica, int* labels, long long n_sites);
+
+/* Device sample stream: number of samples recorded since the last clear, and a copy. */
+int cvf_sample_count(cvf_handle* h, int replica, long long* count);
+int cvf_get_samples(cvf_handle* h, int replica, cvf_sample* out, long long max, long long* n_out);
+int cvf_get_cstats_stream(cvf_handle* h, int replica, cvf_cstats* out, long long max, long long* n_out);
+int cvf_clear_samples(cvf_handle* h);
+/* Observables of one sample (host FP64 formulas of GW:2138-2159). */
+int cvf_sample_observables(const cvf_handle* h, int replica, const cvf_sample* s, cvf_obs* out);
+
+int cvf_get_state(cvf_handle* h, int replica, cvf_state* out);
+int cvf_set_state(cvf_handle* h, int replica, const cvf_state* in);
+
+/* Acceptance thresholds of a replica (U < T with U a uniform 32-bit integer):
+ * out[0..32] sweep, index (dN_hb+1)*11 + dN_sigma+5; out[33..41] cube, index dN_hb+4;
+ * out[42] SW hydrogen-bond link; out[43] SW intra-cell link. */
+int cvf_get_thresholds(const cvf_handle* h, int replica, unsigned long long* out44);
+
+/* The CUDA stream (a cudaStream_t passed as void*) on which all work of the handle is ordered,
+ * for callers that time or order their own work around the engine. No reference counterpart. */
+int cvf_get_stream(cvf_handle* h, void** stream);
+/* Profiling hook: enqueue n launches of one kernel kind outside any graph on the handle's stream:
+ * kind 0 = one checkerboard sweep (two launches, colour 0 then 1; sweep i of the call draws the
+ * random stream of sweep (last step's first sweep + i), so repeated calls reuse streams),
+ * 1 = cube move, 2 = volume move, 3 = measurement. For timing only. No reference counterpart. */
+int cvf_profile_launch(cvf_handle* h, int kind, int n);
+
+/* Histogram reweighting (replaces the Fortran Calcula_Histograma F90:1003-1124 and the finite
+ * differences of CVF_ThermodynamicAnalysis/{AlphaP,CP,KT}derivate.c).
+ *   samples: n rows of (E, V, N_hb, N_sigma) in internal units, grouped by run;
+ *   run_of:  run index of each row; runs: n_runs rows of (beta, P) of the simulations;
+ *   f:       in/out dimensionless free energies -log Z_j (n_runs), refined by n_iter WHAM
+ *            iterations on the device when n_iter > 0;
+ *   theta:   target (beta, P, dJ_hb, dJ_sigma, dv_hb): weights exp(-beta (E' + P V')) with
+ *            E' = E - dJ_hb N_hb - dJ_sigma N_sigma and V' = V + dv_hb N_hb;
+ *   out:     n_obs reweighted means of the columns (E, V, N_hb, N_sigma, H = E + P V, rho = N/V,
+ *            E^2, V^2, H^2, V*H, ...) selected by obs_ids (see cvf_reweight_obs ids below),
+ *            and log Z(theta) in out[n_obs].
+ * cvf_reweight_adjoint returns grad_theta[5] = sum_m g[m] d out[m] / d theta. */
+#define CVF_RW_E 0
+#define CVF_RW_V 1
+#define CVF_RW_NHB 2
+#define CVF_RW_NSIG 3
+#define CVF_RW_H 4
+#define CVF_RW_RHO 5
+#define CVF_RW_H2 6
+#define CVF_RW_V2 7
+#define CVF_RW_VH 8
+int cvf_reweight_forward(int device, const double* samples, const int* run_of, long long n, const double* runs,
+                         int n_runs, double* f, int n_iter, double tol, double n_cells, const double* theta,
+                         const int* obs_ids, int n_obs, double* out);
+int cvf_reweight_adjoint(int device, const double* samples, const int* run_of, long long n, const double* runs,
+                         int n_runs, const double* f, double n_cells, const double* theta, const int* obs_ids,
+                         int n_obs, const double* g, double* grad_theta);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
