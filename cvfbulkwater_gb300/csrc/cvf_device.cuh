@@ -31,6 +31,7 @@ struct ReplicaDesc {
   const int* freq;
   int n_shells;
   int L, H;
+  int lgL, lgH;       // log2 of L and H when they are powers of two, else -1
   int start;          // Flag_config of the replica (0 disordered, 1 from file, 2 ordered)
   uint32_t key0, key1, replica;
   float T, P, Rc;
@@ -88,8 +89,10 @@ constexpr int kThreads = 256;
 
 void launch_init_lattice(const BatchDev& b, cudaStream_t s);
 void init_device_tables();
-void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, cudaStream_t s);
-void launch_cube_move(const BatchDev& b, cudaStream_t s);
+void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do_volume, cudaStream_t s);
+// Cube moves of all replicas (do_cubes) and, in extra blocks of the same launch, their volume
+// moves (do_volume): the two moves are independent, so the volume move hides under the cubes.
+void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s);
 void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s);
 void launch_measure(const BatchDev& b, int record, cudaStream_t s);
 void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s);

@@ -2,6 +2,7 @@
 // descriptors, captures Monte Carlo steps into CUDA graphs and replays them.
 // There is no CPU fallback: every Monte Carlo move runs in the kernels of cvf_mc.cu / cvf_sw.cu.
 #include <cuda_runtime.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -73,6 +74,10 @@ static int upload_descs(cvf_handle* h) {
 static int build_tables(cvf_handle* h) {
   const int n = (int)h->reps.size();
   int vec = 4;
+  if (const char* ev = getenv("CVF_SWEEP_VEC")) {
+    int v = atoi(ev);
+    if (v == 1 || v == 2 || v == 4) vec = v;
+  }
   for (auto& r : h->reps) {
     while (vec > 1 && r.H % vec) vec >>= 1;
   }
@@ -129,8 +134,8 @@ static int ensure_sw(cvf_handle* h) {
 }
 
 static void enqueue_step(cvf_handle* h, int nmet, int ncl) {
-  launch_step_begin(h->b, nmet, ncl, 1, h->stream);
-  launch_cube_move(h->b, h->stream);
+  launch_step_begin(h->b, nmet, ncl, 1, 1, h->stream);
+  launch_cube_volume(h->b, 1, 1, h->stream);
   for (int j = 0; j < nmet; ++j) {
     launch_sweep(h->b, 0, j, h->stream);
     launch_sweep(h->b, 1, j, h->stream);
@@ -259,6 +264,9 @@ int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
     d.n_shells = (int)r.dist.size();
     d.L = r.L;
     d.H = r.H;
+    auto lg = [](int v) { return (v & (v - 1)) ? -1 : __builtin_ctz((unsigned)v); };
+    d.lgL = lg(r.L);
+    d.lgH = lg(r.H);
     d.start = r.p.start;
     d.key0 = (uint32_t)((unsigned long long)r.p.seed & 0xffffffffu);
     d.key1 = (uint32_t)((unsigned long long)r.p.seed >> 32);
@@ -590,10 +598,13 @@ int cvf_profile_launch(cvf_handle* h, int kind, int n) {
         launch_sweep(h->b, 1, i, h->stream);
         break;
       case 1:
-        launch_step_begin(h->b, 0, 0, 1, h->stream);
-        launch_cube_move(h->b, h->stream);
+        launch_step_begin(h->b, 0, 0, 1, 0, h->stream);
+        launch_cube_volume(h->b, 1, 0, h->stream);
         break;
-      case 2: launch_step_begin(h->b, 0, 0, 0, h->stream); break;
+      case 2:
+        launch_step_begin(h->b, 0, 0, 0, 1, h->stream);
+        launch_cube_volume(h->b, 0, 1, h->stream);
+        break;
       default: launch_measure(h->b, 0, h->stream); break;
     }
   }

@@ -1,6 +1,12 @@
 // Monte Carlo kernels of the GB300 CVF engine: lattice initialisation, the NPT volume move,
 // the eta cube ("chessboard") move, the checkerboard sigma sweep and the exact int64
 // observable reductions. Reference: SOURCE/gpu_water3D.cu ("GW") of lcoronas/CVFBulkWater.
+//
+// The sweep is integer-issue bound (one Philox4x32-10 block and six table-driven Metropolis
+// decisions per cell), so its hot path is branch-free: every arm is decided with 16-bit
+// uniforms against a shared-memory threshold table, and the two rare events -- a proposal word
+// rejected by the exact uniform draw (p = 6e-7) and a 16-bit tie that needs the low half of the
+// uniform (p ~ 2^-16 per arm) -- leave the hot path for out-of-line exact code.
 #include "cvf_device.cuh"
 #include "cvf_spec.cuh"
 
@@ -8,8 +14,6 @@ namespace cvf {
 
 __constant__ uint32_t c_state_active[9];
 __constant__ uint8_t c_eta_table[72];  // [state*8 + vertex offset] -> 6-bit eta mask
-__constant__ int c_edge_dir[12];
-__constant__ int c_edge_start[12];
 
 void init_sw_device_tables();
 static unsigned long long g_tables_ready = 0;  // bit d: tables copied to device d
@@ -21,19 +25,12 @@ void init_device_tables() {
   if (dev < 64 && ((g_tables_ready >> dev) & 1ull)) return;
   uint32_t act[9];
   uint8_t eta[72];
-  int dir[12], st[12];
   for (int s = 0; s < 9; ++s) {
     act[s] = state_active(s);
     for (int p = 0; p < 8; ++p) eta[s * 8 + p] = (uint8_t)cube_eta_bits(s, p);
   }
-  for (int e = 0; e < 12; ++e) {
-    dir[e] = edge_dir(e);
-    st[e] = edge_start(e);
-  }
   cudaMemcpyToSymbol(c_state_active, act, sizeof(act));
   cudaMemcpyToSymbol(c_eta_table, eta, sizeof(eta));
-  cudaMemcpyToSymbol(c_edge_dir, dir, sizeof(dir));
-  cudaMemcpyToSymbol(c_edge_start, st, sizeof(st));
   init_sw_device_tables();
   if (dev < 64) g_tables_ready |= 1ull << dev;
 }
@@ -49,6 +46,17 @@ __device__ __forceinline__ int find_replica(const int* __restrict__ blk, int nre
   return lo;
 }
 
+// n / d and n % d; shift >= 0 means d = 2^shift.
+__device__ __forceinline__ void divmod32(uint32_t n, uint32_t d, int shift, uint32_t& q, uint32_t& r) {
+  if (shift >= 0) {
+    q = n >> shift;
+    r = n & (d - 1u);
+  } else {
+    q = n / d;
+    r = n - q * d;
+  }
+}
+
 __device__ __forceinline__ uint32_t cell_word_index(int x, int y, int z, int L, int H) {
   return (uint32_t)(x >> 1) + (uint32_t)H * ((uint32_t)y + (uint32_t)L * (uint32_t)z);
 }
@@ -60,10 +68,12 @@ __global__ void k_init_sigma(const ReplicaDesc* __restrict__ reps, const int* __
   const ReplicaDesc& R = reps[r];
   const int start = R.start;
   const int L = R.L, H = R.H;
-  long long c = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
-  long long N = (long long)L * L * L;
+  uint32_t c = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  uint32_t N = (uint32_t)L * L * L;
   if (c >= N) return;
-  int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
+  uint32_t x, yz, y, z;
+  divmod32(c, L, R.lgL, yz, x);
+  divmod32(yz, L, R.lgL, z, y);
   uint32_t w = 0;
   if (start == 2) {
     U4 q = philox(0, 0, kStInitOrder, R.replica, R.key0, R.key1);
@@ -72,11 +82,11 @@ __global__ void k_init_sigma(const ReplicaDesc* __restrict__ reps, const int* __
       v = lemire_retry(6, 0, 0, kStInitOrder, R.replica, R.key0, R.key1);
     for (int a = 0; a < 6; ++a) w |= v << (3 * a);
   } else if (start == 0) {
-    U4 q = philox((uint32_t)c, 0, kStInitSigma, R.replica, R.key0, R.key1);
+    U4 q = philox(c, 0, kStInitSigma, R.replica, R.key0, R.key1);
     uint32_t d;
     if (!lemire_try(q.x, 46656u, d) && !lemire_try(q.y, 46656u, d) && !lemire_try(q.z, 46656u, d) &&
         !lemire_try(q.w, 46656u, d))
-      d = lemire_retry(46656u, (uint32_t)c, 0, kStInitSigma, R.replica, R.key0, R.key1);
+      d = lemire_retry(46656u, c, 0, kStInitSigma, R.replica, R.key0, R.key1);
     for (int a = 0; a < 6; ++a) {
       w |= (d % 6u) << (3 * a);
       d /= 6u;
@@ -90,14 +100,15 @@ __global__ void k_init_cubes(const ReplicaDesc* __restrict__ reps, const int* __
   int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   const int L = R.L, H = R.H;
-  long long q = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
-  long long H3 = (long long)H * H * H;
+  uint32_t q = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  uint32_t H3 = (uint32_t)H * H * H;
   if (q >= 2 * H3) return;
-  int par = q >= H3;
-  long long qi = q - par * H3;
-  int a = (int)(qi % H), b = (int)((qi / H) % H), c = (int)(qi / ((long long)H * H));
-  int x0 = 2 * a + par, y0 = 2 * b + par, z0 = 2 * c + par;
-  uint32_t cid = (uint32_t)x0 + (uint32_t)L * ((uint32_t)y0 + (uint32_t)L * (uint32_t)z0);
+  uint32_t par = q >= H3;
+  uint32_t qi = q - par * H3, a, bc, b, c;
+  divmod32(qi, H, R.lgH, bc, a);
+  divmod32(bc, H, R.lgH, c, b);
+  uint32_t x0 = 2 * a + par, y0 = 2 * b + par, z0 = 2 * c + par;
+  uint32_t cid = x0 + (uint32_t)L * (y0 + (uint32_t)L * z0);
   U4 w = philox(cid, 0, kStInitCube, R.replica, R.key0, R.key1);
   uint32_t st;
   if (!lemire_try(w.x, 9, st) && !lemire_try(w.y, 9, st) && !lemire_try(w.z, 9, st) && !lemire_try(w.w, 9, st))
@@ -105,37 +116,75 @@ __global__ void k_init_cubes(const ReplicaDesc* __restrict__ reps, const int* __
   R.cubes[par][qi] = (uint8_t)st;
 }
 
-// ------------------------------------------------------------------ step begin: volume move
-// One thread per replica. Snapshots the move counters used by this step's kernels and performs
-// the NPT volume move of GW:1740-1781 in FP64 with every operation rounded separately.
-__global__ void k_step_begin(const ReplicaDesc* __restrict__ reps, ReplicaState* __restrict__ st, int nrep,
-                             int nmet, int ncl, int do_cube) {
+// ------------------------------------------------------------------ step begin: move counters
+// One thread per replica: snapshot the move counters that this step's kernels use.
+__global__ void k_step_begin(ReplicaState* __restrict__ st, int nrep, int nmet, int ncl, int do_cube,
+                             int do_volume) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrep) return;
-  const ReplicaDesc& R = reps[r];
   ReplicaState& S = st[r];
   S.cur[0] = S.ctr[0];
   S.ctr[0] += (uint32_t)nmet;
   S.cur[1] = S.ctr[1];
   S.ctr[1] += (uint32_t)do_cube;
+  S.cur[2] = S.ctr[2];
+  S.ctr[2] += (uint32_t)do_volume;
   S.cur[3] = S.ctr[3];
   S.ctr[3] += (uint32_t)ncl;
-  uint32_t t = S.ctr[2]++;
-  S.cur[2] = t;
+}
 
+// ------------------------------------------------------------------ volume move (one warp)
+// NPT volume move of GW:1740-1781 in FP64, every operation rounded separately. The shell terms
+// of E_vdW(r') are computed by the 32 lanes and summed by lane 0 in shell order, which is the
+// reference's sequential sum.
+__device__ void volume_move_warp(const ReplicaDesc& R, ReplicaState& S) {
+  __shared__ double s_term[kMaxShells];
+  __shared__ double s_trial;
+  const int lane = threadIdx.x;
+  const uint32_t t = S.cur[2];
   U4 q = philox(0, t, kStVolume, R.replica, R.key0, R.key1);
-  double r0 = S.r_cell;
-  double u1 = u53(q.x, q.y);
-  double trial = CVF_DADD(r0, CVF_DMUL(0.01 * 2, CVF_DSUB(u1, 0.5)));
-  for (uint32_t k = 1; trial < 0.0 && k < 64; ++k) {
-    U4 qq = philox(k, t, kStVolume, R.replica, R.key0, R.key1);
-    u1 = u53(qq.x, qq.y);
-    trial = CVF_DADD(r0, CVF_DMUL(0.01 * 2, CVF_DSUB(u1, 0.5)));
+  const double r0 = S.r_cell;
+  if (lane == 0) {
+    double u1 = u53(q.x, q.y);
+    double trial = CVF_DADD(r0, CVF_DMUL(0.01 * 2, CVF_DSUB(u1, 0.5)));
+    for (uint32_t k = 1; trial < 0.0 && k < 64; ++k) {
+      U4 qq = philox(k, t, kStVolume, R.replica, R.key0, R.key1);
+      u1 = u53(qq.x, qq.y);
+      trial = CVF_DADD(r0, CVF_DMUL(0.01 * 2, CVF_DSUB(u1, 0.5)));
+    }
+    s_trial = trial;
+  }
+  __syncwarp();
+  const double trial = s_trial;
+  double tmp = 1.0 / (double)R.Rc;
+  tmp = CVF_DMUL(CVF_DMUL(tmp, tmp), tmp);
+  double att = CVF_DMUL(tmp, tmp);
+  double rep = CVF_DMUL(att, att);
+  const double shift = CVF_DSUB(rep, att);
+  for (int i = lane; i < R.n_shells; i += 32) {
+    double rd = CVF_DMUL(trial, (double)R.dist[i]);
+    double term;
+    if (rd < (double)R.Rc) {
+      double u = 1.0 / rd;
+      u = CVF_DMUL(CVF_DMUL(u, u), u);
+      double a6 = CVF_DMUL(u, u);
+      double a12 = CVF_DMUL(a6, a6);
+      term = CVF_DMUL((double)R.freq[i], CVF_DSUB(CVF_DSUB(a12, a6), shift));
+    } else {
+      term = __longlong_as_double(0x7FF8000000000001ll);  // NaN marks a shell beyond the cut-off
+    }
+    s_term[i] = term;
+  }
+  __syncwarp();
+  if (lane != 0) return;
+  double tE = 0.0;
+  for (int i = 0; i < R.n_shells; ++i) {
+    double term = s_term[i];
+    if (term == term) tE = CVF_DADD(tE, term);
   }
   const double Ld = (double)R.L;
   double tV = CVF_DMUL(CVF_DMUL(CVF_DMUL(CVF_DMUL(CVF_DMUL(trial, trial), trial), Ld), Ld), Ld);
   double dV = CVF_DSUB(tV, S.volume);
-  double tE = evdw(trial, R.dist, R.freq, R.n_shells, R.Rc);
   float Nf = (float)((long long)R.L * R.L * R.L);
   double NT = (double)__fmul_rn(Nf, R.T);
   double dE = CVF_DSUB(CVF_DSUB(tE, S.e_vdw), CVF_DMUL(NT, own_log(tV / S.volume)));
@@ -148,23 +197,31 @@ __global__ void k_step_begin(const ReplicaDesc* __restrict__ reps, ReplicaState*
   }
 }
 
-// ------------------------------------------------------------------ cube move
-// GW:3374-3466. One thread per cube (both parities in one launch: cubes share no edge and
-// sigma is frozen, so all cube decisions are independent). Writes only the cube's state byte.
-__global__ void __launch_bounds__(kThreads) k_cube_move(const ReplicaDesc* __restrict__ reps,
-                                                        const ReplicaState* __restrict__ st,
-                                                        const int* __restrict__ blk, int nrep) {
-  int r = find_replica(blk, nrep, blockIdx.x);
+// ------------------------------------------------------------------ cube move (+ volume blocks)
+// GW:3374-3466. One thread per cube (both parities in one launch: cubes share no edge and sigma
+// is frozen, so all cube decisions are independent). Writes only the cube's state byte.
+// Blocks at and after `nblk_cube` perform the volume move of replica (block - nblk_cube).
+__global__ void __launch_bounds__(kThreads) k_cube_volume(const ReplicaDesc* __restrict__ reps,
+                                                          ReplicaState* __restrict__ st,
+                                                          const int* __restrict__ blk, int nrep, int nblk_cube) {
+  if ((int)blockIdx.x >= nblk_cube) {
+    const int r = blockIdx.x - nblk_cube;
+    if (threadIdx.x < 32 && r < nrep) volume_move_warp(reps[r], st[r]);
+    return;
+  }
+  const int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   const int L = R.L, H = R.H;
-  long long q = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
-  long long H3 = (long long)H * H * H;
+  const uint32_t q = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  const uint32_t H3 = (uint32_t)H * H * H;
   if (q >= 2 * H3) return;
-  int par = q >= H3;
-  long long qi = q - par * H3;
-  int a = (int)(qi % H), b = (int)((qi / H) % H), c = (int)(qi / ((long long)H * H));
-  int x0 = 2 * a + par, y0 = 2 * b + par, z0 = 2 * c + par;
-  int x1 = x0 + 1 == L ? 0 : x0 + 1, y1 = y0 + 1 == L ? 0 : y0 + 1, z1 = z0 + 1 == L ? 0 : z0 + 1;
+  const uint32_t par = q >= H3;
+  const uint32_t qi = q - par * H3;
+  uint32_t a, bc, b, c;
+  divmod32(qi, H, R.lgH, bc, a);
+  divmod32(bc, H, R.lgH, c, b);
+  const int x0 = 2 * a + par, y0 = 2 * b + par, z0 = 2 * c + par;
+  const int x1 = x0 + 1 == L ? 0 : x0 + 1, y1 = y0 + 1 == L ? 0 : y0 + 1, z1 = z0 + 1 == L ? 0 : z0 + 1;
   uint32_t w[8];
 #pragma unroll
   for (int p = 0; p < 8; ++p) {
@@ -178,15 +235,15 @@ __global__ void __launch_bounds__(kThreads) k_cube_move(const ReplicaDesc* __res
     uint32_t s0 = (w[p0] >> (6 * d)) & 7u, s1 = (w[p1] >> (6 * d + 3)) & 7u;
     D |= (uint32_t)(s0 == s1) << e;
   }
-  uint32_t cid = (uint32_t)x0 + (uint32_t)L * ((uint32_t)y0 + (uint32_t)L * (uint32_t)z0);
-  uint32_t t = st[r].cur[1];
+  const uint32_t cid = (uint32_t)x0 + (uint32_t)L * ((uint32_t)y0 + (uint32_t)L * (uint32_t)z0);
+  const uint32_t t = st[r].cur[1];
   U4 rr = philox(cid, t, kStCube, R.replica, R.key0, R.key1);
   uint32_t nw;
   if (!lemire_try(rr.x, 9, nw) && !lemire_try(rr.z, 9, nw) && !lemire_try(rr.w, 9, nw))
     nw = lemire_retry(9, cid, t, kStCube, R.replica, R.key0, R.key1);
   uint8_t* cs = R.cubes[par] + qi;
-  uint32_t old = *cs;
-  int dhb = __popc(c_state_active[nw] & D) - __popc(c_state_active[old] & D);
+  const uint32_t old = *cs;
+  const int dhb = __popc(c_state_active[nw] & D) - __popc(c_state_active[old] & D);
   if ((unsigned long long)rr.y < R.thr_cube[dhb + 4] && nw != old) *cs = (uint8_t)nw;
 }
 
@@ -222,6 +279,34 @@ struct VecLoad<4> {
     *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
   }
 };
+template <int V>
+struct Log2V;
+template <>
+struct Log2V<1> {
+  static constexpr int v = 0;
+};
+template <>
+struct Log2V<2> {
+  static constexpr int v = 1;
+};
+template <>
+struct Log2V<4> {
+  static constexpr int v = 2;
+};
+
+// Thread -> (row segment, y, z) of a replica's colour array: q = hc + (H/V) * (y + L*z).
+template <int V>
+__device__ __forceinline__ bool segment_of(const ReplicaDesc& R, uint32_t q, int& hc, int& y, int& z) {
+  const uint32_t L = R.L, cpr = R.H / V;
+  if (q >= cpr * L * L) return false;
+  uint32_t row, hh, zz, yy;
+  divmod32(q, cpr, R.lgH >= 0 ? R.lgH - Log2V<V>::v : -1, row, hh);
+  divmod32(row, L, R.lgL, zz, yy);
+  hc = (int)hh;
+  y = (int)yy;
+  z = (int)zz;
+  return true;
+}
 
 // Loads the V own words of a thread's row segment, the other colour's words around them and
 // the eta masks of the V cells. Shared by the sweep and the measurement.
@@ -243,19 +328,17 @@ struct CellBlock {
     const uint32_t* oth = R.cells[colour ^ 1];
     const int yp1 = y + 1 == L ? 0 : y + 1, ym1 = y == 0 ? L - 1 : y - 1;
     const int zp1 = z + 1 == L ? 0 : z + 1, zm1 = z == 0 ? L - 1 : z - 1;
-    const size_t row = (size_t)H * ((size_t)y + (size_t)L * z);
+    const uint32_t row = (uint32_t)H * ((uint32_t)y + (uint32_t)L * z);
     own_ptr = R.cells[colour] + row + h0;
     VecLoad<V>::ld(own_ptr, own);
     uint32_t mid[V];
     VecLoad<V>::ld(oth + row + h0, mid);
-    VecLoad<V>::ld(oth + (size_t)H * ((size_t)yp1 + (size_t)L * z) + h0, yp);
-    VecLoad<V>::ld(oth + (size_t)H * ((size_t)ym1 + (size_t)L * z) + h0, ym);
-    VecLoad<V>::ld(oth + (size_t)H * ((size_t)y + (size_t)L * zp1) + h0, zp);
-    VecLoad<V>::ld(oth + (size_t)H * ((size_t)y + (size_t)L * zm1) + h0, zm);
+    VecLoad<V>::ld(oth + (uint32_t)H * ((uint32_t)yp1 + (uint32_t)L * z) + h0, yp);
+    VecLoad<V>::ld(oth + (uint32_t)H * ((uint32_t)ym1 + (uint32_t)L * z) + h0, ym);
+    VecLoad<V>::ld(oth + (uint32_t)H * ((uint32_t)y + (uint32_t)L * zp1) + h0, zp);
+    VecLoad<V>::ld(oth + (uint32_t)H * ((uint32_t)y + (uint32_t)L * zm1) + h0, zm);
     // x neighbours: s == 0 -> x+ at h, x- at h-1; s == 1 -> x+ at h+1, x- at h
-    uint32_t extra;
-    if (s == 0) extra = oth[row + (h0 == 0 ? H - 1 : h0 - 1)];
-    else extra = oth[row + (h0 + V == H ? 0 : h0 + V)];
+    const uint32_t extra = oth[row + (s == 0 ? (h0 == 0 ? H - 1 : h0 - 1) : (h0 + V == H ? 0 : h0 + V))];
 #pragma unroll
     for (int k = 0; k < V; ++k) {
       if (s == 0) {
@@ -268,8 +351,8 @@ struct CellBlock {
     }
     // eta from the even cube (x>>1, y>>1, z>>1) and the odd cube containing the cell
     const int yo = (y & 1) ? y : ym1, zo = (z & 1) ? z : zm1;
-    const size_t erow = (size_t)H * ((size_t)(y >> 1) + (size_t)H * (z >> 1));
-    const size_t orow = (size_t)H * ((size_t)(yo >> 1) + (size_t)H * (zo >> 1));
+    const uint32_t erow = (uint32_t)H * ((uint32_t)(y >> 1) + (uint32_t)H * (z >> 1));
+    const uint32_t orow = (uint32_t)H * ((uint32_t)(yo >> 1) + (uint32_t)H * (zo >> 1));
     const int p = s | ((y & 1) << 1) | ((z & 1) << 2);
 #pragma unroll
     for (int k = 0; k < V; ++k) {
@@ -296,57 +379,89 @@ __device__ __forceinline__ uint32_t sigma_histogram(uint32_t w) {
   return h;
 }
 
-// Metropolis update of the six arms of one cell (GW:1964-2007 energy change, chessboard branch),
-// arms in order 0..5, all decisions integer.
-__device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32_t eta, uint32_t c0,
-                                                uint32_t t, const ReplicaDesc& R, const uint32_t* s_thi,
-                                                const uint16_t* s_tlo) {
-  U4 rr = philox(c0, t, kStSweep, R.replica, R.key0, R.key1);
-  uint32_t d;
-  if (!lemire_try(rr.x, 46656u, d)) d = lemire_retry(46656u, c0, t, kStSweep, R.replica, R.key0, R.key1);
+// Proposal word after the exact uniform draw rejected word 0 of the sweep block (p = 6e-7).
+__device__ __noinline__ uint32_t sweep_proposal_retry(uint32_t c0, uint32_t t, uint32_t rep, uint32_t k0,
+                                                      uint32_t k1) {
+  uint32_t w = 0;
+  for (uint32_t k = 0; k < 256; ++k) {
+    w = philox(c0, t, retry_tag(kStSweep, k), rep, k0, k1).x;
+    if (w * 46656u >= 2560u) return w;
+  }
+  return w;
+}
+
+// Exact update of one cell with the full 32-bit uniforms (high halves from the sweep block,
+// low halves from the refinement block). Taken only when a 16-bit comparison tied.
+__device__ __noinline__ uint32_t sweep_cell_exact(uint32_t w, uint32_t nbs, uint32_t eta, uint32_t u,
+                                                  uint32_t a1, uint32_t a2, uint32_t a3, uint32_t c0, uint32_t t,
+                                                  const ReplicaDesc* R) {
+  const U4 rf = philox(c0, t, kStSweepRefine, R->replica, R->key0, R->key1);
   uint32_t h = sigma_histogram(w);
-  bool have_rf = false;
-  U4 rf = {0, 0, 0, 0};
-#pragma unroll
+  uint32_t f = u;
   for (int a = 0; a < 6; ++a) {
-    uint32_t n = d % 6u;
-    d /= 6u;
-    uint32_t o = (w >> (3 * a)) & 7u;
-    if (n != o) {
-      uint32_t nb = (nbs >> (3 * a)) & 7u;
-      int dhb = ((eta >> a) & 1u) ? ((int)(n == nb) - (int)(o == nb)) : 0;
-      int dns = (int)((h >> (4 * n)) & 15u) - (int)((h >> (4 * o)) & 15u) + 1;
-      int idx = (dhb + 1) * 11 + dns + 5;
-      uint32_t thi = s_thi[idx];
-      uint32_t word = a < 2 ? rr.y : (a < 4 ? rr.z : rr.w);
-      uint32_t hu = (word >> (16 * (a & 1))) & 0xffffu;
-      bool acc = hu < thi;
-      if (hu == thi) {
-        uint32_t tlo = s_tlo[idx];
-        if (tlo) {
-          if (!have_rf) {
-            rf = philox(c0, t, kStSweepRefine, R.replica, R.key0, R.key1);
-            have_rf = true;
-          }
-          uint32_t rw = a < 2 ? rf.x : (a < 4 ? rf.y : rf.z);
-          acc = ((rw >> (16 * (a & 1))) & 0xffffu) < tlo;
-        }
-      }
-      if (acc) {
-        w = (w & ~(7u << (3 * a))) | (n << (3 * a));
-        h += (1u << (4 * n)) - (1u << (4 * o));
-      }
+    unsigned long long m = (unsigned long long)f * 6ull;
+    const uint32_t n = (uint32_t)(m >> 32);
+    f = (uint32_t)m;
+    const uint32_t o = (w >> (3 * a)) & 7u;
+    if (n == o) continue;
+    const uint32_t nb = (nbs >> (3 * a)) & 7u;
+    const int dhb = ((eta >> a) & 1u) ? ((int)(n == nb) - (int)(o == nb)) : 0;
+    const int dns = (int)((h >> (4 * n)) & 15u) - (int)((h >> (4 * o)) & 15u) + 1;
+    const unsigned long long T = R->thr_sweep[(dhb + 1) * 11 + dns + 5];
+    const uint32_t hw = a < 2 ? a1 : (a < 4 ? a2 : a3);
+    const uint32_t lw = a < 2 ? rf.x : (a < 4 ? rf.y : rf.z);
+    const uint32_t sh = 16 * (a & 1);
+    const unsigned long long U = ((unsigned long long)((hw >> sh) & 0xffffu) << 16) | ((lw >> sh) & 0xffffu);
+    if (U < T) {
+      w = (w & ~(7u << (3 * a))) | (n << (3 * a));
+      h += (1u << (4 * n)) - (1u << (4 * o));
     }
   }
   return w;
 }
 
-__device__ __forceinline__ void load_sweep_tables(const ReplicaDesc& R, uint32_t* s_thi, uint16_t* s_tlo,
-                                                  uint8_t* s_eta) {
+// Metropolis update of the six arms of one cell, arms in order 0..5 (GW:1964-2007 energy change,
+// chessboard branch). Proposal of arm a: the a-th most significant base-6 digit of the uniform
+// word u (the high word of u*6 in a multiply chain). s_tv[i] = 2*(T_i >> 16) + ((T_i & 0xffff) != 0)
+// with i = 11*dN_hb + (h_new - h_old) + 17, so "accept" is 2*hu + 2 <= tv and a tie on the high
+// 16 bits is 2*hu + 1 == tv.
+__device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32_t eta, const U4& rr, uint32_t c0,
+                                                uint32_t t, const ReplicaDesc& R, const uint32_t* s_tv) {
+  uint32_t u = rr.x;
+  if (u * 46656u < 2560u) u = sweep_proposal_retry(c0, t, R.replica, R.key0, R.key1);
+  const uint32_t w0 = w;
+  uint32_t h = sigma_histogram(w);
+  uint32_t f = u;
+  bool tie = false;
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    const unsigned long long m = (unsigned long long)f * 6ull;
+    const uint32_t n = (uint32_t)(m >> 32);
+    f = (uint32_t)m;
+    const uint32_t o = (w >> (3 * a)) & 7u;
+    const uint32_t nb = (nbs >> (3 * a)) & 7u;
+    const int e = (int)((eta >> a) & 1u);
+    const int dhb = e * ((int)(n == nb) - (int)(o == nb));
+    const int idx = 11 * dhb + (int)((h >> (4 * n)) & 15u) - (int)((h >> (4 * o)) & 15u) + 17;
+    const uint32_t tv = s_tv[idx];
+    const uint32_t word = a < 2 ? rr.y : (a < 4 ? rr.z : rr.w);
+    const uint32_t u2 = (a & 1) ? ((word >> 15) & 0x1fffeu) : ((word << 1) & 0x1fffeu);
+    const bool diff = n != o;
+    tie |= diff && (u2 + 1u == tv);
+    if (diff && u2 + 2u <= tv) {
+      w = (w & ~(7u << (3 * a))) | (n << (3 * a));
+      h += (1u << (4 * n)) - (1u << (4 * o));
+    }
+  }
+  if (tie) w = sweep_cell_exact(w0, nbs, eta, u, rr.y, rr.z, rr.w, c0, t, &R);
+  return w;
+}
+
+__device__ __forceinline__ void load_sweep_tables(const ReplicaDesc& R, uint32_t* s_tv, uint8_t* s_eta) {
+  // s_tv index 11*dhb + dns' + 17 equals (dhb+1)*11 + dns + 5 of the public table
   for (int i = threadIdx.x; i < 33; i += blockDim.x) {
     unsigned long long T = R.thr_sweep[i];
-    s_thi[i] = (uint32_t)(T >> 16);
-    s_tlo[i] = (uint16_t)(T & 0xffffu);
+    s_tv[i] = 2u * (uint32_t)(T >> 16) + ((T & 0xffffull) != 0);
   }
   for (int i = threadIdx.x; i < 72; i += blockDim.x) s_eta[i] = c_eta_table[i];
 }
@@ -358,32 +473,39 @@ template <int V>
 __global__ void __launch_bounds__(kThreads) k_sweep(const ReplicaDesc* __restrict__ reps,
                                                     const ReplicaState* __restrict__ st,
                                                     const int* __restrict__ blk, int nrep, int colour, int jsweep) {
-  __shared__ uint32_t s_thi[33];
-  __shared__ uint16_t s_tlo[33];
+  __shared__ uint32_t s_tv[33];
   __shared__ uint8_t s_eta[72];
   const int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
-  load_sweep_tables(R, s_thi, s_tlo, s_eta);
+  load_sweep_tables(R, s_tv, s_eta);
   __syncthreads();
-  const int L = R.L, H = R.H;
-  const int cpr = H / V;
-  long long q = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
-  if (q >= (long long)cpr * L * L) return;
-  int hc = (int)(q % cpr);
-  long long row = q / cpr;
-  int y = (int)(row % L), z = (int)(row / L);
-  CellBlock<V> cb;
-  cb.load(R, colour, hc, y, z, s_eta);
+  int hc, y, z;
+  if (!segment_of<V>(R, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, hc, y, z)) return;
+  uint32_t out[V], nbs[V], eta[V];
+  uint32_t* own_ptr;
+  int x0;
+  {
+    CellBlock<V> cb;
+    cb.load(R, colour, hc, y, z, s_eta);
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      nbs[k] = neighbour_sigmas(cb.xp[k], cb.xm[k], cb.yp[k], cb.ym[k], cb.zp[k], cb.zm[k]);
+      eta[k] = cb.eta[k];
+      out[k] = cb.own[k];
+    }
+    own_ptr = cb.own_ptr;
+    x0 = cb.x0;
+  }
   const uint32_t t = st[r].cur[0] + (uint32_t)jsweep;
-  const uint32_t cbase = (uint32_t)L * ((uint32_t)y + (uint32_t)L * (uint32_t)z);
-  uint32_t out[V];
+  const uint32_t L = R.L;
+  const uint32_t cbase = L * ((uint32_t)y + L * (uint32_t)z) + (uint32_t)x0;
 #pragma unroll
   for (int k = 0; k < V; ++k) {
-    uint32_t c0 = (uint32_t)(cb.x0 + 2 * k) + cbase;
-    uint32_t nbs = neighbour_sigmas(cb.xp[k], cb.xm[k], cb.yp[k], cb.ym[k], cb.zp[k], cb.zm[k]);
-    out[k] = update_cell(cb.own[k], nbs, cb.eta[k], c0, t, R, s_thi, s_tlo);
+    const uint32_t c0 = cbase + 2u * k;
+    const U4 rr = philox(c0, t, kStSweep, R.replica, R.key0, R.key1);
+    out[k] = update_cell(out[k], nbs[k], eta[k], rr, c0, t, R, s_tv);
   }
-  VecLoad<V>::st(cb.own_ptr, out);
+  VecLoad<V>::st(own_ptr, out);
 }
 
 // ------------------------------------------------------------------ measurement
@@ -403,31 +525,26 @@ template <int V>
 __global__ void __launch_bounds__(kThreads) k_measure(const ReplicaDesc* __restrict__ reps,
                                                       ReplicaState* __restrict__ st,
                                                       const int* __restrict__ blk, int nrep) {
-  __shared__ uint32_t s_thi[33];
-  __shared__ uint16_t s_tlo[33];
+  __shared__ uint32_t s_tv[33];
   __shared__ uint8_t s_eta[72];
   __shared__ unsigned long long s_acc[2];
   const int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
-  load_sweep_tables(R, s_thi, s_tlo, s_eta);
+  load_sweep_tables(R, s_tv, s_eta);
   if (threadIdx.x < 2) s_acc[threadIdx.x] = 0;
   __syncthreads();
   const int L = R.L, H = R.H;
-  const int cpr = H / V;
-  long long q = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
   uint32_t hb2 = 0, ns = 0;
-  if (q < (long long)cpr * L * L) {
-    int hc = (int)(q % cpr);
-    long long row = q / cpr;
-    int y = (int)(row % L), z = (int)(row / L);
+  int hc, y, z;
+  if (segment_of<V>(R, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, hc, y, z)) {
     CellBlock<V> cb;
     cb.load(R, 0, hc, y, z, s_eta);
     uint32_t w1[V];
-    VecLoad<V>::ld(R.cells[1] + (size_t)H * ((size_t)y + (size_t)L * z) + hc * V, w1);
+    VecLoad<V>::ld(R.cells[1] + (uint32_t)H * ((uint32_t)y + (uint32_t)L * z) + hc * V, w1);
 #pragma unroll
     for (int k = 0; k < V; ++k) {
-      uint32_t w = cb.own[k];
-      uint32_t nbs = neighbour_sigmas(cb.xp[k], cb.xm[k], cb.yp[k], cb.ym[k], cb.zp[k], cb.zm[k]);
+      const uint32_t w = cb.own[k];
+      const uint32_t nbs = neighbour_sigmas(cb.xp[k], cb.xm[k], cb.yp[k], cb.ym[k], cb.zp[k], cb.zm[k]);
 #pragma unroll
       for (int a = 0; a < 6; ++a) {
         uint32_t same = ((w >> (3 * a)) & 7u) == ((nbs >> (3 * a)) & 7u);
@@ -481,12 +598,15 @@ void launch_init_lattice(const BatchDev& b, cudaStream_t s) {
   k_init_cubes<<<b.nblk_cube, kThreads, 0, s>>>(b.reps, b.blk_cube, b.nrep);
 }
 
-void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, cudaStream_t s) {
-  k_step_begin<<<grid1(b.nrep), kThreads, 0, s>>>(b.reps, b.st, b.nrep, nmet, ncl, do_cube);
+void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do_volume, cudaStream_t s) {
+  k_step_begin<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, nmet, ncl, do_cube, do_volume);
 }
 
-void launch_cube_move(const BatchDev& b, cudaStream_t s) {
-  k_cube_move<<<b.nblk_cube, kThreads, 0, s>>>(b.reps, b.st, b.blk_cube, b.nrep);
+void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s) {
+  const int cube_blocks = do_cubes ? b.nblk_cube : 0;
+  const int vol_blocks = do_volume ? b.nrep : 0;
+  if (cube_blocks + vol_blocks == 0) return;
+  k_cube_volume<<<cube_blocks + vol_blocks, kThreads, 0, s>>>(b.reps, b.st, b.blk_cube, b.nrep, cube_blocks);
 }
 
 void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s) {

@@ -32,6 +32,23 @@ __device__ __forceinline__ int find_replica_sw(const int* __restrict__ blk, int 
   return lo;
 }
 
+__device__ __forceinline__ void cell_xyz(const ReplicaDesc& R, uint32_t c, int& x, int& y, int& z) {
+  const uint32_t L = R.L;
+  uint32_t q, rem;
+  if (R.lgL >= 0) {
+    x = (int)(c & (L - 1));
+    q = c >> R.lgL;
+    y = (int)(q & (L - 1));
+    z = (int)(q >> R.lgL);
+  } else {
+    q = c / L;
+    rem = c - q * L;
+    x = (int)rem;
+    z = (int)(q / L);
+    y = (int)(q - (uint32_t)z * L);
+  }
+}
+
 __device__ __forceinline__ uint32_t word_at(const ReplicaDesc& R, int x, int y, int z) {
   return R.cells[(x + y + z) & 1][(uint32_t)(x >> 1) + (uint32_t)R.H * ((uint32_t)y + (uint32_t)R.L * (uint32_t)z)];
 }
@@ -56,10 +73,11 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
   const int r = find_replica_sw(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   const int L = R.L;
-  const long long N = (long long)L * L * L;
-  long long c = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  const uint32_t N = (uint32_t)L * L * L;
+  const uint32_t c = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
   if (c >= N) return;
-  const int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
+  int x, y, z;
+  cell_xyz(R, c, x, y, z);
   const uint32_t t = st[r].cur[3] + (uint32_t)jsw;
   const uint32_t w = word_at(R, x, y, z);
   uint32_t rw[20];
@@ -111,7 +129,7 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
       m = nm;
     }
     int root = __ffs(m) - 1;
-    R.label[(long long)a * N + c] = (int32_t)((long long)root * N + c);
+    R.label[a * N + c] = (int32_t)(root * N + c);
   }
 }
 
@@ -151,21 +169,21 @@ __global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __rest
                                                        const int* __restrict__ blk, int nrep) {
   const int r = find_replica_sw(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
-  const int L = R.L;
-  const long long N = (long long)L * L * L;
-  long long c = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  const uint32_t L = R.L;
+  const uint32_t N = L * L * L;
+  const uint32_t c = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
   if (c >= N) return;
   uint32_t hb = R.hbmask[c];
   if (!hb) return;
-  const int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
-  const long long nb[3] = {(long long)(x + 1 == L ? 0 : x + 1) + (long long)L * (y + (long long)L * z),
-                           (long long)x + (long long)L * ((y + 1 == L ? 0 : y + 1) + (long long)L * z),
-                           (long long)x + (long long)L * (y + (long long)L * (z + 1 == L ? 0 : z + 1))};
+  int xi, yi, zi;
+  cell_xyz(R, c, xi, yi, zi);
+  const uint32_t x = xi, y = yi, z = zi;
+  const uint32_t nb[3] = {(x + 1 == L ? 0 : x + 1) + L * (y + L * z), x + L * ((y + 1 == L ? 0 : y + 1) + L * z),
+                          x + L * (y + L * (z + 1 == L ? 0 : z + 1))};
 #pragma unroll
   for (int d = 0; d < 3; ++d)
     if ((hb >> d) & 1u)
-      if (!uf_unite(R.label, (int32_t)((long long)(2 * d) * N + c), (int32_t)((long long)(2 * d + 1) * N + nb[d])))
-        st[r].err = 1;
+      if (!uf_unite(R.label, (int32_t)((2 * d) * N + c), (int32_t)((2 * d + 1) * N + nb[d]))) st[r].err = 1;
 }
 
 __global__ void __launch_bounds__(kThreads) k_sw_compress(const ReplicaDesc* __restrict__ reps,
@@ -207,15 +225,16 @@ __global__ void __launch_bounds__(kThreads) k_sw_apply(const ReplicaDesc* __rest
   const int r = find_replica_sw(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   const int L = R.L;
-  const long long N = (long long)L * L * L;
-  long long c = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  const uint32_t N = (uint32_t)L * L * L;
+  const uint32_t c = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
   if (c >= N) return;
-  const int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
+  int x, y, z;
+  cell_xyz(R, c, x, y, z);
   uint32_t* wp = R.cells[(x + y + z) & 1] + (uint32_t)(x >> 1) + (uint32_t)R.H * ((uint32_t)y + (uint32_t)L * (uint32_t)z);
   uint32_t w = *wp, out = 0;
 #pragma unroll
   for (int a = 0; a < 6; ++a) {
-    uint32_t sh = R.shift[R.label[(long long)a * N + c]];
+    uint32_t sh = R.shift[R.label[a * N + c]];
     uint32_t v = ((w >> (3 * a)) & 7u) + sh;
     if (v >= 6u) v -= 6u;
     out |= v << (3 * a);
@@ -315,16 +334,13 @@ __global__ void __launch_bounds__(kThreads) k_cs_cover(const ReplicaDesc* __rest
   const int r = find_replica_sw(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   const int L = R.L;
-  const long long N = (long long)L * L * L;
-  long long s = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  const uint32_t N = (uint32_t)L * L * L;
+  const uint32_t s = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
   int k = -1;
   int coord[3] = {0, 0, 0};
   if (s < 6 * N) {
     k = R.cand[R.label[s]];
-    long long c = s % N;
-    coord[0] = (int)(c % L);
-    coord[1] = (int)((c / L) % L);
-    coord[2] = (int)(c / ((long long)L * L));
+    cell_xyz(R, s % N, coord[0], coord[1], coord[2]);
   }
   const unsigned active = __ballot_sync(0xffffffffu, k >= 0);
   if (k < 0) return;

@@ -564,7 +564,8 @@ void oracle_volume_move(oracle_t* o)
 }
 
 /* Metropolis update of all six sigma arms of one cell, arms in order 0..5 (the engine's
- * checkerboard sweep). Energy change as in GW:1964-1996 (chessboard branch):
+ * checkerboard sweep). Proposal of arm a: base-6 digit a, most significant first, of the
+ * uniform d in [0, 46656) drawn from word 0. Energy change as in GW:1964-1996 (chessboard branch):
  *   dN_hb = eta_a [delta(new, s'_opp) - delta(old, s'_opp)],
  *   dN_s  = sum_{b != a} [delta(new, s_b) - delta(old, s_b)],
  * accepted iff U < T[dN_hb, dN_s] with U = 32-bit uniform whose high half is chunk a of
@@ -575,10 +576,10 @@ static void sweep_cell(oracle_t* o, int64_t cell, uint32_t t)
     uint32_t r[4], rf[4];
     int have_rf = 0;
     rng(o, (uint32_t)cell, t, ST_SWEEP, r);
+    static const uint32_t pow6[ARMS] = {7776, 1296, 216, 36, 6, 1};
     uint32_t d = draw_below(o, 46656u, r, 1, (uint32_t)cell, t, ST_SWEEP);
     for (int a = 0; a < ARMS; ++a) {
-        int nw = (int)(d % 6);
-        d /= 6;
+        int nw = (int)((d / pow6[a]) % 6);
         int old = o->s[a * N + cell];
         if (nw == old) continue;
         int nb = o->s[(int64_t)(a ^ 1) * N + neighbour(o->L, cell, a)];
