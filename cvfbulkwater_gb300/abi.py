@@ -89,6 +89,7 @@ def lib():
         "cvf_get_thresholds": (I, [P, I, P]),
         "cvf_get_stream": (I, [P, C.POINTER(P)]),
         "cvf_profile_launch": (I, [P, I, I]),
+        "cvf_cluster_stats_noalloc": (I, [P, I, P, P]),
         "cvf_reweight_forward": (I, [I, P, P, LL, P, I, P, I, D, D, P, P, I, P]),
         "cvf_reweight_adjoint": (I, [I, P, P, LL, P, I, P, D, P, P, I, P, P]),
     }

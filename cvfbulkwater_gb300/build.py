@@ -22,7 +22,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libcvf_gb300.so")
 EXE = os.path.join(BUILD, "gpu_water3D")
 
-CU = ["cvf_mc.cu", "cvf_sw.cu", "cvf_reweight.cu"]
+CU = ["cvf_mc.cu", "cvf_sw.cu", "cvf_reweight.cu", "cvf_noalloc.cu"]
 CPP = ["cvf_engine.cpp", "cvf_host.cpp"]
 DRIVER = []
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

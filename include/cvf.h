@@ -155,6 +155,22 @@ int cvf_get_stream(cvf_handle* h, void** stream);
  * 1 = cube move, 2 = volume move, 3 = measurement. For timing only. No reference counterpart. */
 int cvf_profile_launch(cvf_handle* h, int kind, int n);
 
+/* Cluster statistics (as cvf_cluster_stats) of a caller-owned device array of 6*L^3 labels,
+ * without allocating any device memory. No counterpart in the reference.
+ * For callers that cannot call cudaMalloc: code running while a CUDA graph is captured, processes
+ * whose device memory is reserved by another allocator or capped by a pool, hosts that forbid a
+ * library to grow its footprint after start-up. The work space is a fixed array inside the
+ * library (about 8.6 MB on every GPU that loads it, held until the process exits).
+ *   labels: device pointer, site = arm*N + cell, each label a site id in [0, 6N);
+ *   out7:   device pointer to 7 long longs: largest, second, n_percolating, n_clusters,
+ *           sum_size, sum_size2, sum_size2_wrap32 (n_clusters = -1 if a label is out of range);
+ *   stream: cudaStream_t passed as void* (NULL = legacy default stream); nothing synchronises.
+ * Limit: 6*L^3 <= CVF_NOALLOC_MAX_SITES (even L <= 54); larger L returns CVF_EINVAL.
+ * All calls share the array: calls whose work overlaps on the GPU race and give wrong results.
+ * The first call on a device looks up the array's address; make it before any stream capture. */
+#define CVF_NOALLOC_MAX_SITES 1048576
+int cvf_cluster_stats_noalloc(const int* labels, int L, long long* out7, void* stream);
+
 /* Histogram reweighting (replaces the Fortran Calcula_Histograma F90:1003-1124 and the finite
  * differences of CVF_ThermodynamicAnalysis/{AlphaP,CP,KT}derivate.c).
  *   samples: n rows of (E, V, N_hb, N_sigma) in internal units, grouped by run;
