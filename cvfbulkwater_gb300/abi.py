@@ -49,6 +49,14 @@ class State(C.Structure):
                 ("counters", C.c_uint * 4)]
 
 
+class Input(C.Structure):
+    _fields_ = [("P", C.c_float), ("T", C.c_float), ("seed", C.c_longlong), ("metropolis_steps", C.c_int),
+                ("cluster_steps", C.c_int), ("equilibrium_steps", C.c_int), ("sampling_steps", C.c_int),
+                ("sampling_interval", C.c_int), ("R_cutoff", C.c_float), ("flag_config", C.c_int),
+                ("flag_distances", C.c_int), ("flag_correlation", C.c_int), ("flag_chessboard", C.c_int),
+                ("device_id", C.c_int), ("L", C.c_int)]
+
+
 _lib = None
 
 
@@ -90,6 +98,13 @@ def lib():
         "cvf_get_stream": (I, [P, C.POINTER(P)]),
         "cvf_profile_launch": (I, [P, I, I]),
         "cvf_cluster_stats_noalloc": (I, [P, I, P, P]),
+        "cvf_read_input_data": (I, [C.c_char_p, C.POINTER(Input)]),
+        "cvf_read_config_file": (I, [C.c_char_p, P, LL]),
+        "cvf_write_config_file": (I, [C.c_char_p, P, LL]),
+        "cvf_write_distances_file": (I, [C.c_char_p, I, P, P, I]),
+        "cvf_read_distances_file": (I, [C.c_char_p, I, P, P, I, C.POINTER(I)]),
+        "cvf_format_data_line": (I, [C.c_char_p, I, I, C.POINTER(Obs)]),
+        "cvf_format_cluster_line": (I, [C.c_char_p, I, I, C.POINTER(CStats)]),
         "cvf_reweight_forward": (I, [I, P, P, LL, P, I, P, I, D, D, P, P, I, P]),
         "cvf_reweight_adjoint": (I, [I, P, P, LL, P, I, P, D, P, P, I, P, P]),
     }

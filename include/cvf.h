@@ -146,6 +146,34 @@ int cvf_set_state(cvf_handle* h, int replica, const cvf_state* in);
  * out[42] SW hydrogen-bond link; out[43] SW intra-cell link. */
 int cvf_get_thresholds(const cvf_handle* h, int replica, unsigned long long* out44);
 
+/* ---- File formats of the executable contract (host only, no GPU needed) ---- */
+
+/* The 14 positional "name value" lines of input_data (GW:293-386), plus an optional 15th line
+ * "Lattice_Size L" (the reference fixes L = 32 at compile time, GW:35-37; default 32). */
+typedef struct cvf_input {
+  float P, T;
+  long long seed;
+  int metropolis_steps, cluster_steps, equilibrium_steps, sampling_steps, sampling_interval;
+  float R_cutoff;
+  int flag_config, flag_distances, flag_correlation, flag_chessboard, device_id;
+  int L;
+} cvf_input;
+/* Returns 0, or CVF_EINVAL with the reference's message (e.g. "Error [Pressure]: Can't read
+ * input file") in cvf_last_error_string(). */
+int cvf_read_input_data(const char* path, cvf_input* out);
+/* input_config reader with the reference's checks (GW:730-800): 12 ints per line, sigma in
+ * 0..5, eta in 0..1, exactly n_cells rows. */
+int cvf_read_config_file(const char* path, int* cells12, long long n_cells);
+/* config.out writer (GW:1296-1305). */
+int cvf_write_config_file(const char* path, const int* cells12, long long n_cells);
+/* distances file writer / reader (GW:917-985): header "L L L", then "%f %d" per shell. */
+int cvf_write_distances_file(const char* path, int L, const float* dist, const int* freq, int n);
+int cvf_read_distances_file(const char* path, int L, float* dist, int* freq, int cap, int* n);
+/* One data.out line (GW:2159) and one cluster.out line (GW:2717-2718), NUL-terminated, with the
+ * trailing newline. Return the length or CVF_EINVAL if cap is too small. */
+int cvf_format_data_line(char* buf, int cap, int t, const cvf_obs* o);
+int cvf_format_cluster_line(char* buf, int cap, int t, const cvf_cstats* c);
+
 /* The CUDA stream (a cudaStream_t passed as void*) on which all work of the handle is ordered,
  * for callers that time or order their own work around the engine. No reference counterpart. */
 int cvf_get_stream(cvf_handle* h, void** stream);
