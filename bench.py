@@ -155,6 +155,90 @@ def cpu_baseline_oracle(steps_cap=3, budget_s=30.0):
                       f"OpenMP threads ({dt:.1f} s)"}
 
 
+def timed_steps(lat, steps, flush, nmet=1, ncl=0):
+    """Device time (ms) of `steps` MC steps of a handle, each bracketed by CUDA events on the
+    handle's stream with a 256 MB L2 flush before it."""
+    import torch
+    stream = torch.cuda.ExternalStream(lat.stream_ptr())
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for i in range(steps):
+            flush.fill_(i & 255)
+            ev[i][0].record(stream)
+            lat.run(1, nmet, ncl)
+            ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev)
+
+
+def batch_params(local):
+    """Batched workload: 64 replicas, L drawn from {16,24,32,48,64} with a fixed seed, on the 8x8
+    grid T in [0.55, 0.95] x P in [0.0, 0.60], disordered starts from per-replica seeds."""
+    from cvfbulkwater_gb300.engine import Params
+    rng = np.random.default_rng(20261203)
+    Ls = rng.choice([16, 24, 32, 48, 64], size=64)
+    Ts = np.linspace(0.55, 0.95, 8)
+    Ps = np.linspace(0.0, 0.60, 8)
+    return [Params(L=int(Ls[i]), T=float(Ts[i % 8]), P=float(Ps[i // 8]), seed=SEED + i, start=0, replica=i,
+                   device=local) for i in range(64)]
+
+
+def bench_batch64(steps, warmup, local, flush, verify=4):
+    """One batched handle (one set of launches per step for all 64 replicas, graph-captured,
+    autotuned tile) against the same 64 replicas run one after another as plain handles. The
+    chains are identical (same Philox streams), so "equal error" holds sample for sample; the
+    first `verify` replicas are compared bit for bit."""
+    from cvfbulkwater_gb300.engine import Lattice
+    params = batch_params(local)
+    cells = sum(p.L ** 3 for p in params)
+    batch = Lattice(params)
+    tile = batch.autotune()
+    batch.run(warmup, 1, 0)
+    batch.synchronize()
+    t_batch = timed_steps(batch, steps, flush)
+    t_plain = 0.0
+    same = True
+    for i, p in enumerate(params):
+        h = Lattice(p)
+        h.run(warmup, 1, 0)
+        h.synchronize()
+        t_plain += timed_steps(h, steps, flush)
+        if i < verify:
+            same = same and bool(np.array_equal(h.get_config(), batch.get_config(i)))
+        h.close()
+    batch.close()
+    rs_b = 64 * steps / (t_batch / 1e3)
+    rs_p = 64 * steps / (t_plain / 1e3)
+    return {"workload": "64 replicas, L from {16,24,32,48,64} (seeded), 8x8 grid T 0.55..0.95 x P 0..0.60, "
+                        "disordered starts; 1 cube + 1 volume move + 1 sweep per step",
+            "cells": cells, "steps": steps, "sweep_tile": tile,
+            "batched_replica_sweeps_per_s": round(rs_b, 1),
+            "plain_sequential_replica_sweeps_per_s": round(rs_p, 1),
+            "batched_site_updates_per_ns": round(cells * steps / (t_batch * 1e6), 4),
+            "plain_site_updates_per_ns": round(cells * steps / (t_plain * 1e6), 4),
+            "speedup": round(t_plain / t_batch, 2), "identical_chains_checked": verify, "identical": same,
+            "l2": "256 MB write before every timed step in both arms"}
+
+
+def bench_sw(steps, warmup, local, flush):
+    """Swendsen-Wang path: L=64 and L=128, T=0.60 and 0.75, P=0.45, disordered start,
+    Cluster_Steps=1, Metropolis_Steps=0 (each step: cube move, volume move, one SW step)."""
+    from cvfbulkwater_gb300.engine import Lattice, Params
+    out = []
+    for L in (64, 128):
+        for T in (0.60, 0.75):
+            lat = Lattice(Params(L=L, T=T, P=0.45, seed=SEED, start=0, device=local))
+            lat.run(warmup, 0, 1)
+            lat.synchronize()
+            ms = timed_steps(lat, steps, flush, nmet=0, ncl=1)
+            cs = lat.cluster_stats()
+            out.append({"L": L, "T": T, "sw_steps_per_s": round(steps / (ms / 1e3), 1),
+                        "site_updates_per_ns": round(L ** 3 * steps / (ms * 1e6), 4),
+                        "largest_cluster": int(cs.largest), "n_clusters": int(cs.n_clusters)})
+            lat.close()
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -192,9 +276,7 @@ def run_engine(args):
     L = L_BENCH
     N = L ** 3
     lat = Lattice(Params(L=L, T=T_BENCH, P=P_BENCH, seed=SEED + rank, start=2, replica=rank, device=local))
-    sp = C.c_void_p()
-    abi.check(abi.lib().cvf_get_stream(lat._h, C.byref(sp)))
-    stream = torch.cuda.ExternalStream(sp.value, device=local)
+    stream = torch.cuda.ExternalStream(lat.stream_ptr(), device=local)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
     lat.run(args.warmup, 1, 0)
@@ -267,6 +349,11 @@ def run_engine(args):
                    "the K steps; cells12 host packing included"}
     del out_cfg
 
+    extras = {}
+    if rank == 0 and world == 1 and not args.no_extras:
+        extras["batched"] = bench_batch64(max(10, min(args.steps, 50)), args.warmup, local, flush)
+        extras["swendsen_wang"] = bench_sw(max(10, min(args.steps, 30)), args.warmup, local, flush)
+
     peak, peak_kind = peaks()
     achieved = alg_bytes_launch / launch_s / 1e9
     traffic = ncu_traffic("sweep_l256_traffic.json")
@@ -291,6 +378,7 @@ def run_engine(args):
         "l2_resident_value": round(resident, 4),
         "arm_updates_per_ns": round(6 * value, 4),
     }
+    line.update(extras)
     if rank == 0:
         print(json.dumps(line), flush=True)
     lat.close()
@@ -306,6 +394,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched and Swendsen-Wang sub-benchmarks")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

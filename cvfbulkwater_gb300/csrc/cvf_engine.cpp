@@ -71,13 +71,14 @@ static int upload_descs(cvf_handle* h) {
   return 0;
 }
 
-static int build_tables(cvf_handle* h) {
+static int build_tables(cvf_handle* h, int force_vec = 0) {
   const int n = (int)h->reps.size();
   int vec = 4;
   if (const char* ev = getenv("CVF_SWEEP_VEC")) {
     int v = atoi(ev);
     if (v == 1 || v == 2 || v == 4) vec = v;
   }
+  if (force_vec) vec = force_vec;
   for (auto& r : h->reps) {
     while (vec > 1 && r.H % vec) vec >>= 1;
   }
@@ -579,6 +580,74 @@ int cvf_set_state(cvf_handle* h, int r, const cvf_state* in) {
   s.e_vdw = host_evdw(in->r_cell, R.dist, R.freq, R.p.R_cutoff);
   for (int i = 0; i < 4; ++i) s.ctr[i] = in->counters[i];
   CK(cudaMemcpy(h->b.st + r, &s, sizeof(ReplicaState), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+int cvf_autotune(cvf_handle* h, int* vec_out) {
+  if (!h) return fail(CVF_EINVAL, "null handle");
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  std::vector<int> cands;
+  for (int v : {4, 2, 1}) {
+    bool ok = true;
+    for (auto& r : h->reps) ok = ok && (r.H % v == 0);
+    if (ok) cands.push_back(v);
+  }
+  // save every lattice; the timing sweeps are undone afterwards
+  std::vector<void*> saved;
+  for (auto& r : h->reps) {
+    void* p = nullptr;
+    size_t bytes = (size_t)r.N * sizeof(uint32_t);
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      for (void* q : saved) cudaFree(q);
+      return fail(CVF_ENOMEM, "autotune: cannot allocate the lattice backup");
+    }
+    cudaMemcpyAsync(p, r.desc.cells[0], bytes / 2, cudaMemcpyDeviceToDevice, h->stream);
+    cudaMemcpyAsync((char*)p + bytes / 2, r.desc.cells[1], bytes / 2, cudaMemcpyDeviceToDevice, h->stream);
+    saved.push_back(p);
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int best = h->b.vec;
+  float best_ms = 1e30f;
+  for (int v : cands) {
+    if (int rc = build_tables(h, v)) {  // block counts depend on the tile
+      for (void* q : saved) cudaFree(q);
+      return rc;
+    }
+    launch_sweep(h->b, 0, 0, h->stream);  // warm-up
+    launch_sweep(h->b, 1, 0, h->stream);
+    cudaEventRecord(e0, h->stream);
+    for (int i = 0; i < 5; ++i) {
+      launch_sweep(h->b, 0, i, h->stream);
+      launch_sweep(h->b, 1, i, h->stream);
+    }
+    cudaEventRecord(e1, h->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = v;
+    }
+  }
+  for (size_t i = 0; i < h->reps.size(); ++i) {
+    auto& r = h->reps[i];
+    size_t bytes = (size_t)r.N * sizeof(uint32_t);
+    cudaMemcpyAsync(r.desc.cells[0], saved[i], bytes / 2, cudaMemcpyDeviceToDevice, h->stream);
+    cudaMemcpyAsync(r.desc.cells[1], (char*)saved[i] + bytes / 2, bytes / 2, cudaMemcpyDeviceToDevice, h->stream);
+  }
+  cudaError_t e = cudaStreamSynchronize(h->stream);
+  for (void* q : saved) cudaFree(q);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return fail(CVF_ECUDA, std::string("autotune: ") + cudaGetErrorString(e));
+  // the sweep blocks depend on the tile: rebuild the block tables and drop captured graphs
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+  h->graphs.clear();
+  if (int rc = build_tables(h, best)) return rc;
+  if (vec_out) *vec_out = best;
   return 0;
 }
 

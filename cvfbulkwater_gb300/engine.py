@@ -98,6 +98,17 @@ class Lattice:
         check(lib().cvf_get_distances(self._h, r, _ptr(d), _ptr(f), 512, C.byref(n)))
         return d[: n.value].copy(), f[: n.value].copy()
 
+    def autotune(self) -> int:
+        """Pick the fastest sweep tile (cells per thread) for these replicas; returns it."""
+        v = C.c_int()
+        check(lib().cvf_autotune(self._h, C.byref(v)))
+        return v.value
+
+    def stream_ptr(self) -> int:
+        s = C.c_void_p()
+        check(lib().cvf_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
     # -- running
     def run(self, n_steps: int, n_metropolis: int = 1, n_cluster: int = 0):
         check(lib().cvf_run_steps(self._h, n_steps, n_metropolis, n_cluster))

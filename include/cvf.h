@@ -174,6 +174,13 @@ int cvf_read_distances_file(const char* path, int L, float* dist, int* freq, int
 int cvf_format_data_line(char* buf, int cap, int t, const cvf_obs* o);
 int cvf_format_cluster_line(char* buf, int cap, int t, const cvf_cstats* c);
 
+/* Autotuner: times the checkerboard sweep kernel on this handle's replicas for every supported
+ * cells-per-thread tile (1, 2 or 4 consecutive colour cells: 32-, 64- or 128-bit accesses) and
+ * keeps the fastest. The lattices are saved before and restored after, so the Markov chains are
+ * unchanged (the tile only changes the thread mapping, never the result). vec_out may be NULL.
+ * No reference counterpart. */
+int cvf_autotune(cvf_handle* h, int* vec_out);
+
 /* The CUDA stream (a cudaStream_t passed as void*) on which all work of the handle is ordered,
  * for callers that time or order their own work around the engine. No reference counterpart. */
 int cvf_get_stream(cvf_handle* h, void** stream);
