@@ -37,6 +37,13 @@ struct ReplicaDesc {
   float T, P, Rc;
   double beta, Jeff;
   unsigned long long thr_sweep[33];  // U < T, T in [0, 2^32]; index (dN_hb+1)*11 + dN_s+5
+  // Sweep fast-path tables, read through L1 by the kernels:
+  //   tv[i] = 2*(T_i >> 16) + ((T_i & 0xffff) != 0) for the same index i;
+  //   eta_tab[s*8 + p] = eta bits a cube in state s gives its vertex at offset p;
+  //   nbmask[m] = 7 in every 3-bit field a whose bit a of the 6-bit mask m is set.
+  uint32_t tv[33];
+  uint32_t nbmask[64];
+  uint8_t eta_tab[72];
   unsigned long long thr_cube[9];    // index dN_hb+4
   unsigned long long thr_sw[2];      // hydrogen-bond link, intra-cell link
 };

@@ -278,6 +278,15 @@ int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
     d.beta = r.thr.beta;
     d.Jeff = r.thr.Jeff;
     memcpy(d.thr_sweep, r.thr.sweep, sizeof(d.thr_sweep));
+    for (int i = 0; i < 33; ++i) d.tv[i] = 2u * (uint32_t)(r.thr.sweep[i] >> 16) + ((r.thr.sweep[i] & 0xffffull) != 0);
+    for (int m = 0; m < 64; ++m) {
+      uint32_t v = 0;
+      for (int a = 0; a < 6; ++a)
+        if ((m >> a) & 1) v |= 7u << (3 * a);
+      d.nbmask[m] = v;
+    }
+    for (int st = 0; st < 9; ++st)
+      for (int pp = 0; pp < 8; ++pp) d.eta_tab[st * 8 + pp] = (uint8_t)cube_eta_bits(st, pp);
     memcpy(d.thr_cube, r.thr.cube, sizeof(d.thr_cube));
     memcpy(d.thr_sw, r.thr.sw, sizeof(d.thr_sw));
     ReplicaState& s = st[i];

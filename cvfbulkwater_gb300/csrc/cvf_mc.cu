@@ -422,11 +422,13 @@ __device__ __noinline__ uint32_t sweep_cell_exact(uint32_t w, uint32_t nbs, uint
 
 // Metropolis update of the six arms of one cell, arms in order 0..5 (GW:1964-2007 energy change,
 // chessboard branch). Proposal of arm a: the a-th most significant base-6 digit of the uniform
-// word u (the high word of u*6 in a multiply chain). s_tv[i] = 2*(T_i >> 16) + ((T_i & 0xffff) != 0)
+// word u (the high word of u*6 in a multiply chain). tv[i] = 2*(T_i >> 16) + ((T_i & 0xffff) != 0)
 // with i = 11*dN_hb + (h_new - h_old) + 17, so "accept" is 2*hu + 2 <= tv and a tie on the high
-// 16 bits is 2*hu + 1 == tv.
-__device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32_t eta, const U4& rr, uint32_t c0,
-                                                uint32_t t, const ReplicaDesc& R, const uint32_t* s_tv) {
+// 16 bits is 2*hu + 1 == tv. nbe holds per arm the facing neighbour sigma, or 7 where eta_a = 0,
+// so dN_hb = [new == nbe] - [old == nbe]. A proposal equal to the old value lands on entry 17
+// (dN = 0 up to -J_sigma), which always accepts and changes nothing, so it needs no test.
+__device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32_t nbe, uint32_t eta, const U4& rr,
+                                                uint32_t c0, uint32_t t, const ReplicaDesc& R, const uint32_t* tvt) {
   uint32_t u = rr.x;
   if (u * 46656u < 2560u) u = sweep_proposal_retry(c0, t, R.replica, R.key0, R.key1);
   const uint32_t w0 = w;
@@ -439,16 +441,14 @@ __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32
     const uint32_t n = (uint32_t)(m >> 32);
     f = (uint32_t)m;
     const uint32_t o = (w >> (3 * a)) & 7u;
-    const uint32_t nb = (nbs >> (3 * a)) & 7u;
-    const int e = (int)((eta >> a) & 1u);
-    const int dhb = e * ((int)(n == nb) - (int)(o == nb));
+    const uint32_t nb = (nbe >> (3 * a)) & 7u;
+    const int dhb = (int)(n == nb) - (int)(o == nb);
     const int idx = 11 * dhb + (int)((h >> (4 * n)) & 15u) - (int)((h >> (4 * o)) & 15u) + 17;
-    const uint32_t tv = s_tv[idx];
+    const uint32_t tv = tvt[idx];
     const uint32_t word = a < 2 ? rr.y : (a < 4 ? rr.z : rr.w);
     const uint32_t u2 = (a & 1) ? ((word >> 15) & 0x1fffeu) : ((word << 1) & 0x1fffeu);
-    const bool diff = n != o;
-    tie |= diff && (u2 + 1u == tv);
-    if (diff && u2 + 2u <= tv) {
+    tie |= (u2 + 1u == tv);
+    if (u2 + 2u <= tv) {
       w = (w & ~(7u << (3 * a))) | (n << (3 * a));
       h += (1u << (4 * n)) - (1u << (4 * o));
     }
@@ -457,13 +457,24 @@ __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32
   return w;
 }
 
-__device__ __forceinline__ void load_sweep_tables(const ReplicaDesc& R, uint32_t* s_tv, uint8_t* s_eta) {
-  // s_tv index 11*dhb + dns' + 17 equals (dhb+1)*11 + dns + 5 of the public table
-  for (int i = threadIdx.x; i < 33; i += blockDim.x) {
-    unsigned long long T = R.thr_sweep[i];
-    s_tv[i] = 2u * (uint32_t)(T >> 16) + ((T & 0xffffull) != 0);
-  }
-  for (int i = threadIdx.x; i < 72; i += blockDim.x) s_eta[i] = c_eta_table[i];
+// Warp-private shared-memory copies of the sweep tables (no block barrier: each warp fills and
+// reads its own copy). Layout per warp: tv[33], nbmask[64], eta_tab[72 bytes].
+struct WarpTables {
+  uint32_t tv[33];
+  uint32_t nbmask[64];
+  uint8_t eta[72];
+};
+
+__device__ __forceinline__ const WarpTables* warp_tables(const ReplicaDesc& R, WarpTables* all) {
+  WarpTables* wt = all + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  wt->tv[lane] = R.tv[lane];
+  if (lane == 0) wt->tv[32] = R.tv[32];
+  wt->nbmask[lane] = R.nbmask[lane];
+  wt->nbmask[32 + lane] = R.nbmask[32 + lane];
+  if (lane < 18) reinterpret_cast<uint32_t*>(wt->eta)[lane] = reinterpret_cast<const uint32_t*>(R.eta_tab)[lane];
+  __syncwarp();
+  return wt;
 }
 
 // One colour of the checkerboard sweep: every cell with (x+y+z)&1 == colour updates its six
@@ -473,24 +484,23 @@ template <int V>
 __global__ void __launch_bounds__(kThreads) k_sweep(const ReplicaDesc* __restrict__ reps,
                                                     const ReplicaState* __restrict__ st,
                                                     const int* __restrict__ blk, int nrep, int colour, int jsweep) {
-  __shared__ uint32_t s_tv[33];
-  __shared__ uint8_t s_eta[72];
+  __shared__ WarpTables s_tab[kThreads / 32];
   const int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
-  load_sweep_tables(R, s_tv, s_eta);
-  __syncthreads();
+  const WarpTables* wt = warp_tables(R, s_tab);
   int hc, y, z;
   if (!segment_of<V>(R, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, hc, y, z)) return;
-  uint32_t out[V], nbs[V], eta[V];
+  uint32_t out[V], nbs[V], nbe[V], eta[V];
   uint32_t* own_ptr;
   int x0;
   {
     CellBlock<V> cb;
-    cb.load(R, colour, hc, y, z, s_eta);
+    cb.load(R, colour, hc, y, z, wt->eta);
 #pragma unroll
     for (int k = 0; k < V; ++k) {
       nbs[k] = neighbour_sigmas(cb.xp[k], cb.xm[k], cb.yp[k], cb.ym[k], cb.zp[k], cb.zm[k]);
       eta[k] = cb.eta[k];
+      nbe[k] = nbs[k] | wt->nbmask[~cb.eta[k] & 63u];
       out[k] = cb.own[k];
     }
     own_ptr = cb.own_ptr;
@@ -503,7 +513,7 @@ __global__ void __launch_bounds__(kThreads) k_sweep(const ReplicaDesc* __restric
   for (int k = 0; k < V; ++k) {
     const uint32_t c0 = cbase + 2u * k;
     const U4 rr = philox(c0, t, kStSweep, R.replica, R.key0, R.key1);
-    out[k] = update_cell(out[k], nbs[k], eta[k], rr, c0, t, R, s_tv);
+    out[k] = update_cell(out[k], nbs[k], nbe[k], eta[k], rr, c0, t, R, wt->tv);
   }
   VecLoad<V>::st(own_ptr, out);
 }
@@ -525,12 +535,11 @@ template <int V>
 __global__ void __launch_bounds__(kThreads) k_measure(const ReplicaDesc* __restrict__ reps,
                                                       ReplicaState* __restrict__ st,
                                                       const int* __restrict__ blk, int nrep) {
-  __shared__ uint32_t s_tv[33];
-  __shared__ uint8_t s_eta[72];
   __shared__ unsigned long long s_acc[2];
+  __shared__ WarpTables s_tab[kThreads / 32];
   const int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
-  load_sweep_tables(R, s_tv, s_eta);
+  const WarpTables* wt = warp_tables(R, s_tab);
   if (threadIdx.x < 2) s_acc[threadIdx.x] = 0;
   __syncthreads();
   const int L = R.L, H = R.H;
@@ -538,7 +547,7 @@ __global__ void __launch_bounds__(kThreads) k_measure(const ReplicaDesc* __restr
   int hc, y, z;
   if (segment_of<V>(R, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, hc, y, z)) {
     CellBlock<V> cb;
-    cb.load(R, 0, hc, y, z, s_eta);
+    cb.load(R, 0, hc, y, z, wt->eta);
     uint32_t w1[V];
     VecLoad<V>::ld(R.cells[1] + (uint32_t)H * ((uint32_t)y + (uint32_t)L * z) + hc * V, w1);
 #pragma unroll
