@@ -67,6 +67,7 @@ struct ReplicaState {
   uint32_t ctr[4];  // next move counters: sweep, cube, volume, SW
   uint32_t cur[4];  // counters used by the moves of the current step
   unsigned long long acc_hb2, acc_ns;
+  unsigned long long acc_slot[2][32];  // measurement partial sums, slot = block % 32
   unsigned long long top2[2];
   unsigned long long ncl, sum2, sum2w, nperc;
   int ncand;

@@ -90,7 +90,7 @@ static int build_tables(cvf_handle* h, int force_vec = 0) {
     const auto& r = h->reps[i];
     long long L = r.L, H = r.H;
     ts[i + 1] = ts[i] + blocks((H / vec) * L * L);
-    tc[i + 1] = tc[i] + blocks(2 * H * H * H);
+    tc[i + 1] = tc[i] + 2 * blocks(H * H * H);  // even-origin cubes, then odd-origin cubes
     tl[i + 1] = tl[i] + blocks(r.N);
     tsi[i + 1] = tsi[i] + blocks(6 * r.N);
   }

@@ -57,6 +57,17 @@ __device__ __forceinline__ void divmod32(uint32_t n, uint32_t d, int shift, uint
   }
 }
 
+// Block -> (cube parity, cube index): a replica's cube blocks are split in two equal halves, the
+// first for the cubes with all-even origins, the second for all-odd origins, so the parity is
+// uniform inside a block.
+__device__ __forceinline__ bool cube_of(const int* __restrict__ blk, int r, int H, uint32_t& par, uint32_t& qi) {
+  const int b0 = __ldg(blk + r), half = (__ldg(blk + r + 1) - b0) >> 1;
+  const int lb = blockIdx.x - b0;
+  par = lb >= half;
+  qi = (uint32_t)(lb - (int)par * half) * blockDim.x + threadIdx.x;
+  return qi < (uint32_t)H * H * H;
+}
+
 __device__ __forceinline__ uint32_t cell_word_index(int x, int y, int z, int L, int H) {
   return (uint32_t)(x >> 1) + (uint32_t)H * ((uint32_t)y + (uint32_t)L * (uint32_t)z);
 }
@@ -100,11 +111,9 @@ __global__ void k_init_cubes(const ReplicaDesc* __restrict__ reps, const int* __
   int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   const int L = R.L, H = R.H;
-  uint32_t q = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
-  uint32_t H3 = (uint32_t)H * H * H;
-  if (q >= 2 * H3) return;
-  uint32_t par = q >= H3;
-  uint32_t qi = q - par * H3, a, bc, b, c;
+  uint32_t par, qi;
+  if (!cube_of(blk, r, H, par, qi)) return;
+  uint32_t a, bc, b, c;
   divmod32(qi, H, R.lgH, bc, a);
   divmod32(bc, H, R.lgH, c, b);
   uint32_t x0 = 2 * a + par, y0 = 2 * b + par, z0 = 2 * c + par;
@@ -212,28 +221,35 @@ __global__ void __launch_bounds__(kThreads) k_cube_volume(const ReplicaDesc* __r
   const int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   const int L = R.L, H = R.H;
-  const uint32_t q = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
-  const uint32_t H3 = (uint32_t)H * H * H;
-  if (q >= 2 * H3) return;
-  const uint32_t par = q >= H3;
-  const uint32_t qi = q - par * H3;
+  uint32_t par, qi;
+  if (!cube_of(blk, r, H, par, qi)) return;
   uint32_t a, bc, b, c;
   divmod32(qi, H, R.lgH, bc, a);
   divmod32(bc, H, R.lgH, c, b);
-  const int x0 = 2 * a + par, y0 = 2 * b + par, z0 = 2 * c + par;
-  const int x1 = x0 + 1 == L ? 0 : x0 + 1, y1 = y0 + 1 == L ? 0 : y0 + 1, z1 = z0 + 1 == L ? 0 : z0 + 1;
+  const uint32_t x0 = 2 * a + par, y0 = 2 * b + par, z0 = 2 * c + par;
+  const uint32_t y1 = y0 + 1 == (uint32_t)L ? 0 : y0 + 1, z1 = z0 + 1 == (uint32_t)L ? 0 : z0 + 1;
+  // vertex p = dx | dy<<1 | dz<<2 has colour (par + popc(p)) & 1 and word (x>>1) + H*(y + L*z)
+  const uint32_t xa = a, xb = par ? (a + 1 == (uint32_t)H ? 0 : a + 1) : a;
+  const uint32_t r00 = H * (y0 + L * z0), r10 = H * (y1 + L * z0), r01 = H * (y0 + L * z1), r11 = H * (y1 + L * z1);
+  const uint32_t* c0p = R.cells[par];
+  const uint32_t* c1p = R.cells[par ^ 1];
   uint32_t w[8];
-#pragma unroll
-  for (int p = 0; p < 8; ++p) {
-    int x = (p & 1) ? x1 : x0, y = (p & 2) ? y1 : y0, z = (p & 4) ? z1 : z0;
-    w[p] = __ldg(R.cells[(x + y + z) & 1] + cell_word_index(x, y, z, L, H));
-  }
-  uint32_t D = 0;  // edges whose two arm sigmas agree
+  w[0] = __ldg(c0p + xa + r00);
+  w[1] = __ldg(c1p + xb + r00);
+  w[2] = __ldg(c1p + xa + r10);
+  w[3] = __ldg(c0p + xb + r10);
+  w[4] = __ldg(c1p + xa + r01);
+  w[5] = __ldg(c0p + xb + r01);
+  w[6] = __ldg(c0p + xa + r11);
+  w[7] = __ldg(c1p + xb + r11);
+  // edge e along d from p0 to p1: sigma_{2d}(p0) == sigma_{2d+1}(p1), compared in place by
+  // shifting the start word one field up
+  uint32_t D = 0;
 #pragma unroll
   for (int e = 0; e < 12; ++e) {
     const int d = edge_dir(e), p0 = edge_start(e), p1 = p0 | (1 << d);
-    uint32_t s0 = (w[p0] >> (6 * d)) & 7u, s1 = (w[p1] >> (6 * d + 3)) & 7u;
-    D |= (uint32_t)(s0 == s1) << e;
+    const uint32_t x = ((w[p0] << 3) ^ w[p1]) & (7u << (6 * d + 3));
+    D |= (x == 0u ? 1u : 0u) << e;
   }
   const uint32_t cid = (uint32_t)x0 + (uint32_t)L * ((uint32_t)y0 + (uint32_t)L * (uint32_t)z0);
   const uint32_t t = st[r].cur[1];
@@ -519,14 +535,19 @@ __global__ void __launch_bounds__(kThreads) k_sweep(const ReplicaDesc* __restric
 }
 
 // ------------------------------------------------------------------ measurement
-__device__ __forceinline__ uint32_t pairs_from_hist(uint32_t h) {
-  uint32_t p = 0;
-#pragma unroll
-  for (int v = 0; v < 6; ++v) {
-    uint32_t c = (h >> (4 * v)) & 15u;
-    p += c * (c - 1) / 2;
-  }
-  return p;
+// Number of zero 3-bit fields among the six fields of x.
+__device__ __forceinline__ uint32_t zero_fields(uint32_t x) {
+  return 6u - (uint32_t)__popc((x | (x >> 1) | (x >> 2)) & 0x9249u);
+}
+
+// sum_{a<b} delta(sigma_a, sigma_b) of one cell: with Z_k the number of arms a equal to arm
+// (a+k) mod 6, every unordered pair is counted by Z_k and Z_{6-k}, so the sum is Z_1 + Z_2 + Z_3/2.
+__device__ __forceinline__ uint32_t sigma_pairs(uint32_t w) {
+  w &= 0x3ffffu;
+  const uint32_t r1 = ((w >> 3) | (w << 15)) & 0x3ffffu;
+  const uint32_t r2 = ((w >> 6) | (w << 12)) & 0x3ffffu;
+  const uint32_t r3 = ((w >> 9) | (w << 9)) & 0x3ffffu;
+  return zero_fields(w ^ r1) + zero_fields(w ^ r2) + (zero_fields(w ^ r3) >> 1);
 }
 
 // GW:2014-2160: N_hb2 = sum over bonds of delta * (eta_i + eta_j), counted from the colour-0
@@ -554,12 +575,11 @@ __global__ void __launch_bounds__(kThreads) k_measure(const ReplicaDesc* __restr
     for (int k = 0; k < V; ++k) {
       const uint32_t w = cb.own[k];
       const uint32_t nbs = neighbour_sigmas(cb.xp[k], cb.xm[k], cb.yp[k], cb.ym[k], cb.zp[k], cb.zm[k]);
-#pragma unroll
-      for (int a = 0; a < 6; ++a) {
-        uint32_t same = ((w >> (3 * a)) & 7u) == ((nbs >> (3 * a)) & 7u);
-        hb2 += same * 2u * ((cb.eta[k] >> a) & 1u);
-      }
-      ns += pairs_from_hist(sigma_histogram(w)) + pairs_from_hist(sigma_histogram(w1[k]));
+      // bonds whose two arm sigmas agree, restricted to eta = 1 (bit 3a per arm)
+      const uint32_t x = w ^ nbs;
+      const uint32_t eqm = ~(x | (x >> 1) | (x >> 2)) & wt->nbmask[cb.eta[k] & 63u] & 0x9249u;
+      hb2 += 2u * (uint32_t)__popc(eqm);
+      ns += sigma_pairs(w) + sigma_pairs(w1[k]);
     }
   }
 #pragma unroll
@@ -573,25 +593,34 @@ __global__ void __launch_bounds__(kThreads) k_measure(const ReplicaDesc* __restr
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    atomicAdd(&st[r].acc_hb2, s_acc[0]);
-    atomicAdd(&st[r].acc_ns, s_acc[1]);
+    atomicAdd(&st[r].acc_slot[0][blockIdx.x & 31], s_acc[0]);
+    atomicAdd(&st[r].acc_slot[1][blockIdx.x & 31], s_acc[1]);
   }
 }
 
 __global__ void k_measure_begin(ReplicaState* __restrict__ st, int nrep) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrep) return;
-  st[r].acc_hb2 = 0;
-  st[r].acc_ns = 0;
+  for (int i = 0; i < 32; ++i) {
+    st[r].acc_slot[0][i] = 0;
+    st[r].acc_slot[1][i] = 0;
+  }
 }
 
 __global__ void k_measure_end(ReplicaState* __restrict__ st, int nrep, int record) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrep) return;
   ReplicaState& S = st[r];
+  unsigned long long hb2 = 0, ns = 0;
+  for (int i = 0; i < 32; ++i) {
+    hb2 += S.acc_slot[0][i];
+    ns += S.acc_slot[1][i];
+  }
+  S.acc_hb2 = hb2;
+  S.acc_ns = ns;
   SampleRec rec;
-  rec.n_hb2 = (long long)S.acc_hb2;
-  rec.n_sigma = (long long)S.acc_ns;
+  rec.n_hb2 = (long long)hb2;
+  rec.n_sigma = (long long)ns;
   rec.r_cell = S.r_cell;
   rec.volume = S.volume;
   S.last = rec;
