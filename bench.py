@@ -343,7 +343,7 @@ def run_engine(args):
     packed = 4 * N + 2 * (L // 2) ** 3
     e2e = {"value": round(world * N * args.steps / (e2e_s * 1e9), 4), "unit": "site-updates/ns",
            "h2d_bytes_per_step": int(round(packed / args.steps)),
-           "d2h_bytes_per_step": int(round(packed / args.steps)) + 320,
+           "d2h_bytes_per_step": int(round(packed / args.steps)) + 32,
            "note": "per step: cvf_run_steps(1 step) + cvf_observables (sync + counts D2H); "
                    "lattice upload (cvf_set_config) and download (cvf_get_config) amortised over "
                    "the K steps; cells12 host packing included"}

@@ -84,7 +84,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                 print(o)
     lib_objs = [os.path.join(BUILD, f + ".o") for f in CU + CPP]
     tmp = LIB + f".tmp{os.getpid()}"
-    _run([nvcc, "-shared", "-o", tmp] + lib_objs + ARCH + ["-cudart", "static", "-Xlinker", "-z,defs"])
+    _run([nvcc, "-shared", "-o", tmp] + lib_objs + ARCH + ["-cudart", "static", "-Xlinker", "-z,defs", "-lpthread"])
     os.replace(tmp, LIB)
     if DRIVER:
         drv_objs = [os.path.join(BUILD, f + ".o") for f in DRIVER]

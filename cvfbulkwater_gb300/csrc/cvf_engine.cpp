@@ -450,11 +450,13 @@ int cvf_observables(cvf_handle* h, int r, cvf_obs* out) {
   if (!out) return fail(CVF_EINVAL, "null out");
   CK(cudaSetDevice(h->device));
   launch_measure(h->b, 0, h->stream);
-  ReplicaState s;
-  if (int rc = read_state(h, r, &s)) return rc;
+  SampleRec last;  // only the 32-byte measurement record crosses to the host
+  CK(cudaMemcpyAsync(&last, (char*)(h->b.st + r) + offsetof(ReplicaState, last), sizeof(SampleRec),
+                     cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
   const ReplicaHost& R = h->reps[r];
-  fill_obs(out, s.last.n_hb2, s.last.n_sigma, s.r_cell, s.volume, host_evdw(s.r_cell, R.dist, R.freq, R.p.R_cutoff),
-           R.N, R.p.P);
+  fill_obs(out, last.n_hb2, last.n_sigma, last.r_cell, last.volume,
+           host_evdw(last.r_cell, R.dist, R.freq, R.p.R_cutoff), R.N, R.p.P);
   return 0;
 }
 

@@ -4,6 +4,10 @@
 
 #include <math.h>
 
+#include <algorithm>
+#include <atomic>
+#include <thread>
+
 #include "cvf_spec.cuh"
 
 namespace cvf {
@@ -92,6 +96,25 @@ static inline size_t word_index(int L, int x, int y, int z) {
   return (size_t)(x >> 1) + (size_t)H * ((size_t)y + (size_t)L * z);
 }
 
+// Runs body(begin, end) over [0, n) split across up to 16 host threads.
+template <class F>
+static void parallel_for(long long n, F body) {
+  unsigned hw = std::thread::hardware_concurrency();
+  int nt = (int)std::min<unsigned>(hw ? hw : 1u, 16u);
+  if (n < (1 << 16) || nt <= 1) {
+    body(0LL, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  long long chunk = (n + nt - 1) / nt;
+  for (int i = 0; i < nt; ++i) {
+    long long b = i * chunk, e = std::min(n, b + chunk);
+    if (b >= e) break;
+    th.emplace_back([=]() { body(b, e); });
+  }
+  for (auto& t : th) t.join();
+}
+
 bool pack_config(int L, const int* c12, std::vector<uint32_t>& cells0, std::vector<uint32_t>& cells1,
                  std::vector<uint8_t>& ce, std::vector<uint8_t>& co, std::string& err) {
   const int H = L / 2;
@@ -100,9 +123,29 @@ bool pack_config(int L, const int* c12, std::vector<uint32_t>& cells0, std::vect
   cells1.assign((size_t)(N / 2), 0);
   ce.assign((size_t)H * H * H, 0);
   co.assign((size_t)H * H * H, 0);
-  for (long long c = 0; c < N; ++c) {
-    int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
-    uint32_t w = 0;
+  // first offending cell, if any (smallest index wins, as in a sequential reader)
+  std::atomic<long long> bad{N};
+  parallel_for(N, [&](long long b, long long e) {
+    for (long long c = b; c < e; ++c) {
+      int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
+      uint32_t w = 0;
+      bool ok = true;
+      for (int a = 0; a < 6; ++a) {
+        int s = c12[c * 12 + a], t = c12[c * 12 + 6 + a];
+        ok = ok && s >= 0 && s <= 5 && t >= 0 && t <= 1;
+        w |= (uint32_t)(s & 7) << (3 * a);
+      }
+      if (!ok) {
+        long long cur = bad.load();
+        while (c < cur && !bad.compare_exchange_weak(cur, c)) {
+        }
+        break;
+      }
+      ((x + y + z) & 1 ? cells1 : cells0)[word_index(L, x, y, z)] = w;
+    }
+  });
+  if (bad.load() < N) {
+    long long c = bad.load();
     for (int a = 0; a < 6; ++a) {
       int s = c12[c * 12 + a], e = c12[c * 12 + 6 + a];
       if (s < 0 || s > 5) {
@@ -113,20 +156,20 @@ bool pack_config(int L, const int* c12, std::vector<uint32_t>& cells0, std::vect
         err = "Unexpected value for active_bond (" + std::to_string(e) + ") appeared in line " + std::to_string(c);
         return false;
       }
-      w |= (uint32_t)s << (3 * a);
     }
-    ((x + y + z) & 1 ? cells1 : cells0)[word_index(L, x, y, z)] = w;
   }
   auto eta = [&](int arm, int x, int y, int z) -> int {
     return c12[((long long)x + (long long)L * (y + (long long)L * z)) * 12 + 6 + arm];
   };
-  for (int par = 0; par < 2; ++par)
-    for (int c = 0; c < H; ++c)
-      for (int b = 0; b < H; ++b)
+  // cube states from eta with the decision tree of GW:3330-3369 (vertices v1 = origin, v2 x+1,
+  // v3 y+1, v6 y+1 z+1, v7 x+1 z+1, v8 x+1 y+1)
+  parallel_for(2LL * H, [&](long long b, long long e) {
+    for (long long pc = b; pc < e; ++pc) {
+      int par = (int)(pc / H), c = (int)(pc % H);
+      for (int bb = 0; bb < H; ++bb)
         for (int a = 0; a < H; ++a) {
-          int x = 2 * a + par, y = 2 * b + par, z = 2 * c + par;
+          int x = 2 * a + par, y = 2 * bb + par, z = 2 * c + par;
           int xp = (x + 1) % L, yp = (y + 1) % L, zp = (z + 1) % L;
-          // vertices v1 (x,y,z), v2 x+1, v3 y+1, v6 y+1,z+1, v7 x+1,z+1, v8 x+1,y+1 (GW:3330-3337)
           int st;
           if (eta(0, x, y, z) == 0) {
             if (eta(0, x, yp, zp) == 0) st = 2;
@@ -141,8 +184,10 @@ bool pack_config(int L, const int* c12, std::vector<uint32_t>& cells0, std::vect
             else if (eta(4, xp, yp, z) == 0) st = 1;
             else st = 6;
           }
-          (par ? co : ce)[(size_t)a + (size_t)H * ((size_t)b + (size_t)H * c)] = (uint8_t)st;
+          (par ? co : ce)[(size_t)a + (size_t)H * ((size_t)bb + (size_t)H * c)] = (uint8_t)st;
         }
+    }
+  });
   return true;
 }
 
@@ -153,19 +198,21 @@ void unpack_config(int L, const std::vector<uint32_t>& cells0, const std::vector
   uint8_t tab[72];
   for (int s = 0; s < 9; ++s)
     for (int p = 0; p < 8; ++p) tab[s * 8 + p] = (uint8_t)cube_eta_bits(s, p);
-  for (long long c = 0; c < N; ++c) {
-    int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
-    uint32_t w = ((x + y + z) & 1 ? cells1 : cells0)[word_index(L, x, y, z)];
-    int xo = (x & 1) ? x : (x + L - 1) % L, yo = (y & 1) ? y : (y + L - 1) % L, zo = (z & 1) ? z : (z + L - 1) % L;
-    int p = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
-    uint32_t se = ce[(size_t)(x >> 1) + (size_t)H * ((size_t)(y >> 1) + (size_t)H * (z >> 1))];
-    uint32_t so = co[(size_t)(xo >> 1) + (size_t)H * ((size_t)(yo >> 1) + (size_t)H * (zo >> 1))];
-    uint32_t eta = (uint32_t)tab[se * 8 + p] | (uint32_t)tab[so * 8 + (p ^ 7)];
-    for (int a = 0; a < 6; ++a) {
-      c12[c * 12 + a] = (int)((w >> (3 * a)) & 7u);
-      c12[c * 12 + 6 + a] = (int)((eta >> a) & 1u);
+  parallel_for(N, [&](long long b, long long e) {
+    for (long long c = b; c < e; ++c) {
+      int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
+      uint32_t w = ((x + y + z) & 1 ? cells1 : cells0)[word_index(L, x, y, z)];
+      int xo = (x & 1) ? x : (x + L - 1) % L, yo = (y & 1) ? y : (y + L - 1) % L, zo = (z & 1) ? z : (z + L - 1) % L;
+      int p = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+      uint32_t se = ce[(size_t)(x >> 1) + (size_t)H * ((size_t)(y >> 1) + (size_t)H * (z >> 1))];
+      uint32_t so = co[(size_t)(xo >> 1) + (size_t)H * ((size_t)(yo >> 1) + (size_t)H * (zo >> 1))];
+      uint32_t eta = (uint32_t)tab[se * 8 + p] | (uint32_t)tab[so * 8 + (p ^ 7)];
+      for (int a = 0; a < 6; ++a) {
+        c12[c * 12 + a] = (int)((w >> (3 * a)) & 7u);
+        c12[c * 12 + 6 + a] = (int)((eta >> a) & 1u);
+      }
     }
-  }
+  });
 }
 
 }  // namespace cvf
