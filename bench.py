@@ -42,6 +42,13 @@ def dist_env():
     return rank, world, local
 
 
+def replica_params(rank, local=0):
+    """The lattice rank `rank` steps: the L=256 workload with its own seed and replica id, so the
+    ranks' chains are independent and need no collective (weak scaling, replicas only)."""
+    from cvfbulkwater_gb300.engine import Params
+    return Params(L=L_BENCH, T=T_BENCH, P=P_BENCH, seed=SEED + rank, start=2, replica=rank, device=local)
+
+
 class Dist:
     """Barrier and max-over-ranks on a CPU (gloo) group; a no-op for one process."""
 
@@ -136,10 +143,10 @@ def ncu_traffic(name):
         return None
 
 
-def cpu_baseline_oracle(steps_cap=3, budget_s=30.0):
-    """The CPU oracle on all host cores over a bounded sample of the same workload."""
+def cpu_baseline_oracle(steps_cap=3, budget_s=30.0, threads=None):
+    """The CPU oracle on all host cores (or `threads`) over a bounded sample of the same workload."""
     from oracle import oracle as O
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     o = O.Oracle(L_BENCH, T_BENCH, P_BENCH, SEED, 6.0, 0, 2, threads=threads)
     o.step(1, 0)  # warm-up
     t0 = time.perf_counter()
@@ -220,6 +227,29 @@ def bench_batch64(steps, warmup, local, flush, verify=4):
             "l2": "256 MB write before every timed step in both arms"}
 
 
+def bench_plain_l16(steps, warmup, local, flush):
+    """Plain small run: L=16, disordered start, T=0.815, P=0.45, 1 sweep + volume + cube per step.
+    Launch-latency bound, so the per-step time inside a 32-step graph replay is reported too."""
+    import torch
+    from cvfbulkwater_gb300.engine import Lattice, Params
+    lat = Lattice(Params(L=16, T=0.815, P=0.45, seed=SEED, start=0, device=local))
+    lat.run(warmup, 1, 0)
+    lat.synchronize()
+    ms = timed_steps(lat, steps, flush)
+    stream = torch.cuda.ExternalStream(lat.stream_ptr())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        lat.run(32 * 20, 1, 0)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    replay_us = e0.elapsed_time(e1) * 1e3 / 640
+    lat.close()
+    return {"workload": "L=16 disordered start, T=0.815, P=0.45, 1 cube + 1 volume move + 1 sweep per step",
+            "steps_per_s": round(steps / (ms / 1e3), 1), "site_updates_per_ns": round(4096 * steps / (ms * 1e6), 4),
+            "graph_replay_us_per_step": round(replay_us, 3)}
+
+
 def bench_sw(steps, warmup, local, flush):
     """Swendsen-Wang path: L=64 and L=128, T=0.60 and 0.75, P=0.45, disordered start,
     Cluster_Steps=1, Metropolis_Steps=0 (each step: cube move, volume move, one SW step)."""
@@ -275,7 +305,7 @@ def run_engine(args):
     torch.cuda.set_device(local)
     L = L_BENCH
     N = L ** 3
-    lat = Lattice(Params(L=L, T=T_BENCH, P=P_BENCH, seed=SEED + rank, start=2, replica=rank, device=local))
+    lat = Lattice(replica_params(rank, local))
     stream = torch.cuda.ExternalStream(lat.stream_ptr(), device=local)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
@@ -353,6 +383,9 @@ def run_engine(args):
     if rank == 0 and world == 1 and not args.no_extras:
         extras["batched"] = bench_batch64(max(10, min(args.steps, 50)), args.warmup, local, flush)
         extras["swendsen_wang"] = bench_sw(max(10, min(args.steps, 30)), args.warmup, local, flush)
+        extras["plain_l16"] = bench_plain_l16(max(10, min(args.steps, 50)), args.warmup, local, flush)
+        if not args.no_cpu_baseline:
+            extras["cpu_baseline_1thread"] = cpu_baseline_oracle(steps_cap=1, budget_s=10.0, threads=1)
 
     peak, peak_kind = peaks()
     achieved = alg_bytes_launch / launch_s / 1e9

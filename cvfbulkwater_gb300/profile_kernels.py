@@ -3,8 +3,9 @@
   python -m cvfbulkwater_gb300.profile_kernels --L 256 --kind sweep --launches 2
 
 Creates one lattice (ordered start, T=0.70, P=0.45), runs --warmup full Monte Carlo steps
-(4 launches each: volume move, cube move, two sweep colours) and then --launches profiled
-repetitions of the chosen kind through cvf_profile_launch (sweep = 2 launches per repetition).
+and then --launches profiled repetitions of the chosen kind: a single kernel kind through
+cvf_profile_launch (sweep = 2 launches per repetition), or whole steps (kind "step": cube +
+volume + sweep; kind "step_sw": cube + volume + one Swendsen-Wang step).
 Prints the mean time per repetition measured with CUDA events on the engine's stream.
 """
 from __future__ import annotations
@@ -13,12 +14,13 @@ import argparse
 import ctypes as C
 
 KINDS = {"sweep": 0, "cube": 1, "volume": 2, "measure": 3}
+STEPS = {"step": (1, 0), "step_sw": (0, 1)}  # full MC steps: (Metropolis sweeps, SW steps)
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--L", type=int, default=256)
-    ap.add_argument("--kind", default="sweep", choices=sorted(KINDS))
+    ap.add_argument("--kind", default="sweep", choices=sorted(KINDS) + sorted(STEPS))
     ap.add_argument("--launches", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--start", type=int, default=2)
@@ -31,14 +33,18 @@ def main():
     from .engine import Lattice, Params
     build.build()
     lat = Lattice(Params(L=a.L, T=a.T, P=a.P, seed=44648604, start=a.start))
-    lat.run(a.warmup, 1, 0)
+    nmet, ncl = STEPS.get(a.kind, (1, 0))
+    lat.run(a.warmup, nmet, ncl)
     lat.synchronize()
     sp = C.c_void_p()
     abi.check(abi.lib().cvf_get_stream(lat._h, C.byref(sp)))
     s = torch.cuda.ExternalStream(sp.value)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(s)
-    abi.check(abi.lib().cvf_profile_launch(lat._h, KINDS[a.kind], a.launches))
+    if a.kind in STEPS:
+        lat.run(a.launches, nmet, ncl)
+    else:
+        abi.check(abi.lib().cvf_profile_launch(lat._h, KINDS[a.kind], a.launches))
     e1.record(s)
     torch.cuda.synchronize()
     print(f"L={a.L} kind={a.kind} repetitions={a.launches} ms/rep={e0.elapsed_time(e1) / max(a.launches, 1):.4f}")
