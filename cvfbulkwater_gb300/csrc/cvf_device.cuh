@@ -90,7 +90,8 @@ struct BatchDev {
   int* blk_cube;
   int* blk_cell;        // one thread per cell
   int* blk_site;        // one thread per arm site (6N)
-  int nblk_sweep, nblk_cube, nblk_cell, nblk_site;
+  int* blk_site4;       // one thread per 4 arm sites
+  int nblk_sweep, nblk_cube, nblk_cell, nblk_site, nblk_site4;
 };
 
 constexpr int kThreads = 256;

@@ -105,32 +105,32 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
     }
   }
   R.hbmask[c] = (uint8_t)hb;
-  uint32_t adj[6] = {0, 0, 0, 0, 0, 0};
+  // intra-cell bonds: bit l-3 for link l = 3..17, pairs (a<b) in row-major order
+  uint32_t bm = 0;
   int l = 3;
 #pragma unroll
   for (int a = 0; a < 5; ++a)
 #pragma unroll
     for (int b = a + 1; b < 6; ++b, ++l) {
-      bool bond = ((w >> (3 * a)) & 7u) == ((w >> (3 * b)) & 7u) && (unsigned long long)rw[l] < ts;
-      if (bond) {
-        adj[a] |= 1u << b;
-        adj[b] |= 1u << a;
-      }
+      const bool bond = ((w >> (3 * a)) & 7u) == ((w >> (3 * b)) & 7u) && (unsigned long long)rw[l] < ts;
+      bm |= (uint32_t)bond << (l - 3);
     }
-#pragma unroll
-  for (int a = 0; a < 6; ++a) {
-    uint32_t m = 1u << a;
-#pragma unroll
-    for (int it = 0; it < 5; ++it) {
-      uint32_t nm = m;
-#pragma unroll
-      for (int b = 0; b < 6; ++b)
-        if ((m >> b) & 1u) nm |= adj[b];
-      m = nm;
-    }
-    int root = __ffs(m) - 1;
-    R.label[a * N + c] = (int32_t)(root * N + c);
+  // in-cell components: lab holds 3 bits per arm, the smallest arm of its component; merging
+  // two components rewrites every field equal to the larger minimum with the smaller one
+  const unsigned long long kPairA = 0x11b491248000ull, kPairB = 0x16cb1d8d58d1ull;  // e -> (a, b), 3 bits each
+  uint32_t lab = 0x2c688u;  // fields 0,1,2,3,4,5
+  while (bm) {
+    const int e = __ffs(bm) - 1;
+    bm &= bm - 1u;
+    const uint32_t a = (uint32_t)(kPairA >> (3 * e)) & 7u, b = (uint32_t)(kPairB >> (3 * e)) & 7u;
+    const uint32_t la = (lab >> (3 * a)) & 7u, lb = (lab >> (3 * b)) & 7u;
+    const uint32_t lo = la < lb ? la : lb, hi = la < lb ? lb : la;
+    const uint32_t x = lab ^ (hi * 0x9249u);
+    const uint32_t m7 = (~(x | (x >> 1) | (x >> 2)) & 0x9249u) * 7u;
+    lab = (lab & ~m7) | ((lo * 0x9249u) & m7);
   }
+#pragma unroll
+  for (int a = 0; a < 6; ++a) R.label[a * N + c] = (int32_t)(((lab >> (3 * a)) & 7u) * N + c);
 }
 
 // ---------------------------------------------------------------- union-find
@@ -202,22 +202,33 @@ __global__ void __launch_bounds__(kThreads) k_sw_compress(const ReplicaDesc* __r
   R.label[s] = x;
 }
 
-// GW:2531-2542: every cluster gets one uniform shift in 0..5, drawn from its root's stream.
+// GW:2531-2542: every cluster gets one uniform shift in 0..5. Thread = 4 consecutive sites; the
+// shift of root i is an exact uniform from word (i & 3) of the flip block of counter i >> 2
+// (retry streams of site i on a rejection).
 __global__ void __launch_bounds__(kThreads) k_sw_roots(const ReplicaDesc* __restrict__ reps,
                                                        const ReplicaState* __restrict__ st,
                                                        const int* __restrict__ blk, int nrep, int jsw) {
   const int r = find_replica_sw(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
-  const long long NS = 6LL * R.L * R.L * R.L;
-  long long s = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
-  if (s >= NS) return;
-  if (R.label[s] != (int32_t)s) return;
+  const uint32_t NS4 = (uint32_t)(6LL * R.L * R.L * R.L / 4);
+  const uint32_t q = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  if (q >= NS4) return;
+  const int4 lab = reinterpret_cast<const int4*>(R.label)[q];
+  const uint32_t s0 = 4u * q;
+  const bool root[4] = {lab.x == (int)s0, lab.y == (int)(s0 + 1), lab.z == (int)(s0 + 2), lab.w == (int)(s0 + 3)};
+  if (!(root[0] | root[1] | root[2] | root[3])) return;
   const uint32_t t = st[r].cur[3] + (uint32_t)jsw;
-  U4 q = philox((uint32_t)s, t, kStSwFlip, R.replica, R.key0, R.key1);
-  uint32_t k;
-  if (!lemire_try(q.x, 6, k) && !lemire_try(q.y, 6, k) && !lemire_try(q.z, 6, k) && !lemire_try(q.w, 6, k))
-    k = lemire_retry(6, (uint32_t)s, t, kStSwFlip, R.replica, R.key0, R.key1);
-  R.shift[s] = (uint8_t)k;
+  const U4 qq = philox(q, t, kStSwFlip, R.replica, R.key0, R.key1);
+  const uint32_t words[4] = {qq.x, qq.y, qq.z, qq.w};
+  uint32_t out = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (!root[k]) continue;
+    uint32_t v;
+    if (!lemire_try(words[k], 6, v)) v = lemire_retry(6, s0 + k, t, kStSwFlip, R.replica, R.key0, R.key1);
+    out |= v << (8 * k);
+  }
+  reinterpret_cast<uint32_t*>(R.shift)[q] = out;
 }
 
 __global__ void __launch_bounds__(kThreads) k_sw_apply(const ReplicaDesc* __restrict__ reps,
@@ -424,7 +435,7 @@ void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s) {
   k_sw_local<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.st, b.blk_cell, b.nrep, jsw);
   k_sw_union<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.st, b.blk_cell, b.nrep);
   k_sw_compress<<<b.nblk_site, kThreads, 0, s>>>(b.reps, b.blk_site, b.nrep);
-  k_sw_roots<<<b.nblk_site, kThreads, 0, s>>>(b.reps, b.st, b.blk_site, b.nrep, jsw);
+  k_sw_roots<<<b.nblk_site4, kThreads, 0, s>>>(b.reps, b.st, b.blk_site4, b.nrep, jsw);
   k_sw_apply<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.blk_cell, b.nrep);
 }
 

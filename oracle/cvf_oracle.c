@@ -672,12 +672,14 @@ void oracle_sw_step(oracle_t* o)
                     uf_union(p, (int32_t)(a * N + c), (int32_t)(b * N + c));
     }
     for (int64_t i = 0; i < NS; ++i) p[i] = uf_find(p, (int32_t)i);
+    /* the shift of root i is an exact uniform in [0,6) from word (i & 3) of the flip block of
+     * sites 4*(i>>2)..4*(i>>2)+3, falling back to the retry streams of site i */
     uint8_t* shift = (uint8_t*)malloc(NS > 0 ? (size_t)NS : 1);
     for (int64_t i = 0; i < NS; ++i) {
         if (p[i] != i) continue;
         uint32_t r[4];
-        rng(o, (uint32_t)i, t, ST_SW_FLIP, r);
-        shift[i] = (uint8_t)draw_below(o, 6, r, 4, (uint32_t)i, t, ST_SW_FLIP);
+        rng(o, (uint32_t)(i >> 2), t, ST_SW_FLIP, r);
+        shift[i] = (uint8_t)draw_below(o, 6, &r[i & 3], 1, (uint32_t)i, t, ST_SW_FLIP);
     }
     for (int64_t i = 0; i < NS; ++i) o->s[i] = (uint8_t)((o->s[i] + shift[p[i]]) % Q);
     free(shift);
