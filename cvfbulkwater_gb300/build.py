@@ -70,6 +70,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
                "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off"] + ARCH + inc
         if verbose:
             cmd += ["-Xptxas", "-v"]
+        cmd += os.environ.get("CVF_NVCC_EXTRA", "").split()  # tuning experiments only
         jobs.append((obj, cmd))
     for f in CPP + DRIVER:
         obj = os.path.join(BUILD, f + ".o")

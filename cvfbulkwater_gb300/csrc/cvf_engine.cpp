@@ -76,7 +76,7 @@ static int build_tables(cvf_handle* h, int force_vec = 0) {
   int vec = 4;
   if (const char* ev = getenv("CVF_SWEEP_VEC")) {
     int v = atoi(ev);
-    if (v == 1 || v == 2 || v == 4) vec = v;
+    if (v == 1 || v == 2 || v == 4 || v == 8) vec = v;
   }
   if (force_vec) vec = force_vec;
   for (auto& r : h->reps) {
@@ -603,7 +603,7 @@ int cvf_autotune(cvf_handle* h, int* vec_out) {
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
   std::vector<int> cands;
-  for (int v : {4, 2, 1}) {
+  for (int v : {8, 4, 2, 1}) {
     bool ok = true;
     for (auto& r : h->reps) ok = ok && (r.H % v == 0);
     if (ok) cands.push_back(v);

@@ -295,8 +295,23 @@ struct VecLoad<4> {
     *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
   }
 };
+template <>
+struct VecLoad<8> {
+  static __device__ __forceinline__ void ld(const uint32_t* p, uint32_t* w) {
+    VecLoad<4>::ld(p, w);
+    VecLoad<4>::ld(p + 4, w + 4);
+  }
+  static __device__ __forceinline__ void st(uint32_t* p, const uint32_t* w) {
+    VecLoad<4>::st(p, w);
+    VecLoad<4>::st(p + 4, w + 4);
+  }
+};
 template <int V>
 struct Log2V;
+template <>
+struct Log2V<8> {
+  static constexpr int v = 3;
+};
 template <>
 struct Log2V<1> {
   static constexpr int v = 0;
@@ -496,8 +511,14 @@ __device__ __forceinline__ const WarpTables* warp_tables(const ReplicaDesc& R, W
 // One colour of the checkerboard sweep: every cell with (x+y+z)&1 == colour updates its six
 // arms; its six neighbours have the other colour and stay frozen. Thread = V consecutive
 // colour cells of one row, read and written with 128-bit accesses when V = 4.
+// Resident blocks per SM the register allocation must allow: 4 (64 registers) for tiles up to 4
+// cells, 3 (80 registers, no spills) for the 8-cell tile.
 template <int V>
-__global__ void __launch_bounds__(kThreads) k_sweep(const ReplicaDesc* __restrict__ reps,
+struct SweepMinBlocks {
+  static constexpr int v = V >= 8 ? 3 : 4;
+};
+template <int V>
+__global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const ReplicaDesc* __restrict__ reps,
                                                     const ReplicaState* __restrict__ st,
                                                     const int* __restrict__ blk, int nrep, int colour, int jsweep) {
   __shared__ WarpTables s_tab[kThreads / 32];
@@ -649,6 +670,7 @@ void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStre
 
 void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s) {
   switch (b.vec) {
+    case 8: k_sweep<8><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
     case 4: k_sweep<4><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
     case 2: k_sweep<2><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
     default: k_sweep<1><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
@@ -658,6 +680,7 @@ void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s) {
 void launch_measure(const BatchDev& b, int record, cudaStream_t s) {
   k_measure_begin<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep);
   switch (b.vec) {
+    case 8: k_measure<8><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep); break;
     case 4: k_measure<4><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep); break;
     case 2: k_measure<2><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep); break;
     default: k_measure<1><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep); break;

@@ -175,7 +175,7 @@ int cvf_format_data_line(char* buf, int cap, int t, const cvf_obs* o);
 int cvf_format_cluster_line(char* buf, int cap, int t, const cvf_cstats* c);
 
 /* Autotuner: times the checkerboard sweep kernel on this handle's replicas for every supported
- * cells-per-thread tile (1, 2 or 4 consecutive colour cells: 32-, 64- or 128-bit accesses) and
+ * cells-per-thread tile (1, 2, 4 or 8 consecutive colour cells: 32-, 64-, 128- or 2x128-bit accesses) and
  * keeps the fastest. The lattices are saved before and restored after, so the Markov chains are
  * unchanged (the tile only changes the thread mapping, never the result). vec_out may be NULL.
  * No reference counterpart. */
