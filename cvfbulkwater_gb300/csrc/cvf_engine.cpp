@@ -55,7 +55,22 @@ struct cvf_handle {
   bool sw_done = false;
   unsigned long long* blocktop = nullptr;
   std::map<std::tuple<int, int, int, int>, cudaGraphExec_t> graphs;
+  void* staging = nullptr;  // pinned host buffer for configuration transfers (lazily allocated)
+  size_t staging_bytes = 0;
 };
+
+// Pinned host staging for one replica's packed lattice (N words) and cube states (2 (L/2)^3 B).
+static int ensure_staging(cvf_handle* h, const ReplicaHost& R) {
+  size_t need = (size_t)R.N * 4 + 2 * (size_t)R.H * R.H * R.H;
+  if (h->staging_bytes >= need) return 0;
+  if (h->staging) cudaFreeHost(h->staging);
+  h->staging = nullptr;
+  h->staging_bytes = 0;
+  cudaError_t e = cudaHostAlloc(&h->staging, need, cudaHostAllocDefault);
+  if (e != cudaSuccess) return fail(CVF_ENOMEM, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+  h->staging_bytes = need;
+  return 0;
+}
 
 static int dev_alloc(cvf_handle* h, void** p, size_t bytes) {
   cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
@@ -328,6 +343,7 @@ int cvf_destroy(cvf_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
   for (void* p : h->allocs) cudaFree(p);
+  if (h->staging) cudaFreeHost(h->staging);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return 0;
@@ -339,16 +355,21 @@ int cvf_set_config(cvf_handle* h, int r, const int* c12, long long n_cells) {
   if (int rc = check_rep(h, r)) return rc;
   ReplicaHost& R = h->reps[r];
   if (!c12 || n_cells != R.N) return fail(CVF_EINVAL, "cells12 must hold 12 ints for each of the N cells");
-  std::vector<uint32_t> c0, c1;
-  std::vector<uint8_t> ce, co;
-  std::string err;
-  if (!pack_config(R.L, c12, c0, c1, ce, co, err)) return fail(CVF_ECONFIG, err);
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
-  CK(cudaMemcpy(R.desc.cells[0], c0.data(), c0.size() * 4, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(R.desc.cells[1], c1.data(), c1.size() * 4, cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(R.desc.cubes[0], ce.data(), ce.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(R.desc.cubes[1], co.data(), co.size(), cudaMemcpyHostToDevice));
+  if (int rc = ensure_staging(h, R)) return rc;
+  const size_t half = (size_t)(R.N / 2), nc = (size_t)R.H * R.H * R.H;
+  uint32_t* c0 = (uint32_t*)h->staging;
+  uint32_t* c1 = c0 + half;
+  uint8_t* ce = (uint8_t*)(c1 + half);
+  uint8_t* co = ce + nc;
+  std::string err;
+  if (!pack_config(R.L, c12, c0, c1, ce, co, err)) return fail(CVF_ECONFIG, err);
+  CK(cudaMemcpyAsync(R.desc.cells[0], c0, half * 4, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(R.desc.cells[1], c1, half * 4, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(R.desc.cubes[0], ce, nc, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(R.desc.cubes[1], co, nc, cudaMemcpyHostToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));  // the staging buffer is reused by the next call
   return 0;
 }
 
@@ -358,12 +379,17 @@ int cvf_get_config(cvf_handle* h, int r, int* c12, long long n_cells) {
   if (!c12 || n_cells != R.N) return fail(CVF_EINVAL, "cells12 must hold 12 ints for each of the N cells");
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
-  std::vector<uint32_t> c0((size_t)(R.N / 2)), c1((size_t)(R.N / 2));
-  std::vector<uint8_t> ce((size_t)R.H * R.H * R.H), co(ce.size());
-  CK(cudaMemcpy(c0.data(), R.desc.cells[0], c0.size() * 4, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(c1.data(), R.desc.cells[1], c1.size() * 4, cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(ce.data(), R.desc.cubes[0], ce.size(), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(co.data(), R.desc.cubes[1], co.size(), cudaMemcpyDeviceToHost));
+  if (int rc = ensure_staging(h, R)) return rc;
+  const size_t half = (size_t)(R.N / 2), nc = (size_t)R.H * R.H * R.H;
+  uint32_t* c0 = (uint32_t*)h->staging;
+  uint32_t* c1 = c0 + half;
+  uint8_t* ce = (uint8_t*)(c1 + half);
+  uint8_t* co = ce + nc;
+  CK(cudaMemcpyAsync(c0, R.desc.cells[0], half * 4, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(c1, R.desc.cells[1], half * 4, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(ce, R.desc.cubes[0], nc, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(co, R.desc.cubes[1], nc, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
   unpack_config(R.L, c0, c1, ce, co, c12);
   return 0;
 }

@@ -115,33 +115,33 @@ static void parallel_for(long long n, F body) {
   for (auto& t : th) t.join();
 }
 
-bool pack_config(int L, const int* c12, std::vector<uint32_t>& cells0, std::vector<uint32_t>& cells1,
-                 std::vector<uint8_t>& ce, std::vector<uint8_t>& co, std::string& err) {
+bool pack_config(int L, const int* c12, uint32_t* cells0, uint32_t* cells1, uint8_t* ce, uint8_t* co,
+                 std::string& err) {
   const int H = L / 2;
   const long long N = (long long)L * L * L;
-  cells0.assign((size_t)(N / 2), 0);
-  cells1.assign((size_t)(N / 2), 0);
-  ce.assign((size_t)H * H * H, 0);
-  co.assign((size_t)H * H * H, 0);
   // first offending cell, if any (smallest index wins, as in a sequential reader)
   std::atomic<long long> bad{N};
-  parallel_for(N, [&](long long b, long long e) {
-    for (long long c = b; c < e; ++c) {
-      int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
-      uint32_t w = 0;
-      bool ok = true;
-      for (int a = 0; a < 6; ++a) {
-        int s = c12[c * 12 + a], t = c12[c * 12 + 6 + a];
-        ok = ok && s >= 0 && s <= 5 && t >= 0 && t <= 1;
-        w |= (uint32_t)(s & 7) << (3 * a);
-      }
-      if (!ok) {
-        long long cur = bad.load();
-        while (c < cur && !bad.compare_exchange_weak(cur, c)) {
+  parallel_for((long long)L * L, [&](long long b, long long e) {
+    for (long long row = b; row < e; ++row) {
+      const int y = (int)(row % L), z = (int)(row / L);
+      const long long c_row = row * L;
+      uint32_t* dst[2] = {cells0 + (size_t)H * row, cells1 + (size_t)H * row};
+      for (int x = 0; x < L; ++x) {
+        const int* v = c12 + (c_row + x) * 12;
+        uint32_t w = 0;
+        bool ok = true;
+        for (int a = 0; a < 6; ++a) {
+          ok = ok && v[a] >= 0 && v[a] <= 5 && v[6 + a] >= 0 && v[6 + a] <= 1;
+          w |= (uint32_t)(v[a] & 7) << (3 * a);
         }
-        break;
+        if (!ok) {
+          long long c = c_row + x, cur = bad.load();
+          while (c < cur && !bad.compare_exchange_weak(cur, c)) {
+          }
+          return;
+        }
+        dst[(x + y + z) & 1][x >> 1] = w;
       }
-      ((x + y + z) & 1 ? cells1 : cells0)[word_index(L, x, y, z)] = w;
     }
   });
   if (bad.load() < N) {
@@ -169,7 +169,7 @@ bool pack_config(int L, const int* c12, std::vector<uint32_t>& cells0, std::vect
       for (int bb = 0; bb < H; ++bb)
         for (int a = 0; a < H; ++a) {
           int x = 2 * a + par, y = 2 * bb + par, z = 2 * c + par;
-          int xp = (x + 1) % L, yp = (y + 1) % L, zp = (z + 1) % L;
+          int xp = x + 1 == L ? 0 : x + 1, yp = y + 1 == L ? 0 : y + 1, zp = z + 1 == L ? 0 : z + 1;
           int st;
           if (eta(0, x, y, z) == 0) {
             if (eta(0, x, yp, zp) == 0) st = 2;
@@ -191,25 +191,30 @@ bool pack_config(int L, const int* c12, std::vector<uint32_t>& cells0, std::vect
   return true;
 }
 
-void unpack_config(int L, const std::vector<uint32_t>& cells0, const std::vector<uint32_t>& cells1,
-                   const std::vector<uint8_t>& ce, const std::vector<uint8_t>& co, int* c12) {
+void unpack_config(int L, const uint32_t* cells0, const uint32_t* cells1, const uint8_t* ce, const uint8_t* co,
+                   int* c12) {
   const int H = L / 2;
-  const long long N = (long long)L * L * L;
   uint8_t tab[72];
   for (int s = 0; s < 9; ++s)
     for (int p = 0; p < 8; ++p) tab[s * 8 + p] = (uint8_t)cube_eta_bits(s, p);
-  parallel_for(N, [&](long long b, long long e) {
-    for (long long c = b; c < e; ++c) {
-      int x = (int)(c % L), y = (int)((c / L) % L), z = (int)(c / ((long long)L * L));
-      uint32_t w = ((x + y + z) & 1 ? cells1 : cells0)[word_index(L, x, y, z)];
-      int xo = (x & 1) ? x : (x + L - 1) % L, yo = (y & 1) ? y : (y + L - 1) % L, zo = (z & 1) ? z : (z + L - 1) % L;
-      int p = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
-      uint32_t se = ce[(size_t)(x >> 1) + (size_t)H * ((size_t)(y >> 1) + (size_t)H * (z >> 1))];
-      uint32_t so = co[(size_t)(xo >> 1) + (size_t)H * ((size_t)(yo >> 1) + (size_t)H * (zo >> 1))];
-      uint32_t eta = (uint32_t)tab[se * 8 + p] | (uint32_t)tab[so * 8 + (p ^ 7)];
-      for (int a = 0; a < 6; ++a) {
-        c12[c * 12 + a] = (int)((w >> (3 * a)) & 7u);
-        c12[c * 12 + 6 + a] = (int)((eta >> a) & 1u);
+  parallel_for((long long)L * L, [&](long long b, long long e) {
+    for (long long row = b; row < e; ++row) {
+      const int y = (int)(row % L), z = (int)(row / L);
+      const int yo = (y & 1) ? y : (y + L - 1) % L, zo = (z & 1) ? z : (z + L - 1) % L;
+      const uint32_t* src[2] = {cells0 + (size_t)H * row, cells1 + (size_t)H * row};
+      const uint8_t* erow = ce + (size_t)H * ((size_t)(y >> 1) + (size_t)H * (z >> 1));
+      const uint8_t* orow = co + (size_t)H * ((size_t)(yo >> 1) + (size_t)H * (zo >> 1));
+      int* out = c12 + row * L * 12;
+      for (int x = 0; x < L; ++x) {
+        const uint32_t w = src[(x + y + z) & 1][x >> 1];
+        const int xo = (x & 1) ? x : (x + L - 1) % L;
+        const int p = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+        const uint32_t eta = (uint32_t)tab[erow[x >> 1] * 8 + p] | (uint32_t)tab[orow[xo >> 1] * 8 + (p ^ 7)];
+        int* v = out + 12 * x;
+        for (int a = 0; a < 6; ++a) {
+          v[a] = (int)((w >> (3 * a)) & 7u);
+          v[6 + a] = (int)((eta >> a) & 1u);
+        }
       }
     }
   });

@@ -29,11 +29,12 @@ void fill_obs(cvf_obs* o, long long n_hb2, long long n_sigma, double r_cell, dou
               long long N, float P);
 void fill_cstats(cvf_cstats* c);
 
-// cells12 (config.out order) -> colour-split words and cube states; returns false on a value
-// out of range. eta is read with the decision tree of GW:3314-3371.
-bool pack_config(int L, const int* cells12, std::vector<uint32_t>& cells0, std::vector<uint32_t>& cells1,
-                 std::vector<uint8_t>& cubes_even, std::vector<uint8_t>& cubes_odd, std::string& err);
-void unpack_config(int L, const std::vector<uint32_t>& cells0, const std::vector<uint32_t>& cells1,
-                   const std::vector<uint8_t>& cubes_even, const std::vector<uint8_t>& cubes_odd, int* cells12);
+// cells12 (config.out order) -> colour-split words (cells0/cells1: N/2 words each) and cube
+// states (cubes_even/cubes_odd: (L/2)^3 bytes each); returns false on a value out of range.
+// eta is read with the decision tree of GW:3314-3371. Threaded over rows of the lattice.
+bool pack_config(int L, const int* cells12, uint32_t* cells0, uint32_t* cells1, uint8_t* cubes_even,
+                 uint8_t* cubes_odd, std::string& err);
+void unpack_config(int L, const uint32_t* cells0, const uint32_t* cells1, const uint8_t* cubes_even,
+                   const uint8_t* cubes_odd, int* cells12);
 
 }  // namespace cvf
