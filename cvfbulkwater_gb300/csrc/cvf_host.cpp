@@ -96,12 +96,13 @@ static inline size_t word_index(int L, int x, int y, int z) {
   return (size_t)(x >> 1) + (size_t)H * ((size_t)y + (size_t)L * z);
 }
 
-// Runs body(begin, end) over [0, n) split across up to 16 host threads.
+// Runs body(begin, end) over [0, n) split across up to 16 host threads; `work` is the total
+// amount of work (elements touched), below 2^16 of which the call stays on the calling thread.
 template <class F>
-static void parallel_for(long long n, F body) {
+static void parallel_for(long long n, long long work, F body) {
   unsigned hw = std::thread::hardware_concurrency();
   int nt = (int)std::min<unsigned>(hw ? hw : 1u, 16u);
-  if (n < (1 << 16) || nt <= 1) {
+  if (work < (1 << 16) || nt <= 1 || n < 2) {
     body(0LL, n);
     return;
   }
@@ -121,7 +122,7 @@ bool pack_config(int L, const int* c12, uint32_t* cells0, uint32_t* cells1, uint
   const long long N = (long long)L * L * L;
   // first offending cell, if any (smallest index wins, as in a sequential reader)
   std::atomic<long long> bad{N};
-  parallel_for((long long)L * L, [&](long long b, long long e) {
+  parallel_for((long long)L * L, N, [&](long long b, long long e) {
     for (long long row = b; row < e; ++row) {
       const int y = (int)(row % L), z = (int)(row / L);
       const long long c_row = row * L;
@@ -163,7 +164,7 @@ bool pack_config(int L, const int* c12, uint32_t* cells0, uint32_t* cells1, uint
   };
   // cube states from eta with the decision tree of GW:3330-3369 (vertices v1 = origin, v2 x+1,
   // v3 y+1, v6 y+1 z+1, v7 x+1 z+1, v8 x+1 y+1)
-  parallel_for(2LL * H, [&](long long b, long long e) {
+  parallel_for(2LL * H, N / 4, [&](long long b, long long e) {
     for (long long pc = b; pc < e; ++pc) {
       int par = (int)(pc / H), c = (int)(pc % H);
       for (int bb = 0; bb < H; ++bb)
@@ -197,7 +198,7 @@ void unpack_config(int L, const uint32_t* cells0, const uint32_t* cells1, const 
   uint8_t tab[72];
   for (int s = 0; s < 9; ++s)
     for (int p = 0; p < 8; ++p) tab[s * 8 + p] = (uint8_t)cube_eta_bits(s, p);
-  parallel_for((long long)L * L, [&](long long b, long long e) {
+  parallel_for((long long)L * L, (long long)L * L * L, [&](long long b, long long e) {
     for (long long row = b; row < e; ++row) {
       const int y = (int)(row % L), z = (int)(row / L);
       const int yo = (y & 1) ? y : (y + L - 1) % L, zo = (z & 1) ? z : (z + L - 1) % L;

@@ -477,9 +477,10 @@ __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32
     const int idx = 11 * dhb + (int)((h >> (4 * n)) & 15u) - (int)((h >> (4 * o)) & 15u) + 17;
     const uint32_t tv = tvt[idx];
     const uint32_t word = a < 2 ? rr.y : (a < 4 ? rr.z : rr.w);
-    const uint32_t u2 = (a & 1) ? ((word >> 15) & 0x1fffeu) : ((word << 1) & 0x1fffeu);
-    tie |= (u2 + 1u == tv);
-    if (u2 + 2u <= tv) {
+    const int hu = (int)((a & 1) ? (word >> 16) : (word & 0xffffu));
+    const int d = (int)tv - 2 * hu;  // accept: 2 hu + 2 <= tv; tie: 2 hu + 1 == tv
+    tie |= (d == 1);
+    if (d >= 2) {
       w = (w & ~(7u << (3 * a))) | (n << (3 * a));
       h += (1u << (4 * n)) - (1u << (4 * o));
     }

@@ -81,8 +81,11 @@ class Lattice:
         a = np.ascontiguousarray(cells12, dtype=np.int32)
         check(lib().cvf_set_config(self._h, r, _ptr(a), a.size // 12))
 
-    def get_config(self, r: int = 0) -> np.ndarray:
-        a = np.zeros((self.N(r), 12), dtype=np.int32)
+    def get_config(self, r: int = 0, out: np.ndarray = None) -> np.ndarray:
+        """cells12 of replica r; pass `out` (int32, (N, 12), C-contiguous) to reuse a buffer."""
+        a = np.empty((self.N(r), 12), dtype=np.int32) if out is None else out
+        if a.dtype != np.int32 or a.shape != (self.N(r), 12) or not a.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous int32 array of shape (N, 12)")
         check(lib().cvf_get_config(self._h, r, _ptr(a), self.N(r)))
         return a
 
