@@ -451,62 +451,117 @@ __device__ __noinline__ uint32_t sweep_cell_exact(uint32_t w, uint32_t nbs, uint
   return w;
 }
 
-// Metropolis update of the six arms of one cell, arms in order 0..5 (GW:1964-2007 energy change,
-// chessboard branch). Proposal of arm a: the a-th most significant base-6 digit of the uniform
-// word u (the high word of u*6 in a multiply chain). tv[i] = 2*(T_i >> 16) + ((T_i & 0xffff) != 0)
-// with i = 11*dN_hb + (h_new - h_old) + 17, so "accept" is 2*hu + 2 <= tv and a tie on the high
-// 16 bits is 2*hu + 1 == tv. nbe holds per arm the facing neighbour sigma, or 7 where eta_a = 0,
-// so dN_hb = [new == nbe] - [old == nbe]. A proposal equal to the old value lands on entry 17
-// (dN = 0 up to -J_sigma), which always accepts and changes nothing, so it needs no test.
-__device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32_t nbe, uint32_t eta, const U4& rr,
-                                                uint32_t c0, uint32_t t, const ReplicaDesc& R, const uint32_t* tvt) {
-  uint32_t u = rr.x;
-  if (u * 46656u < 2560u) u = sweep_proposal_retry(c0, t, R.replica, R.key0, R.key1);
-  const uint32_t w0 = w;
-  uint32_t h = sigma_histogram(w);
-  uint32_t f = u;
-  bool tie = false;
-#pragma unroll
-  for (int a = 0; a < 6; ++a) {
-    const unsigned long long m = (unsigned long long)f * 6ull;
-    const uint32_t n = (uint32_t)(m >> 32);
-    f = (uint32_t)m;
-    const uint32_t o = (w >> (3 * a)) & 7u;
-    const uint32_t nb = (nbe >> (3 * a)) & 7u;
-    const int dhb = (int)(n == nb) - (int)(o == nb);
-    const int idx = 11 * dhb + (int)((h >> (4 * n)) & 15u) - (int)((h >> (4 * o)) & 15u) + 17;
-    const uint32_t tv = tvt[idx];
-    const uint32_t word = a < 2 ? rr.y : (a < 4 ? rr.z : rr.w);
-    const int hu = (int)((a & 1) ? (word >> 16) : (word & 0xffffu));
-    const int d = (int)tv - 2 * hu;  // accept: 2 hu + 2 <= tv; tie: 2 hu + 1 == tv
-    tie |= (d == 1);
-    if (d >= 2) {
-      w = (w & ~(7u << (3 * a))) | (n << (3 * a));
-      h += (1u << (4 * n)) - (1u << (4 * o));
-    }
-  }
-  if (tie) w = sweep_cell_exact(w0, nbs, eta, u, rr.y, rr.z, rr.w, c0, t, &R);
-  return w;
+// Byte select: byte i of the result is byte ((sel >> 4i) & 7) of the eight bytes {hi:lo}. Every
+// selector nibble used here is below 8 (no sign replication).
+__device__ __forceinline__ uint32_t prmt(uint32_t lo, uint32_t hi, uint32_t sel) {
+  uint32_t r;
+  asm("prmt.b32 %0, %1, %2, %3;" : "=r"(r) : "r"(lo), "r"(hi), "r"(sel));
+  return r;
 }
 
-// Warp-private shared-memory copies of the sweep tables (no block barrier: each warp fills and
-// reads its own copy). Layout per warp: tv[33], nbmask[64], eta_tab[72 bytes].
-struct WarpTables {
-  uint32_t tv[33];
+// Warp-private shared-memory tables (no block barrier: each warp fills and reads its own copy).
+// The measurement needs the eta tables only; the sweep adds its decision tables.
+//   nbmask  per 6-bit eta mask, the value 7 in the 3-bit field of every arm with eta = 0
+//   eta     cube state x vertex offset -> 6-bit eta mask
+struct EtaTables {
   uint32_t nbmask[64];
   uint8_t eta[72];
 };
+// Histograms are eight bytes {hi:lo} holding 4x the count of each sigma value 0..5 (bytes 6, 7
+// zero). All sweep tables index with at most 8 distinct entries of 8 bytes or a 33-word array, so
+// a warp's random lookups never conflict in a shared-memory bank.
+//   cnt[v]  4 at byte v (v = 0..5), zero for v = 6, 7: one arm of value v
+//   nbw[v]  44 at byte v (v = 0..5), zero for v = 6, 7 (7 marks an arm with eta = 0)
+//   tv[i]   2*(T_i >> 16) + ((T_i & 0xffff) != 0) for the threshold T_i of entry
+//           i = 11*dN_hb + (h_new - h_old) + 17
+struct SweepTables {
+  uint2 cnt[8];
+  uint2 nbw[8];
+  uint32_t tv[33];
+  EtaTables et;
+};
 
-__device__ __forceinline__ const WarpTables* warp_tables(const ReplicaDesc& R, WarpTables* all) {
-  WarpTables* wt = all + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
+__device__ __forceinline__ uint2 count_bytes(uint32_t v, uint32_t b) {
+  return v < 4 ? make_uint2(b << (8 * v), 0u) : (v < 6 ? make_uint2(0u, b << (8 * (v - 4))) : make_uint2(0u, 0u));
+}
+
+__device__ __forceinline__ void fill_eta_tables(const ReplicaDesc& R, EtaTables* et, int lane) {
+  et->nbmask[lane] = R.nbmask[lane];
+  et->nbmask[32 + lane] = R.nbmask[32 + lane];
+  if (lane < 18) reinterpret_cast<uint32_t*>(et->eta)[lane] = reinterpret_cast<const uint32_t*>(R.eta_tab)[lane];
+}
+
+__device__ __forceinline__ const EtaTables* warp_eta_tables(const ReplicaDesc& R, EtaTables* all) {
+  EtaTables* et = all + (threadIdx.x >> 5);
+  fill_eta_tables(R, et, threadIdx.x & 31);
+  __syncwarp();
+  return et;
+}
+
+__device__ __forceinline__ const SweepTables* warp_sweep_tables(const ReplicaDesc& R, SweepTables* all) {
+  SweepTables* wt = all + (threadIdx.x >> 5);
+  const uint32_t lane = threadIdx.x & 31;
+  fill_eta_tables(R, &wt->et, lane);
   wt->tv[lane] = R.tv[lane];
   if (lane == 0) wt->tv[32] = R.tv[32];
-  wt->nbmask[lane] = R.nbmask[lane];
-  wt->nbmask[32 + lane] = R.nbmask[32 + lane];
-  if (lane < 18) reinterpret_cast<uint32_t*>(wt->eta)[lane] = reinterpret_cast<const uint32_t*>(R.eta_tab)[lane];
+  if (lane < 8) {
+    wt->cnt[lane] = count_bytes(lane, 4u);
+    wt->nbw[lane] = count_bytes(lane, 44u);
+  }
   __syncwarp();
   return wt;
+}
+
+// Metropolis update of the six arms of one cell, arms in order 0..5 (GW:1964-2007 energy change,
+// chessboard branch). Proposal of arm a: the a-th most significant base-6 digit of the uniform
+// word u (the high word of u*6 in a multiply chain). The threshold entry is
+// i = 11*dN_hb + (h_new - h_old) + 17, with h the count of the cell's arms per sigma value and
+// dN_hb = [new == nb] - [old == nb] for the facing neighbour value nb (7 where eta_a = 0). Both
+// terms come from byte selects on G = 4h + 44*[v == nb]: the selector v + 0x7770 picks byte v
+// with zeros above it, so G[new] - G[old] + 68 is the byte offset 4i into tv. The proposal's
+// selector is the high word of u*6 + (0x7770 << 32).
+// Accept is 2*hu + 2 <= tv for the 16-bit high half hu of the acceptance uniform; a tie
+// 2*hu + 1 == tv needs the low half. A tie makes the product of (tv - 2*hu - 1) over the six arms
+// zero; a product that wraps to zero without a tie only sends the cell through the exact path
+// as well, which decides every arm from the full 32-bit uniforms. A proposal equal to the old
+// value lands on entry 17 (dN = 0), which always accepts and changes nothing.
+__device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32_t nbe, uint32_t eta, const U4& rr,
+                                                uint32_t c0, uint32_t t, const ReplicaDesc& R, const SweepTables* wt) {
+  uint32_t u = rr.x;
+  if (u * 46656u < 2560u) u = sweep_proposal_retry(c0, t, R.replica, R.key0, R.key1);
+  const uint32_t w0 = w;
+  uint32_t hx = 0, hy = 0;
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    const uint2 c = wt->cnt[(w0 >> (3 * a)) & 7u];
+    hx += c.x;
+    hy += c.y;
+  }
+  const char* tvb = reinterpret_cast<const char*>(wt->tv) + 68;
+  uint32_t f = u, tprod = 1u;
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    const unsigned long long m = (unsigned long long)f * 6ull + (0x7770ull << 32);
+    const uint32_t sn = (uint32_t)(m >> 32);
+    f = (uint32_t)m;
+    const uint32_t o = (w0 >> (3 * a)) & 7u;
+    const uint2 e = wt->nbw[(nbe >> (3 * a)) & 7u];
+    const uint32_t gx = hx + e.x, gy = hy + e.y;
+    const int off = (int)(prmt(gx, gy, sn) - prmt(gx, gy, o | 0x7770u));
+    const uint32_t tv = *reinterpret_cast<const uint32_t*>(tvb + off);
+    const uint32_t word = a < 2 ? rr.y : (a < 4 ? rr.z : rr.w);
+    const uint32_t hu = (a & 1) ? (word >> 16) : (word & 0xffffu);
+    const int d = (int)(tv - 2u * hu);
+    tprod *= (uint32_t)(d - 1);
+    const uint2 cn = wt->cnt[sn - 0x7770u], co = wt->cnt[o];
+    const uint32_t dw = (sn - 0x7770u - o) << (3 * a);
+    asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %3, 2;\n\t@p add.u32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;"
+        "\n\t@p sub.u32 %1, %1, %6;\n\t@p add.u32 %2, %2, %7;\n\t@p sub.u32 %2, %2, %8;\n\t}"
+        : "+r"(w), "+r"(hx), "+r"(hy)
+        : "r"(d), "r"(dw), "r"(cn.x), "r"(co.x), "r"(cn.y), "r"(co.y));
+  }
+  if (tprod == 0u) w = sweep_cell_exact(w0, nbs, eta, u, rr.y, rr.z, rr.w, c0, t, &R);
+  return w;
 }
 
 // One colour of the checkerboard sweep: every cell with (x+y+z)&1 == colour updates its six
@@ -522,10 +577,10 @@ template <int V>
 __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const ReplicaDesc* __restrict__ reps,
                                                     const ReplicaState* __restrict__ st,
                                                     const int* __restrict__ blk, int nrep, int colour, int jsweep) {
-  __shared__ WarpTables s_tab[kThreads / 32];
+  __shared__ SweepTables s_tab[kThreads / 32];
   const int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
-  const WarpTables* wt = warp_tables(R, s_tab);
+  const SweepTables* wt = warp_sweep_tables(R, s_tab);
   int hc, y, z;
   if (!segment_of<V>(R, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, hc, y, z)) return;
   uint32_t out[V], nbs[V], nbe[V], eta[V];
@@ -533,12 +588,12 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const 
   int x0;
   {
     CellBlock<V> cb;
-    cb.load(R, colour, hc, y, z, wt->eta);
+    cb.load(R, colour, hc, y, z, wt->et.eta);
 #pragma unroll
     for (int k = 0; k < V; ++k) {
       nbs[k] = neighbour_sigmas(cb.xp[k], cb.xm[k], cb.yp[k], cb.ym[k], cb.zp[k], cb.zm[k]);
       eta[k] = cb.eta[k];
-      nbe[k] = nbs[k] | wt->nbmask[~cb.eta[k] & 63u];
+      nbe[k] = nbs[k] | wt->et.nbmask[~cb.eta[k] & 63u];
       out[k] = cb.own[k];
     }
     own_ptr = cb.own_ptr;
@@ -551,7 +606,7 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const 
   for (int k = 0; k < V; ++k) {
     const uint32_t c0 = cbase + 2u * k;
     const U4 rr = philox(c0, t, kStSweep, R.replica, R.key0, R.key1);
-    out[k] = update_cell(out[k], nbs[k], nbe[k], eta[k], rr, c0, t, R, wt->tv);
+    out[k] = update_cell(out[k], nbs[k], nbe[k], eta[k], rr, c0, t, R, wt);
   }
   VecLoad<V>::st(own_ptr, out);
 }
@@ -579,10 +634,10 @@ __global__ void __launch_bounds__(kThreads) k_measure(const ReplicaDesc* __restr
                                                       ReplicaState* __restrict__ st,
                                                       const int* __restrict__ blk, int nrep) {
   __shared__ unsigned long long s_acc[2];
-  __shared__ WarpTables s_tab[kThreads / 32];
+  __shared__ EtaTables s_tab[kThreads / 32];
   const int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
-  const WarpTables* wt = warp_tables(R, s_tab);
+  const EtaTables* wt = warp_eta_tables(R, s_tab);
   if (threadIdx.x < 2) s_acc[threadIdx.x] = 0;
   __syncthreads();
   const int L = R.L, H = R.H;
