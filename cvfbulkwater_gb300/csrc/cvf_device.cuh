@@ -71,7 +71,7 @@ struct ReplicaState {
   unsigned long long top2[2];
   unsigned long long ncl, sum2, sum2w, nperc;
   int ncand;
-  int err;  // nonzero: a bounded loop gave up (1 SW union, 2 candidate overflow)
+  int err;  // nonzero: a bounded loop gave up (1 SW union, 2 candidate overflow, 3 grid barrier)
   uint32_t n_samples, n_cstats;
   uint32_t cap_samples, cap_cstats;
   SampleRec* samples;   // device sample stream
@@ -80,18 +80,27 @@ struct ReplicaState {
   CStatsRec last_cstats;
 };
 
+// Grid barrier state of the persistent step kernel (zeroed at creation and after an error).
+struct GridSync {
+  unsigned int count;  // blocks arrived at the current barrier
+  unsigned int gen;    // barrier generation
+  int err;             // nonzero: a barrier wait gave up
+  unsigned int ticket; // block tickets handed out in the current launch
+};
+
 // ------------------------------------------------------------- launch entry points
 struct BatchDev {
   ReplicaDesc* reps;    // device array [nrep]
   ReplicaState* st;     // device array [nrep]
   int nrep;
-  int vec;              // cells per thread in the sweep (1, 2 or 4; divides every H)
+  int vec;              // cells per thread in the sweep (1, 2, 4 or 8; divides every H)
   int* blk_sweep;       // device prefix tables (nrep+1) of blocks per replica
   int* blk_cube;
   int* blk_cell;        // one thread per cell
   int* blk_site;        // one thread per arm site (6N)
   int* blk_site4;       // one thread per 4 arm sites
   int nblk_sweep, nblk_cube, nblk_cell, nblk_site, nblk_site4;
+  GridSync* gsync;      // device barrier state of the persistent step kernel
 };
 
 constexpr int kThreads = 256;
@@ -104,6 +113,10 @@ void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do
 void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s);
 void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s);
 void launch_measure(const BatchDev& b, int record, cudaStream_t s);
+// Persistent cooperative launch of nsteps Metropolis steps (cube + volume move, nmet sweeps) of
+// every replica, with a recorded measurement after every step s with s % interval == 0 when
+// interval > 0. Same lattice, counters and samples as the per-phase kernels.
+cudaError_t launch_run(const BatchDev& b, int nsteps, int nmet, int interval, cudaStream_t s);
 void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s);
 void launch_cluster_stats_impl(const BatchDev& b, unsigned long long* blocktop, int record, cudaStream_t s);
 

@@ -55,6 +55,10 @@ struct cvf_handle {
   bool sw_done = false;
   unsigned long long* blocktop = nullptr;
   std::map<std::tuple<int, int, int, int>, cudaGraphExec_t> graphs;
+  // 0 (default): one launch per phase (step begin, cube + volume, each sweep colour,
+  // measurement) in a captured graph; 1: Metropolis-only steps run as one persistent
+  // cooperative launch per graph.
+  int launch_mode = 0;
   void* staging = nullptr;  // pinned host buffer for configuration transfers (lazily allocated)
   size_t staging_bytes = 0;
 };
@@ -182,6 +186,27 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     return 0;
   }
   cudaGraph_t g;
+  if (h->launch_mode == 1 && ncl == 0) {
+    // one persistent launch; a driver that cannot capture a cooperative launch leaves the
+    // handle on the per-phase kernels
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t el = launch_run(h->b, steps, nmet, record ? steps : 0, h->stream);
+    cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+    cudaGraphExec_t ex = nullptr;
+    if (el == cudaSuccess && ec == cudaSuccess) {
+      cudaError_t ei = cudaGraphInstantiate(&ex, g, 0);
+      cudaGraphDestroy(g);
+      if (ei == cudaSuccess) {
+        h->graphs[key] = ex;
+        *out = ex;
+        return 0;
+      }
+    } else if (ec == cudaSuccess) {
+      cudaGraphDestroy(g);
+    }
+    cudaGetLastError();
+    h->launch_mode = 0;
+  }
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   for (int i = 0; i < steps; ++i) {
     enqueue_step(h, nmet, ncl);
@@ -217,7 +242,10 @@ static int check_err(cvf_handle* h) {
   for (int r = 0; r < (int)h->reps.size(); ++r) {
     int err = 0;
     CK(cudaMemcpy(&err, (char*)(h->b.st + r) + offsetof(ReplicaState, err), sizeof(int), cudaMemcpyDeviceToHost));
-    if (err) return fail(CVF_ELIMIT, "device loop limit reached (code " + std::to_string(err) + ") in replica " + std::to_string(r));
+    if (err) {
+      if (err == 3) cudaMemset(h->b.gsync, 0, sizeof(GridSync));  // the barrier state is stale
+      return fail(CVF_ELIMIT, "device loop limit reached (code " + std::to_string(err) + ") in replica " + std::to_string(r));
+    }
   }
   return 0;
 }
@@ -322,8 +350,10 @@ int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
   h->b.nrep = n;
   int rc;
   if ((rc = dev_alloc(h, (void**)&h->b.reps, n * sizeof(ReplicaDesc))) ||
-      (rc = dev_alloc(h, (void**)&h->b.st, n * sizeof(ReplicaState))))
+      (rc = dev_alloc(h, (void**)&h->b.st, n * sizeof(ReplicaState))) ||
+      (rc = dev_alloc(h, (void**)&h->b.gsync, sizeof(GridSync))))
     return bail(rc);
+  if (cudaMemset(h->b.gsync, 0, sizeof(GridSync)) != cudaSuccess) return bail(fail(CVF_ECUDA, "barrier reset failed"));
   if (cudaMemcpy(h->b.st, st.data(), n * sizeof(ReplicaState), cudaMemcpyHostToDevice) != cudaSuccess)
     return bail(fail(CVF_ECUDA, "state upload failed"));
   if ((rc = upload_descs(h)) || (rc = build_tables(h))) return bail(rc);
@@ -719,6 +749,23 @@ int cvf_profile_launch(cvf_handle* h, int kind, int n) {
     }
   }
   CK(cudaGetLastError());
+  return 0;
+}
+
+int cvf_set_launch_mode(cvf_handle* h, int mode) {
+  if (!h || mode < 0 || mode > 1) return fail(CVF_EINVAL, "launch mode must be 0 or 1");
+  if (mode == h->launch_mode) return 0;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+  h->graphs.clear();
+  h->launch_mode = mode;
+  return 0;
+}
+
+int cvf_get_launch_mode(const cvf_handle* h, int* mode) {
+  if (!h || !mode) return fail(CVF_EINVAL, "null handle/out");
+  *mode = h->launch_mode;
   return 0;
 }
 

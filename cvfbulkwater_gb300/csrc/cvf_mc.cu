@@ -57,12 +57,13 @@ __device__ __forceinline__ void divmod32(uint32_t n, uint32_t d, int shift, uint
   }
 }
 
-// Block -> (cube parity, cube index): a replica's cube blocks are split in two equal halves, the
-// first for the cubes with all-even origins, the second for all-odd origins, so the parity is
-// uniform inside a block.
-__device__ __forceinline__ bool cube_of(const int* __restrict__ blk, int r, int H, uint32_t& par, uint32_t& qi) {
+// Block vb of the cube table -> (cube parity, cube index): a replica's cube blocks are split in
+// two equal halves, the first for the cubes with all-even origins, the second for all-odd
+// origins, so the parity is uniform inside a block.
+__device__ __forceinline__ bool cube_of(const int* __restrict__ blk, int r, int vb, int H, uint32_t& par,
+                                        uint32_t& qi) {
   const int b0 = __ldg(blk + r), half = (__ldg(blk + r + 1) - b0) >> 1;
-  const int lb = blockIdx.x - b0;
+  const int lb = vb - b0;
   par = lb >= half;
   qi = (uint32_t)(lb - (int)par * half) * blockDim.x + threadIdx.x;
   return qi < (uint32_t)H * H * H;
@@ -112,7 +113,7 @@ __global__ void k_init_cubes(const ReplicaDesc* __restrict__ reps, const int* __
   const ReplicaDesc& R = reps[r];
   const int L = R.L, H = R.H;
   uint32_t par, qi;
-  if (!cube_of(blk, r, H, par, qi)) return;
+  if (!cube_of(blk, r, blockIdx.x, H, par, qi)) return;
   uint32_t a, bc, b, c;
   divmod32(qi, H, R.lgH, bc, a);
   divmod32(bc, H, R.lgH, c, b);
@@ -146,11 +147,10 @@ __global__ void k_step_begin(ReplicaState* __restrict__ st, int nrep, int nmet, 
 // NPT volume move of GW:1740-1781 in FP64, every operation rounded separately. The shell terms
 // of E_vdW(r') are computed by the 32 lanes and summed by lane 0 in shell order, which is the
 // reference's sequential sum.
-__device__ void volume_move_warp(const ReplicaDesc& R, ReplicaState& S) {
+__device__ void volume_move_warp(const ReplicaDesc& R, ReplicaState& S, uint32_t t) {
   __shared__ double s_term[kMaxShells];
   __shared__ double s_trial;
-  const int lane = threadIdx.x;
-  const uint32_t t = S.cur[2];
+  const int lane = threadIdx.x & 31;
   U4 q = philox(0, t, kStVolume, R.replica, R.key0, R.key1);
   const double r0 = S.r_cell;
   if (lane == 0) {
@@ -207,22 +207,31 @@ __device__ void volume_move_warp(const ReplicaDesc& R, ReplicaState& S) {
 }
 
 // ------------------------------------------------------------------ cube move (+ volume blocks)
-// GW:3374-3466. One thread per cube (both parities in one launch: cubes share no edge and sigma
-// is frozen, so all cube decisions are independent). Writes only the cube's state byte.
-// Blocks at and after `nblk_cube` perform the volume move of replica (block - nblk_cube).
-__global__ void __launch_bounds__(kThreads) k_cube_volume(const ReplicaDesc* __restrict__ reps,
-                                                          ReplicaState* __restrict__ st,
-                                                          const int* __restrict__ blk, int nrep, int nblk_cube) {
-  if ((int)blockIdx.x >= nblk_cube) {
-    const int r = blockIdx.x - nblk_cube;
-    if (threadIdx.x < 32 && r < nrep) volume_move_warp(reps[r], st[r]);
-    return;
+// Warp-private copy of the cube tables (a warp reads 9 distinct words at most, so the random
+// lookups of its 32 cubes neither serialise like divergent constant-bank reads nor conflict).
+//   act[s]  12-bit mask of the cube edges that carry eta = 1 in state s
+//   thr[i]  acceptance threshold of dN_hb = i - 4 (U < thr, thr in [0, 2^32])
+struct CubeTables {
+  unsigned long long thr[9];
+  uint32_t act[9];
+};
+
+__device__ __forceinline__ void fill_cube_tables(const ReplicaDesc& R, CubeTables* ct, int lane) {
+  if (lane < 9) {
+    ct->thr[lane] = R.thr_cube[lane];
+    ct->act[lane] = c_state_active[lane];
   }
-  const int r = find_replica(blk, nrep, blockIdx.x);
-  const ReplicaDesc& R = reps[r];
+}
+
+// GW:3374-3466. One thread per cube (both parities in one launch: cubes share no edge and sigma
+// is frozen, so all cube decisions are independent). Writes only the cube's state byte. vb is
+// the block of the cube table and t the cube-move counter of the step. Plain (coherent) loads:
+// the persistent step kernel reads cells that other blocks wrote earlier in the same launch.
+__device__ __forceinline__ void cube_move(const ReplicaDesc& R, const CubeTables* ct, const int* __restrict__ blk,
+                                          int r, int vb, uint32_t t) {
   const int L = R.L, H = R.H;
   uint32_t par, qi;
-  if (!cube_of(blk, r, H, par, qi)) return;
+  if (!cube_of(blk, r, vb, H, par, qi)) return;
   uint32_t a, bc, b, c;
   divmod32(qi, H, R.lgH, bc, a);
   divmod32(bc, H, R.lgH, c, b);
@@ -234,14 +243,14 @@ __global__ void __launch_bounds__(kThreads) k_cube_volume(const ReplicaDesc* __r
   const uint32_t* c0p = R.cells[par];
   const uint32_t* c1p = R.cells[par ^ 1];
   uint32_t w[8];
-  w[0] = __ldg(c0p + xa + r00);
-  w[1] = __ldg(c1p + xb + r00);
-  w[2] = __ldg(c1p + xa + r10);
-  w[3] = __ldg(c0p + xb + r10);
-  w[4] = __ldg(c1p + xa + r01);
-  w[5] = __ldg(c0p + xb + r01);
-  w[6] = __ldg(c0p + xa + r11);
-  w[7] = __ldg(c1p + xb + r11);
+  w[0] = c0p[xa + r00];
+  w[1] = c1p[xb + r00];
+  w[2] = c1p[xa + r10];
+  w[3] = c0p[xb + r10];
+  w[4] = c1p[xa + r01];
+  w[5] = c0p[xb + r01];
+  w[6] = c0p[xa + r11];
+  w[7] = c1p[xb + r11];
   // edge e along d from p0 to p1: sigma_{2d}(p0) == sigma_{2d+1}(p1), compared in place by
   // shifting the start word one field up
   uint32_t D = 0;
@@ -252,15 +261,33 @@ __global__ void __launch_bounds__(kThreads) k_cube_volume(const ReplicaDesc* __r
     D |= (x == 0u ? 1u : 0u) << e;
   }
   const uint32_t cid = (uint32_t)x0 + (uint32_t)L * ((uint32_t)y0 + (uint32_t)L * (uint32_t)z0);
-  const uint32_t t = st[r].cur[1];
   U4 rr = philox(cid, t, kStCube, R.replica, R.key0, R.key1);
   uint32_t nw;
   if (!lemire_try(rr.x, 9, nw) && !lemire_try(rr.z, 9, nw) && !lemire_try(rr.w, 9, nw))
     nw = lemire_retry(9, cid, t, kStCube, R.replica, R.key0, R.key1);
   uint8_t* cs = R.cubes[par] + qi;
   const uint32_t old = *cs;
-  const int dhb = __popc(c_state_active[nw] & D) - __popc(c_state_active[old] & D);
-  if ((unsigned long long)rr.y < R.thr_cube[dhb + 4] && nw != old) *cs = (uint8_t)nw;
+  const int dhb = __popc(ct->act[nw] & D) - __popc(ct->act[old] & D);
+  if ((unsigned long long)rr.y < ct->thr[dhb + 4] && nw != old) *cs = (uint8_t)nw;
+}
+
+// Cube moves of every replica, then (blocks at and after nblk_cube) the volume move of replica
+// (block - nblk_cube), both with the counters of the current step.
+__global__ void __launch_bounds__(kThreads) k_cube_volume(const ReplicaDesc* __restrict__ reps,
+                                                          ReplicaState* __restrict__ st,
+                                                          const int* __restrict__ blk, int nrep, int nblk_cube) {
+  if ((int)blockIdx.x >= nblk_cube) {
+    const int r = blockIdx.x - nblk_cube;
+    if (threadIdx.x < 32 && r < nrep) volume_move_warp(reps[r], st[r], st[r].cur[2]);
+    return;
+  }
+  __shared__ CubeTables s_ct[kThreads / 32];
+  const int r = find_replica(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  CubeTables* ct = s_ct + (threadIdx.x >> 5);
+  fill_cube_tables(R, ct, threadIdx.x & 31);
+  __syncwarp();
+  cube_move(R, ct, blk, r, blockIdx.x, st[r].cur[1]);
 }
 
 // ------------------------------------------------------------------ checkerboard sweep
@@ -389,8 +416,8 @@ struct CellBlock {
     for (int k = 0; k < V; ++k) {
       int ae = h0 + k;
       int ao = s ? ae : (ae == 0 ? H - 1 : ae - 1);
-      uint32_t se = __ldg(R.cubes[0] + erow + ae);
-      uint32_t so = __ldg(R.cubes[1] + orow + ao);
+      uint32_t se = R.cubes[0][erow + ae];
+      uint32_t so = R.cubes[1][orow + ao];
       eta[k] = (uint32_t)s_eta[se * 8 + p] | (uint32_t)s_eta[so * 8 + (p ^ 7)];
     }
   }
@@ -498,9 +525,7 @@ __device__ __forceinline__ const EtaTables* warp_eta_tables(const ReplicaDesc& R
   return et;
 }
 
-__device__ __forceinline__ const SweepTables* warp_sweep_tables(const ReplicaDesc& R, SweepTables* all) {
-  SweepTables* wt = all + (threadIdx.x >> 5);
-  const uint32_t lane = threadIdx.x & 31;
+__device__ __forceinline__ void fill_sweep_tables(const ReplicaDesc& R, SweepTables* wt, uint32_t lane) {
   fill_eta_tables(R, &wt->et, lane);
   wt->tv[lane] = R.tv[lane];
   if (lane == 0) wt->tv[32] = R.tv[32];
@@ -508,6 +533,11 @@ __device__ __forceinline__ const SweepTables* warp_sweep_tables(const ReplicaDes
     wt->cnt[lane] = count_bytes(lane, 4u);
     wt->nbw[lane] = count_bytes(lane, 44u);
   }
+}
+
+__device__ __forceinline__ const SweepTables* warp_sweep_tables(const ReplicaDesc& R, SweepTables* all) {
+  SweepTables* wt = all + (threadIdx.x >> 5);
+  fill_sweep_tables(R, wt, threadIdx.x & 31);
   __syncwarp();
   return wt;
 }
@@ -573,16 +603,12 @@ template <int V>
 struct SweepMinBlocks {
   static constexpr int v = V >= 8 ? 3 : 4;
 };
+// Row segment q (V cells) of one colour of replica R with sweep counter t.
 template <int V>
-__global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const ReplicaDesc* __restrict__ reps,
-                                                    const ReplicaState* __restrict__ st,
-                                                    const int* __restrict__ blk, int nrep, int colour, int jsweep) {
-  __shared__ SweepTables s_tab[kThreads / 32];
-  const int r = find_replica(blk, nrep, blockIdx.x);
-  const ReplicaDesc& R = reps[r];
-  const SweepTables* wt = warp_sweep_tables(R, s_tab);
+__device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepTables* wt, uint32_t q, int colour,
+                                              uint32_t t) {
   int hc, y, z;
-  if (!segment_of<V>(R, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, hc, y, z)) return;
+  if (!segment_of<V>(R, q, hc, y, z)) return;
   uint32_t out[V], nbs[V], nbe[V], eta[V];
   uint32_t* own_ptr;
   int x0;
@@ -599,7 +625,6 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const 
     own_ptr = cb.own_ptr;
     x0 = cb.x0;
   }
-  const uint32_t t = st[r].cur[0] + (uint32_t)jsweep;
   const uint32_t L = R.L;
   const uint32_t cbase = L * ((uint32_t)y + L * (uint32_t)z) + (uint32_t)x0;
 #pragma unroll
@@ -609,6 +634,18 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const 
     out[k] = update_cell(out[k], nbs[k], nbe[k], eta[k], rr, c0, t, R, wt);
   }
   VecLoad<V>::st(own_ptr, out);
+}
+
+template <int V>
+__global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const ReplicaDesc* __restrict__ reps,
+                                                    const ReplicaState* __restrict__ st,
+                                                    const int* __restrict__ blk, int nrep, int colour, int jsweep) {
+  __shared__ SweepTables s_tab[kThreads / 32];
+  const int r = find_replica(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  const SweepTables* wt = warp_sweep_tables(R, s_tab);
+  sweep_segment<V>(R, wt, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
+                   st[r].cur[0] + (uint32_t)jsweep);
 }
 
 // ------------------------------------------------------------------ measurement
@@ -629,36 +666,35 @@ __device__ __forceinline__ uint32_t sigma_pairs(uint32_t w) {
 
 // GW:2014-2160: N_hb2 = sum over bonds of delta * (eta_i + eta_j), counted from the colour-0
 // end of every bond (each bond joins the two colours); N_sigma over cells of both colours.
+// Counts of the V-cell colour-0 segment q of replica R, added to hb2 and ns.
 template <int V>
-__global__ void __launch_bounds__(kThreads) k_measure(const ReplicaDesc* __restrict__ reps,
-                                                      ReplicaState* __restrict__ st,
-                                                      const int* __restrict__ blk, int nrep) {
-  __shared__ unsigned long long s_acc[2];
-  __shared__ EtaTables s_tab[kThreads / 32];
-  const int r = find_replica(blk, nrep, blockIdx.x);
-  const ReplicaDesc& R = reps[r];
-  const EtaTables* wt = warp_eta_tables(R, s_tab);
+__device__ __forceinline__ void measure_segment(const ReplicaDesc& R, const EtaTables* et, uint32_t q, uint32_t& hb2,
+                                                uint32_t& ns) {
+  int hc, y, z;
+  if (!segment_of<V>(R, q, hc, y, z)) return;
+  const int L = R.L, H = R.H;
+  CellBlock<V> cb;
+  cb.load(R, 0, hc, y, z, et->eta);
+  uint32_t w1[V];
+  VecLoad<V>::ld(R.cells[1] + (uint32_t)H * ((uint32_t)y + (uint32_t)L * z) + hc * V, w1);
+#pragma unroll
+  for (int k = 0; k < V; ++k) {
+    const uint32_t w = cb.own[k];
+    const uint32_t nbs = neighbour_sigmas(cb.xp[k], cb.xm[k], cb.yp[k], cb.ym[k], cb.zp[k], cb.zm[k]);
+    // bonds whose two arm sigmas agree, restricted to eta = 1 (bit 3a per arm)
+    const uint32_t x = w ^ nbs;
+    const uint32_t eqm = ~(x | (x >> 1) | (x >> 2)) & et->nbmask[cb.eta[k] & 63u] & 0x9249u;
+    hb2 += 2u * (uint32_t)__popc(eqm);
+    ns += sigma_pairs(w) + sigma_pairs(w1[k]);
+  }
+}
+
+// Block sum of the per-thread counts into slot vb % 32 of replica state S (all threads of the
+// block call it; s_acc is the block's two-word scratch).
+__device__ __forceinline__ void measure_accumulate(ReplicaState& S, int vb, uint32_t hb2, uint32_t ns,
+                                                   unsigned long long* s_acc) {
   if (threadIdx.x < 2) s_acc[threadIdx.x] = 0;
   __syncthreads();
-  const int L = R.L, H = R.H;
-  uint32_t hb2 = 0, ns = 0;
-  int hc, y, z;
-  if (segment_of<V>(R, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, hc, y, z)) {
-    CellBlock<V> cb;
-    cb.load(R, 0, hc, y, z, wt->eta);
-    uint32_t w1[V];
-    VecLoad<V>::ld(R.cells[1] + (uint32_t)H * ((uint32_t)y + (uint32_t)L * z) + hc * V, w1);
-#pragma unroll
-    for (int k = 0; k < V; ++k) {
-      const uint32_t w = cb.own[k];
-      const uint32_t nbs = neighbour_sigmas(cb.xp[k], cb.xm[k], cb.yp[k], cb.ym[k], cb.zp[k], cb.zm[k]);
-      // bonds whose two arm sigmas agree, restricted to eta = 1 (bit 3a per arm)
-      const uint32_t x = w ^ nbs;
-      const uint32_t eqm = ~(x | (x >> 1) | (x >> 2)) & wt->nbmask[cb.eta[k] & 63u] & 0x9249u;
-      hb2 += 2u * (uint32_t)__popc(eqm);
-      ns += sigma_pairs(w) + sigma_pairs(w1[k]);
-    }
-  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     hb2 += __shfl_xor_sync(0xffffffffu, hb2, o);
@@ -670,24 +706,35 @@ __global__ void __launch_bounds__(kThreads) k_measure(const ReplicaDesc* __restr
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    atomicAdd(&st[r].acc_slot[0][blockIdx.x & 31], s_acc[0]);
-    atomicAdd(&st[r].acc_slot[1][blockIdx.x & 31], s_acc[1]);
+    atomicAdd(&S.acc_slot[0][vb & 31], s_acc[0]);
+    atomicAdd(&S.acc_slot[1][vb & 31], s_acc[1]);
   }
 }
 
-__global__ void k_measure_begin(ReplicaState* __restrict__ st, int nrep) {
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrep) return;
+template <int V>
+__global__ void __launch_bounds__(kThreads) k_measure(const ReplicaDesc* __restrict__ reps,
+                                                      ReplicaState* __restrict__ st,
+                                                      const int* __restrict__ blk, int nrep) {
+  __shared__ unsigned long long s_acc[2];
+  __shared__ EtaTables s_tab[kThreads / 32];
+  const int r = find_replica(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  const EtaTables* et = warp_eta_tables(R, s_tab);
+  uint32_t hb2 = 0, ns = 0;
+  measure_segment<V>(R, et, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, hb2, ns);
+  measure_accumulate(st[r], blockIdx.x, hb2, ns, s_acc);
+}
+
+__device__ __forceinline__ void measure_zero(ReplicaState& S) {
   for (int i = 0; i < 32; ++i) {
-    st[r].acc_slot[0][i] = 0;
-    st[r].acc_slot[1][i] = 0;
+    S.acc_slot[0][i] = 0;
+    S.acc_slot[1][i] = 0;
   }
 }
 
-__global__ void k_measure_end(ReplicaState* __restrict__ st, int nrep, int record) {
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrep) return;
-  ReplicaState& S = st[r];
+// Sums the slots into the replica's last measurement and appends it to the sample stream when
+// record is set.
+__device__ __forceinline__ void measure_finish(ReplicaState& S, int record) {
   unsigned long long hb2 = 0, ns = 0;
   for (int i = 0; i < 32; ++i) {
     hb2 += S.acc_slot[0][i];
@@ -703,6 +750,175 @@ __global__ void k_measure_end(ReplicaState* __restrict__ st, int nrep, int recor
   S.last = rec;
   if (record && S.samples && S.n_samples < S.cap_samples) S.samples[S.n_samples] = rec;
   if (record) S.n_samples++;
+}
+
+__global__ void k_measure_begin(ReplicaState* __restrict__ st, int nrep) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nrep) measure_zero(st[r]);
+}
+
+__global__ void k_measure_end(ReplicaState* __restrict__ st, int nrep, int record) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nrep) measure_finish(st[r], record);
+}
+
+// ------------------------------------------------------------------ persistent step kernel
+// Grid barrier of the persistent kernel; every block of the cooperative launch is resident. A
+// waiting block polls the generation word at most kBarrierPolls times (with a short sleep
+// between polls, about a second in all); when the bound is reached it sets gs->err and error
+// code 3 of replica 0, and every block leaves the kernel at its next barrier.
+constexpr unsigned int kBarrierPolls = 1u << 24;
+
+__device__ __noinline__ bool grid_barrier(GridSync* gs, ReplicaState* st0) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = &gs->gen;
+    volatile int* err = &gs->err;
+    const unsigned int g = *gen;
+    __threadfence();
+    int ok = 1;
+    if (atomicAdd(&gs->count, 1u) == gridDim.x - 1) {
+      atomicExch(&gs->count, 0u);
+      __threadfence();
+      atomicAdd(&gs->gen, 1u);
+    } else {
+      for (unsigned int polls = 0; *gen == g; ++polls) {
+        if (*err != 0 || polls >= kBarrierPolls) {
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+      if (!ok && atomicExch(&gs->err, 1) == 0) atomicExch(&st0->err, 3);
+    }
+    __threadfence();
+    s_ok = ok && *err == 0;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Per-warp tables of the persistent kernel: the sweep and cube tables of one replica, reloaded
+// when the warp moves to a block of another replica.
+struct StepTables {
+  SweepTables sw;
+  CubeTables cube;
+};
+
+__device__ __forceinline__ void ensure_tables(const ReplicaDesc* reps, int r, StepTables* wt, int& held) {
+  if (held == r) return;
+  __syncwarp();
+  const uint32_t lane = threadIdx.x & 31;
+  fill_sweep_tables(reps[r], &wt->sw, lane);
+  fill_cube_tables(reps[r], &wt->cube, lane);
+  __syncwarp();
+  if (lane == 0) held = r;
+  __syncwarp();
+}
+
+// Dynamic dealing of a phase's n blocks: tickets come from one counter that grows through the
+// launch; every block takes tickets until one lies past the phase's range, so the counter ends
+// each phase at base + n + gridDim.x and the next phase's base is known to every block.
+struct Dealer {
+  unsigned int base;
+  int slot;
+};
+
+template <typename F>
+__device__ __forceinline__ void deal(GridSync* gs, Dealer& d, int n, int* s_vb, F&& work) {
+  if (threadIdx.x == 0) s_vb[d.slot] = (int)(atomicAdd(&gs->ticket, 1u) - d.base);
+  __syncthreads();
+  for (;;) {
+    const int vb = s_vb[d.slot];
+    if (vb >= n) break;
+    if (threadIdx.x == 0) s_vb[d.slot ^ 1] = (int)(atomicAdd(&gs->ticket, 1u) - d.base);
+    work(vb);
+    __syncthreads();
+    d.slot ^= 1;
+  }
+  d.base += (unsigned int)n + gridDim.x;
+}
+
+// nsteps Metropolis steps of every replica in one cooperative launch. Each phase (cube moves with
+// one volume block per replica, then every sweep colour, then the measurement of a recorded
+// step) deals the blocks of its per-phase table (blk_cube, blk_sweep) to the resident blocks
+// through tickets, and a grid barrier closes the phase. Step s uses the counters the per-phase
+// kernels get from k_step_begin: sweep ctr[0] + s*nmet + j, cube ctr[1] + s, volume
+// ctr[2] + s; the counters advance once, after the last step. With interval > 0 a measurement
+// follows every step s with s % interval == 0; its slots are zeroed by the volume warp at the
+// start of the step and summed into the sample stream by the same warp at the start of the
+// next step (before that step's volume move), or after the last barrier.
+template <int V>
+__global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_run(BatchDev b, int nsteps, int nmet,
+                                                                         int interval) {
+  __shared__ StepTables s_tab[kThreads / 32];
+  __shared__ unsigned long long s_acc[2];
+  __shared__ int s_held[kThreads / 32];
+  __shared__ int s_vb[2];
+  if ((threadIdx.x & 31) == 0) s_held[threadIdx.x >> 5] = -1;
+  __syncwarp();
+  Dealer d{0u, 0};
+  const int pps = 2 + 2 * nmet;  // phases per step: cube/volume, 2 per sweep, measurement
+  for (int ph = 0; ph < nsteps * pps; ++ph) {
+    const int s = ph / pps, k = ph - s * pps;
+    if (k == 0) {
+      const bool rec = interval > 0 && s % interval == 0;
+      const bool prev_rec = interval > 0 && s > 0 && (s - 1) % interval == 0;
+      deal(b.gsync, d, b.nblk_cube + b.nrep, s_vb, [&](int vb) {
+        if (vb < b.nblk_cube) {
+          const int r = find_replica(b.blk_cube, b.nrep, vb);
+          StepTables* wt = s_tab + (threadIdx.x >> 5);
+          ensure_tables(b.reps, r, wt, s_held[threadIdx.x >> 5]);
+          cube_move(b.reps[r], &wt->cube, b.blk_cube, r, vb, b.st[r].ctr[1] + (uint32_t)s);
+        } else if (threadIdx.x < 32) {
+          const int r = vb - b.nblk_cube;
+          ReplicaState& S = b.st[r];
+          if (threadIdx.x == 0) {
+            if (prev_rec) measure_finish(S, 1);
+            if (rec) measure_zero(S);
+          }
+          __syncwarp();
+          volume_move_warp(b.reps[r], S, S.ctr[2] + (uint32_t)s);
+        }
+      });
+    } else if (k < pps - 1) {
+      const int colour = (k - 1) & 1;
+      const uint32_t toff = (uint32_t)(s * nmet + ((k - 1) >> 1));
+      deal(b.gsync, d, b.nblk_sweep, s_vb, [&](int vb) {
+        const int r = find_replica(b.blk_sweep, b.nrep, vb);
+        StepTables* wt = s_tab + (threadIdx.x >> 5);
+        ensure_tables(b.reps, r, wt, s_held[threadIdx.x >> 5]);
+        sweep_segment<V>(b.reps[r], &wt->sw, (uint32_t)(vb - b.blk_sweep[r]) * blockDim.x + threadIdx.x, colour,
+                         b.st[r].ctr[0] + toff);
+      });
+    } else {
+      if (!(interval > 0 && s % interval == 0)) continue;  // no measurement after this step
+      deal(b.gsync, d, b.nblk_sweep, s_vb, [&](int vb) {
+        const int r = find_replica(b.blk_sweep, b.nrep, vb);
+        StepTables* wt = s_tab + (threadIdx.x >> 5);
+        ensure_tables(b.reps, r, wt, s_held[threadIdx.x >> 5]);
+        uint32_t hb2 = 0, ns = 0;
+        measure_segment<V>(b.reps[r], &wt->sw.et, (uint32_t)(vb - b.blk_sweep[r]) * blockDim.x + threadIdx.x, hb2,
+                           ns);
+        measure_accumulate(b.st[r], vb, hb2, ns, s_acc);
+      });
+    }
+    if (!grid_barrier(b.gsync, b.st)) return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) b.gsync->ticket = 0u;  // every ticket of the launch is taken
+  const bool last_rec = interval > 0 && (nsteps - 1) % interval == 0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < b.nrep; r += gridDim.x * blockDim.x) {
+    ReplicaState& S = b.st[r];
+    if (last_rec) measure_finish(S, 1);
+    S.cur[0] = S.ctr[0] + (uint32_t)((nsteps - 1) * nmet);
+    S.ctr[0] += (uint32_t)(nsteps * nmet);
+    S.cur[1] = S.ctr[1] + (uint32_t)(nsteps - 1);
+    S.ctr[1] += (uint32_t)nsteps;
+    S.cur[2] = S.ctr[2] + (uint32_t)(nsteps - 1);
+    S.ctr[2] += (uint32_t)nsteps;
+    S.cur[3] = S.ctr[3];
+  }
 }
 
 // ------------------------------------------------------------------ launchers
@@ -742,6 +958,38 @@ void launch_measure(const BatchDev& b, int record, cudaStream_t s) {
     default: k_measure<1><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep); break;
   }
   k_measure_end<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, record);
+}
+
+template <int V>
+static cudaError_t launch_run_v(const BatchDev& b, int nsteps, int nmet, int interval, cudaStream_t s) {
+  int dev = 0, nsm = 0, per = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_run<V>, kThreads, 0);
+  if (e != cudaSuccess) return e;
+  if (per < 1) return cudaErrorInvalidConfiguration;
+  const int work = b.nblk_sweep > b.nblk_cube + b.nrep ? b.nblk_sweep : b.nblk_cube + b.nrep;
+  const int grid = nsm * per < work ? nsm * per : work;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(kThreads);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_run<V>, b, nsteps, nmet, interval);
+}
+
+cudaError_t launch_run(const BatchDev& b, int nsteps, int nmet, int interval, cudaStream_t s) {
+  if (nsteps <= 0) return cudaSuccess;
+  switch (b.vec) {
+    case 8: return launch_run_v<8>(b, nsteps, nmet, interval, s);
+    case 4: return launch_run_v<4>(b, nsteps, nmet, interval, s);
+    case 2: return launch_run_v<2>(b, nsteps, nmet, interval, s);
+    default: return launch_run_v<1>(b, nsteps, nmet, interval, s);
+  }
 }
 
 }  // namespace cvf

@@ -107,6 +107,17 @@ class Lattice:
         check(lib().cvf_autotune(self._h, C.byref(v)))
         return v.value
 
+    @property
+    def launch_mode(self) -> int:
+        """1: Metropolis-only steps run as one persistent launch per graph; 0: one launch per phase."""
+        m = C.c_int()
+        check(lib().cvf_get_launch_mode(self._h, C.byref(m)))
+        return m.value
+
+    @launch_mode.setter
+    def launch_mode(self, mode: int):
+        check(lib().cvf_set_launch_mode(self._h, int(mode)))
+
     def stream_ptr(self) -> int:
         s = C.c_void_p()
         check(lib().cvf_get_stream(self._h, C.byref(s)))

@@ -26,6 +26,7 @@ def main():
     ap.add_argument("--start", type=int, default=2)
     ap.add_argument("--T", type=float, default=0.70)
     ap.add_argument("--P", type=float, default=0.45)
+    ap.add_argument("--mode", type=int, default=None, help="launch mode of the step kinds (0 per phase, 1 persistent)")
     a = ap.parse_args()
     import torch
 
@@ -33,6 +34,8 @@ def main():
     from .engine import Lattice, Params
     build.build()
     lat = Lattice(Params(L=a.L, T=a.T, P=a.P, seed=44648604, start=a.start))
+    if a.mode is not None:
+        lat.launch_mode = a.mode
     nmet, ncl = STEPS.get(a.kind, (1, 0))
     lat.run(a.warmup, nmet, ncl)
     lat.synchronize()
@@ -47,7 +50,8 @@ def main():
         abi.check(abi.lib().cvf_profile_launch(lat._h, KINDS[a.kind], a.launches))
     e1.record(s)
     torch.cuda.synchronize()
-    print(f"L={a.L} kind={a.kind} repetitions={a.launches} ms/rep={e0.elapsed_time(e1) / max(a.launches, 1):.4f}")
+    print(f"L={a.L} kind={a.kind} mode={lat.launch_mode} repetitions={a.launches} "
+          f"ms/rep={e0.elapsed_time(e1) / max(a.launches, 1):.4f}")
     lat.synchronize()
     lat.close()
 

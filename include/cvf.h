@@ -181,6 +181,19 @@ int cvf_format_cluster_line(char* buf, int cap, int t, const cvf_cstats* c);
  * No reference counterpart. */
 int cvf_autotune(cvf_handle* h, int* vec_out);
 
+/* Launch mode of Metropolis-only steps (n_cluster == 0). 0 (default): a captured CUDA graph per
+ * chunk of steps with one kernel per phase (cube + volume moves, each sweep colour, the recorded
+ * measurements). 1: each captured chunk is one persistent cooperative kernel that runs every
+ * phase of every step of every replica, dealing blocks through tickets, with grid barriers
+ * between the phases. Both give the same lattices, counters and samples bit for bit; steps with
+ * Swendsen-Wang moves always use per-phase launches. If the CUDA driver cannot capture the
+ * cooperative launch, the handle falls back to mode 0 (cvf_get_launch_mode then reports 0). A
+ * barrier wait that gives up (about a second) ends the launch and reports CVF_ELIMIT with code 3
+ * at the next cvf_synchronize. No reference counterpart (the reference launches one kernel per
+ * arm and parity). */
+int cvf_set_launch_mode(cvf_handle* h, int mode);
+int cvf_get_launch_mode(const cvf_handle* h, int* mode);
+
 /* The CUDA stream (a cudaStream_t passed as void*) on which all work of the handle is ordered,
  * for callers that time or order their own work around the engine. No reference counterpart. */
 int cvf_get_stream(cvf_handle* h, void** stream);
