@@ -33,6 +33,7 @@ struct ReplicaDesc {
   int L, H;
   int lgL, lgH;       // log2 of L and H when they are powers of two, else -1
   int start;          // Flag_config of the replica (0 disordered, 1 from file, 2 ordered)
+  int cvec;           // consecutive cubes per thread in the cube move: 4, 2 or 1 (divides H)
   uint32_t key0, key1, replica;
   float T, P, Rc;
   double beta, Jeff;
@@ -95,11 +96,12 @@ struct BatchDev {
   int nrep;
   int vec;              // cells per thread in the sweep (1, 2, 4 or 8; divides every H)
   int* blk_sweep;       // device prefix tables (nrep+1) of blocks per replica
-  int* blk_cube;
+  int* blk_cube;        // one thread per cube (initialisation)
+  int* blk_cubev;       // one thread per cvec consecutive cubes (cube move)
   int* blk_cell;        // one thread per cell
   int* blk_site;        // one thread per arm site (6N)
   int* blk_site4;       // one thread per 4 arm sites
-  int nblk_sweep, nblk_cube, nblk_cell, nblk_site, nblk_site4;
+  int nblk_sweep, nblk_cube, nblk_cubev, nblk_cell, nblk_site, nblk_site4;
   GridSync* gsync;      // device barrier state of the persistent step kernel
 };
 

@@ -102,32 +102,36 @@ static int build_tables(cvf_handle* h, int force_vec = 0) {
     while (vec > 1 && r.H % vec) vec >>= 1;
   }
   h->b.vec = vec;
-  std::vector<int> ts(n + 1), tc(n + 1), tl(n + 1), tsi(n + 1), ts4(n + 1);
-  ts[0] = tc[0] = tl[0] = tsi[0] = ts4[0] = 0;
+  std::vector<int> ts(n + 1), tc(n + 1), tcv(n + 1), tl(n + 1), tsi(n + 1), ts4(n + 1);
+  ts[0] = tc[0] = tcv[0] = tl[0] = tsi[0] = ts4[0] = 0;
   auto blocks = [](long long threads) { return (int)((threads + kThreads - 1) / kThreads); };
   for (int i = 0; i < n; ++i) {
     const auto& r = h->reps[i];
     long long L = r.L, H = r.H;
     ts[i + 1] = ts[i] + blocks((H / vec) * L * L);
     tc[i + 1] = tc[i] + 2 * blocks(H * H * H);  // even-origin cubes, then odd-origin cubes
+    tcv[i + 1] = tcv[i] + 2 * blocks(H * H * H / r.desc.cvec);
     tl[i + 1] = tl[i] + blocks(r.N);
     tsi[i + 1] = tsi[i] + blocks(6 * r.N);
     ts4[i + 1] = ts4[i] + blocks(6 * r.N / 4);
   }
   int* d;
-  if (int rc = dev_alloc(h, (void**)&d, sizeof(int) * 5 * (n + 1))) return rc;
+  if (int rc = dev_alloc(h, (void**)&d, sizeof(int) * 6 * (n + 1))) return rc;
   std::vector<int> all;
   all.insert(all.end(), ts.begin(), ts.end());
   all.insert(all.end(), tc.begin(), tc.end());
   all.insert(all.end(), tl.begin(), tl.end());
   all.insert(all.end(), tsi.begin(), tsi.end());
   all.insert(all.end(), ts4.begin(), ts4.end());
+  all.insert(all.end(), tcv.begin(), tcv.end());
   CK(cudaMemcpy(d, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
   h->b.blk_sweep = d;
   h->b.blk_cube = d + (n + 1);
   h->b.blk_cell = d + 2 * (n + 1);
   h->b.blk_site = d + 3 * (n + 1);
   h->b.blk_site4 = d + 4 * (n + 1);
+  h->b.blk_cubev = d + 5 * (n + 1);
+  h->b.nblk_cubev = tcv[n];
   h->b.nblk_site4 = ts4[n];
   h->b.nblk_sweep = ts[n];
   h->b.nblk_cube = tc[n];
@@ -316,6 +320,7 @@ int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
     d.lgL = lg(r.L);
     d.lgH = lg(r.H);
     d.start = r.p.start;
+    d.cvec = r.H % 4 == 0 ? 4 : (r.H % 2 == 0 ? 2 : 1);
     d.key0 = (uint32_t)((unsigned long long)r.p.seed & 0xffffffffu);
     d.key1 = (uint32_t)((unsigned long long)r.p.seed >> 32);
     d.replica = r.p.replica;

@@ -206,91 +206,7 @@ __device__ void volume_move_warp(const ReplicaDesc& R, ReplicaState& S, uint32_t
   }
 }
 
-// ------------------------------------------------------------------ cube move (+ volume blocks)
-// Warp-private copy of the cube tables (a warp reads 9 distinct words at most, so the random
-// lookups of its 32 cubes neither serialise like divergent constant-bank reads nor conflict).
-//   act[s]  12-bit mask of the cube edges that carry eta = 1 in state s
-//   thr[i]  acceptance threshold of dN_hb = i - 4 (U < thr, thr in [0, 2^32])
-struct CubeTables {
-  unsigned long long thr[9];
-  uint32_t act[9];
-};
-
-__device__ __forceinline__ void fill_cube_tables(const ReplicaDesc& R, CubeTables* ct, int lane) {
-  if (lane < 9) {
-    ct->thr[lane] = R.thr_cube[lane];
-    ct->act[lane] = c_state_active[lane];
-  }
-}
-
-// GW:3374-3466. One thread per cube (both parities in one launch: cubes share no edge and sigma
-// is frozen, so all cube decisions are independent). Writes only the cube's state byte. vb is
-// the block of the cube table and t the cube-move counter of the step. Plain (coherent) loads:
-// the persistent step kernel reads cells that other blocks wrote earlier in the same launch.
-__device__ __forceinline__ void cube_move(const ReplicaDesc& R, const CubeTables* ct, const int* __restrict__ blk,
-                                          int r, int vb, uint32_t t) {
-  const int L = R.L, H = R.H;
-  uint32_t par, qi;
-  if (!cube_of(blk, r, vb, H, par, qi)) return;
-  uint32_t a, bc, b, c;
-  divmod32(qi, H, R.lgH, bc, a);
-  divmod32(bc, H, R.lgH, c, b);
-  const uint32_t x0 = 2 * a + par, y0 = 2 * b + par, z0 = 2 * c + par;
-  const uint32_t y1 = y0 + 1 == (uint32_t)L ? 0 : y0 + 1, z1 = z0 + 1 == (uint32_t)L ? 0 : z0 + 1;
-  // vertex p = dx | dy<<1 | dz<<2 has colour (par + popc(p)) & 1 and word (x>>1) + H*(y + L*z)
-  const uint32_t xa = a, xb = par ? (a + 1 == (uint32_t)H ? 0 : a + 1) : a;
-  const uint32_t r00 = H * (y0 + L * z0), r10 = H * (y1 + L * z0), r01 = H * (y0 + L * z1), r11 = H * (y1 + L * z1);
-  const uint32_t* c0p = R.cells[par];
-  const uint32_t* c1p = R.cells[par ^ 1];
-  uint32_t w[8];
-  w[0] = c0p[xa + r00];
-  w[1] = c1p[xb + r00];
-  w[2] = c1p[xa + r10];
-  w[3] = c0p[xb + r10];
-  w[4] = c1p[xa + r01];
-  w[5] = c0p[xb + r01];
-  w[6] = c0p[xa + r11];
-  w[7] = c1p[xb + r11];
-  // edge e along d from p0 to p1: sigma_{2d}(p0) == sigma_{2d+1}(p1), compared in place by
-  // shifting the start word one field up
-  uint32_t D = 0;
-#pragma unroll
-  for (int e = 0; e < 12; ++e) {
-    const int d = edge_dir(e), p0 = edge_start(e), p1 = p0 | (1 << d);
-    const uint32_t x = ((w[p0] << 3) ^ w[p1]) & (7u << (6 * d + 3));
-    D |= (x == 0u ? 1u : 0u) << e;
-  }
-  const uint32_t cid = (uint32_t)x0 + (uint32_t)L * ((uint32_t)y0 + (uint32_t)L * (uint32_t)z0);
-  U4 rr = philox(cid, t, kStCube, R.replica, R.key0, R.key1);
-  uint32_t nw;
-  if (!lemire_try(rr.x, 9, nw) && !lemire_try(rr.z, 9, nw) && !lemire_try(rr.w, 9, nw))
-    nw = lemire_retry(9, cid, t, kStCube, R.replica, R.key0, R.key1);
-  uint8_t* cs = R.cubes[par] + qi;
-  const uint32_t old = *cs;
-  const int dhb = __popc(ct->act[nw] & D) - __popc(ct->act[old] & D);
-  if ((unsigned long long)rr.y < ct->thr[dhb + 4] && nw != old) *cs = (uint8_t)nw;
-}
-
-// Cube moves of every replica, then (blocks at and after nblk_cube) the volume move of replica
-// (block - nblk_cube), both with the counters of the current step.
-__global__ void __launch_bounds__(kThreads) k_cube_volume(const ReplicaDesc* __restrict__ reps,
-                                                          ReplicaState* __restrict__ st,
-                                                          const int* __restrict__ blk, int nrep, int nblk_cube) {
-  if ((int)blockIdx.x >= nblk_cube) {
-    const int r = blockIdx.x - nblk_cube;
-    if (threadIdx.x < 32 && r < nrep) volume_move_warp(reps[r], st[r], st[r].cur[2]);
-    return;
-  }
-  __shared__ CubeTables s_ct[kThreads / 32];
-  const int r = find_replica(blk, nrep, blockIdx.x);
-  const ReplicaDesc& R = reps[r];
-  CubeTables* ct = s_ct + (threadIdx.x >> 5);
-  fill_cube_tables(R, ct, threadIdx.x & 31);
-  __syncwarp();
-  cube_move(R, ct, blk, r, blockIdx.x, st[r].cur[1]);
-}
-
-// ------------------------------------------------------------------ checkerboard sweep
+// ------------------------------------------------------------------ vector access helpers
 template <int V>
 struct VecLoad;
 template <>
@@ -352,6 +268,131 @@ struct Log2V<4> {
   static constexpr int v = 2;
 };
 
+// ------------------------------------------------------------------ cube move (+ volume blocks)
+// Warp-private copy of the cube tables (a warp reads 9 distinct words at most, so the random
+// lookups of its 32 cubes neither serialise like divergent constant-bank reads nor conflict).
+//   act[s]  12-bit mask of the cube edges that carry eta = 1 in state s
+//   thr[i]  acceptance threshold of dN_hb = i - 4 (U < thr, thr in [0, 2^32])
+struct CubeTables {
+  unsigned long long thr[9];
+  uint32_t act[9];
+};
+
+__device__ __forceinline__ void fill_cube_tables(const ReplicaDesc& R, CubeTables* ct, int lane) {
+  if (lane < 9) {
+    ct->thr[lane] = R.thr_cube[lane];
+    ct->act[lane] = c_state_active[lane];
+  }
+}
+
+// GW:3374-3466. One thread per VC consecutive cubes along x of one parity (both parities in one
+// launch: cubes share no edge and sigma is frozen, so all cube decisions are independent). The
+// block's half of the replica's blocks in the table blk (blk_cubev) gives the parity: even
+// origins (2a,2b,2c) first, then odd origins (2a+1,2b+1,2c+1). Vertex p = dx | dy<<1 | dz<<2 of
+// cube (a,b,c) has colour (parity + popc(p)) & 1 and word (x>>1) + H*(y + L*z), which is a for
+// every vertex except dx = 1 of an odd cube (a + 1, wrapping at the row end): the VC cubes read
+// each vertex row with one VC-word access, the odd dx = 1 rows with one more word. Their VC state
+// bytes are one aligned word, written back when a state changed. t is the cube-move counter of
+// the step. Plain (coherent) loads: the persistent step kernel reads cells that other blocks
+// wrote earlier in the same launch.
+template <int VC>
+__device__ __forceinline__ void cube_move_v(const ReplicaDesc& R, const CubeTables* ct, const int* __restrict__ blk,
+                                            int r, int vb, uint32_t t) {
+  const uint32_t L = R.L, H = R.H, cpr = H / VC;
+  const int b0 = __ldg(blk + r), half = (__ldg(blk + r + 1) - b0) >> 1;
+  const int lb = vb - b0;
+  const uint32_t par = lb >= half;
+  const uint32_t qi = (uint32_t)(lb - (int)par * half) * blockDim.x + threadIdx.x;
+  if (qi >= cpr * H * H) return;
+  uint32_t seg, bc, b, c;
+  divmod32(qi, cpr, R.lgH >= 0 ? R.lgH - Log2V<VC>::v : -1, bc, seg);
+  divmod32(bc, H, R.lgH, c, b);
+  const uint32_t a0 = seg * VC;
+  const uint32_t y0 = 2 * b + par, z0 = 2 * c + par;
+  const uint32_t y1 = y0 + 1 == L ? 0 : y0 + 1, z1 = z0 + 1 == L ? 0 : z0 + 1;
+  const uint32_t rows[4] = {H * (y0 + L * z0), H * (y1 + L * z0), H * (y0 + L * z1), H * (y1 + L * z1)};
+  const uint32_t anext = a0 + VC == H ? 0 : a0 + VC;
+  uint32_t w[8][VC];
+#pragma unroll
+  for (int p = 0; p < 8; ++p) {
+    const uint32_t* arr = R.cells[(par + (uint32_t)__popc(p)) & 1u] + rows[p >> 1];
+    VecLoad<VC>::ld(arr + a0, w[p]);
+    if ((p & 1) && par) {  // x = 2a + 2: words a0+1 .. a0+VC
+      const uint32_t nxt = arr[anext];
+#pragma unroll
+      for (int k = 0; k < VC; ++k) w[p][k] = k + 1 < VC ? w[p][k + 1] : nxt;
+    }
+  }
+  uint8_t* cs = R.cubes[par] + a0 + H * bc;
+  uint32_t st[VC];
+  uint32_t packed;
+  if (VC == 4) packed = *reinterpret_cast<const uint32_t*>(cs);
+  else if (VC == 2) packed = *reinterpret_cast<const uint16_t*>(cs);
+  else packed = *cs;
+#pragma unroll
+  for (int k = 0; k < VC; ++k) st[k] = (packed >> (8 * k)) & 0xffu;
+  const uint32_t cid0 = 2 * a0 + par + L * (y0 + L * z0);
+  bool changed = false;
+#pragma unroll
+  for (int k = 0; k < VC; ++k) {
+    // edge e along d from p0 to p1: sigma_{2d}(p0) == sigma_{2d+1}(p1), compared in place by
+    // shifting the start word one field up
+    uint32_t D = 0;
+#pragma unroll
+    for (int e = 0; e < 12; ++e) {
+      const int d = edge_dir(e), p0 = edge_start(e), p1 = p0 | (1 << d);
+      const uint32_t x = ((w[p0][k] << 3) ^ w[p1][k]) & (7u << (6 * d + 3));
+      D |= (x == 0u ? 1u : 0u) << e;
+    }
+    const uint32_t cid = cid0 + 2u * k;
+    const U4 rr = philox(cid, t, kStCube, R.replica, R.key0, R.key1);
+    uint32_t nw;
+    if (!lemire_try(rr.x, 9, nw) && !lemire_try(rr.z, 9, nw) && !lemire_try(rr.w, 9, nw))
+      nw = lemire_retry(9, cid, t, kStCube, R.replica, R.key0, R.key1);
+    const uint32_t old = st[k];
+    const int dhb = __popc(ct->act[nw] & D) - __popc(ct->act[old] & D);
+    if ((unsigned long long)rr.y < ct->thr[dhb + 4] && nw != old) {
+      st[k] = nw;
+      changed = true;
+    }
+  }
+  if (changed) {
+    uint32_t out = 0;
+#pragma unroll
+    for (int k = 0; k < VC; ++k) out |= st[k] << (8 * k);
+    if (VC == 4) *reinterpret_cast<uint32_t*>(cs) = out;
+    else if (VC == 2) *reinterpret_cast<uint16_t*>(cs) = (uint16_t)out;
+    else *cs = (uint8_t)out;
+  }
+}
+
+__device__ __forceinline__ void cube_move(const ReplicaDesc& R, const CubeTables* ct, const int* __restrict__ blk,
+                                          int r, int vb, uint32_t t) {
+  if (R.cvec == 4) cube_move_v<4>(R, ct, blk, r, vb, t);
+  else if (R.cvec == 2) cube_move_v<2>(R, ct, blk, r, vb, t);
+  else cube_move_v<1>(R, ct, blk, r, vb, t);
+}
+
+// Cube moves of every replica, then (blocks at and after nblk_cube) the volume move of replica
+// (block - nblk_cube), both with the counters of the current step.
+__global__ void __launch_bounds__(kThreads) k_cube_volume(const ReplicaDesc* __restrict__ reps,
+                                                          ReplicaState* __restrict__ st,
+                                                          const int* __restrict__ blk, int nrep, int nblk_cube) {
+  if ((int)blockIdx.x >= nblk_cube) {
+    const int r = blockIdx.x - nblk_cube;
+    if (threadIdx.x < 32 && r < nrep) volume_move_warp(reps[r], st[r], st[r].cur[2]);
+    return;
+  }
+  __shared__ CubeTables s_ct[kThreads / 32];
+  const int r = find_replica(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  CubeTables* ct = s_ct + (threadIdx.x >> 5);
+  fill_cube_tables(R, ct, threadIdx.x & 31);
+  __syncwarp();
+  cube_move(R, ct, blk, r, blockIdx.x, st[r].cur[1]);
+}
+
+// ------------------------------------------------------------------ checkerboard sweep
 // Thread -> (row segment, y, z) of a replica's colour array: q = hc + (H/V) * (y + L*z).
 template <int V>
 __device__ __forceinline__ bool segment_of(const ReplicaDesc& R, uint32_t q, int& hc, int& y, int& z) {
@@ -842,7 +883,7 @@ __device__ __forceinline__ void deal(GridSync* gs, Dealer& d, int n, int* s_vb, 
 
 // nsteps Metropolis steps of every replica in one cooperative launch. Each phase (cube moves with
 // one volume block per replica, then every sweep colour, then the measurement of a recorded
-// step) deals the blocks of its per-phase table (blk_cube, blk_sweep) to the resident blocks
+// step) deals the blocks of its per-phase table (blk_cubev, blk_sweep) to the resident blocks
 // through tickets, and a grid barrier closes the phase. Step s uses the counters the per-phase
 // kernels get from k_step_begin: sweep ctr[0] + s*nmet + j, cube ctr[1] + s, volume
 // ctr[2] + s; the counters advance once, after the last step. With interval > 0 a measurement
@@ -865,14 +906,14 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_run(BatchDev
     if (k == 0) {
       const bool rec = interval > 0 && s % interval == 0;
       const bool prev_rec = interval > 0 && s > 0 && (s - 1) % interval == 0;
-      deal(b.gsync, d, b.nblk_cube + b.nrep, s_vb, [&](int vb) {
-        if (vb < b.nblk_cube) {
-          const int r = find_replica(b.blk_cube, b.nrep, vb);
+      deal(b.gsync, d, b.nblk_cubev + b.nrep, s_vb, [&](int vb) {
+        if (vb < b.nblk_cubev) {
+          const int r = find_replica(b.blk_cubev, b.nrep, vb);
           StepTables* wt = s_tab + (threadIdx.x >> 5);
           ensure_tables(b.reps, r, wt, s_held[threadIdx.x >> 5]);
-          cube_move(b.reps[r], &wt->cube, b.blk_cube, r, vb, b.st[r].ctr[1] + (uint32_t)s);
+          cube_move(b.reps[r], &wt->cube, b.blk_cubev, r, vb, b.st[r].ctr[1] + (uint32_t)s);
         } else if (threadIdx.x < 32) {
-          const int r = vb - b.nblk_cube;
+          const int r = vb - b.nblk_cubev;
           ReplicaState& S = b.st[r];
           if (threadIdx.x == 0) {
             if (prev_rec) measure_finish(S, 1);
@@ -934,10 +975,10 @@ void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do
 }
 
 void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s) {
-  const int cube_blocks = do_cubes ? b.nblk_cube : 0;
+  const int cube_blocks = do_cubes ? b.nblk_cubev : 0;
   const int vol_blocks = do_volume ? b.nrep : 0;
   if (cube_blocks + vol_blocks == 0) return;
-  k_cube_volume<<<cube_blocks + vol_blocks, kThreads, 0, s>>>(b.reps, b.st, b.blk_cube, b.nrep, cube_blocks);
+  k_cube_volume<<<cube_blocks + vol_blocks, kThreads, 0, s>>>(b.reps, b.st, b.blk_cubev, b.nrep, cube_blocks);
 }
 
 void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s) {
@@ -968,7 +1009,7 @@ static cudaError_t launch_run_v(const BatchDev& b, int nsteps, int nmet, int int
   if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_run<V>, kThreads, 0);
   if (e != cudaSuccess) return e;
   if (per < 1) return cudaErrorInvalidConfiguration;
-  const int work = b.nblk_sweep > b.nblk_cube + b.nrep ? b.nblk_sweep : b.nblk_cube + b.nrep;
+  const int work = b.nblk_sweep > b.nblk_cubev + b.nrep ? b.nblk_sweep : b.nblk_cubev + b.nrep;
   const int grid = nsm * per < work ? nsm * per : work;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
