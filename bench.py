@@ -309,7 +309,7 @@ def run_engine(args):
     stream = torch.cuda.ExternalStream(lat.stream_ptr(), device=local)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
-    tile = lat.autotune()
+    tile = lat.set_sweep_tile(args.tile) if args.tile else lat.autotune()
     lat.run(args.warmup, 1, 0)
     lat.synchronize()
     # roofline of the dominant kernel (the sweep), two launches per profiled sweep
@@ -445,6 +445,8 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and Swendsen-Wang sub-benchmarks")
+    ap.add_argument("--tile", type=int, default=0,
+                    help="sweep tile (cells per thread) instead of the autotuner's choice, e.g. to profile one tile")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

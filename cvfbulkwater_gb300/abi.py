@@ -97,6 +97,7 @@ def lib():
         "cvf_get_thresholds": (I, [P, I, P]),
         "cvf_get_stream": (I, [P, C.POINTER(P)]),
         "cvf_autotune": (I, [P, C.POINTER(I)]),
+        "cvf_set_sweep_tile": (I, [P, I, C.POINTER(I)]),
         "cvf_set_launch_mode": (I, [P, I]),
         "cvf_get_launch_mode": (I, [P, C.POINTER(I)]),
         "cvf_profile_launch": (I, [P, I, I]),

@@ -727,6 +727,17 @@ int cvf_autotune(cvf_handle* h, int* vec_out) {
   return 0;
 }
 
+int cvf_set_sweep_tile(cvf_handle* h, int vec, int* vec_out) {
+  if (!h || !(vec == 1 || vec == 2 || vec == 4 || vec == 8)) return fail(CVF_EINVAL, "tile must be 1, 2, 4 or 8");
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+  h->graphs.clear();
+  if (int rc = build_tables(h, vec)) return rc;
+  if (vec_out) *vec_out = h->b.vec;
+  return 0;
+}
+
 int cvf_get_stream(cvf_handle* h, void** stream) {
   if (!h || !stream) return fail(CVF_EINVAL, "null handle/out");
   *stream = (void*)h->stream;

@@ -107,6 +107,12 @@ class Lattice:
         check(lib().cvf_autotune(self._h, C.byref(v)))
         return v.value
 
+    def set_sweep_tile(self, vec: int) -> int:
+        """Set the sweep tile (cells per thread) by hand; returns the tile in effect."""
+        v = C.c_int()
+        check(lib().cvf_set_sweep_tile(self._h, int(vec), C.byref(v)))
+        return v.value
+
     @property
     def launch_mode(self) -> int:
         """1: Metropolis-only steps run as one persistent launch per graph; 0: one launch per phase."""

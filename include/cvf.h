@@ -180,6 +180,11 @@ int cvf_format_cluster_line(char* buf, int cap, int t, const cvf_cstats* c);
  * unchanged (the tile only changes the thread mapping, never the result). vec_out may be NULL.
  * No reference counterpart. */
 int cvf_autotune(cvf_handle* h, int* vec_out);
+/* Sets the sweep tile by hand (1, 2, 4 or 8 cells per thread; reduced to the largest that divides
+ * every replica's L/2), as the autotuner would. The environment variable CVF_SWEEP_VEC gives the
+ * tile a new handle starts with (default 4). Returns the tile in effect through vec_out (may be
+ * NULL). No reference counterpart. */
+int cvf_set_sweep_tile(cvf_handle* h, int vec, int* vec_out);
 
 /* Launch mode of Metropolis-only steps (n_cluster == 0). 0 (default): a captured CUDA graph per
  * chunk of steps with one kernel per phase (cube + volume moves, each sweep colour, the recorded
