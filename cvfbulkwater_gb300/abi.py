@@ -100,6 +100,8 @@ def lib():
         "cvf_set_sweep_tile": (I, [P, I, C.POINTER(I)]),
         "cvf_set_launch_mode": (I, [P, I]),
         "cvf_get_launch_mode": (I, [P, C.POINTER(I)]),
+        "cvf_set_io_mode": (I, [P, I]),
+        "cvf_get_io_mode": (I, [P, C.POINTER(I)]),
         "cvf_profile_launch": (I, [P, I, I]),
         "cvf_cluster_stats_noalloc": (I, [P, I, P, P]),
         "cvf_read_input_data": (I, [C.c_char_p, C.POINTER(Input)]),

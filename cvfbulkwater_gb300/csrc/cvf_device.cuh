@@ -109,17 +109,30 @@ constexpr int kThreads = 256;
 
 void launch_init_lattice(const BatchDev& b, cudaStream_t s);
 void init_device_tables();
-void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do_volume, cudaStream_t s);
+// Snapshot of this step's move counters; zero_slots also clears the measurement slots of a
+// step whose measurement is fused into its last colour-1 sweep.
+void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do_volume, cudaStream_t s,
+                       int zero_slots = 0);
 // Cube moves of all replicas (do_cubes) and, in extra blocks of the same launch, their volume
 // moves (do_volume): the two moves are independent, so the volume move hides under the cubes.
 void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s);
 void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s);
 void launch_measure(const BatchDev& b, int record, cudaStream_t s);
+// Colour-1 sweep jsweep fused with the measurement of the step (slots zeroed by the step's
+// launch_step_begin), and the summation of the slots into the replica's record.
+void launch_sweep_measure(const BatchDev& b, int jsweep, cudaStream_t s);
+void launch_measure_end(const BatchDev& b, int record, cudaStream_t s);
 // Persistent cooperative launch of nsteps Metropolis steps (cube + volume move, nmet sweeps) of
 // every replica, with a recorded measurement after every step s with s % interval == 0 when
 // interval > 0. Same lattice, counters and samples as the per-phase kernels.
 cudaError_t launch_run(const BatchDev& b, int nsteps, int nmet, int interval, cudaStream_t s);
 void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s);
+// Configuration upload read in place from host memory (the GPU must access pageable host
+// memory): pack the caller's cells12 array into cells0/cells1/ce/co (scratch buffers of the
+// replica's sizes; eta6 holds N bytes; *bad must start at N and receives the smallest invalid
+// cell).
+cudaError_t launch_pack_config(const ReplicaDesc& R, const int* c12, uint32_t* cells0, uint32_t* cells1, uint8_t* eta6,
+                               uint8_t* ce, uint8_t* co, unsigned long long* bad, cudaStream_t s);
 void launch_cluster_stats_impl(const BatchDev& b, unsigned long long* blocktop, int record, cudaStream_t s);
 
 }  // namespace cvf

@@ -116,6 +116,16 @@ static void parallel_for(long long n, long long work, F body) {
   for (auto& t : th) t.join();
 }
 
+std::string config_value_error(const int* c12, long long c) {
+  for (int a = 0; a < 6; ++a) {
+    int s = c12[c * 12 + a], e = c12[c * 12 + 6 + a];
+    if (s < 0 || s > 5) return "Unexpected value for spin (" + std::to_string(s) + ") appeared in line " + std::to_string(c);
+    if (e < 0 || e > 1)
+      return "Unexpected value for active_bond (" + std::to_string(e) + ") appeared in line " + std::to_string(c);
+  }
+  return "invalid cell " + std::to_string(c);
+}
+
 bool pack_config(int L, const int* c12, uint32_t* cells0, uint32_t* cells1, uint8_t* ce, uint8_t* co,
                  std::string& err) {
   const int H = L / 2;
@@ -146,18 +156,8 @@ bool pack_config(int L, const int* c12, uint32_t* cells0, uint32_t* cells1, uint
     }
   });
   if (bad.load() < N) {
-    long long c = bad.load();
-    for (int a = 0; a < 6; ++a) {
-      int s = c12[c * 12 + a], e = c12[c * 12 + 6 + a];
-      if (s < 0 || s > 5) {
-        err = "Unexpected value for spin (" + std::to_string(s) + ") appeared in line " + std::to_string(c);
-        return false;
-      }
-      if (e < 0 || e > 1) {
-        err = "Unexpected value for active_bond (" + std::to_string(e) + ") appeared in line " + std::to_string(c);
-        return false;
-      }
-    }
+    err = config_value_error(c12, bad.load());
+    return false;
   }
   auto eta = [&](int arm, int x, int y, int z) -> int {
     return c12[((long long)x + (long long)L * (y + (long long)L * z)) * 12 + 6 + arm];

@@ -34,6 +34,8 @@ void fill_cstats(cvf_cstats* c);
 // eta is read with the decision tree of GW:3314-3371. Threaded over rows of the lattice.
 bool pack_config(int L, const int* cells12, uint32_t* cells0, uint32_t* cells1, uint8_t* cubes_even,
                  uint8_t* cubes_odd, std::string& err);
+// The reader's message (GW:776-790) for the first invalid value of cell c.
+std::string config_value_error(const int* c12, long long c);
 void unpack_config(int L, const uint32_t* cells0, const uint32_t* cells1, const uint8_t* cubes_even,
                    const uint8_t* cubes_odd, int* cells12);
 

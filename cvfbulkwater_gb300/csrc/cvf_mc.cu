@@ -73,6 +73,56 @@ __device__ __forceinline__ uint32_t cell_word_index(int x, int y, int z, int L, 
   return (uint32_t)(x >> 1) + (uint32_t)H * ((uint32_t)y + (uint32_t)L * (uint32_t)z);
 }
 
+// ------------------------------------------------------------------ measurement slots
+// Block sum of the per-thread counts into slot vb % 32 of replica state S (all threads of the
+// block call it; s_acc is the block's two-word scratch).
+__device__ __forceinline__ void measure_accumulate(ReplicaState& S, int vb, uint32_t hb2, uint32_t ns,
+                                                   unsigned long long* s_acc) {
+  if (threadIdx.x < 2) s_acc[threadIdx.x] = 0;
+  __syncthreads();
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    hb2 += __shfl_xor_sync(0xffffffffu, hb2, o);
+    ns += __shfl_xor_sync(0xffffffffu, ns, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&s_acc[0], (unsigned long long)hb2);
+    atomicAdd(&s_acc[1], (unsigned long long)ns);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    atomicAdd(&S.acc_slot[0][vb & 31], s_acc[0]);
+    atomicAdd(&S.acc_slot[1][vb & 31], s_acc[1]);
+  }
+}
+
+__device__ __forceinline__ void measure_zero(ReplicaState& S) {
+  for (int i = 0; i < 32; ++i) {
+    S.acc_slot[0][i] = 0;
+    S.acc_slot[1][i] = 0;
+  }
+}
+
+// Sums the slots into the replica's last measurement and appends it to the sample stream when
+// record is set.
+__device__ __forceinline__ void measure_finish(ReplicaState& S, int record) {
+  unsigned long long hb2 = 0, ns = 0;
+  for (int i = 0; i < 32; ++i) {
+    hb2 += S.acc_slot[0][i];
+    ns += S.acc_slot[1][i];
+  }
+  S.acc_hb2 = hb2;
+  S.acc_ns = ns;
+  SampleRec rec;
+  rec.n_hb2 = (long long)hb2;
+  rec.n_sigma = (long long)ns;
+  rec.r_cell = S.r_cell;
+  rec.volume = S.volume;
+  S.last = rec;
+  if (record && S.samples && S.n_samples < S.cap_samples) S.samples[S.n_samples] = rec;
+  if (record) S.n_samples++;
+}
+
 // ------------------------------------------------------------------ initialisation
 // GW:812-825: disordered start draws each sigma uniformly, ordered start one common value.
 __global__ void k_init_sigma(const ReplicaDesc* __restrict__ reps, const int* __restrict__ blk, int nrep) {
@@ -129,10 +179,11 @@ __global__ void k_init_cubes(const ReplicaDesc* __restrict__ reps, const int* __
 // ------------------------------------------------------------------ step begin: move counters
 // One thread per replica: snapshot the move counters that this step's kernels use.
 __global__ void k_step_begin(ReplicaState* __restrict__ st, int nrep, int nmet, int ncl, int do_cube,
-                             int do_volume) {
+                             int do_volume, int zero_slots) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrep) return;
   ReplicaState& S = st[r];
+  if (zero_slots) measure_zero(S);
   S.cur[0] = S.ctr[0];
   S.ctr[0] += (uint32_t)nmet;
   S.cur[1] = S.ctr[1];
@@ -471,6 +522,21 @@ __device__ __forceinline__ uint32_t neighbour_sigmas(uint32_t xp, uint32_t xm, u
          (((zp >> 15) & 7u) << 12) | (((zm >> 12) & 7u) << 15);
 }
 
+// Number of zero 3-bit fields among the six fields of x.
+__device__ __forceinline__ uint32_t zero_fields(uint32_t x) {
+  return 6u - (uint32_t)__popc((x | (x >> 1) | (x >> 2)) & 0x9249u);
+}
+
+// sum_{a<b} delta(sigma_a, sigma_b) of one cell: with Z_k the number of arms a equal to arm
+// (a+k) mod 6, every unordered pair is counted by Z_k and Z_{6-k}, so the sum is Z_1 + Z_2 + Z_3/2.
+__device__ __forceinline__ uint32_t sigma_pairs(uint32_t w) {
+  w &= 0x3ffffu;
+  const uint32_t r1 = ((w >> 3) | (w << 15)) & 0x3ffffu;
+  const uint32_t r2 = ((w >> 6) | (w << 12)) & 0x3ffffu;
+  const uint32_t r3 = ((w >> 9) | (w << 9)) & 0x3ffffu;
+  return zero_fields(w ^ r1) + zero_fields(w ^ r2) + (zero_fields(w ^ r3) >> 1);
+}
+
 __device__ __forceinline__ uint32_t sigma_histogram(uint32_t w) {
   uint32_t h = 0;
 #pragma unroll
@@ -644,10 +710,15 @@ template <int V>
 struct SweepMinBlocks {
   static constexpr int v = V >= 8 ? 3 : 4;
 };
-// Row segment q (V cells) of one colour of replica R with sweep counter t.
-template <int V>
+// Row segment q (V cells) of one colour of replica R with sweep counter t. With kMeasure (the
+// colour-1 sweep of a recorded step) it also adds the segment's share of the measurement of
+// GW:2014-2160 to hb2 and ns after the update: every bond has exactly one colour-1 end, so the
+// colour-1 cells count all bonds (delta of the facing sigmas times the bond's eta, twice), and
+// each colour-1 cell adds the sigma pairs of itself and of the colour-0 cell with the same word
+// index (the x-neighbour the segment loads anyway).
+template <int V, bool kMeasure>
 __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepTables* wt, uint32_t q, int colour,
-                                              uint32_t t) {
+                                              uint32_t t, uint32_t& hb2, uint32_t& ns) {
   int hc, y, z;
   if (!segment_of<V>(R, q, hc, y, z)) return;
   uint32_t out[V], nbs[V], nbe[V], eta[V];
@@ -662,6 +733,7 @@ __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepT
       eta[k] = cb.eta[k];
       nbe[k] = nbs[k] | wt->et.nbmask[~cb.eta[k] & 63u];
       out[k] = cb.own[k];
+      if (kMeasure) ns += sigma_pairs(cb.s == 0 ? cb.xp[k] : cb.xm[k]);
     }
     own_ptr = cb.own_ptr;
     x0 = cb.x0;
@@ -675,6 +747,15 @@ __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepT
     out[k] = update_cell(out[k], nbs[k], nbe[k], eta[k], rr, c0, t, R, wt);
   }
   VecLoad<V>::st(own_ptr, out);
+  if (kMeasure) {
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const uint32_t x = out[k] ^ nbs[k];
+      const uint32_t eqm = ~(x | (x >> 1) | (x >> 2)) & wt->et.nbmask[eta[k] & 63u] & 0x9249u;
+      hb2 += 2u * (uint32_t)__popc(eqm);
+      ns += sigma_pairs(out[k]);
+    }
+  }
 }
 
 template <int V>
@@ -685,26 +766,29 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const 
   const int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   const SweepTables* wt = warp_sweep_tables(R, s_tab);
-  sweep_segment<V>(R, wt, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
-                   st[r].cur[0] + (uint32_t)jsweep);
+  uint32_t hb2 = 0, ns = 0;
+  sweep_segment<V, false>(R, wt, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
+                          st[r].cur[0] + (uint32_t)jsweep, hb2, ns);
+}
+
+// Colour-1 sweep of a recorded step fused with its measurement: the counts go to the slots
+// that k_step_begin zeroed, k_measure_end sums them after the step.
+template <int V>
+__global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep_measure(
+    const ReplicaDesc* __restrict__ reps, ReplicaState* __restrict__ st, const int* __restrict__ blk, int nrep,
+    int jsweep) {
+  __shared__ SweepTables s_tab[kThreads / 32];
+  __shared__ unsigned long long s_acc[2];
+  const int r = find_replica(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  const SweepTables* wt = warp_sweep_tables(R, s_tab);
+  uint32_t hb2 = 0, ns = 0;
+  sweep_segment<V, true>(R, wt, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, 1,
+                         st[r].cur[0] + (uint32_t)jsweep, hb2, ns);
+  measure_accumulate(st[r], blockIdx.x, hb2, ns, s_acc);
 }
 
 // ------------------------------------------------------------------ measurement
-// Number of zero 3-bit fields among the six fields of x.
-__device__ __forceinline__ uint32_t zero_fields(uint32_t x) {
-  return 6u - (uint32_t)__popc((x | (x >> 1) | (x >> 2)) & 0x9249u);
-}
-
-// sum_{a<b} delta(sigma_a, sigma_b) of one cell: with Z_k the number of arms a equal to arm
-// (a+k) mod 6, every unordered pair is counted by Z_k and Z_{6-k}, so the sum is Z_1 + Z_2 + Z_3/2.
-__device__ __forceinline__ uint32_t sigma_pairs(uint32_t w) {
-  w &= 0x3ffffu;
-  const uint32_t r1 = ((w >> 3) | (w << 15)) & 0x3ffffu;
-  const uint32_t r2 = ((w >> 6) | (w << 12)) & 0x3ffffu;
-  const uint32_t r3 = ((w >> 9) | (w << 9)) & 0x3ffffu;
-  return zero_fields(w ^ r1) + zero_fields(w ^ r2) + (zero_fields(w ^ r3) >> 1);
-}
-
 // GW:2014-2160: N_hb2 = sum over bonds of delta * (eta_i + eta_j), counted from the colour-0
 // end of every bond (each bond joins the two colours); N_sigma over cells of both colours.
 // Counts of the V-cell colour-0 segment q of replica R, added to hb2 and ns.
@@ -730,28 +814,6 @@ __device__ __forceinline__ void measure_segment(const ReplicaDesc& R, const EtaT
   }
 }
 
-// Block sum of the per-thread counts into slot vb % 32 of replica state S (all threads of the
-// block call it; s_acc is the block's two-word scratch).
-__device__ __forceinline__ void measure_accumulate(ReplicaState& S, int vb, uint32_t hb2, uint32_t ns,
-                                                   unsigned long long* s_acc) {
-  if (threadIdx.x < 2) s_acc[threadIdx.x] = 0;
-  __syncthreads();
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    hb2 += __shfl_xor_sync(0xffffffffu, hb2, o);
-    ns += __shfl_xor_sync(0xffffffffu, ns, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&s_acc[0], (unsigned long long)hb2);
-    atomicAdd(&s_acc[1], (unsigned long long)ns);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    atomicAdd(&S.acc_slot[0][vb & 31], s_acc[0]);
-    atomicAdd(&S.acc_slot[1][vb & 31], s_acc[1]);
-  }
-}
-
 template <int V>
 __global__ void __launch_bounds__(kThreads) k_measure(const ReplicaDesc* __restrict__ reps,
                                                       ReplicaState* __restrict__ st,
@@ -764,33 +826,6 @@ __global__ void __launch_bounds__(kThreads) k_measure(const ReplicaDesc* __restr
   uint32_t hb2 = 0, ns = 0;
   measure_segment<V>(R, et, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, hb2, ns);
   measure_accumulate(st[r], blockIdx.x, hb2, ns, s_acc);
-}
-
-__device__ __forceinline__ void measure_zero(ReplicaState& S) {
-  for (int i = 0; i < 32; ++i) {
-    S.acc_slot[0][i] = 0;
-    S.acc_slot[1][i] = 0;
-  }
-}
-
-// Sums the slots into the replica's last measurement and appends it to the sample stream when
-// record is set.
-__device__ __forceinline__ void measure_finish(ReplicaState& S, int record) {
-  unsigned long long hb2 = 0, ns = 0;
-  for (int i = 0; i < 32; ++i) {
-    hb2 += S.acc_slot[0][i];
-    ns += S.acc_slot[1][i];
-  }
-  S.acc_hb2 = hb2;
-  S.acc_ns = ns;
-  SampleRec rec;
-  rec.n_hb2 = (long long)hb2;
-  rec.n_sigma = (long long)ns;
-  rec.r_cell = S.r_cell;
-  rec.volume = S.volume;
-  S.last = rec;
-  if (record && S.samples && S.n_samples < S.cap_samples) S.samples[S.n_samples] = rec;
-  if (record) S.n_samples++;
 }
 
 __global__ void k_measure_begin(ReplicaState* __restrict__ st, int nrep) {
@@ -930,8 +965,9 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_run(BatchDev
         const int r = find_replica(b.blk_sweep, b.nrep, vb);
         StepTables* wt = s_tab + (threadIdx.x >> 5);
         ensure_tables(b.reps, r, wt, s_held[threadIdx.x >> 5]);
-        sweep_segment<V>(b.reps[r], &wt->sw, (uint32_t)(vb - b.blk_sweep[r]) * blockDim.x + threadIdx.x, colour,
-                         b.st[r].ctr[0] + toff);
+        uint32_t hb2 = 0, ns = 0;
+        sweep_segment<V, false>(b.reps[r], &wt->sw, (uint32_t)(vb - b.blk_sweep[r]) * blockDim.x + threadIdx.x,
+                                colour, b.st[r].ctr[0] + toff, hb2, ns);
       });
     } else {
       if (!(interval > 0 && s % interval == 0)) continue;  // no measurement after this step
@@ -970,8 +1006,22 @@ void launch_init_lattice(const BatchDev& b, cudaStream_t s) {
   k_init_cubes<<<b.nblk_cube, kThreads, 0, s>>>(b.reps, b.blk_cube, b.nrep);
 }
 
-void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do_volume, cudaStream_t s) {
-  k_step_begin<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, nmet, ncl, do_cube, do_volume);
+void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do_volume, cudaStream_t s,
+                       int zero_slots) {
+  k_step_begin<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, nmet, ncl, do_cube, do_volume, zero_slots);
+}
+
+void launch_sweep_measure(const BatchDev& b, int jsweep, cudaStream_t s) {
+  switch (b.vec) {
+    case 8: k_sweep_measure<8><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, jsweep); break;
+    case 4: k_sweep_measure<4><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, jsweep); break;
+    case 2: k_sweep_measure<2><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, jsweep); break;
+    default: k_sweep_measure<1><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, jsweep); break;
+  }
+}
+
+void launch_measure_end(const BatchDev& b, int record, cudaStream_t s) {
+  k_measure_end<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, record);
 }
 
 void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s) {

@@ -114,6 +114,17 @@ class Lattice:
         return v.value
 
     @property
+    def io_mode(self) -> int:
+        """1: set_config reads the caller's array in host memory from the GPU; 0: host packing."""
+        m = C.c_int()
+        check(lib().cvf_get_io_mode(self._h, C.byref(m)))
+        return m.value
+
+    @io_mode.setter
+    def io_mode(self, mode: int):
+        check(lib().cvf_set_io_mode(self._h, int(mode)))
+
+    @property
     def launch_mode(self) -> int:
         """1: Metropolis-only steps run as one persistent launch per graph; 0: one launch per phase."""
         m = C.c_int()

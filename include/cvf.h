@@ -199,6 +199,17 @@ int cvf_set_sweep_tile(cvf_handle* h, int vec, int* vec_out);
 int cvf_set_launch_mode(cvf_handle* h, int mode);
 int cvf_get_launch_mode(const cvf_handle* h, int* mode);
 
+/* Transfer mode of cvf_set_config. 1: kernels read and pack the caller's cells12 array where it
+ * lies in host memory (the GPU accesses pageable host memory through the host page tables, as
+ * over NVLink-C2C on GB300); the default when the device reports
+ * cudaDevAttrPageableMemoryAccess. 0: host threads pack into pinned memory, then one copy (the
+ * only mode on other systems; cvf_set_io_mode(h, 1) then fails with CVF_EINVAL). Both modes give
+ * the same lattice and the same error for an invalid value (the lattice is left unchanged).
+ * cvf_get_config always copies the packed lattice and unpacks it with host threads, which is the
+ * faster direction on GB300. No reference counterpart. */
+int cvf_set_io_mode(cvf_handle* h, int mode);
+int cvf_get_io_mode(const cvf_handle* h, int* mode);
+
 /* The CUDA stream (a cudaStream_t passed as void*) on which all work of the handle is ordered,
  * for callers that time or order their own work around the engine. No reference counterpart. */
 int cvf_get_stream(cvf_handle* h, void** stream);

@@ -146,3 +146,21 @@ def test_l256_bit_exact_after_ten_sweeps(engine_lib, oracle_mod):
     for _ in range(10):
         ora.step(1, 0)
     assert_same(eng, ora)
+
+
+@pytest.mark.parametrize("tile", [1, 2, 4, 8])
+def test_recorded_samples_every_tile(engine_lib, oracle_mod, tile):
+    """Recorded steps fuse the measurement into the last colour-1 sweep; every tile must give the
+    oracle's counts (L=16: H=8 admits all four tiles)."""
+    eng, ora = pair(oracle_mod, 16, 0.72, 0.45, 99, 0)
+    assert eng.set_sweep_tile(tile) == tile
+    eng.run_sampled(9, 2, 0, 3)
+    smp = eng.samples()
+    assert len(smp) == 3
+    for i in range(9):
+        ora.step(2, 0)
+        if i % 3 == 0:
+            ob = ora.measure()
+            s = smp[i // 3]
+            assert s["n_hb2"] == ob.n_hb2 and s["n_sigma"] == ob.n_sigma and s["r_cell"] == ob.r_cell
+    assert_same(eng, ora)
