@@ -49,6 +49,25 @@ class State(C.Structure):
                 ("counters", C.c_uint * 4)]
 
 
+class RunStats(C.Structure):
+    _fields_ = [("L", C.c_int), ("P", C.c_double), ("T", C.c_double), ("mean", C.c_double * 6),
+                ("var", C.c_double * 6), ("n", C.c_longlong)]
+
+
+_POINT = ("T", "energy", "energy_err", "enthalpy", "enthalpy_err", "volume", "volume_err", "density",
+          "density_err", "nhb", "nhb_err", "ncoop", "ncoop_err", "rcell", "rcell_err", "cp_fluc", "kt_fluc")
+_POINT_SI = ("T_K", "density", "density_err", "enthalpy", "enthalpy_err", "energy", "energy_err", "cp_fluc",
+             "cp_fluc_err", "nhb", "nhb_err", "ncoop", "ncoop_err")
+
+
+class IsobarPoint(C.Structure):
+    _fields_ = [(n, C.c_double) for n in _POINT]
+
+
+class IsobarPointSI(C.Structure):
+    _fields_ = [(n, C.c_double) for n in _POINT_SI]
+
+
 class Input(C.Structure):
     _fields_ = [("P", C.c_float), ("T", C.c_float), ("seed", C.c_longlong), ("metropolis_steps", C.c_int),
                 ("cluster_steps", C.c_int), ("equilibrium_steps", C.c_int), ("sampling_steps", C.c_int),
@@ -111,6 +130,10 @@ def lib():
         "cvf_read_distances_file": (I, [C.c_char_p, I, P, P, I, C.POINTER(I)]),
         "cvf_format_data_line": (I, [C.c_char_p, I, I, C.POINTER(Obs)]),
         "cvf_format_cluster_line": (I, [C.c_char_p, I, I, C.POINTER(CStats)]),
+        "cvf_run_statistics": (I, [P, C.POINTER(RunStats), I]),
+        "cvf_isobar_point_from_stats": (I, [C.POINTER(RunStats), C.POINTER(IsobarPoint)]),
+        "cvf_isobar_point_to_si": (I, [C.POINTER(IsobarPoint), D, C.POINTER(IsobarPointSI)]),
+        "cvf_alpha_p_derivative": (I, [P, P, P, P, I, P, P, P, C.POINTER(I)]),
         "cvf_reweight_forward": (I, [I, P, P, LL, P, I, P, I, D, D, P, P, I, P]),
         "cvf_reweight_adjoint": (I, [I, P, P, LL, P, I, P, D, P, P, I, P, P]),
     }

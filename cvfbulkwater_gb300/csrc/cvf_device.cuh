@@ -127,6 +127,10 @@ void launch_measure_end(const BatchDev& b, int record, cudaStream_t s);
 // interval > 0. Same lattice, counters and samples as the per-phase kernels.
 cudaError_t launch_run(const BatchDev& b, int nsteps, int nmet, int interval, cudaStream_t s);
 void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s);
+// Run statistics of every replica from its sample stream: out[r*14 + k] = mean of data.out
+// column k (k < 6: energy, enthalpy, volume, N_hb, m, r_cell), variance of column k - 6
+// (6 <= k < 12), number of stored samples used (k = 12), number recorded (k = 13).
+cudaError_t launch_run_stats(const BatchDev& b, double* out, cudaStream_t s);
 // Configuration upload read in place from host memory (the GPU must access pageable host
 // memory): pack the caller's cells12 array into cells0/cells1/ce/co (scratch buffers of the
 // replica's sizes; eta6 holds N bytes; *bad must start at N and receives the smallest invalid

@@ -68,6 +68,7 @@ struct cvf_handle {
   void* io_scratch = nullptr;  // device: packed cells, eta bytes and cube states of one replica
   size_t io_scratch_bytes = 0;
   unsigned long long* io_bad = nullptr;  // device: smallest invalid cell of a device-side pack
+  double* stats = nullptr;               // device: 14 doubles per replica for cvf_run_statistics
 };
 
 // Device scratch for a device-side pack of one replica (freed with the handle).
@@ -870,6 +871,36 @@ int cvf_get_io_mode(const cvf_handle* h, int* mode) {
 int cvf_get_launch_mode(const cvf_handle* h, int* mode) {
   if (!h || !mode) return fail(CVF_EINVAL, "null handle/out");
   *mode = h->launch_mode;
+  return 0;
+}
+
+int cvf_run_statistics(cvf_handle* h, cvf_run_stats* out, int n_out) {
+  if (!h || !out) return fail(CVF_EINVAL, "null handle/out");
+  const int n = (int)h->reps.size();
+  if (n_out < n) return fail(CVF_EINVAL, "out must hold one row per replica");
+  CK(cudaSetDevice(h->device));
+  if (!h->stats) {
+    if (int rc = dev_alloc(h, (void**)&h->stats, (size_t)n * 14 * sizeof(double))) return rc;
+  }
+  CK(launch_run_stats(h->b, h->stats, h->stream));
+  std::vector<double> v((size_t)n * 14);
+  CK(cudaMemcpyAsync(v.data(), h->stats, v.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int r = 0; r < n; ++r) {
+    cvf_run_stats& o = out[r];
+    o.L = h->reps[r].L;
+    o.P = (double)h->reps[r].p.P;
+    o.T = (double)h->reps[r].p.T;
+    for (int k = 0; k < 6; ++k) {
+      o.mean[k] = v[r * 14 + k];
+      o.var[k] = v[r * 14 + 6 + k];
+    }
+    o.n = (long long)v[r * 14 + 12];
+  }
+  for (int r = 0; r < n; ++r)
+    if (v[r * 14 + 13] > v[r * 14 + 12])
+      return fail(CVF_ELIMIT, "sample stream of replica " + std::to_string(r) +
+                                  " overflowed its capacity: statistics of the stored samples only");
   return 0;
 }
 

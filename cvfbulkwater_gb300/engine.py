@@ -107,6 +107,14 @@ class Lattice:
         check(lib().cvf_autotune(self._h, C.byref(v)))
         return v.value
 
+    def run_statistics(self):
+        """Mean and <x^2> - <x>^2 of the data.out columns over each replica's recorded samples,
+        computed on the GPU (the awk stage of the reference's isobar analysis)."""
+        n = self.n_replicas
+        rows = (abi.RunStats * n)()
+        check(lib().cvf_run_statistics(self._h, rows, n))
+        return [{"L": r.L, "P": r.P, "T": r.T, "mean": list(r.mean), "var": list(r.var), "n": r.n} for r in rows]
+
     def set_sweep_tile(self, vec: int) -> int:
         """Set the sweep tile (cells per thread) by hand; returns the tile in effect."""
         v = C.c_int()

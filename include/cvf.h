@@ -174,6 +174,58 @@ int cvf_read_distances_file(const char* path, int L, float* dist, int* freq, int
 int cvf_format_data_line(char* buf, int cap, int t, const cvf_obs* o);
 int cvf_format_cluster_line(char* buf, int cap, int t, const cvf_cstats* c);
 
+/* ---------------------------------------------------------------- isobar analysis
+ * The reference's thermodynamic analysis (CVF_ThermodynamicAnalysis/) on the engine's results.
+ *
+ * Run statistics (replaces the awk stage of TA/script_analisi.sh:35): for every replica of the
+ * handle, the mean and the variance <x^2> - <x>^2 of the six data.out columns (GW:2138-2159:
+ * energy, enthalpy, volume, N_hb, m = N_sigma/(15N), r_cell) over the samples recorded so far,
+ * computed on the GPU from the on-device sample stream; only the statistics cross to the host.
+ * out holds n_out >= number of replicas rows. When a replica recorded more samples than its
+ * capacity, every row still holds the statistics of the stored (first) samples and the call
+ * returns CVF_ELIMIT, as cvf_get_samples does. */
+typedef struct cvf_run_stats {
+  int L;
+  double P, T;
+  double mean[6]; /* energy, enthalpy, volume, n_hb, m, r_cell */
+  double var[6];  /* <x^2> - <x>^2, the formula of the reference's awk stage */
+  long long n;    /* samples */
+} cvf_run_stats;
+int cvf_run_statistics(cvf_handle* h, cvf_run_stats* out, int n_out);
+
+/* One isobar point per run (TA/calculadora.sh:41-61): per-cell means and errors
+ * sqrt(3 var / n) / N (the factor 3 is the reference's fixed 1 + 2 tau / dt), density N / <V>,
+ * N_hb / 2N, the cooperative fraction m, r_cell with error sqrt(var / n), and the fluctuation
+ * estimates C_P = var(H) / (T^2 N) and K_T = var(V) / (T <V>). */
+typedef struct cvf_isobar_point {
+  double T;
+  double energy, energy_err, enthalpy, enthalpy_err, volume, volume_err, density, density_err;
+  double nhb, nhb_err, ncoop, ncoop_err, rcell, rcell_err;
+  double cp_fluc, kt_fluc;
+} cvf_isobar_point;
+int cvf_isobar_point_from_stats(const cvf_run_stats* s, cvf_isobar_point* out);
+
+/* SI units of an isobar point at pressure P (internal units), TA/conversor.sh: T in K
+ * (conversor.sh:2-3,20), density in kg/m^3 (:6-7,20), enthalpy in kJ/mol as h*Hs + Hi*T with
+ * error err*Hi (:11-12,24, kept as the reference writes it), energy E = H - 18 (P Ps + Pi) / rho
+ * with the reference's error expression (:76), C_P = cp*CPs + CPi (:8-9,32; the reference's
+ * error column is empty, 0), N_hb and m unchanged (:28). */
+typedef struct cvf_isobar_point_si {
+  double T_K, density, density_err, enthalpy, enthalpy_err, energy, energy_err, cp_fluc, cp_fluc_err;
+  double nhb, nhb_err, ncoop, ncoop_err;
+} cvf_isobar_point_si;
+int cvf_isobar_point_to_si(const cvf_isobar_point* p, double P, cvf_isobar_point_si* out);
+
+/* Thermal expansion alpha_P = (1/V) dV/dT along an isobar by finite differences
+ * (TA/AlphaPderivate.c:56-134): the m points (T, V, variance of V, samples) in any order are
+ * sorted by T; central differences inside, one-sided at the ends; the error combines the
+ * sample error sqrt(3 var / n), the third-derivative term and the neighbours' errors. Like the
+ * reference, only the points 2 .. m-3 of the sorted list are returned (m_out = max(m - 4, 0));
+ * the outputs hold m entries. The differentiable reweighting (cvf_reweight_*) gives alpha_P,
+ * K_T and C_P without finite differences. */
+int cvf_alpha_p_derivative(const double* T, const double* V, const double* V2, const long long* n, int m,
+                           double* T_out, double* ap_out, double* err_out, int* m_out);
+
 /* Autotuner: times the checkerboard sweep kernel on this handle's replicas for every supported
  * cells-per-thread tile (1, 2, 4 or 8 consecutive colour cells: 32-, 64-, 128- or 2x128-bit accesses) and
  * keeps the fastest. The lattices are saved before and restored after, so the Markov chains are

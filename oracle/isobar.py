@@ -1,0 +1,147 @@
+"""CPU restatement of the reference's isobar analysis (CVF_ThermodynamicAnalysis/ of
+lcoronas/CVFBulkWater). Test infrastructure only: it checks the engine's run statistics on the
+GPU and the library's host functions; nothing in the library calls it.
+
+  run_stats      script_analisi.sh:35   mean and <x^2> - <x>^2 of data.out columns 2-7 (awk, in
+                                        double precision, sums in file order)
+  isobar_point   calculadora.sh:41-61   per-cell means, errors sqrt(3 var / n) / N, density,
+                                        N_hb / 2N, ncoop, r_cell (error sqrt(var / n)), C_P and
+                                        K_T from the fluctuations
+  to_si          conversor.sh:2-12 (constants), :20 (density), :24 (enthalpy), :28 (nhb, ncoop),
+                 :32 (C_P fluctuation; its third column is an empty awk field, so 0), :76 (energy
+                 from enthalpy and density)
+  alpha_p        AlphaPderivate.c:56-134 (order by T, central differences, one-sided at the ends,
+                 error from the sample variance, the third derivative and the neighbours' errors;
+                 only points 2 .. n-3 are written)
+  alpha_p_text   conversor.sh:54-66 as a text pipeline: awk's %.6g output between the stages,
+                 AlphaPderivate's "%lf", the x1000 conversion and the nan/inf filter
+
+Pinned by tests/golden/isobars_L32*.txt (the reference's own L32_P*_density.dat,
+L32_P*_density.dat.SI and L32_P*_AlphaPderivate.dat.SI for all 47 isobars).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+# conversor.sh:2-12
+TS, TI = 140.5678, 185.4676
+PS, PI = 469.459, -211.15552
+RHOS, RHOI = 1527.3, -23.1017
+CPS, CPI = 4.455, 3.56843
+HS, HI = 11.272132, 9.028924
+
+COLUMNS = ("energy", "enthalpy", "volume", "n_hb", "m", "r_cell")
+
+
+def run_stats(obs):
+    """obs: (n, 6) data.out columns 2-7 in file order -> (mean[6], var[6], n)."""
+    obs = np.asarray(obs, dtype=np.float64)
+    n = len(obs)
+    s = np.zeros(6)
+    s2 = np.zeros(6)
+    for row in obs:  # awk adds line by line
+        s += row
+        s2 += row * row
+    mean = s / n
+    return mean, s2 / n - mean * mean, n
+
+
+def isobar_point(L, T, mean, var, n):
+    N = float(L) * L * L
+    m, v = mean, var
+    err = lambda k, scale: math.sqrt(3 * v[k] / n) / scale  # noqa: E731
+    return {
+        "T": T,
+        "energy": m[0] / N, "energy_err": err(0, N),
+        "enthalpy": m[1] / N, "enthalpy_err": err(1, N),
+        "volume": m[2] / N, "volume_err": err(2, N),
+        "density": N / m[2], "density_err": N * math.sqrt(3 * v[2] / n) / (m[2] * m[2]),
+        "nhb": m[3] / (2 * N), "nhb_err": err(3, 2 * N),
+        "ncoop": m[4], "ncoop_err": math.sqrt(3 * v[4] / n),
+        "rcell": m[5], "rcell_err": math.sqrt(v[5] / n),
+        "cp_fluc": v[1] / (T * T * float(L) * L * L),
+        "kt_fluc": v[2] / (T * m[2]),
+    }
+
+
+def to_si(p, P):
+    T = p["T"]
+    rho = p["density"] * RHOS + RHOI
+    rho_err = p["density_err"] * RHOS
+    h = p["enthalpy"] * HS + HI * T
+    h_err = p["enthalpy_err"] * HI
+    return {
+        "T_K": T * TS + TI,
+        "density": rho, "density_err": rho_err,
+        "enthalpy": h, "enthalpy_err": h_err,
+        "energy": h - 18 * (P * PS + PI) / rho,
+        "energy_err": h_err - 18 * (P * PS + PI) * rho_err / (rho * rho),
+        "cp_fluc": p["cp_fluc"] * CPS + CPI, "cp_fluc_err": 0.0,
+        "nhb": p["nhb"], "nhb_err": p["nhb_err"], "ncoop": p["ncoop"], "ncoop_err": p["ncoop_err"],
+    }
+
+
+def alpha_p(T, V, V2, n):
+    """AlphaPderivate.c on arrays (any order): returns the rows (T, alpha_P, error) it writes."""
+    T, V, V2, n = (np.asarray(a, dtype=np.float64) for a in (T, V, V2, n))
+    o = np.argsort(T, kind="stable")
+    T, V, V2, n = T[o], V[o], V2[o], n[o]
+    m = len(T)
+    if m < 2:
+        return []
+    ap = np.empty(m)
+    ev = np.empty(m)
+    for j in range(m):
+        if j == 0:
+            ap[j] = (V[j + 1] - V[j]) / (T[j + 1] - T[j])
+        elif j == m - 1:
+            ap[j] = (V[j] - V[j - 1]) / (T[j] - T[j - 1])
+        else:
+            ap[j] = (V[j + 1] - V[j - 1]) / (T[j + 1] - T[j - 1])
+        ap[j] *= 1.0 / V[j]
+        ev[j] = math.sqrt((V2[j] / n[j]) * 3)
+    rows = []
+    for j in range(2, m - 2):
+        dT = (T[j + 1] - T[j - 1]) / 2.0
+        der = abs(V[j + 2] / 2.0 - V[j + 1] + V[j - 1] - V[j - 2] / 2.0) / (dT * dT * dT)
+        der *= dT * dT / 6.0
+        est = (ev[j + 1] + ev[j - 1]) / (2.0 * dT)
+        e = math.sqrt(ap[j] * ap[j] * ev[j] * ev[j] / (V[j] * V[j]) + der * der / (V[j] * V[j])
+                      + est * est / (V[j] * V[j]))
+        rows.append((T[j], ap[j], e))
+    return rows
+
+
+def awk_g(x):
+    """awk's print of a computed number: integers as integers, otherwise %.6g."""
+    if x == int(x) and abs(x) < 1e16:
+        return str(int(x))
+    return "%.6g" % x
+
+
+def density_si_text(T, rho, err):
+    """conversor.sh:20 on one density.dat line (the fields as text) -> the three printed fields."""
+    return [awk_g(float(T) * TS + TI), awk_g(float(rho) * RHOS + RHOI), awk_g(float(err) * RHOS)]
+
+
+def alpha_p_text(si_lines, n=1, derivative=alpha_p):
+    """conversor.sh:54-66 on one isobar's density.dat.SI lines [(T_K, rho, err) as text]; the
+    sample count n cancels from the error up to the %.6g rounding. Returns the printed lines."""
+    T, V, V2, N = [], [], [], []
+    for t, r, e in si_lines:
+        r, e = float(r), float(e)
+        v = awk_g(1.0 / r)
+        x = awk_g(e * e / (3 * r * r * r * r))
+        T.append(float(t))
+        V.append(float(v))
+        V2.append(float(awk_g(float(x) * n)))
+        N.append(float(n))
+    out = []
+    for t, a, e in derivative(T, V, V2, N):
+        ts, as_, es = "%f" % t, "%f" % a, "%f" % e
+        if as_ in ("-nan", "nan", "inf", "-inf") or es == "inf":
+            continue
+        out.append((ts, awk_g(float(as_) * 1000), awk_g(float(es) * 1000)))
+    return out

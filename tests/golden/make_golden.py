@@ -14,6 +14,11 @@ to what the tests need:
   data_out_stats.json       means and 20-block errors of data.out columns 2-7 (L=32, T=0.815,
                             P=0.45, 10000 samples): the statistical golden of the engine
   isobar_P0.45_density.txt  PROCESSED_DATA/CVF_isobars.tar.gz: L32_P0.45_density.dat
+  isobars_L32.txt           every isobar of the same archive, one line per point:
+                            P T rho err (L32_P*_density.dat, calculadora.sh output)
+  isobars_L32_si.txt        P T_K rho_SI err_SI (L32_P*_density.dat.SI, conversor.sh:20)
+  isobars_L32_alphap_si.txt P T_K alpha_P err (L32_P*_AlphaPderivate.dat.SI, conversor.sh:54-66
+                            with AlphaPderivate.c), the printed text kept as it is
 """
 from __future__ import annotations
 
@@ -58,6 +63,21 @@ def main(ref: str):
         m = t.getmember("CVF_isobars/L32_P0.45_density.dat")
         data = t.extractfile(m).read().decode()
     open(os.path.join(HERE, "isobar_P0.45_density.txt"), "w").write(data)
+    kinds = [("density.dat", "isobars_L32.txt"), ("density.dat.SI", "isobars_L32_si.txt"),
+             ("AlphaPderivate.dat.SI", "isobars_L32_alphap_si.txt")]
+    with tarfile.open(os.path.join(ref, "PROCESSED_DATA", "CVF_isobars.tar.gz")) as t:
+        names = t.getnames()
+        for suffix, out in kinds:
+            lines = []
+            for n in sorted(names):
+                base = os.path.basename(n)
+                if not (base.startswith("L32_P") and base.endswith("_" + suffix)):
+                    continue
+                P = base[len("L32_P"):-len("_" + suffix)]
+                for line in t.extractfile(n).read().decode().splitlines():
+                    if line.strip():
+                        lines.append(P + " " + line.strip())
+            open(os.path.join(HERE, out), "w").write("\n".join(lines) + "\n")
 
 
 if __name__ == "__main__":

@@ -1,0 +1,136 @@
+"""Isobar analysis (the reference's CVF_ThermodynamicAnalysis/ scripts), CPU part.
+
+The oracle (oracle/isobar.py) is pinned on the reference's own outputs: every line of the 47
+L32_P*_density.dat.SI files (conversor.sh:20 applied to L32_P*_density.dat) and every line of the
+47 L32_P*_AlphaPderivate.dat.SI files (conversor.sh:54-66 with AlphaPderivate.c applied to the
+density.dat.SI files), text for text. The library's host functions (cvf_isobar_point_from_stats,
+cvf_isobar_point_to_si, cvf_alpha_p_derivative) must then give the oracle's doubles exactly and
+reproduce the same files. No GPU is needed."""
+import collections
+import math
+import os
+
+import numpy as np
+import pytest
+
+from oracle import isobar as I
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _read(name):
+    out = collections.OrderedDict()
+    for line in open(os.path.join(GOLD, name)):
+        f = line.split()
+        out.setdefault(f[0], []).append(tuple(f[1:]))
+    return out
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return _read("isobars_L32.txt"), _read("isobars_L32_si.txt"), _read("isobars_L32_alphap_si.txt")
+
+
+@pytest.fixture(scope="module")
+def ana(engine_lib):
+    from cvfbulkwater_gb300 import analysis
+    return analysis
+
+
+def test_golden_covers_all_isobars(golden):
+    src, si, ap = golden
+    assert len(src) == len(si) == len(ap) == 47
+    assert sum(len(v) for v in src.values()) == 1947
+    assert sum(len(v) for v in ap.values()) == 1759
+
+
+def test_oracle_density_si_matches_reference(golden):
+    src, si, _ = golden
+    for P in src:
+        for a, b in zip(src[P], si[P]):
+            assert I.density_si_text(*a) == list(b), (P, a, b)
+
+
+def test_oracle_alpha_p_matches_reference(golden):
+    _, si, ap = golden
+    for P in si:
+        assert I.alpha_p_text(si[P]) == [tuple(x) for x in ap[P]], P
+
+
+def test_library_alpha_p_matches_reference(golden, ana):
+    _, si, ap = golden
+
+    def lib_derivative(T, V, V2, n):
+        t, a, e = ana.alpha_p_derivative(T, V, V2, np.asarray(n, dtype=np.int64))
+        return list(zip(t, a, e))
+
+    for P in si:
+        assert I.alpha_p_text(si[P], derivative=lib_derivative) == [tuple(x) for x in ap[P]], P
+
+
+def test_library_alpha_p_equals_oracle_unsorted(ana):
+    rng = np.random.default_rng(3)
+    m = 23
+    T = rng.permutation(np.linspace(0.5, 1.2, m))
+    V = 1.0 + 0.1 * np.sin(3 * T) + 1e-3 * rng.standard_normal(m)
+    V2 = 1e-4 * (1 + rng.random(m))
+    n = rng.integers(100, 5000, m)
+    t, a, e = ana.alpha_p_derivative(T, V, V2, n)
+    want = I.alpha_p(T, V, V2, n)
+    assert len(t) == m - 4 == len(want)
+    for x, y in zip(zip(t, a, e), want):
+        assert tuple(float(v) for v in x) == tuple(float(v) for v in y)
+
+
+def test_library_alpha_p_edge_cases(ana):
+    for m in (0, 1, 2, 4):
+        t, a, e = ana.alpha_p_derivative(np.arange(m, dtype=float), np.ones(m), np.ones(m), np.ones(m))
+        assert len(t) == 0
+    from cvfbulkwater_gb300.abi import CvfError
+    with pytest.raises(CvfError):
+        ana.alpha_p_derivative(np.arange(6.0), np.ones(6), np.ones(6), np.zeros(6))
+
+
+def _random_stats(rng, L):
+    N = L ** 3
+    mean = [-1.7 * N * rng.random(), -0.9 * N * rng.random(), N * (1 + rng.random()), 1.5 * N * rng.random(),
+            rng.random(), 1 + 0.01 * rng.random()]
+    var = [abs(x) * 1e-3 * rng.random() for x in mean]
+    return {"L": L, "P": float(rng.uniform(-0.5, 0.8)), "T": float(rng.uniform(0.05, 1.5)), "mean": mean,
+            "var": var, "n": int(rng.integers(10, 100000))}
+
+
+def test_library_isobar_point_and_si_equal_oracle(ana):
+    rng = np.random.default_rng(7)
+    for L in (8, 16, 32, 48):
+        for _ in range(20):
+            s = _random_stats(rng, L)
+            got = ana.isobar_point(s)
+            want = I.isobar_point(L, s["T"], np.array(s["mean"]), np.array(s["var"]), s["n"])
+            assert set(got) == set(want)
+            for k in want:
+                assert got[k] == float(want[k]), (k, got[k], want[k])
+            got_si = ana.to_si(got, s["P"])
+            want_si = I.to_si(want, s["P"])
+            for k in want_si:
+                assert got_si[k] == float(want_si[k]), (k, got_si[k], want_si[k])
+
+
+def test_library_si_reproduces_reference_density_files(golden, ana):
+    """The library's SI conversion of the reference's density points prints the reference's
+    density.dat.SI lines."""
+    src, si, _ = golden
+    for P in list(src)[::5]:
+        for (T, rho, err), want in zip(src[P], si[P]):
+            point = {k: 0.0 for k in I.isobar_point(8, 1.0, np.ones(6), np.ones(6), 1)}
+            point.update(T=float(T), density=float(rho), density_err=float(err))
+            got = ana.to_si(point, float(P))
+            assert [I.awk_g(got["T_K"]), I.awk_g(got["density"]), I.awk_g(got["density_err"])] == list(want)
+
+
+def test_run_stats_oracle_formula():
+    x = np.array([[1.0, 2, 3, 4, 5, 6], [2.0, 4, 6, 8, 10, 12], [4.0, 1, 1, 1, 1, 1]])
+    mean, var, n = I.run_stats(x)
+    assert n == 3
+    assert np.allclose(mean, x.mean(0)) and np.allclose(var, x.var(0))
+    assert math.isclose(var[0], (1 + 4 + 16) / 3 - (7 / 3) ** 2)
