@@ -81,6 +81,24 @@ struct ReplicaState {
   CStatsRec last_cstats;
 };
 
+// Multi-tau correlator of one replica (GW:165-181, GW:2983-3128): kCorrLevels levels of kCorrP
+// channels, kCorrM values averaged into the next level. It correlates, step by step, the
+// fraction of arms in the most populated sigma value (GW:1245-1272); hist collects the counts of
+// the step being added.
+constexpr int kCorrLevels = 32, kCorrP = 16, kCorrM = 2;
+struct CorrState {
+  double shift[kCorrLevels][kCorrP];
+  double correlation[kCorrLevels][kCorrP];
+  long long ncorrelation[kCorrLevels][kCorrP];
+  double accumulator[kCorrLevels];
+  int naccumulator[kCorrLevels];
+  int insertindex[kCorrLevels];
+  int kmax;
+  int pad;
+  double accval;
+  unsigned long long hist[6];
+};
+
 // Grid barrier state of the persistent step kernel (zeroed at creation and after an error).
 struct GridSync {
   unsigned int count;  // blocks arrived at the current barrier
@@ -103,6 +121,7 @@ struct BatchDev {
   int* blk_site4;       // one thread per 4 arm sites
   int nblk_sweep, nblk_cube, nblk_cubev, nblk_cell, nblk_site, nblk_site4;
   GridSync* gsync;      // device barrier state of the persistent step kernel
+  CorrState* corr;      // device array [nrep] of correlators (null until enabled)
 };
 
 constexpr int kThreads = 256;
@@ -127,6 +146,9 @@ void launch_measure_end(const BatchDev& b, int record, cudaStream_t s);
 // interval > 0. Same lattice, counters and samples as the per-phase kernels.
 cudaError_t launch_run(const BatchDev& b, int nsteps, int nmet, int interval, cudaStream_t s);
 void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s);
+// One correlator step of every replica: the sigma histogram of the lattice, then the add of the
+// most-populated fraction to the replica's correlator (b.corr must be allocated).
+cudaError_t launch_corr_step(const BatchDev& b, cudaStream_t s);
 // Run statistics of every replica from its sample stream: out[r*14 + k] = mean of data.out
 // column k (k < 6: energy, enthalpy, volume, N_hb, m, r_cell), variance of column k - 6
 // (6 <= k < 12), number of stored samples used (k = 12), number recorded (k = 13).

@@ -3,6 +3,7 @@
 // There is no CPU fallback: every Monte Carlo move runs in the kernels of cvf_mc.cu / cvf_sw.cu.
 #include <cuda_runtime.h>
 #include <stdlib.h>
+#include <math.h>
 #include <string.h>
 
 #include <algorithm>
@@ -69,7 +70,17 @@ struct cvf_handle {
   size_t io_scratch_bytes = 0;
   unsigned long long* io_bad = nullptr;  // device: smallest invalid cell of a device-side pack
   double* stats = nullptr;               // device: 14 doubles per replica for cvf_run_statistics
+  bool corr_on = false;                  // every captured step feeds the replicas' correlators
 };
+
+// A correlator in its initial state (GW:2983-3008): empty channels hold -2e10.
+static CorrState corr_initial() {
+  CorrState c;
+  memset(&c, 0, sizeof(c));
+  for (int k = 0; k < kCorrLevels; ++k)
+    for (int i = 0; i < kCorrP; ++i) c.shift[k][i] = -2E10;
+  return c;
+}
 
 // Device scratch for a device-side pack of one replica (freed with the handle).
 static int ensure_io_scratch(cvf_handle* h, const ReplicaHost& R) {
@@ -228,7 +239,7 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     return 0;
   }
   cudaGraph_t g;
-  if (h->launch_mode == 1 && ncl == 0) {
+  if (h->launch_mode == 1 && ncl == 0 && !h->corr_on) {
     // one persistent launch; a driver that cannot capture a cooperative launch leaves the
     // handle on the per-phase kernels
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -253,13 +264,14 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
   for (int i = 0; i < steps; ++i) {
     if (i == 0 && record && ncl == 0 && nmet > 0) {
       enqueue_recorded_metropolis_step(h, nmet);
-      continue;
+    } else {
+      enqueue_step(h, nmet, ncl);
+      if (i == 0 && record) {
+        launch_measure(h->b, 1, h->stream);
+        if (ncl > 0) enqueue_cstats(h, 1);
+      }
     }
-    enqueue_step(h, nmet, ncl);
-    if (i == 0 && record) {
-      launch_measure(h->b, 1, h->stream);
-      if (ncl > 0) enqueue_cstats(h, 1);
-    }
+    if (h->corr_on) launch_corr_step(h->b, h->stream);  // after the step's measurement, as GW:1245
   }
   CK(cudaStreamEndCapture(h->stream, &g));
   cudaGraphExec_t ex;
@@ -871,6 +883,54 @@ int cvf_get_io_mode(const cvf_handle* h, int* mode) {
 int cvf_get_launch_mode(const cvf_handle* h, int* mode) {
   if (!h || !mode) return fail(CVF_EINVAL, "null handle/out");
   *mode = h->launch_mode;
+  return 0;
+}
+
+int cvf_set_correlation(cvf_handle* h, int enable) {
+  if (!h || enable < 0 || enable > 1) return fail(CVF_EINVAL, "enable must be 0 or 1");
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  const int n = (int)h->reps.size();
+  if (enable) {
+    if (!h->b.corr) {
+      if (int rc = dev_alloc(h, (void**)&h->b.corr, (size_t)n * sizeof(CorrState))) return rc;
+    }
+    std::vector<CorrState> init((size_t)n, corr_initial());
+    CK(cudaMemcpy(h->b.corr, init.data(), init.size() * sizeof(CorrState), cudaMemcpyHostToDevice));
+  }
+  h->corr_on = enable != 0;
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+  h->graphs.clear();
+  return 0;
+}
+
+// GW:3078-3112 (evaluate with norm = 1) on a copy of the replica's correlator.
+int cvf_get_correlation(cvf_handle* h, int r, double* t, double* f, int cap, int* n_out) {
+  if (int rc = check_rep(h, r)) return rc;
+  if (!t || !f || !n_out || cap < 0) return fail(CVF_EINVAL, "null arrays/count");
+  if (!h->b.corr) return fail(CVF_EINVAL, "the correlation was never enabled (cvf_set_correlation)");
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  CorrState C;
+  CK(cudaMemcpy(&C, h->b.corr + r, sizeof(C), cudaMemcpyDeviceToHost));
+  const int dmin = kCorrP / kCorrM;
+  double aux = 0;
+  if (C.ncorrelation[0][0] > 0) aux = (C.accval / C.ncorrelation[0][0]) * (C.accval / C.ncorrelation[0][0]);
+  int im = 0;
+  auto put = [&](double tt, double ff) {
+    if (im < cap) {
+      t[im] = tt;
+      f[im] = ff;
+    }
+    ++im;
+  };
+  for (int i = 0; i < kCorrP; ++i)
+    if (C.ncorrelation[0][i] > 0) put((double)i, C.correlation[0][i] / C.ncorrelation[0][i] - aux);
+  for (int k = 1; k < C.kmax; ++k)
+    for (int i = dmin; i < kCorrP; ++i)
+      if (C.ncorrelation[k][i] > 0) put(i * pow((double)kCorrM, k), C.correlation[k][i] / C.ncorrelation[k][i] - aux);
+  *n_out = im;
+  if (im > cap) return fail(CVF_EINVAL, "capacity too small for the correlation points");
   return 0;
 }
 

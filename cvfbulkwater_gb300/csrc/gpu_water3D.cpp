@@ -31,8 +31,6 @@ int main(int argc, char** argv) {
     if (!strcmp(argv[i], "-L")) in.L = atoi(argv[i + 1]);
   const int L = in.L;
   const long long N = (long long)L * L * L;
-  if (in.flag_correlation == 1)
-    fprintf(stderr, "Warning: Flag_correlation=1 is not supported; correlation.dat is not written\n");
   if (in.sampling_interval < 1) die("Error[Sampling_Interval]: must be >= 1");
 
   FILE* odata = fopen("data.out", "w");
@@ -98,6 +96,8 @@ int main(int argc, char** argv) {
 
   // equilibration, GW:1176-1194
   check(cvf_run_steps(h, in.equilibrium_steps, in.metropolis_steps, in.cluster_steps));
+  // every production step feeds the correlator (GW:1245-1272)
+  if (in.flag_correlation == 1) check(cvf_set_correlation(h, 1));
 
   // production, GW:1204-1275: a sample after every step i with i % N_MEASURE == 0
   double E = 0, E2 = 0, M = 0, M2 = 0;
@@ -151,6 +151,15 @@ int main(int argc, char** argv) {
   fprintf(log, "Energy:\t\t%1.6lf\t+/-\t%1.6lf\n", E, sqrt(E2 - E * E));
   check(cvf_get_config(h, 0, cells.data(), N));
   check(cvf_write_config_file("config.out", cells.data(), N));
+  if (in.flag_correlation == 1) {  // GW:1307-1313, printCorr GW:3109-3128
+    std::vector<double> ct(32 * 16), cf(32 * 16);
+    int nc = 0;
+    check(cvf_get_correlation(h, 0, ct.data(), cf.data(), (int)ct.size(), &nc));
+    FILE* fc = fopen("correlation.dat", "w");
+    if (!fc) die("Can't create correlation.dat");
+    for (int i = 0; i < nc; ++i) fprintf(fc, "%.0f\t%f\n", ct[i], cf[i] / cf[0]);
+    fclose(fc);
+  }
   // the union-find labelling needs one pass per SW step; -1 when no SW step ran (GW:1557-1559)
   fprintf(log, "Max_SW_scans = %d\n", in.cluster_steps > 0 ? 1 : -1);
   fprintf(log, " ** simulation done\n");

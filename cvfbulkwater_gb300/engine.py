@@ -107,6 +107,18 @@ class Lattice:
         check(lib().cvf_autotune(self._h, C.byref(v)))
         return v.value
 
+    def set_correlation(self, enable: bool):
+        """Start (and reset) or stop the per-step multi-tau autocorrelation of every replica."""
+        check(lib().cvf_set_correlation(self._h, 1 if enable else 0))
+
+    def correlation(self, r: int = 0):
+        """(t, f) of replica r's correlator, evaluated as the reference does at the end of a run."""
+        n = C.c_int()
+        cap = 32 * 16
+        t, f = np.zeros(cap), np.zeros(cap)
+        check(lib().cvf_get_correlation(self._h, r, _ptr(t), _ptr(f), cap, C.byref(n)))
+        return t[: n.value].copy(), f[: n.value].copy()
+
     def run_statistics(self):
         """Mean and <x^2> - <x>^2 of the data.out columns over each replica's recorded samples,
         computed on the GPU (the awk stage of the reference's isobar analysis)."""

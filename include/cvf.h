@@ -174,6 +174,18 @@ int cvf_read_distances_file(const char* path, int L, float* dist, int* freq, int
 int cvf_format_data_line(char* buf, int cap, int t, const cvf_obs* o);
 int cvf_format_cluster_line(char* buf, int cap, int t, const cvf_cstats* c);
 
+/* Multi-tau autocorrelation (Flag_correlation = 1; GW:1245-1313, GW:2983-3128). Enabling (1)
+ * resets every replica's correlator; from then on every step of cvf_run_steps /
+ * cvf_run_sampled adds, per replica, the fraction of arms in the most populated sigma value
+ * (counted on the GPU) to a correlator of 32 levels x 16 channels that averages pairs into the
+ * next level, kept on the device. 0 stops adding (the state stays readable). Steps run with
+ * launch mode 1 fall back to per-phase launches while the correlation is on.
+ * cvf_get_correlation evaluates replica r's correlator as the reference does at the end of a
+ * run (GW:3078-3112, mean squared subtracted): n_out points (t, f), up to cap of them written;
+ * correlation.dat prints t and f / f[0]. No other reference counterpart. */
+int cvf_set_correlation(cvf_handle* h, int enable);
+int cvf_get_correlation(cvf_handle* h, int r, double* t, double* f, int cap, int* n_out);
+
 /* ---------------------------------------------------------------- isobar analysis
  * The reference's thermodynamic analysis (CVF_ThermodynamicAnalysis/) on the engine's results.
  *

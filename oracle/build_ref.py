@@ -1,0 +1,43 @@
+"""Build recipe for oracle/_ref/ (test infrastructure only): the reference's own multi-tau
+correlator, compiled from SOURCE/gpu_water3D.cu and SOURCE/mersenne_inline.cu where they lie in
+the reference checkout (main renamed, nothing else changed), linked with oracle/ref_correlator.cpp, which calls its
+initialize / add / evaluate. Run where the reference checkout exists (argument: its path);
+elsewhere the tests that need the library skip. Nothing from the reference is copied into the
+repository; the output stays in the git-ignored oracle/_ref/.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+LIB = os.path.join(OUT, "libref_correlator.so")
+
+
+def build(ref: str = "/root/reference", force: bool = False):
+    src = os.path.join(ref, "SOURCE", "gpu_water3D.cu")
+    if not os.path.exists(src):
+        return None
+    harness = os.path.join(HERE, "ref_correlator.cpp")
+    newest = max(os.path.getmtime(harness), os.path.getmtime(os.path.abspath(__file__)))
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) > newest:
+        return LIB
+    os.makedirs(OUT, exist_ok=True)
+    objs = []
+    for name in ("gpu_water3D.cu", "mersenne_inline.cu"):  # the reference's own two sources
+        obj = os.path.join(OUT, name + ".o")
+        subprocess.run(["nvcc", "-c", "-w", "-Xcompiler", "-fPIC", "-Dmain=cvf_reference_main",
+                        "-gencode", "arch=compute_103a,code=sm_103a", "-o", obj,
+                        os.path.join(ref, "SOURCE", name)], check=True)
+        objs.append(obj)
+    tmp = LIB + f".tmp{os.getpid()}"
+    subprocess.run(["nvcc", "-shared", "-Xcompiler", "-fPIC", "-o", tmp, harness] + objs + ["-cudart", "static", "-lm"],
+                   check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(*(sys.argv[1:2])))

@@ -19,6 +19,9 @@ to what the tests need:
   isobars_L32_si.txt        P T_K rho_SI err_SI (L32_P*_density.dat.SI, conversor.sh:20)
   isobars_L32_alphap_si.txt P T_K alpha_P err (L32_P*_AlphaPderivate.dat.SI, conversor.sh:54-66
                             with AlphaPderivate.c), the printed text kept as it is
+  correlator_ref.json       the reference's own multi-tau correlator (initialize/add/evaluate of
+                            SOURCE/gpu_water3D.cu, built by oracle/build_ref.py) on a seeded
+                            random walk of 20000 values: the evaluated (t, f), as hex floats
 """
 from __future__ import annotations
 
@@ -78,6 +81,30 @@ def main(ref: str):
                     if line.strip():
                         lines.append(P + " " + line.strip())
             open(os.path.join(HERE, out), "w").write("\n".join(lines) + "\n")
+    correlator_golden(ref)
+
+
+def correlator_input():
+    rng = np.random.default_rng(20261203)
+    return 0.5 + 0.01 * np.cumsum(rng.standard_normal(20000))
+
+
+def correlator_golden(ref):
+    import ctypes as C
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from oracle import build_ref
+    lib = build_ref.build(ref)
+    if lib is None:
+        return
+    L = C.CDLL(lib)
+    w = np.ascontiguousarray(correlator_input())
+    t, f = np.zeros(512), np.zeros(512)
+    n = L.ref_corr_run(w.ctypes.data_as(C.c_void_p), len(w), t.ctypes.data_as(C.c_void_p),
+                       f.ctypes.data_as(C.c_void_p), 512)
+    json.dump({"source": "SOURCE/gpu_water3D.cu initialize/add/evaluate (GW:2983-3107), norm=1",
+               "input": "0.5 + 0.01*cumsum(numpy default_rng(20261203).standard_normal(20000))",
+               "t": [float(x).hex() for x in t[:n]], "f": [float(x).hex() for x in f[:n]]},
+              open(os.path.join(HERE, "correlator_ref.json"), "w"), indent=0)
 
 
 if __name__ == "__main__":
