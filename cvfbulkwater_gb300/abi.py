@@ -130,6 +130,8 @@ def lib():
         "cvf_read_distances_file": (I, [C.c_char_p, I, P, P, I, C.POINTER(I)]),
         "cvf_format_data_line": (I, [C.c_char_p, I, I, C.POINTER(Obs)]),
         "cvf_format_cluster_line": (I, [C.c_char_p, I, I, C.POINTER(CStats)]),
+        "cvf_set_replica_groups": (I, [P, I]),
+        "cvf_get_replica_groups": (I, [P, C.POINTER(I)]),
         "cvf_set_correlation": (I, [P, I]),
         "cvf_get_correlation": (I, [P, I, P, P, I, C.POINTER(I)]),
         "cvf_run_statistics": (I, [P, C.POINTER(RunStats), I]),

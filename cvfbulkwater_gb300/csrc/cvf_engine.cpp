@@ -71,6 +71,19 @@ struct cvf_handle {
   unsigned long long* io_bad = nullptr;  // device: smallest invalid cell of a device-side pack
   double* stats = nullptr;               // device: 14 doubles per replica for cvf_run_statistics
   bool corr_on = false;                  // every captured step feeds the replicas' correlators
+  // Replica groups: Metropolis-only steps of a batch are captured as one chain of per-phase
+  // kernels per group of consecutive replicas, on parallel branches of the graph, so that one
+  // group's blocks fill the tails of another group's kernels. 0 = automatic.
+  int group_setting = 0;
+  struct Group {
+    BatchDev b;
+    cudaStream_t s = nullptr;
+    cudaEvent_t done = nullptr;
+    int r0 = 0, r1 = 0;
+  };
+  std::vector<Group> groups;
+  int groups_vec = 0;
+  cudaEvent_t fork = nullptr;
 };
 
 // A correlator in its initial state (GW:2983-3008): empty channels hold -2e10.
@@ -126,6 +139,8 @@ static int upload_descs(cvf_handle* h) {
   return 0;
 }
 
+static int fill_tables(cvf_handle* h, int r0, int r1, int vec, BatchDev& b);
+
 static int build_tables(cvf_handle* h, int force_vec = 0) {
   const int n = (int)h->reps.size();
   int vec = 4;
@@ -138,11 +153,17 @@ static int build_tables(cvf_handle* h, int force_vec = 0) {
     while (vec > 1 && r.H % vec) vec >>= 1;
   }
   h->b.vec = vec;
+  return fill_tables(h, 0, n, vec, h->b);
+}
+
+// Block prefix tables of replicas [r0, r1) (a new device allocation) into b.
+static int fill_tables(cvf_handle* h, int r0, int r1, int vec, BatchDev& b) {
+  const int n = r1 - r0;
   std::vector<int> ts(n + 1), tc(n + 1), tcv(n + 1), tl(n + 1), tsi(n + 1), ts4(n + 1);
   ts[0] = tc[0] = tcv[0] = tl[0] = tsi[0] = ts4[0] = 0;
   auto blocks = [](long long threads) { return (int)((threads + kThreads - 1) / kThreads); };
   for (int i = 0; i < n; ++i) {
-    const auto& r = h->reps[i];
+    const auto& r = h->reps[r0 + i];
     long long L = r.L, H = r.H;
     ts[i + 1] = ts[i] + blocks((H / vec) * L * L);
     tc[i + 1] = tc[i] + 2 * blocks(H * H * H);  // even-origin cubes, then odd-origin cubes
@@ -161,18 +182,70 @@ static int build_tables(cvf_handle* h, int force_vec = 0) {
   all.insert(all.end(), ts4.begin(), ts4.end());
   all.insert(all.end(), tcv.begin(), tcv.end());
   CK(cudaMemcpy(d, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
-  h->b.blk_sweep = d;
-  h->b.blk_cube = d + (n + 1);
-  h->b.blk_cell = d + 2 * (n + 1);
-  h->b.blk_site = d + 3 * (n + 1);
-  h->b.blk_site4 = d + 4 * (n + 1);
-  h->b.blk_cubev = d + 5 * (n + 1);
-  h->b.nblk_cubev = tcv[n];
-  h->b.nblk_site4 = ts4[n];
-  h->b.nblk_sweep = ts[n];
-  h->b.nblk_cube = tc[n];
-  h->b.nblk_cell = tl[n];
-  h->b.nblk_site = tsi[n];
+  b.blk_sweep = d;
+  b.blk_cube = d + (n + 1);
+  b.blk_cell = d + 2 * (n + 1);
+  b.blk_site = d + 3 * (n + 1);
+  b.blk_site4 = d + 4 * (n + 1);
+  b.blk_cubev = d + 5 * (n + 1);
+  b.nblk_cubev = tcv[n];
+  b.nblk_site4 = ts4[n];
+  b.nblk_sweep = ts[n];
+  b.nblk_cube = tc[n];
+  b.nblk_cell = tl[n];
+  b.nblk_site = tsi[n];
+  return 0;
+}
+
+// Number of replica groups in effect: the setting, or automatically 4 for batches of 8 or more
+// replicas, 2 for 2..7, never more than the replicas.
+static int group_count(const cvf_handle* h) {
+  const int n = (int)h->reps.size();
+  int g = h->group_setting > 0 ? h->group_setting : (n >= 8 ? 4 : (n >= 2 ? 2 : 1));
+  return g < n ? g : n;
+}
+
+// (Re)builds the group views: consecutive replicas cut where the running cell count crosses
+// multiples of total / G, each group with its own block tables, stream and completion event.
+static int build_groups(cvf_handle* h) {
+  const int G = group_count(h);
+  const int n = (int)h->reps.size();
+  if (G <= 1) {
+    h->groups.clear();
+    return 0;
+  }
+  if ((int)h->groups.size() != G || h->groups_vec != h->b.vec) {
+    long long total = 0;
+    for (auto& r : h->reps) total += r.N;
+    std::vector<int> cut{0};
+    long long acc = 0;
+    for (int i = 0; i < n && (int)cut.size() < G; ++i) {
+      acc += h->reps[i].N;
+      const long long target = total * (long long)cut.size() / G;
+      if (acc >= target && i + 1 < n && n - (i + 1) >= G - (int)cut.size()) cut.push_back(i + 1);
+    }
+    cut.push_back(n);
+    for (auto& g : h->groups) {
+      if (g.s) cudaStreamDestroy(g.s);
+      if (g.done) cudaEventDestroy(g.done);
+    }
+    h->groups.assign(cut.size() - 1, cvf_handle::Group());
+    for (size_t k = 0; k + 1 < cut.size(); ++k) {
+      auto& g = h->groups[k];
+      g.r0 = cut[k];
+      g.r1 = cut[k + 1];
+      g.b = h->b;
+      if (int rc = fill_tables(h, g.r0, g.r1, h->b.vec, g.b)) return rc;
+      g.b.reps = h->b.reps + g.r0;
+      g.b.st = h->b.st + g.r0;
+      g.b.nrep = g.r1 - g.r0;
+      CK(cudaStreamCreateWithFlags(&g.s, cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming));
+    }
+    if (!h->fork) CK(cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming));
+    h->groups_vec = h->b.vec;
+  }
+  for (auto& g : h->groups) g.b.corr = h->b.corr ? h->b.corr + g.r0 : nullptr;
   return 0;
 }
 
@@ -220,6 +293,30 @@ static void enqueue_recorded_metropolis_step(cvf_handle* h, int nmet) {
   launch_measure_end(h->b, 1, h->stream);
 }
 
+// One Metropolis-only step of the replicas of view b on stream s, with the recorded measurement
+// when record is set and the correlator step when corr is set.
+static void enqueue_metropolis_on(const BatchDev& b, cudaStream_t s, int nmet, bool record, bool corr) {
+  if (record && nmet > 0) {
+    launch_step_begin(b, nmet, 0, 1, 1, s, 1);
+    launch_cube_volume(b, 1, 1, s);
+    for (int j = 0; j < nmet; ++j) {
+      launch_sweep(b, 0, j, s);
+      if (j + 1 < nmet) launch_sweep(b, 1, j, s);
+      else launch_sweep_measure(b, j, s);
+    }
+    launch_measure_end(b, 1, s);
+  } else {
+    launch_step_begin(b, nmet, 0, 1, 1, s);
+    launch_cube_volume(b, 1, 1, s);
+    for (int j = 0; j < nmet; ++j) {
+      launch_sweep(b, 0, j, s);
+      launch_sweep(b, 1, j, s);
+    }
+    if (record) launch_measure(b, 1, s);
+  }
+  if (corr) launch_corr_step(b, s);
+}
+
 static void enqueue_cstats(cvf_handle* h, int record) {
   for (auto& r : h->reps) {
     cudaMemsetAsync(r.desc.csize, 0, (size_t)(6 * r.N) * sizeof(int32_t), h->stream);
@@ -259,6 +356,26 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     }
     cudaGetLastError();
     h->launch_mode = 0;
+  }
+  if (ncl == 0 && group_count(h) > 1) {
+    if (int rc = build_groups(h)) return rc;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    CK(cudaEventRecord(h->fork, h->stream));
+    for (auto& gr : h->groups) CK(cudaStreamWaitEvent(gr.s, h->fork, 0));
+    for (auto& gr : h->groups)
+      for (int i = 0; i < steps; ++i) enqueue_metropolis_on(gr.b, gr.s, nmet, i == 0 && record, h->corr_on);
+    for (auto& gr : h->groups) {
+      CK(cudaEventRecord(gr.done, gr.s));
+      CK(cudaStreamWaitEvent(h->stream, gr.done, 0));
+    }
+    CK(cudaStreamEndCapture(h->stream, &g));
+    cudaGraphExec_t ex;
+    cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(CVF_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    h->graphs[key] = ex;
+    *out = ex;
+    return 0;
   }
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   for (int i = 0; i < steps; ++i) {
@@ -438,6 +555,11 @@ int cvf_destroy(cvf_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+  for (auto& g : h->groups) {
+    if (g.s) cudaStreamDestroy(g.s);
+    if (g.done) cudaEventDestroy(g.done);
+  }
+  if (h->fork) cudaEventDestroy(h->fork);
   for (void* p : h->allocs) cudaFree(p);
   if (h->io_scratch) cudaFree(h->io_scratch);
   if (h->io_bad) cudaFree(h->io_bad);
@@ -883,6 +1005,22 @@ int cvf_get_io_mode(const cvf_handle* h, int* mode) {
 int cvf_get_launch_mode(const cvf_handle* h, int* mode) {
   if (!h || !mode) return fail(CVF_EINVAL, "null handle/out");
   *mode = h->launch_mode;
+  return 0;
+}
+
+int cvf_set_replica_groups(cvf_handle* h, int groups) {
+  if (!h || groups < 0) return fail(CVF_EINVAL, "groups must be >= 0 (0 = automatic)");
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  h->group_setting = groups;
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+  h->graphs.clear();
+  return 0;
+}
+
+int cvf_get_replica_groups(const cvf_handle* h, int* groups) {
+  if (!h || !groups) return fail(CVF_EINVAL, "null handle/out");
+  *groups = group_count(h);
   return 0;
 }
 

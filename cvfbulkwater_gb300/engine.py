@@ -107,6 +107,17 @@ class Lattice:
         check(lib().cvf_autotune(self._h, C.byref(v)))
         return v.value
 
+    @property
+    def replica_groups(self) -> int:
+        """Groups of consecutive replicas captured on parallel graph branches (count in effect)."""
+        g = C.c_int()
+        check(lib().cvf_get_replica_groups(self._h, C.byref(g)))
+        return g.value
+
+    @replica_groups.setter
+    def replica_groups(self, groups: int):
+        check(lib().cvf_set_replica_groups(self._h, int(groups)))
+
     def set_correlation(self, enable: bool):
         """Start (and reset) or stop the per-step multi-tau autocorrelation of every replica."""
         check(lib().cvf_set_correlation(self._h, 1 if enable else 0))

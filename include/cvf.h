@@ -263,6 +263,15 @@ int cvf_set_sweep_tile(cvf_handle* h, int vec, int* vec_out);
 int cvf_set_launch_mode(cvf_handle* h, int mode);
 int cvf_get_launch_mode(const cvf_handle* h, int* mode);
 
+/* Replica groups of a batch (0 = automatic: 4 groups for 8 or more replicas, 2 for 2 to 7).
+ * Metropolis-only steps of a batch are captured as one chain of per-phase kernels per group of
+ * consecutive replicas (groups of about equal cell counts), on parallel branches of the CUDA
+ * graph, so that the blocks of one group fill the tails of another group's kernels. The results
+ * do not depend on the grouping. cvf_get_replica_groups reports the count in effect. No
+ * reference counterpart. */
+int cvf_set_replica_groups(cvf_handle* h, int groups);
+int cvf_get_replica_groups(const cvf_handle* h, int* groups);
+
 /* Transfer mode of cvf_set_config. 1: kernels read and pack the caller's cells12 array where it
  * lies in host memory (the GPU accesses pageable host memory through the host page tables, as
  * over NVLink-C2C on GB300); the default when the device reports

@@ -1,0 +1,44 @@
+"""Replica groups: a batch's Metropolis-only steps captured as one kernel chain per group of
+replicas on parallel graph branches. Any grouping must leave the same lattices, counters,
+volume chains, recorded samples and correlators as one chain for the whole batch."""
+import numpy as np
+import pytest
+
+from cvfbulkwater_gb300.engine import Lattice, Params
+
+pytestmark = pytest.mark.gpu
+
+SPECS = [(6, 0.6, 0.0), (16, 0.9, 0.6), (24, 0.75, 0.3), (12, 0.55, 0.45), (40, 0.8, 0.2), (8, 0.7, 0.45),
+         (16, 0.65, 0.1), (10, 0.85, 0.5), (32, 0.72, 0.4)]
+
+
+def run(groups, corr):
+    lat = Lattice([Params(L=L, T=T, P=P, seed=300 + i, start=0, replica=i) for i, (L, T, P) in enumerate(SPECS)])
+    lat.replica_groups = groups
+    assert lat.replica_groups == min(groups, len(SPECS)) if groups else lat.replica_groups == 4
+    lat.run(5, 1, 0)
+    if corr:
+        lat.set_correlation(True)
+    lat.run(35, 1, 0)
+    lat.run_sampled(23, 2, 0, 4)
+    out = []
+    for r in range(len(SPECS)):
+        item = [lat.get_config(r), lat.state(r), lat.samples(r)]
+        if corr:
+            item.append(lat.correlation(r))
+        out.append(item)
+    lat.close()
+    return out
+
+
+@pytest.mark.parametrize("corr", [False, True])
+def test_groupings_identical(engine_lib, corr):
+    ref = run(1, corr)
+    for g in (0, 2, 3, 9):
+        got = run(g, corr)
+        for r, (a, b) in enumerate(zip(ref, got)):
+            assert np.array_equal(a[0], b[0]), (g, r)
+            assert a[1][0] == b[1][0] and a[1][1] == b[1][1] and list(a[1][3]) == list(b[1][3]), (g, r)
+            assert len(a[2]) == len(b[2]) and all(x == y for x, y in zip(a[2], b[2])), (g, r)
+            if corr:
+                assert np.array_equal(a[3][0], b[3][0]) and np.array_equal(a[3][1], b[3][1]), (g, r)
