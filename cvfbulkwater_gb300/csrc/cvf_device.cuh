@@ -21,7 +21,6 @@ struct ReplicaDesc {
   // Swendsen-Wang work arrays (null until the first SW step)
   int32_t* label;     // 6N parents / labels
   uint8_t* hbmask;    // N: bits 0..2 = active x+, y+, z+ cluster bonds
-  uint8_t* shift;     // 6N: cluster shift of each root
   int32_t* csize;     // 6N: cluster sizes by root
   int32_t* cand;      // 6N: percolation candidate id by root (-1 none)
   uint32_t* cover;    // max_cand * 3 * W: coordinate coverage bitmaps

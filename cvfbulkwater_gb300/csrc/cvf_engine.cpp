@@ -257,7 +257,6 @@ static int ensure_sw(cvf_handle* h) {
     r.desc.max_cand = 3 * r.L * r.L;  // at most 6N / 2L clusters of size >= 2L
     if (int rc = dev_alloc(h, (void**)&r.desc.label, NS * sizeof(int32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.hbmask, (size_t)r.N)) return rc;
-    if (int rc = dev_alloc(h, (void**)&r.desc.shift, NS)) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.csize, NS * sizeof(int32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.cand, NS * sizeof(int32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.cover, (size_t)r.desc.max_cand * 3 * W * sizeof(uint32_t))) return rc;

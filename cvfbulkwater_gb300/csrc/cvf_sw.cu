@@ -186,66 +186,51 @@ __global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __rest
       if (!uf_unite(R.label, (int32_t)((2 * d) * N + c), (int32_t)((2 * d + 1) * N + nb[d]))) st[r].err = 1;
 }
 
-__global__ void __launch_bounds__(kThreads) k_sw_compress(const ReplicaDesc* __restrict__ reps,
-                                                          const int* __restrict__ blk, int nrep) {
-  const int r = find_replica_sw(blk, nrep, blockIdx.x);
-  const ReplicaDesc& R = reps[r];
-  const long long NS = 6LL * R.L * R.L * R.L;
-  long long s = (long long)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
-  if (s >= NS) return;
-  int32_t x = (int32_t)s;
-  for (int it = 0; it < (1 << 30); ++it) {
-    int32_t px = __ldcg(R.label + x);
-    if (px == x) break;
-    x = px;
-  }
-  R.label[s] = x;
-}
-
-// GW:2531-2542: every cluster gets one uniform shift in 0..5. Thread = 4 consecutive sites; the
-// shift of root i is an exact uniform from word (i & 3) of the flip block of counter i >> 2
-// (retry streams of site i on a rejection).
-__global__ void __launch_bounds__(kThreads) k_sw_roots(const ReplicaDesc* __restrict__ reps,
-                                                       const ReplicaState* __restrict__ st,
-                                                       const int* __restrict__ blk, int nrep, int jsw) {
-  const int r = find_replica_sw(blk, nrep, blockIdx.x);
-  const ReplicaDesc& R = reps[r];
-  const uint32_t NS4 = (uint32_t)(6LL * R.L * R.L * R.L / 4);
-  const uint32_t q = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
-  if (q >= NS4) return;
-  const int4 lab = reinterpret_cast<const int4*>(R.label)[q];
-  const uint32_t s0 = 4u * q;
-  const bool root[4] = {lab.x == (int)s0, lab.y == (int)(s0 + 1), lab.z == (int)(s0 + 2), lab.w == (int)(s0 + 3)};
-  if (!(root[0] | root[1] | root[2] | root[3])) return;
-  const uint32_t t = st[r].cur[3] + (uint32_t)jsw;
-  const U4 qq = philox(q, t, kStSwFlip, R.replica, R.key0, R.key1);
-  const uint32_t words[4] = {qq.x, qq.y, qq.z, qq.w};
-  uint32_t out = 0;
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    if (!root[k]) continue;
-    uint32_t v;
-    if (!lemire_try(words[k], 6, v)) v = lemire_retry(6, s0 + k, t, kStSwFlip, R.replica, R.key0, R.key1);
-    out |= v << (8 * k);
-  }
-  reinterpret_cast<uint32_t*>(R.shift)[q] = out;
-}
-
-__global__ void __launch_bounds__(kThreads) k_sw_apply(const ReplicaDesc* __restrict__ reps,
-                                                       const int* __restrict__ blk, int nrep) {
+// Compression, cluster shift and update in one pass, one thread per cell: each of the cell's six
+// sites walks to its root (the component's minimum site id) and stores it as its label, then
+// draws the root's shift itself -- GW:2531-2542 gives every cluster one uniform shift in 0..5;
+// here it is the exact uniform from word (root & 3) of the flip block of counter root >> 2
+// (retry streams of the root on a rejection), so every site of a cluster draws the same value --
+// and shifts its sigma. A repeated root reuses the previous arm's draw.
+__global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __restrict__ reps,
+                                                        const ReplicaState* __restrict__ st,
+                                                        const int* __restrict__ blk, int nrep, int jsw) {
   const int r = find_replica_sw(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   const int L = R.L;
   const uint32_t N = (uint32_t)L * L * L;
   const uint32_t c = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
   if (c >= N) return;
+  const uint32_t t = st[r].cur[3] + (uint32_t)jsw;
+  int32_t roots[6];
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    int32_t x = (int32_t)(a * N + c);
+    for (int it = 0; it < (1 << 30); ++it) {
+      const int32_t px = __ldcg(R.label + x);
+      if (px == x) break;
+      x = px;
+    }
+    roots[a] = x;
+  }
+#pragma unroll
+  for (int a = 0; a < 6; ++a) R.label[a * N + c] = roots[a];
   int x, y, z;
   cell_xyz(R, c, x, y, z);
   uint32_t* wp = R.cells[(x + y + z) & 1] + (uint32_t)(x >> 1) + (uint32_t)R.H * ((uint32_t)y + (uint32_t)L * (uint32_t)z);
-  uint32_t w = *wp, out = 0;
+  const uint32_t w = *wp;
+  uint32_t out = 0, sh = 0;
+  int32_t last = -1;
 #pragma unroll
   for (int a = 0; a < 6; ++a) {
-    uint32_t sh = R.shift[R.label[a * N + c]];
+    const int32_t root = roots[a];
+    if (root != last) {
+      const U4 qq = philox((uint32_t)root >> 2, t, kStSwFlip, R.replica, R.key0, R.key1);
+      const uint32_t k = (uint32_t)root & 3u;
+      const uint32_t word = k == 0 ? qq.x : (k == 1 ? qq.y : (k == 2 ? qq.z : qq.w));
+      if (!lemire_try(word, 6, sh)) sh = lemire_retry(6, (uint32_t)root, t, kStSwFlip, R.replica, R.key0, R.key1);
+      last = root;
+    }
     uint32_t v = ((w >> (3 * a)) & 7u) + sh;
     if (v >= 6u) v -= 6u;
     out |= v << (3 * a);
@@ -434,9 +419,7 @@ __global__ void k_cs_begin(ReplicaState* __restrict__ st, int nrep) {
 void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s) {
   k_sw_local<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.st, b.blk_cell, b.nrep, jsw);
   k_sw_union<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.st, b.blk_cell, b.nrep);
-  k_sw_compress<<<b.nblk_site, kThreads, 0, s>>>(b.reps, b.blk_site, b.nrep);
-  k_sw_roots<<<b.nblk_site4, kThreads, 0, s>>>(b.reps, b.st, b.blk_site4, b.nrep, jsw);
-  k_sw_apply<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.blk_cell, b.nrep);
+  k_sw_finish<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.st, b.blk_cell, b.nrep, jsw);
 }
 
 // Needs csize zeroed and cover zeroed by the caller (memset nodes); blocktop sized 2*nblk_site.
