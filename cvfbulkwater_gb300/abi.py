@@ -132,6 +132,11 @@ def lib():
         "cvf_format_cluster_line": (I, [C.c_char_p, I, I, C.POINTER(CStats)]),
         "cvf_set_replica_groups": (I, [P, I]),
         "cvf_get_replica_groups": (I, [P, C.POINTER(I)]),
+        "cvf_h2d_create": (I, [I, P, P, P, LL, P, P, I, I, D, I, C.POINTER(P)]),
+        "cvf_h2d_info": (I, [P, C.POINTER(I), C.POINTER(I), C.POINTER(D), C.POINTER(D), C.POINTER(D), C.POINTER(D), P]),
+        "cvf_h2d_reweight": (I, [P, D, D, P, C.POINTER(D), C.POINTER(D)]),
+        "cvf_h2d_mixed": (I, [P, D, P, P, C.POINTER(D)]),
+        "cvf_h2d_destroy": (I, [P]),
         "cvf_set_correlation": (I, [P, I]),
         "cvf_get_correlation": (I, [P, I, P, P, I, C.POINTER(I)]),
         "cvf_run_statistics": (I, [P, C.POINTER(RunStats), I]),

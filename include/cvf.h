@@ -174,6 +174,28 @@ int cvf_read_distances_file(const char* path, int L, float* dist, int* freq, int
 int cvf_format_data_line(char* buf, int cap, int t, const cvf_obs* o);
 int cvf_format_cluster_line(char* buf, int cap, int t, const cvf_cstats* c);
 
+/* ---------------------------------------------------------------- 2-D histogram reweighting
+ * Binned (E, rho) histogram reweighting of HistogramReweighting/
+ * histogram_reweighting_mixed_paramSI_norm_x.f90 ("F90") on the GPU. Inputs per sample: the
+ * enthalpy per cell h = H/N and the density rho = N/V in internal units (F90:160-165) and its run;
+ * per run the internal T and P. cvf_h2d_create converts every sample to SI energy (kJ/mol) and
+ * density (kg/m^3) (F90:155-181), bins them as the F90 does (F90:220-279; n_bin2D scales with
+ * bin_factor) and runs `steps` iterations of the F90's constants (F90:398-425), failing with
+ * CVF_ELIMIT when they have not converged to 1e-7. cvf_h2d_reweight gives the normalised
+ * distribution on the n_bin2D x n_bin2D grid at (T, P) (internal units; grid may be NULL) and the
+ * Binder cumulants of E and rho (F90:737-759, F90:2610-2662); cvf_h2d_mixed then the distribution
+ * of the mixed order parameter at angle alpha, M = sin(alpha) E + cos(alpha) rho, normalised and
+ * mapped as the F90 does (F90:1383-1620; n_bin_mixed points, x and q may be NULL) and its Binder
+ * cumulant (F90:2580-2608). The Ising-distribution comparisons of the F90 are not provided. */
+typedef struct cvf_h2d cvf_h2d;
+int cvf_h2d_create(int device, const double* h, const double* rho, const int* run_of, long long n, const double* That,
+                   const double* Phat, int n_runs, int L, double bin_factor, int steps, cvf_h2d** out);
+int cvf_h2d_info(const cvf_h2d* H, int* n_bin2d, int* n_bin_mixed, double* Emin, double* dE, double* Dmin, double* dD,
+                 double* ctes);
+int cvf_h2d_reweight(cvf_h2d* H, double T_hat, double P_hat, double* grid, double* binder_e, double* binder_rho);
+int cvf_h2d_mixed(cvf_h2d* H, double alpha, double* x, double* q, double* binder_m);
+int cvf_h2d_destroy(cvf_h2d* H);
+
 /* Multi-tau autocorrelation (Flag_correlation = 1; GW:1245-1313, GW:2983-3128). Enabling (1)
  * resets every replica's correlator; from then on every step of cvf_run_steps /
  * cvf_run_sampled adds, per replica, the fraction of arms in the most populated sigma value
