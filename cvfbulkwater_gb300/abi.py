@@ -136,6 +136,10 @@ def lib():
         "cvf_h2d_info": (I, [P, C.POINTER(I), C.POINTER(I), C.POINTER(D), C.POINTER(D), C.POINTER(D), C.POINTER(D), P]),
         "cvf_h2d_reweight": (I, [P, D, D, P, C.POINTER(D), C.POINTER(D)]),
         "cvf_h2d_mixed": (I, [P, D, P, P, C.POINTER(D)]),
+        "cvf_h2d_mixed_batch": (I, [P, P, I, P, P, P]),
+        "cvf_h2d_ising": (I, [P, P, I, D, P]),
+        "cvf_h2d_scan": (I, [P, P, I, P, I, P, I, D, P, P, P]),
+        "cvf_h2d_set_constants": (I, [P, P]),
         "cvf_h2d_destroy": (I, [P]),
         "cvf_set_correlation": (I, [P, I]),
         "cvf_get_correlation": (I, [P, I, P, P, I, C.POINTER(I)]),

@@ -58,6 +58,29 @@ def alpha_p_derivative(T, V, V2, n):
     return tuple(o[: k.value] for o in outs)
 
 
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def f90_range(start, stop, step, inclusive=True):
+    """The values a Fortran `do while (v <= stop)` (or `< stop`) loop with `v = v + step` visits,
+    accumulated as the F90's search does (F90:732-891)."""
+    out, v = [], float(start)
+    while (v <= stop) if inclusive else (v < stop):
+        out.append(v)
+        v = v + step
+    return np.array(out)
+
+
+def ising_compare(x, q, B=1.0):
+    """ConfrontIsing, ZeroTest and HeightTest of the F90 on a mixed distribution (cvf_h2d_ising):
+    dict of liu_2D, liu_3D, kl_2D, kl_3D, zero, height."""
+    x, q = (np.ascontiguousarray(v, dtype=np.float64) for v in (x, q))
+    out = np.zeros(6)
+    check(lib().cvf_h2d_ising(_ptr(x), _ptr(q), len(x), float(B), _ptr(out)))
+    return dict(zip(("liu_2D", "liu_3D", "kl_2D", "kl_3D", "zero", "height"), out.tolist()))
+
+
 class Histogram2D:
     """Binned (E, rho) histogram reweighting of the reference's F90 reweighting program on the GPU
     (cvf_h2d_*): h = H/N and rho = N/V per sample (internal units), the run of each sample and
@@ -93,6 +116,36 @@ class Histogram2D:
         check(lib().cvf_h2d_mixed(self._h, float(alpha), x.ctypes.data_as(C.c_void_p), q.ctypes.data_as(C.c_void_p),
                                   C.byref(b)))
         return x, q, b.value
+
+    def mixed_batch(self, alphas):
+        """x, q (n x n_bin_mixed) and the Binder cumulants of n angles, binned in one pass."""
+        a = np.ascontiguousarray(alphas, dtype=np.float64).ravel()
+        x, q, b = np.zeros((len(a), self.n_bin_mixed)), np.zeros((len(a), self.n_bin_mixed)), np.zeros(len(a))
+        check(lib().cvf_h2d_mixed_batch(self._h, _ptr(a), len(a), _ptr(x), _ptr(q), _ptr(b)))
+        return x, q, b
+
+    def set_constants(self, ctes):
+        """The runs' constants as given (the F90's Constants_L file) instead of iterated."""
+        c = np.ascontiguousarray(ctes, dtype=np.float64)
+        if c.shape != (self.n_runs,):
+            raise ValueError("one constant per run")
+        check(lib().cvf_h2d_set_constants(self._h, _ptr(c)))
+        self.ctes = c.copy()
+
+    def scan(self, T_hats, P_hats, S_list, B=1.0):
+        """The F90's search over pressures (outer), temperatures and angles (inner), internal
+        units: (tp_rows [n_P, n_T, 2] = binder_e, binder_rho; rows [n_P, n_T, n_S, 7] = binder_m,
+        liu_2D, liu_3D, kl_2D, kl_3D, zero, height; best: dict of the (P, T, S) indices of the
+        smallest liu_2D, liu_3D, zero, height and zero + height, None where none)."""
+        T, P, S = (np.ascontiguousarray(v, dtype=np.float64).ravel() for v in (T_hats, P_hats, S_list))
+        tp = np.zeros((len(P), len(T), 2))
+        rows = np.zeros((len(P), len(T), len(S), 7))
+        best = np.zeros(5, dtype=np.int64)
+        check(lib().cvf_h2d_scan(self._h, _ptr(T), len(T), _ptr(P), len(P), _ptr(S), len(S), float(B), _ptr(tp),
+                                 _ptr(rows), _ptr(best)))
+        names = ("liu_2D", "liu_3D", "zero", "height", "zero_height")
+        return tp, rows, {k: (None if r < 0 else np.unravel_index(int(r), (len(P), len(T), len(S))))
+                          for k, r in zip(names, best)}
 
     def close(self):
         if getattr(self, "_h", None):

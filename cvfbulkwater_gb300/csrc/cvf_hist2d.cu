@@ -4,8 +4,9 @@
 // iteration, the reweighted distribution at any (T, P), the Binder cumulants of E, rho and of the
 // mixed order parameter M = sin(a) E + cos(a) rho. The bins are reweighted on the GPU -- one
 // thread per bin, all runs' log-sum-exp in registers, every target (T, P) of a WHAM step in one
-// launch -- and reduced in a fixed order, so results do not depend on scheduling. The 1-D stages
-// (mixed-parameter histogram of ~sqrt(n_bin2D) bins, Binder sums) run on the host.
+// launch -- and reduced in a fixed order, so results do not depend on scheduling. The mixed
+// parameter is binned on the GPU for a batch of angles at once; the 1-D stages on its
+// ~sqrt(n_bin2D) bins (normalisation, sine map, Binder sums, Ising comparisons) run on the host.
 #include <math.h>
 #include <string.h>
 
@@ -33,17 +34,23 @@ struct cvf_h2d {
   double* d_part = nullptr;   // partial reductions
   double* d_grid = nullptr;   // nb*nb: normalised reweighted distribution
   int nblk = 0;
-  std::vector<double> grid;   // host copy for the mixed parameter (filled on demand)
-  std::vector<unsigned char> mask;
-  bool grid_ready = false, host_grid = false;
+  double* d_scratch = nullptr;  // mixed-parameter binning of a batch of angles
+  size_t scratch_n = 0;
+  bool grid_ready = false;
 };
 
 namespace {
 
-constexpr double kTs = 140.5678, kTi = 185.4676;  // F90:81-88
-constexpr double kPs = 4694.59, kPi = -2111.5552;
-constexpr double kRhos = 1527.3, kRhoi = -23.1017;
-constexpr double kHs = 11.272132, kHi = 9.028914;
+// The F90 is built with plain gfortran, so every literal it assigns to or mixes with a real*8 is
+// a default-kind (single precision) constant: the float nearest the decimal, widened.
+constexpr double kTs = (double)140.5678f, kTi = (double)185.4676f;  // F90:81-88
+constexpr double kPs = (double)4694.59f, kPi = (double)-2111.5552f;
+constexpr double kRhos = (double)1527.3f, kRhoi = (double)-23.1017f;
+constexpr double kHs = (double)11.272132f, kHi = (double)9.028914f;
+constexpr double kE18 = (double)1.8f;      // F90:161, 245
+constexpr double kKb = (double)0.2293f;    // F90:1013, 1042
+constexpr double kMw = (double)0.018f;     // F90:1031
+constexpr double kConv = (double)1E-07f;   // F90:468
 constexpr int kT = 256;
 
 int h2d_fail(int code, const std::string& m) {
@@ -81,7 +88,7 @@ __global__ void k_h2d_logp(const double* __restrict__ hsum, int nb, double Emin,
     const int i = b / nb, w = b - i * nb;
     const double E = __dmul_rn(__dadd_rn(Emin, __dmul_rn((double)i + 0.5, dE)), N);
     const double dens = __dadd_rn(Dmin, __dmul_rn((double)w + 0.5, dD));
-    const double V = __dmul_rn(__ddiv_rn(0.018, dens), N);
+    const double V = __dmul_rn(__ddiv_rn(kMw, dens), N);
     const double beta1 = tgt[2 * k], pres1 = tgt[2 * k + 1];
     const double a1 = __dmul_rn(beta1, __dadd_rn(E, __dmul_rn(pres1, V)));
     bool flag = false;
@@ -230,7 +237,7 @@ int upload_runs(cvf_h2d* H) {
   const int R = H->R;
   std::vector<double> run(4 * (size_t)R);
   for (int j = 0; j < R; ++j) {
-    run[j] = 1000. / (0.2293 * H->Tk[j]);
+    run[j] = 1000. / (kKb * H->Tk[j]);
     run[R + j] = H->Pbar[j] * 100.0;
     run[2 * R + j] = H->ctes[j];
     run[3 * R + j] = H->log_medidas[j];
@@ -242,18 +249,356 @@ int upload_runs(cvf_h2d* H) {
 int set_targets(cvf_h2d* H, const std::vector<double>& temp, const std::vector<double>& pres) {
   std::vector<double> t(2 * temp.size());
   for (size_t k = 0; k < temp.size(); ++k) {
-    t[2 * k] = 1000. / (0.2293 * temp[k]);
+    t[2 * k] = 1000. / (kKb * temp[k]);
     t[2 * k + 1] = pres[k] * 100.0;
   }
   HK(cudaMemcpyAsync(H->d_tgt, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice, H->s));
   return 0;
 }
 
+// ---------------------------------------------------------------- mixed order parameter
+// Calcula_Histograma_Rotado_normX F90:1383-1462 on the GPU for a batch of angles: X = sin(a) E +
+// cos(a) rho (Rotate, F90:1126-1138) of every bin with g > 0, its range widened by two bins on
+// each side, and the sum of g per X bin. Along one energy row X is monotone in the density bin,
+// so the bin index of 32 consecutive bins is monotone across a warp: a segmented warp scan adds
+// the runs of equal index and the last lane of each run adds its sum to the warp's own shared
+// histogram, in a fixed order, so the result does not depend on scheduling.
+constexpr int kMaxAngles = 64;
+constexpr int kXWarps = 8;
+
+__device__ __forceinline__ double mixed_x(int i, int w, double Emin, double dE, double Dmin, double dD, double sa,
+                                          double ca) {
+  const double E = __dadd_rn(Emin, __dmul_rn((double)i + 0.5, dE));
+  const double D = __dadd_rn(Dmin, __dmul_rn((double)w + 0.5, dD));
+  return __dadd_rn(__dmul_rn(E, sa), __dmul_rn(D, ca));
+}
+
+__global__ void k_h2d_xrange(const double* __restrict__ grid, int nb, double Emin, double dE, double Dmin, double dD,
+                             const double* __restrict__ sc, int nblk, double* __restrict__ part) {
+  __shared__ double slo[kT], shi[kT];
+  const int a = blockIdx.y;
+  const double sa = sc[2 * a], ca = sc[2 * a + 1];
+  const long long nb2 = (long long)nb * nb;
+  double lo = INFINITY, hi = -INFINITY;
+  for (long long b = (long long)blockIdx.x * kT + threadIdx.x; b < nb2; b += (long long)nblk * kT)
+    if (grid[b] > 0) {
+      const int i = (int)(b / nb), w = (int)(b - (long long)i * nb);
+      const double X = mixed_x(i, w, Emin, dE, Dmin, dD, sa, ca);
+      lo = fmin(lo, X);
+      hi = fmax(hi, X);
+    }
+  slo[threadIdx.x] = lo;
+  shi[threadIdx.x] = hi;
+  __syncthreads();
+  for (int st = kT / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) {
+      slo[threadIdx.x] = fmin(slo[threadIdx.x], slo[threadIdx.x + st]);
+      shi[threadIdx.x] = fmax(shi[threadIdx.x], shi[threadIdx.x + st]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[2 * ((size_t)a * nblk + blockIdx.x)] = slo[0];
+    part[2 * ((size_t)a * nblk + blockIdx.x) + 1] = shi[0];
+  }
+}
+
+// One thread per angle: Xmin and the bin width of F90:1418-1428; err[0] = 1 when no bin is
+// occupied or the width is not positive.
+__global__ void k_h2d_xparams(const double* __restrict__ part, int nblk, int n, int nbm, double* __restrict__ xp,
+                              int* __restrict__ err) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n) return;
+  double lo = INFINITY, hi = -INFINITY;
+  for (int b = 0; b < nblk; ++b) {
+    lo = fmin(lo, part[2 * ((size_t)a * nblk + b)]);
+    hi = fmax(hi, part[2 * ((size_t)a * nblk + b) + 1]);
+  }
+  double rX = __dsub_rn(hi, lo);
+  double t = __ddiv_rn(rX, (double)nbm);
+  rX = __dadd_rn(rX, __dmul_rn(4.0, t));
+  const double Xmin = __dsub_rn(lo, __dmul_rn(2.0, t));
+  t = __ddiv_rn(rX, (double)nbm);
+  xp[2 * a] = Xmin;
+  xp[2 * a + 1] = t;
+  if (!(t > 0) || !(lo <= hi)) atomicExch(err, 1);
+}
+
+__global__ void __launch_bounds__(32 * kXWarps) k_h2d_xhist(const double* __restrict__ grid, int nb, double Emin,
+                                                           double dE, double Dmin, double dD,
+                                                           const double* __restrict__ sc,
+                                                           const double* __restrict__ xp, int nbm, int nwarps,
+                                                           double* __restrict__ wpart, int* __restrict__ err) {
+  extern __shared__ double hs[];
+  const int a = blockIdx.y, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* h = hs + (size_t)warp * nbm;
+  for (int k = lane; k < nbm; k += 32) h[k] = 0.0;
+  __syncwarp();
+  const double sa = sc[2 * a], ca = sc[2 * a + 1], Xmin = xp[2 * a], t = xp[2 * a + 1];
+  const double tiny = (double)1E-10f;  // F90:1449
+  const int gw = blockIdx.x * kXWarps + warp;
+  const int r0 = (int)((long long)gw * nb / nwarps), r1 = (int)((long long)(gw + 1) * nb / nwarps);
+  bool bad = false;
+  for (int i = r0; i < r1; ++i) {
+    const double* row = grid + (size_t)i * nb;
+    for (int w0 = 0; w0 < nb; w0 += 32) {
+      const int w = w0 + lane;
+      const double g = w < nb ? row[w] : 0.0;
+      const double X = mixed_x(i, w, Emin, dE, Dmin, dD, sa, ca);
+      const double tq = trunc(__ddiv_rn(__dsub_rn(X, Xmin), t));  // int() of F90:1446
+      const bool in = tq >= 0.0 && tq < (double)nbm;
+      int key = (int)fmin(fmax(tq, 0.0), (double)(nbm - 1));
+      double v = 0.0;
+      if (g > 0) {
+        if (in || fabs(__dsub_rn(X, Xmin)) < tiny) v = g;
+        else bad = true;
+        if (!in && fabs(__dsub_rn(X, Xmin)) < tiny) key = 0;
+      }
+      for (int d = 1; d < 32; d <<= 1) {
+        const double ov = __shfl_up_sync(0xffffffffu, v, d);
+        const int ok = __shfl_up_sync(0xffffffffu, key, d);
+        if (lane >= d && ok == key) v = __dadd_rn(ov, v);
+      }
+      const int nk = __shfl_down_sync(0xffffffffu, key, 1);
+      if (lane == 31 || nk != key) h[key] = __dadd_rn(h[key], v);
+      __syncwarp();
+    }
+  }
+  if (bad) atomicExch(err, 2);
+  for (int k = lane; k < nbm; k += 32) wpart[((size_t)a * nwarps + gw) * nbm + k] = h[k];
+}
+
+// Sum of the warps' histograms in warp order: q[a][k].
+__global__ void k_h2d_xsum(const double* __restrict__ wpart, int nwarps, int nbm, double* __restrict__ q) {
+  const int a = blockIdx.y, k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nbm) return;
+  double s = 0.0;
+  for (int g = 0; g < nwarps; ++g) s = __dadd_rn(s, wpart[((size_t)a * nwarps + g) * nbm + k]);
+  q[(size_t)a * nbm + k] = s;
+}
+
+// Raw mixed-parameter histograms of n <= kMaxAngles angles: qraw (n x nbm) and xp (Xmin, width).
+int bin_mixed(cvf_h2d* H, const double* alpha, int n, std::vector<double>& qraw, std::vector<double>& xp) {
+  const int nb = H->nb, nbm = H->nbm;
+  if (nbm < 3) return h2d_fail(CVF_EINVAL, "too few mixed-parameter bins");
+  HK(cudaSetDevice(H->device));
+  const int nwb = std::max(1, std::min(128, (nb + kXWarps - 1) / kXWarps)), nwarps = nwb * kXWarps;
+  const size_t need = 2 * (size_t)n + 2 * (size_t)n * H->nblk + 2 * (size_t)n + (size_t)n * nwarps * nbm +
+                      (size_t)n * nbm + 1;
+  if (need > H->scratch_n) {
+    if (H->d_scratch) cudaFree(H->d_scratch);
+    H->d_scratch = nullptr;
+    H->scratch_n = 0;
+    HK(cudaMalloc(&H->d_scratch, need * sizeof(double)));
+    H->scratch_n = need;
+  }
+  double* d_sc = H->d_scratch;
+  double* d_part = d_sc + 2 * (size_t)n;
+  double* d_xp = d_part + 2 * (size_t)n * H->nblk;
+  double* d_w = d_xp + 2 * (size_t)n;
+  double* d_q = d_w + (size_t)n * nwarps * nbm;
+  int* d_err = reinterpret_cast<int*>(d_q + (size_t)n * nbm);
+  std::vector<double> sc(2 * (size_t)n);
+  for (int a = 0; a < n; ++a) {
+    sc[2 * a] = sin(alpha[a]);
+    sc[2 * a + 1] = cos(alpha[a]);
+  }
+  HK(cudaMemcpyAsync(d_sc, sc.data(), sc.size() * sizeof(double), cudaMemcpyHostToDevice, H->s));
+  HK(cudaMemsetAsync(d_err, 0, sizeof(int), H->s));
+  k_h2d_xrange<<<dim3(H->nblk, n), kT, 0, H->s>>>(H->d_grid, nb, H->Emin, H->dE, H->Dmin, H->dD, d_sc, H->nblk,
+                                                  d_part);
+  k_h2d_xparams<<<(n + 31) / 32, 32, 0, H->s>>>(d_part, H->nblk, n, nbm, d_xp, d_err);
+  k_h2d_xhist<<<dim3(nwb, n), 32 * kXWarps, (size_t)kXWarps * nbm * sizeof(double), H->s>>>(
+      H->d_grid, nb, H->Emin, H->dE, H->Dmin, H->dD, d_sc, d_xp, nbm, nwarps, d_w, d_err);
+  k_h2d_xsum<<<dim3((nbm + 127) / 128, n), 128, 0, H->s>>>(d_w, nwarps, nbm, d_q);
+  HK(cudaGetLastError());
+  qraw.resize((size_t)n * nbm);
+  xp.resize(2 * (size_t)n);
+  int err = 0;
+  HK(cudaMemcpyAsync(qraw.data(), d_q, qraw.size() * sizeof(double), cudaMemcpyDeviceToHost, H->s));
+  HK(cudaMemcpyAsync(xp.data(), d_xp, xp.size() * sizeof(double), cudaMemcpyDeviceToHost, H->s));
+  HK(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, H->s));
+  HK(cudaStreamSynchronize(H->s));
+  if (err == 1) return h2d_fail(CVF_EINVAL, "no width for the mixed-parameter histogram");
+  if (err == 2) return h2d_fail(CVF_EINVAL, "point outside the mixed-parameter histogram");
+  return 0;
+}
+
+// F90:1478-1562: bin centres, normalisation, zero mean and unit variance, the sine map with
+// b = 1.53, normalised again over the mapped bin widths. a1 and media are those binder() uses.
+int mixed_1d(int nbm, double Xmin, double t, const double* qraw, std::vector<double>& m, std::vector<double>& q,
+             double& a1_out, double& media_out) {
+  q.assign(qraw, qraw + nbm);
+  m.resize(nbm);
+  for (int i = 0; i < nbm; ++i) m[i] = Xmin + (i + 0.5) * t;
+  double norma = 0;
+  for (int i = 0; i < nbm; ++i) norma += q[i];
+  for (auto& v : q) v = v / (norma * t);
+  double media = 0;
+  for (int i = 0; i < nbm; ++i) media += m[i] * q[i] * t;
+  for (auto& v : m) v -= media;
+  norma = 0;
+  double var = 0;
+  for (int i = 0; i < nbm; ++i)
+    if (q[i] > 0) {
+      norma += q[i] * t;
+      var += m[i] * m[i] * q[i] * t;
+    }
+  double a1 = sqrt(norma / var), a2 = 1 / (norma * a1);
+  for (int i = 0; i < nbm; ++i) {
+    m[i] *= a1;
+    q[i] *= a2;
+  }
+  const double b = (double)1.53f, alh = 1.0, bt = 1.0, pi = (double)3.14159f;  // F90:1544-1548
+  for (auto& v : m) v = alh * b * b * sin(pi * v / b) / (pi * pi) + bt * v;
+  std::vector<double> wdt(nbm);
+  wdt[0] = m[1] - m[0];
+  for (int i = 1; i < nbm - 1; ++i) wdt[i] = (m[i + 1] - m[i - 1]) / 2.0;
+  wdt[nbm - 1] = m[nbm - 1] - m[nbm - 2];
+  norma = 0;
+  for (int i = 0; i < nbm; ++i) norma += q[i] * wdt[i];
+  for (auto& v : q) v /= norma;
+  double media_rx = 0;
+  for (int i = 0; i < nbm; ++i) media_rx += m[i] * q[i] * wdt[i];
+  for (auto& v : m) v -= media_rx;
+  norma = 0;
+  var = 0;
+  for (int i = 0; i < nbm; ++i)
+    if (q[i] > 0) {
+      norma += q[i] * wdt[i];
+      var += m[i] * m[i] * q[i] * wdt[i];
+    }
+  a1 = sqrt(norma / var);
+  a2 = 1 / (norma * a1);
+  for (int i = 0; i < nbm; ++i) {
+    m[i] *= a1;
+    q[i] *= a2;
+  }
+  a1_out = a1;
+  media_out = media;
+  return 0;
+}
+
+// binder F90:2580-2608: the cumulant of M = x / a1 + media.
+double binder_of(const std::vector<double>& m, const std::vector<double>& q, double a1, double media) {
+  double nq = 0;
+  for (double v : q) nq += v;
+  double u2 = 0, u4 = 0;
+  for (size_t i = 0; i < m.size(); ++i) {
+    const double op = m[i] / a1 + media, m2 = op * op;
+    u2 += m2 * q[i] / nq;
+    u4 += m2 * m2 * q[i] / nq;
+  }
+  return 1.0 - u4 / (3.0 * u2 * u2);
+}
+
+// ---------------------------------------------------------------- Ising comparisons
+// Ising2D F90:2216-2232 (the fit of Liu and Panagiotopoulos, JCP 2010) and Ising3D F90:2234-2252
+// (Tsypin, PRE 62, 2000, normalised to unit norm and variance); z**16 by repeated squaring as
+// gfortran expands a constant integer power.
+double ising2d(double z) {
+  const double a = (double)0.058137f, b = (double)-2.68949f, c = (double)-0.11235f, d = (double)2.884162f;
+  const double z2 = z * z, z4 = z2 * z2, z8 = z4 * z4, z16 = z8 * z8;
+  return exp(-(a * z16 + b * z * z + c * fabs(z) + d));
+}
+double ising3d(double z) {
+  const double a = (double)0.196f, c = (double)0.807f, M0 = (double)1.141059404f, A0 = (double)0.436591191f;
+  const double u = z * z / (M0 * M0) - 1;
+  return A0 * exp(-(u * u * (a * z * z / (M0 * M0) + c)));
+}
+
+// Ising_Peak F90:1148-1222: ternary searches for the maxima on [0.1, 2].
+int ising_peaks(double& p2, double& p3) {
+  for (int which = 0; which < 2; ++which) {
+    auto f = [which](double z) { return which == 0 ? ising2d(z) : ising3d(z); };
+    double xmin = (double)0.1f, xmax = 2;
+    double x1 = xmin + (xmax - xmin) / 3, x2 = xmin + 2 * (xmax - xmin) / 3;
+    for (int it = 0;; ++it) {
+      if (it > 10000) return h2d_fail(CVF_ELIMIT, "Ising peak search did not end");
+      if (f(x1) > f(x2)) {
+        xmax = x2;
+      } else if (f(x2) > f(x1)) {
+        xmin = x1;
+      } else {
+        return h2d_fail(CVF_EINVAL, "Ising peak search met equal values");
+      }
+      x1 = xmin + (xmax - xmin) / 3;
+      x2 = xmin + 2 * (xmax - xmin) / 3;
+      const bool done = which == 0 ? fabs(x1 - x2) < (double)1E-06f : fabs(f(x1) - f(x2)) < (double)1E-06f;
+      if (done) {
+        (which == 0 ? p2 : p3) = f(x1) > f(x2) ? f(x1) : f(x2);
+        break;
+      }
+    }
+  }
+  return 0;
+}
+
+// out = liu_2D, liu_3D, kl_2D, kl_3D, zero, height for abscissae m and histogram q.
+void confront(const double* m, const double* q, int n, double peak2, double peak3, double* out) {
+  double kl2 = 0, kl3 = 0, liu2 = 0, liu3 = 0;
+  int n_liu = 0;
+  for (int i = 0; i < n; ++i) {
+    const double hist = q[i];
+    if (hist == 0) continue;
+    const double i2 = ising2d(m[i]), i3 = ising3d(m[i]);
+    if (i2 > 0) kl2 = kl2 + (log(i2) - log(hist)) * i2;
+    if (i3 > 0) kl3 = kl3 + (log(i3) - log(hist)) * i3;
+    liu2 = liu2 + sqrt(hist) * fabs(hist - i2);
+    liu3 = liu3 + sqrt(hist) * fabs(hist - i3);
+    ++n_liu;
+  }
+  liu2 = liu2 / ((peak2 - ising2d(0.0)) * n_liu);
+  liu3 = liu3 / ((peak3 - ising3d(0.0)) * n_liu);
+  const double vis = (double)(6.0f / 0.8f);  // F90:2066, 2118
+  // ZeroTest: the lowest bin with -1 < m < 1 against Ising3D(0); none such reads as 1E3
+  double hmin = (double)1E12f, zero = 1E3;
+  int imin = -1;
+  for (int i = 0; i < n; ++i)
+    if (m[i] > -1 && m[i] < 1 && q[i] < hmin) {
+      hmin = q[i];
+      imin = i;
+    }
+  if (imin >= 0) {
+    const double d = q[imin] - ising3d(0.0);
+    zero = d * d * vis * vis;
+    zero = zero + m[imin] * m[imin];
+  }
+  // HeightTest: the highest bin on each side of 0 against the Ising3D maxima at -+1.14
+  double h1 = -10, h2 = -10, height = 1E3;
+  int i1 = -1, i2 = -1;
+  for (int i = 0; i < n; ++i) {
+    if (m[i] < 0) {
+      if (q[i] > h1) {
+        h1 = q[i];
+        i1 = i;
+      }
+    } else if (q[i] > h2) {
+      h2 = q[i];
+      i2 = i;
+    }
+  }
+  if (i1 >= 0 && i2 >= 0) {
+    const double x1 = (double)-1.14f, x2 = (double)1.14f;
+    const double d1 = q[i1] - ising3d(x1), d2 = q[i2] - ising3d(x2);
+    height = d1 * d1 * vis * vis;
+    height = height + d2 * d2 * vis * vis;
+    height = height + (m[i1] - x1) * (m[i1] - x1);
+    height = height + (m[i2] - x2) * (m[i2] - x2);
+  }
+  out[0] = liu2;
+  out[1] = liu3;
+  out[2] = kl2;
+  out[3] = kl3;
+  out[4] = zero;
+  out[5] = height;
+}
+
 void destroy(cvf_h2d* H) {
   if (!H) return;
   cudaSetDevice(H->device);
   if (H->s) cudaStreamSynchronize(H->s);
-  for (double* p : {H->d_hsum, H->d_logp, H->d_run, H->d_tgt, H->d_part, H->d_grid})
+  for (double* p : {H->d_hsum, H->d_logp, H->d_run, H->d_tgt, H->d_part, H->d_grid, H->d_scratch})
     if (p) cudaFree(p);
   if (H->s) cudaStreamDestroy(H->s);
   delete H;
@@ -296,7 +641,7 @@ int cvf_h2d_create(int device, const double* h, const double* rho, const int* ru
   for (long long i = 0; i < n; ++i) {
     const int j = run_of[i];
     const double dens = kRhos * rho[i] + kRhoi;
-    const double e = kHs * h[i] + kHi * That[j] - 1.8 * H->Pbar[j] / dens;
+    const double e = kHs * h[i] + kHi * That[j] - kE18 * H->Pbar[j] / dens;
     E[i] = e;
     D[i] = dens;
     if (i == 0) {
@@ -388,7 +733,7 @@ int cvf_h2d_create(int device, const double* h, const double* rho, const int* ru
   d_cell = nullptr;
   d_norma = nullptr;
   if (e != cudaSuccess) return bail(CVF_ECUDA, std::string("histograms: ") + cudaGetErrorString(e));
-  // F90:398-425: Jacobi iteration of the constants, every run's log Z in one launch per step
+  // F90:446-472: Jacobi iteration of the constants, every run's log Z in one launch per step
   H->ctes.assign(R, 0.0);
   std::vector<double> ctes2(R, 0.0), logz;
   if (int rc = set_targets(H, H->Tk, H->Pbar)) return bail(rc, "targets");
@@ -402,7 +747,7 @@ int cvf_h2d_create(int device, const double* h, const double* rho, const int* ru
     for (int k = 0; k < R; ++k) ctes2[k] = logz[k] - logz[0];
   }
   for (int k = 0; k < R && steps > 0; ++k)
-    if (fabs(H->ctes[k] - ctes2[k]) > 1E-07) return bail(CVF_ELIMIT, "the constants did not converge: use more steps");
+    if (fabs(H->ctes[k] - ctes2[k]) > kConv) return bail(CVF_ELIMIT, "the constants did not converge: use more steps");
   H->ctes = ctes2;
   if (int rc = upload_runs(H)) return bail(rc, "runs");
   *out = H;
@@ -447,7 +792,6 @@ int cvf_h2d_reweight(cvf_h2d* H, double T_hat, double P_hat, double* grid, doubl
   if (grid) HK(cudaMemcpyAsync(grid, H->d_grid, (size_t)nb2 * sizeof(double), cudaMemcpyDeviceToHost, H->s));
   HK(cudaStreamSynchronize(H->s));
   H->grid_ready = true;
-  H->host_grid = false;
   double tot = 0.0;
   for (int i = 0; i < nb; ++i) tot += marg[i];
   double u2 = 0, u4 = 0, v2 = 0, v4 = 0;
@@ -467,99 +811,106 @@ int cvf_h2d_reweight(cvf_h2d* H, double T_hat, double P_hat, double* grid, doubl
 // Calcula_Histograma_Rotado_normX F90:1383-1620 and binder F90:2580-2608 on the last reweighted
 // grid; x and q hold n_bin_mixed values (may be NULL).
 int cvf_h2d_mixed(cvf_h2d* H, double alpha, double* x_out, double* q_out, double* binder_m) {
+  return cvf_h2d_mixed_batch(H, &alpha, 1, x_out, q_out, binder_m);
+}
+
+// The same for n angles at once: the 2-D grid is binned on the GPU for every angle, the 1-D
+// stages run on the host. x and q hold n x n_bin_mixed values, binder_m n (each may be NULL).
+int cvf_h2d_mixed_batch(cvf_h2d* H, const double* alpha, int n, double* x_out, double* q_out, double* binder_m) {
   if (!H || !H->grid_ready) return h2d_fail(CVF_EINVAL, "call cvf_h2d_reweight first");
-  const int nb = H->nb, nbm = H->nbm;
-  if (nbm < 3) return h2d_fail(CVF_EINVAL, "too few mixed-parameter bins");
-  if (!H->host_grid) {
-    H->grid.resize((size_t)nb * nb);
-    HK(cudaSetDevice(H->device));
-    HK(cudaMemcpy(H->grid.data(), H->d_grid, H->grid.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    H->host_grid = true;
-  }
-  const double sa = sin(alpha), ca = cos(alpha);
-  double Xmin = 1E12, Xmax = -1E12;
-  for (int i = 0; i < nb; ++i)
-    for (int w = 0; w < nb; ++w)
-      if (H->grid[(size_t)i * nb + w] > 0) {
-        const double X = (H->Emin + (i + 0.5) * H->dE) * sa + (H->Dmin + (w + 0.5) * H->dD) * ca;
-        Xmax = std::max(Xmax, X);
-        Xmin = std::min(Xmin, X);
-      }
-  double rX = Xmax - Xmin, t = rX / nbm;
-  rX = rX + 4 * t;
-  Xmin = Xmin - 2 * t;
-  t = rX / nbm;
-  std::vector<double> q(nbm, 0.0), m(nbm);
-  for (int i = 0; i < nb; ++i)
-    for (int w = 0; w < nb; ++w) {
-      const double g = H->grid[(size_t)i * nb + w];
-      if (!(g > 0)) continue;
-      const double X = (H->Emin + (i + 0.5) * H->dE) * sa + (H->Dmin + (w + 0.5) * H->dD) * ca;
-      long long ix = (long long)((X - Xmin) / t);
-      if (ix < 0 || ix >= nbm) {
-        if (fabs(X - Xmin) < 1E-10) ix = 0;
-        else return h2d_fail(CVF_EINVAL, "point outside the mixed-parameter histogram");
-      }
-      q[ix] += g;
+  if (!alpha || n < 1) return h2d_fail(CVF_EINVAL, "null or empty angle list");
+  const int nbm = H->nbm;
+  std::vector<double> x, q;
+  double a1 = 0, media = 0;
+  for (int c0 = 0; c0 < n; c0 += kMaxAngles) {
+    const int c = std::min(kMaxAngles, n - c0);
+    std::vector<double> qraw, xp;
+    if (int rc = bin_mixed(H, alpha + c0, c, qraw, xp)) return rc;
+    for (int k = 0; k < c; ++k) {
+      const int a = c0 + k;
+      if (int rc = mixed_1d(nbm, xp[2 * k], xp[2 * k + 1], qraw.data() + (size_t)k * nbm, x, q, a1, media)) return rc;
+      if (x_out) std::copy(x.begin(), x.end(), x_out + (size_t)a * nbm);
+      if (q_out) std::copy(q.begin(), q.end(), q_out + (size_t)a * nbm);
+      if (binder_m) binder_m[a] = binder_of(x, q, a1, media);
     }
-  for (int i = 0; i < nbm; ++i) m[i] = Xmin + (i + 0.5) * t;
-  double norma = 0;
-  for (int i = 0; i < nbm; ++i) norma += q[i];
-  for (auto& v : q) v = v / (norma * t);
-  double media = 0;
-  for (int i = 0; i < nbm; ++i) media += m[i] * q[i] * t;
-  for (auto& v : m) v -= media;
-  norma = 0;
-  double var = 0;
-  for (int i = 0; i < nbm; ++i)
-    if (q[i] > 0) {
-      norma += q[i] * t;
-      var += m[i] * m[i] * q[i] * t;
-    }
-  double a1 = sqrt(norma / var), a2 = 1 / (norma * a1);
-  for (int i = 0; i < nbm; ++i) {
-    m[i] *= a1;
-    q[i] *= a2;
-  }
-  const double b = 1.53, alh = 1.0, bt = 1.0, pi = 3.14159;
-  for (auto& v : m) v = alh * b * b * sin(pi * v / b) / (pi * pi) + bt * v;
-  std::vector<double> wdt(nbm);
-  wdt[0] = m[1] - m[0];
-  for (int i = 1; i < nbm - 1; ++i) wdt[i] = (m[i + 1] - m[i - 1]) / 2.0;
-  wdt[nbm - 1] = m[nbm - 1] - m[nbm - 2];
-  norma = 0;
-  for (int i = 0; i < nbm; ++i) norma += q[i] * wdt[i];
-  for (auto& v : q) v /= norma;
-  double media_rx = 0;
-  for (int i = 0; i < nbm; ++i) media_rx += m[i] * q[i] * wdt[i];
-  for (auto& v : m) v -= media_rx;
-  norma = 0;
-  var = 0;
-  for (int i = 0; i < nbm; ++i)
-    if (q[i] > 0) {
-      norma += q[i] * wdt[i];
-      var += m[i] * m[i] * q[i] * wdt[i];
-    }
-  a1 = sqrt(norma / var);
-  a2 = 1 / (norma * a1);
-  for (int i = 0; i < nbm; ++i) {
-    m[i] *= a1;
-    q[i] *= a2;
-  }
-  if (x_out) std::copy(m.begin(), m.end(), x_out);
-  if (q_out) std::copy(q.begin(), q.end(), q_out);
-  if (binder_m) {
-    double nq = 0;
-    for (double v : q) nq += v;
-    double u2 = 0, u4 = 0;
-    for (int i = 0; i < nbm; ++i) {
-      const double op = m[i] / a1 + media, m2 = op * op;
-      u2 += m2 * q[i] / nq;
-      u4 += m2 * m2 * q[i] / nq;
-    }
-    *binder_m = 1.0 - u4 / (3.0 * u2 * u2);
   }
   return 0;
+}
+
+// ConfrontIsing F90:2127-2182, ZeroTest F90:2042-2074 and HeightTest F90:2076-2125 of a mixed
+// distribution whose abscissae are scaled by B (F90:807): out = liu_2D, liu_3D, kl_2D, kl_3D,
+// zero, height.
+int cvf_h2d_ising(const double* x, const double* q, int n_bin_mixed, double B, double* out) {
+  if (!x || !q || !out || n_bin_mixed < 1) return h2d_fail(CVF_EINVAL, "null array or bad size");
+  double peak2, peak3;
+  if (int rc = ising_peaks(peak2, peak3)) return rc;
+  std::vector<double> m(n_bin_mixed);
+  for (int i = 0; i < n_bin_mixed; ++i) m[i] = B * x[i];
+  confront(m.data(), q, n_bin_mixed, peak2, peak3, out);
+  return 0;
+}
+
+// The F90's search loop F90:732-891: for every pressure (outer), temperature and angle S (inner)
+// in the given lists (internal units), the reweighted distribution, its Binder cumulants of E and
+// rho (tp_rows: n_P x n_T x 2), and per angle the Binder cumulant of the mixed parameter and the
+// Ising comparisons at scale B (rows: n_P x n_T x n_S x 7: binder_m, liu_2D, liu_3D, kl_2D, kl_3D,
+// zero, height). best[5] receives the row of the smallest liu_2D, liu_3D, zero, height and
+// zero + height (the first one in loop order, as the F90's strict comparisons pick; -1 if none is
+// below the F90's start value 1E12). Any output may be NULL.
+int cvf_h2d_scan(cvf_h2d* H, const double* T_hat, int n_T, const double* P_hat, int n_P, const double* S, int n_S,
+                 double B, double* tp_rows, double* rows, long long* best) {
+  if (!H || !T_hat || !P_hat || !S || n_T < 1 || n_P < 1 || n_S < 1)
+    return h2d_fail(CVF_EINVAL, "null or empty parameter list");
+  double peak2, peak3;
+  if (int rc = ising_peaks(peak2, peak3)) return rc;
+  const int nbm = H->nbm;
+  const double start = (double)1E12f;  // F90:725-729
+  double lo[5] = {start, start, start, start, start};
+  long long arg[5] = {-1, -1, -1, -1, -1};
+  std::vector<double> x, q, m(nbm);
+  double a1 = 0, media = 0, be = 0, br = 0;
+  for (int p = 0; p < n_P; ++p)
+    for (int t = 0; t < n_T; ++t) {
+      if (int rc = cvf_h2d_reweight(H, T_hat[t], P_hat[p], nullptr, &be, &br)) return rc;
+      const long long tp = (long long)p * n_T + t;
+      if (tp_rows) {
+        tp_rows[2 * tp] = be;
+        tp_rows[2 * tp + 1] = br;
+      }
+      for (int c0 = 0; c0 < n_S; c0 += kMaxAngles) {
+        const int c = std::min(kMaxAngles, n_S - c0);
+        std::vector<double> qraw, xp;
+        if (int rc = bin_mixed(H, S + c0, c, qraw, xp)) return rc;
+        for (int k = 0; k < c; ++k) {
+          if (int rc = mixed_1d(nbm, xp[2 * k], xp[2 * k + 1], qraw.data() + (size_t)k * nbm, x, q, a1, media))
+            return rc;
+          const long long r = tp * n_S + c0 + k;
+          double v[7];
+          v[0] = binder_of(x, q, a1, media);
+          for (int i = 0; i < nbm; ++i) m[i] = B * x[i];
+          confront(m.data(), q.data(), nbm, peak2, peak3, v + 1);
+          if (rows) std::copy(v, v + 7, rows + 7 * r);
+          const double crit[5] = {v[1], v[2], v[5], v[6], v[5] + v[6]};
+          for (int j = 0; j < 5; ++j)
+            if (lo[j] > crit[j]) {
+              lo[j] = crit[j];
+              arg[j] = r;
+            }
+        }
+      }
+    }
+  if (best) std::copy(arg, arg + 5, best);
+  return 0;
+}
+
+// Constants of the runs given directly (the F90 reads them from its Constants_L file when it
+// exists and matches the runs, F90:396-440); n_runs values, made relative to run 1 as given.
+int cvf_h2d_set_constants(cvf_h2d* H, const double* ctes) {
+  if (!H || !ctes) return h2d_fail(CVF_EINVAL, "null handle or array");
+  HK(cudaSetDevice(H->device));
+  H->ctes.assign(ctes, ctes + H->R);
+  H->grid_ready = false;
+  return upload_runs(H);
 }
 
 int cvf_h2d_destroy(cvf_h2d* H) {

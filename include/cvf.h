@@ -178,22 +178,35 @@ int cvf_format_cluster_line(char* buf, int cap, int t, const cvf_cstats* c);
  * Binned (E, rho) histogram reweighting of HistogramReweighting/
  * histogram_reweighting_mixed_paramSI_norm_x.f90 ("F90") on the GPU. Inputs per sample: the
  * enthalpy per cell h = H/N and the density rho = N/V in internal units (F90:160-165) and its run;
- * per run the internal T and P. cvf_h2d_create converts every sample to SI energy (kJ/mol) and
- * density (kg/m^3) (F90:155-181), bins them as the F90 does (F90:220-279; n_bin2D scales with
- * bin_factor) and runs `steps` iterations of the F90's constants (F90:398-425), failing with
- * CVF_ELIMIT when they have not converged to 1e-7. cvf_h2d_reweight gives the normalised
- * distribution on the n_bin2D x n_bin2D grid at (T, P) (internal units; grid may be NULL) and the
- * Binder cumulants of E and rho (F90:737-759, F90:2610-2662); cvf_h2d_mixed then the distribution
- * of the mixed order parameter at angle alpha, M = sin(alpha) E + cos(alpha) rho, normalised and
- * mapped as the F90 does (F90:1383-1620; n_bin_mixed points, x and q may be NULL) and its Binder
- * cumulant (F90:2580-2608). The Ising-distribution comparisons of the F90 are not provided. */
+ * per run the internal T and P. The F90's literals are single precision (plain gfortran), and so
+ * are its constants here. cvf_h2d_create converts every sample to SI energy (kJ/mol) and density
+ * (kg/m^3) (F90:155-181), bins them as the F90 does (F90:220-279; n_bin2D scales with bin_factor)
+ * and runs `steps` iterations of the F90's constants (F90:446-472), failing with CVF_ELIMIT when
+ * they have not converged to 1e-7; cvf_h2d_set_constants takes them as given instead (the F90's
+ * Constants_L file, F90:380-440). cvf_h2d_reweight gives the normalised distribution on the
+ * n_bin2D x n_bin2D grid at (T, P) (internal units; grid may be NULL) and the Binder cumulants of
+ * E and rho (F90:737-759, F90:2610-2662); cvf_h2d_mixed then the distribution of the mixed order
+ * parameter at angle alpha, M = sin(alpha) E + cos(alpha) rho, normalised and mapped as the F90
+ * does (F90:1383-1620; n_bin_mixed points, x and q may be NULL) and its Binder cumulant
+ * (F90:2580-2608); cvf_h2d_mixed_batch the same for n angles (x, q: n x n_bin_mixed).
+ * cvf_h2d_ising compares a mixed distribution, abscissae scaled by B, with the 2-D and 3-D Ising
+ * order-parameter distributions (ConfrontIsing, ZeroTest, HeightTest, F90:2042-2254): out[6] =
+ * liu_2D, liu_3D, kl_2D, kl_3D, zero, height. cvf_h2d_scan runs the F90's search (F90:732-891)
+ * over the given pressures (outer), temperatures and angles (inner): tp_rows n_P x n_T x
+ * {binder_e, binder_rho}; rows n_P x n_T x n_S x {binder_m, liu_2D, liu_3D, kl_2D, kl_3D, zero,
+ * height}; best[5] the row of the smallest liu_2D, liu_3D, zero, height, zero + height (-1: none). */
 typedef struct cvf_h2d cvf_h2d;
 int cvf_h2d_create(int device, const double* h, const double* rho, const int* run_of, long long n, const double* That,
                    const double* Phat, int n_runs, int L, double bin_factor, int steps, cvf_h2d** out);
 int cvf_h2d_info(const cvf_h2d* H, int* n_bin2d, int* n_bin_mixed, double* Emin, double* dE, double* Dmin, double* dD,
                  double* ctes);
+int cvf_h2d_set_constants(cvf_h2d* H, const double* ctes);
 int cvf_h2d_reweight(cvf_h2d* H, double T_hat, double P_hat, double* grid, double* binder_e, double* binder_rho);
 int cvf_h2d_mixed(cvf_h2d* H, double alpha, double* x, double* q, double* binder_m);
+int cvf_h2d_mixed_batch(cvf_h2d* H, const double* alpha, int n, double* x, double* q, double* binder_m);
+int cvf_h2d_ising(const double* x, const double* q, int n_bin_mixed, double B, double* out);
+int cvf_h2d_scan(cvf_h2d* H, const double* T_hat, int n_T, const double* P_hat, int n_P, const double* S, int n_S,
+                 double B, double* tp_rows, double* rows, long long* best);
 int cvf_h2d_destroy(cvf_h2d* H);
 
 /* Multi-tau autocorrelation (Flag_correlation = 1; GW:1245-1313, GW:2983-3128). Enabling (1)

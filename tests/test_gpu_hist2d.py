@@ -1,7 +1,8 @@
 """Binned 2-D (E, rho) histogram reweighting on the GPU (cvf_h2d_*) against the oracle's
 restatement of the reference's F90 (oracle/hist2d.py; parity with the F90 itself unpinned). The
 bin layout must agree exactly; the reweighted grid, the constants, the Binder cumulants and the
-mixed-parameter distribution to 1e-9 relative (sums run in another order on the GPU)."""
+mixed-parameter distribution to 1e-9 relative (sums run in another order on the GPU); the search
+over (T, P, angle) with its Ising comparisons to 1e-8 and the same best rows."""
 import numpy as np
 import pytest
 
@@ -79,4 +80,55 @@ def test_engine_runs_constants_and_reweighting(engine_runs):
     assert np.allclose(H.ctes, co, rtol=1e-9, atol=1e-9)
     o.ctes = H.ctes.copy()  # the same constants for the comparison of the reweighted grids
     compare(H, o, 0.75, 0.45)
+    H.close()
+
+
+def test_mixed_batch_equals_single_angles(engine_lib):
+    from cvfbulkwater_gb300.analysis import Histogram2D
+    h, rho, run, That, Phat = synthetic(seed=4)
+    H = Histogram2D(h, rho, run, That, Phat, 8, bin_factor=0.6, steps=0)
+    o = H2D(h, rho, run, That, Phat, 8, 0.6)
+    H.reweight(0.76, 0.45, grid=False)
+    go, _ = o.reweighted(0.76, 0.45)
+    alphas = np.linspace(-1.4, 1.4, 71)  # more than one batch of 64
+    xb, qb, bb = H.mixed_batch(alphas)
+    for k in (0, 17, 35, 64, 70):
+        x, q, b = H.mixed(alphas[k])
+        assert np.array_equal(x, xb[k]) and np.array_equal(q, qb[k]) and b == bb[k]
+        xo, qo, a1, media = o.mixed(go, alphas[k])
+        assert np.allclose(xb[k], xo, rtol=1e-8, atol=1e-10) and np.allclose(qb[k], qo, rtol=1e-8, atol=1e-10)
+    H.close()
+
+
+def test_scan_matches_oracle(engine_lib):
+    from oracle import hist2d as O
+    from cvfbulkwater_gb300.analysis import Histogram2D, f90_range
+    h, rho, run, That, Phat = synthetic(seed=6)
+    H = Histogram2D(h, rho, run, That, Phat, 8, bin_factor=0.3, steps=0)
+    o = H2D(h, rho, run, That, Phat, 8, 0.3)
+    T = f90_range(0.73, 0.77, 0.02)
+    P = f90_range(0.44, 0.46, 0.02)
+    S = f90_range(-0.6, 0.6, 0.3, inclusive=False)
+    tp, rows, best = H.scan(T, P, S)
+    tpo, rowso, besto = O.scan(o, T, P, S)
+    assert np.allclose(tp.reshape(-1, 2), tpo, rtol=1e-9)
+    assert np.allclose(rows.reshape(-1, 7), rowso, rtol=1e-8, atol=1e-12)
+    names = ("liu_2D", "liu_3D", "zero", "height", "zero_height")
+    shape = (len(P), len(T), len(S))
+    for k, b in zip(names, besto):
+        assert best[k] == (None if b < 0 else np.unravel_index(b, shape))
+    H.close()
+
+
+def test_given_constants_replace_the_iteration(engine_lib):
+    from cvfbulkwater_gb300.analysis import Histogram2D
+    h, rho, run, That, Phat = synthetic(seed=2)
+    H = Histogram2D(h, rho, run, That, Phat, 8, bin_factor=0.2, steps=0)
+    o = H2D(h, rho, run, That, Phat, 8, 0.2)
+    c = np.array([0.0, 0.4, -0.3, 1.1])
+    H.set_constants(c)
+    o.ctes = c.copy()
+    compare(H, o, 0.75, 0.45, alphas=(0.2,))
+    with pytest.raises(ValueError):
+        H.set_constants(c[:3])
     H.close()
