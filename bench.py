@@ -436,6 +436,142 @@ def run_engine(args):
     dist.close()
     return 0
 
+def _timed(fn, reps=1):
+    """Wall seconds of the fastest of reps calls of fn (which synchronizes itself)."""
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        fn()
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return best
+
+
+def run_analysis(args):
+    """One JSON line for the analysis stages built around the step loop: the isobar run
+    statistics, the multi-tau correlator and the 2-D reweighting search, each on the GPU through
+    the library and as the oracle's CPU restatement (one host thread, a bounded sample, scaled
+    to the same unit)."""
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    import torch
+    from cvfbulkwater_gb300 import build as b
+    b.build()
+    from cvfbulkwater_gb300.analysis import Histogram2D, f90_range
+    from cvfbulkwater_gb300.engine import Lattice, Params
+    from oracle import correlator as OC
+    from oracle import hist2d as OH
+    from oracle import isobar as OI
+    torch.cuda.set_device(local)
+    rows = {}
+
+    # isobar run statistics: 64 replicas of L=16 (the isobar sizes' smallest), 20,000 records each
+    R, L, K = 64, 16, 20000
+    lat = Lattice([Params(L=L, T=0.6 + 0.005 * i, P=0.45, seed=700 + i, start=0, replica=i, device=local)
+                   for i in range(R)])
+    lat.run(200, 1, 0)
+    lat.run_sampled(K, 1, 0, 1)
+    lat.synchronize()
+    t_gpu = _timed(lambda: lat.run_statistics(), reps=5)
+    cols = []
+    for s in lat.samples(0)[:4000]:
+        o = lat.sample_observables(s, 0)
+        cols.append([o.energy, o.enthalpy, o.v_total, o.n_hb, o.m, o.r_cell])
+    cols = np.array(cols)
+    t_cpu = _timed(lambda: OI.run_stats(cols))
+    lat.close()
+    rows["isobar_run_statistics"] = {
+        "workload": f"mean and variance of the six data.out columns over {K} records of each of {R} replicas "
+                    f"(L={L}), read from the on-device sample stream",
+        "gpu": {"value": round(R * K / t_gpu / 1e6, 3), "unit": "M records/s"},
+        "cpu_baseline": {"value": round(len(cols) / t_cpu / 1e6, 4), "unit": "M records/s", "cores": 1,
+                         "kind": "port", "sample": f"{len(cols)} records of one replica (the awk sums in file order)"}}
+
+    # multi-tau correlator on the bench lattice: per-step cost of the sigma histogram + correlator
+    lat = Lattice(Params(L=L_BENCH, T=T_BENCH, P=P_BENCH, seed=SEED, start=2, device=local))
+    lat.run(20, 1, 0)
+    lat.synchronize()
+    n = 200
+    t_off = _timed(lambda: (lat.run(n, 1, 0), lat.synchronize()), reps=3)
+    lat.set_correlation(True)
+    t_on = _timed(lambda: (lat.run(n, 1, 0), lat.synchronize()), reps=3)
+    lat.set_correlation(False)
+    cells = lat.get_config()
+    lat.close()
+    mt = OC.MultiTau()
+    nc = 5
+
+    def cpu_corr():
+        for _ in range(nc):
+            mt.add(OC.max_mass(cells))
+    t_cpu = _timed(cpu_corr)
+    rows["multi_tau_correlator"] = {
+        "workload": f"per MC step: histogram of the 6N sigma arms of the L={L_BENCH} lattice and one correlator "
+                    "update (Flag_correlation = 1)",
+        "gpu": {"value": round(max(t_on - t_off, 0.0) / n * 1e6, 2), "unit": "us/step",
+                "note": "extra time of run(200) with the correlator on, device-resident lattice"},
+        "cpu_baseline": {"value": round(t_cpu / nc * 1e6, 1), "unit": "us/step", "cores": 1, "kind": "port",
+                         "sample": f"{nc} steps on a host copy of the lattice (the reference copies it to the host "
+                                   "every step; that copy is not counted)"}}
+
+    # 2-D histogram reweighting search of the F90 on 8 engine chains (L=8, T = 0.70 .. 0.77,
+    # P = 0.45), 50,000 records each, bin_factor 1
+    That = np.array([float(np.float32(0.70 + 0.01 * j)) for j in range(8)])
+    ns = 50000
+    lat = Lattice([Params(L=8, T=float(t), P=0.45, seed=900 + j, start=0, replica=j, device=local)
+                   for j, t in enumerate(That)])
+    lat.run(2000, 1, 0)
+    lat.run_sampled(ns, 1, 0, 1)
+    h, rho, run = [], [], []
+    for j in range(8):
+        for smp in lat.samples(j):
+            ob = lat.sample_observables(smp, j)
+            h.append(ob.enthalpy / 512.0)
+            rho.append(512.0 / ob.v_total)
+            run.append(j)
+    lat.close()
+    h, rho, run = np.array(h), np.array(rho), np.array(run)
+    That = That.copy()
+    Phat = np.full(8, float(np.float32(0.45)))
+    o = OH.H2D(h, rho, run, That, Phat, 8, 1.0)
+    n_it = 1500
+    t0 = time.perf_counter()
+    H = Histogram2D(h, rho, run, That, Phat, 8, bin_factor=1.0, steps=n_it, device=local)
+    t_wham = time.perf_counter() - t0
+    o.ctes = H.ctes.copy()  # the oracle reweights with the converged constants
+
+    def cpu_wham_step():
+        try:
+            o.wham(1)
+        except RuntimeError:  # one step from zero has not converged; only its time counts
+            pass
+    t_wham_cpu = _timed(cpu_wham_step)
+    o.ctes = H.ctes.copy()
+    T = f90_range(0.72, 0.76, 0.01)
+    P = np.array([0.45])
+    S = f90_range(-0.5, 0.5, 0.05, inclusive=False)
+    t_gpu = _timed(lambda: H.scan(T, P, S), reps=2)
+    t_cpu = _timed(lambda: OH.scan(o, T[:1], P, S[:4]))
+    nbm = H.n_bin_mixed
+    H.close()
+    n_gpu, n_cpu = len(T) * len(P) * len(S), 4
+    rows["hist2d_search"] = {
+        "workload": f"F90 search over {len(T)} T x {len(P)} P x {len(S)} angles: reweighted {o.nb}x{o.nb} grid "
+                    f"(8 engine chains, L=8, x {ns} records, bin_factor 1), mixed parameter ({nbm} bins), Binder cumulants "
+                    "and Ising comparisons per angle",
+        "gpu": {"value": round(n_gpu / t_gpu, 1), "unit": "(T, P, angle) rows/s"},
+        "cpu_baseline": {"value": round(n_cpu / t_cpu, 2), "unit": "(T, P, angle) rows/s", "cores": 1,
+                         "kind": "port", "sample": "1 (T, P) point x 4 angles (one reweighting + 4 mixed histograms)"},
+        "constants": {"gpu": {"value": round(n_it / t_wham, 1), "unit": "iterations/s",
+                              "note": f"{n_it} iterations of the 8 runs' constants incl. binning the samples"},
+                      "cpu_baseline": {"value": round(1 / t_wham_cpu, 3), "unit": "iterations/s", "cores": 1,
+                                       "kind": "port", "sample": "1 iteration"}}}
+    line = {"metric": "analysis stages around the step loop (isobar statistics, correlator, 2-D reweighting)",
+            "impl": "engine", "n_gpus": 1, "data": "synthetic", "rows": rows}
+    print(json.dumps(line), flush=True)
+    return 0
+
 
 def main():
     ap = argparse.ArgumentParser()
@@ -447,7 +583,11 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the batched and Swendsen-Wang sub-benchmarks")
     ap.add_argument("--tile", type=int, default=0,
                     help="sweep tile (cells per thread) instead of the autotuner's choice, e.g. to profile one tile")
+    ap.add_argument("--analysis", action="store_true",
+                    help="print one line timing the analysis stages (GPU against the oracle) instead")
     args = ap.parse_args()
+    if args.analysis:
+        return run_analysis(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -85,6 +85,7 @@ struct ReplicaState {
 // fraction of arms in the most populated sigma value (GW:1245-1272); hist collects the counts of
 // the step being added.
 constexpr int kCorrLevels = 32, kCorrP = 16, kCorrM = 2;
+constexpr int kCorrSlots = 32;
 struct CorrState {
   double shift[kCorrLevels][kCorrP];
   double correlation[kCorrLevels][kCorrP];
@@ -95,7 +96,7 @@ struct CorrState {
   int kmax;
   int pad;
   double accval;
-  unsigned long long hist[6];
+  unsigned long long hist[kCorrSlots][6];  // per-block sums spread over slots (block % kCorrSlots)
 };
 
 // Grid barrier state of the persistent step kernel (zeroed at creation and after an error).
@@ -118,7 +119,8 @@ struct BatchDev {
   int* blk_cell;        // one thread per cell
   int* blk_site;        // one thread per arm site (6N)
   int* blk_site4;       // one thread per 4 arm sites
-  int nblk_sweep, nblk_cube, nblk_cubev, nblk_cell, nblk_site, nblk_site4;
+  int* blk_cell4;       // one thread per 4 cell words
+  int nblk_sweep, nblk_cube, nblk_cubev, nblk_cell, nblk_site, nblk_site4, nblk_cell4;
   GridSync* gsync;      // device barrier state of the persistent step kernel
   CorrState* corr;      // device array [nrep] of correlators (null until enabled)
 };

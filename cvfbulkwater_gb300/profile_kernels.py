@@ -5,7 +5,8 @@
 Creates one lattice (ordered start, T=0.70, P=0.45), runs --warmup full Monte Carlo steps
 and then --launches profiled repetitions of the chosen kind: a single kernel kind through
 cvf_profile_launch (sweep = 2 launches per repetition), or whole steps (kind "step": cube +
-volume + sweep; kind "step_sw": cube + volume + one Swendsen-Wang step).
+volume + sweep; kind "step_sw": cube + volume + one Swendsen-Wang step; --correlation adds
+the multi-tau correlator's histogram and update to every step).
 Prints the mean time per repetition measured with CUDA events on the engine's stream.
 """
 from __future__ import annotations
@@ -27,6 +28,8 @@ def main():
     ap.add_argument("--T", type=float, default=0.70)
     ap.add_argument("--P", type=float, default=0.45)
     ap.add_argument("--mode", type=int, default=None, help="launch mode of the step kinds (0 per phase, 1 persistent)")
+    ap.add_argument("--correlation", action="store_true",
+                    help="step kinds with the multi-tau correlator on (Flag_correlation = 1)")
     a = ap.parse_args()
     import torch
 
@@ -36,6 +39,8 @@ def main():
     lat = Lattice(Params(L=a.L, T=a.T, P=a.P, seed=44648604, start=a.start))
     if a.mode is not None:
         lat.launch_mode = a.mode
+    if a.correlation:
+        lat.set_correlation(True)
     nmet, ncl = STEPS.get(a.kind, (1, 0))
     lat.run(a.warmup, nmet, ncl)
     lat.synchronize()
