@@ -33,6 +33,8 @@ struct cvf_h2d {
   double* d_tgt = nullptr;    // 2R: beta1, pres1 of each target
   double* d_part = nullptr;   // partial reductions
   double* d_grid = nullptr;   // nb*nb: normalised reweighted distribution
+  double* d_colpart = nullptr;  // kColChunks*nb: column sums of row chunks of the grid
+  int* d_rowext = nullptr;      // 2*nb: first and last column with g > 0 of every grid row
   int nblk = 0;
   double* d_scratch = nullptr;  // mixed-parameter binning of a batch of angles
   size_t scratch_n = 0;
@@ -172,25 +174,56 @@ __global__ void k_h2d_grid(const double* __restrict__ hsum, const double* __rest
 }
 
 // grid /= norma, then the marginals: rows (energy bins) into marg[0..nb), columns (density bins)
-// into marg[nb..2nb), each summed in bin order by one thread.
+// into marg[nb..2nb), each in a fixed order (empty bins hold 0 in the grid and add nothing).
 __global__ void k_h2d_scale(double* __restrict__ grid, int nb2, double norma) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b < nb2) grid[b] = __ddiv_rn(grid[b], norma);
 }
-__global__ void k_h2d_marginals(const double* __restrict__ hsum, const double* __restrict__ grid, int nb,
-                                double* __restrict__ marg) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 2 * nb) return;
+constexpr int kColChunks = 32;
+// One warp per row: its sum (lanes over the row, then a fixed shuffle tree) and the first and
+// last column with g > 0 (nb and -1 for a row without any).
+__global__ void k_h2d_rows(const double* __restrict__ grid, int nb, double* __restrict__ marg,
+                           int* __restrict__ rowext) {
+  const int i = blockIdx.x * (kT / 32) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (i >= nb) return;
+  const double* row = grid + (size_t)i * nb;
   double s = 0.0;
-  if (t < nb) {
-    for (int w = 0; w < nb; ++w)
-      if (hsum[t * nb + w] != 0.0) s = __dadd_rn(s, grid[t * nb + w]);
-  } else {
-    const int w = t - nb;
-    for (int i = 0; i < nb; ++i)
-      if (hsum[i * nb + w] != 0.0) s = __dadd_rn(s, grid[i * nb + w]);
+  int lo = nb, hi = -1;
+  for (int w = lane; w < nb; w += 32) {
+    const double g = row[w];
+    s = __dadd_rn(s, g);
+    if (g > 0) {
+      lo = min(lo, w);
+      hi = max(hi, w);
+    }
   }
-  marg[t] = s;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s = __dadd_rn(s, __shfl_xor_sync(0xffffffffu, s, o));
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if (lane == 0) {
+    marg[i] = s;
+    rowext[2 * i] = lo;
+    rowext[2 * i + 1] = hi;
+  }
+}
+// Column sums in two passes: chunk c of the rows per thread and column, then the chunks in order.
+__global__ void k_h2d_cols_part(const double* __restrict__ grid, int nb, double* __restrict__ part) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+  if (w >= nb) return;
+  const int i0 = (int)((long long)c * nb / kColChunks), i1 = (int)((long long)(c + 1) * nb / kColChunks);
+  double s = 0.0;
+  for (int i = i0; i < i1; ++i) s = __dadd_rn(s, grid[(size_t)i * nb + w]);
+  part[(size_t)c * nb + w] = s;
+}
+__global__ void k_h2d_cols(const double* __restrict__ part, int nb, double* __restrict__ marg) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nb) return;
+  double s = 0.0;
+  for (int c = 0; c < kColChunks; ++c) s = __dadd_rn(s, part[(size_t)c * nb + w]);
+  marg[nb + w] = s;
 }
 
 #define HK(x)                                                                          \
@@ -273,20 +306,24 @@ __device__ __forceinline__ double mixed_x(int i, int w, double Emin, double dE, 
   return __dadd_rn(__dmul_rn(E, sa), __dmul_rn(D, ca));
 }
 
-__global__ void k_h2d_xrange(const double* __restrict__ grid, int nb, double Emin, double dE, double Dmin, double dD,
-                             const double* __restrict__ sc, int nblk, double* __restrict__ part) {
+// Range of X over the bins with g > 0 for angle a = blockIdx.x, then Xmin, the bin width and its
+// reciprocal (F90:1418-1428) into xp[3a..3a+2]. Along a row X is monotone in the column, so its
+// extremes over the row's occupied bins are at the row's first and last occupied column.
+// err[0] = 1 when no bin is occupied or the width is not positive.
+__global__ void k_h2d_xrange(const int* __restrict__ rowext, int nb, double Emin, double dE, double Dmin,
+                             double dD, const double* __restrict__ sc, int nbm, double* __restrict__ xp,
+                             int* __restrict__ err) {
   __shared__ double slo[kT], shi[kT];
-  const int a = blockIdx.y;
+  const int a = blockIdx.x;
   const double sa = sc[2 * a], ca = sc[2 * a + 1];
-  const long long nb2 = (long long)nb * nb;
   double lo = INFINITY, hi = -INFINITY;
-  for (long long b = (long long)blockIdx.x * kT + threadIdx.x; b < nb2; b += (long long)nblk * kT)
-    if (grid[b] > 0) {
-      const int i = (int)(b / nb), w = (int)(b - (long long)i * nb);
-      const double X = mixed_x(i, w, Emin, dE, Dmin, dD, sa, ca);
-      lo = fmin(lo, X);
-      hi = fmax(hi, X);
-    }
+  for (int i = threadIdx.x; i < nb; i += kT) {
+    const int w0 = rowext[2 * i], w1 = rowext[2 * i + 1];
+    if (w1 < w0) continue;
+    const double x0 = mixed_x(i, w0, Emin, dE, Dmin, dD, sa, ca), x1 = mixed_x(i, w1, Emin, dE, Dmin, dD, sa, ca);
+    lo = fmin(lo, fmin(x0, x1));
+    hi = fmax(hi, fmax(x0, x1));
+  }
   slo[threadIdx.x] = lo;
   shi[threadIdx.x] = hi;
   __syncthreads();
@@ -298,33 +335,31 @@ __global__ void k_h2d_xrange(const double* __restrict__ grid, int nb, double Emi
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    part[2 * ((size_t)a * nblk + blockIdx.x)] = slo[0];
-    part[2 * ((size_t)a * nblk + blockIdx.x) + 1] = shi[0];
+    lo = slo[0];
+    hi = shi[0];
+    double rX = __dsub_rn(hi, lo);
+    double t = __ddiv_rn(rX, (double)nbm);
+    rX = __dadd_rn(rX, __dmul_rn(4.0, t));
+    const double Xmin = __dsub_rn(lo, __dmul_rn(2.0, t));
+    t = __ddiv_rn(rX, (double)nbm);
+    xp[3 * a] = Xmin;
+    xp[3 * a + 1] = t;
+    xp[3 * a + 2] = t > 0 ? __drcp_rn(t) : 0.0;
+    if (!(t > 0) || !(lo <= hi)) atomicExch(err, 1);
   }
 }
 
-// One thread per angle: Xmin and the bin width of F90:1418-1428; err[0] = 1 when no bin is
-// occupied or the width is not positive.
-__global__ void k_h2d_xparams(const double* __restrict__ part, int nblk, int n, int nbm, double* __restrict__ xp,
-                              int* __restrict__ err) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= n) return;
-  double lo = INFINITY, hi = -INFINITY;
-  for (int b = 0; b < nblk; ++b) {
-    lo = fmin(lo, part[2 * ((size_t)a * nblk + b)]);
-    hi = fmax(hi, part[2 * ((size_t)a * nblk + b) + 1]);
-  }
-  double rX = __dsub_rn(hi, lo);
-  double t = __ddiv_rn(rX, (double)nbm);
-  rX = __dadd_rn(rX, __dmul_rn(4.0, t));
-  const double Xmin = __dsub_rn(lo, __dmul_rn(2.0, t));
-  t = __ddiv_rn(rX, (double)nbm);
-  xp[2 * a] = Xmin;
-  xp[2 * a + 1] = t;
-  if (!(t > 0) || !(lo <= hi)) atomicExch(err, 1);
+// int((X - Xmin) / t) of F90:1446 with the quotient rounded as one division: the product with
+// the rounded reciprocal is within 1e-15 relative of it, so it gives the same integer part unless
+// it lies within 1e-12 of an integer, where the division itself decides.
+__device__ __forceinline__ double mixed_bin(double num, double t, double inv_t) {
+  double q = __dmul_rn(num, inv_t);
+  if (fabs(q - rint(q)) <= 1e-12 * fmax(1.0, fabs(q))) q = __ddiv_rn(num, t);
+  return trunc(q);
 }
 
-__global__ void __launch_bounds__(32 * kXWarps) k_h2d_xhist(const double* __restrict__ grid, int nb, double Emin,
+__global__ void __launch_bounds__(32 * kXWarps) k_h2d_xhist(const double* __restrict__ grid,
+                                                           const int* __restrict__ rowext, int nb, double Emin,
                                                            double dE, double Dmin, double dD,
                                                            const double* __restrict__ sc,
                                                            const double* __restrict__ xp, int nbm, int nwarps,
@@ -334,25 +369,29 @@ __global__ void __launch_bounds__(32 * kXWarps) k_h2d_xhist(const double* __rest
   double* h = hs + (size_t)warp * nbm;
   for (int k = lane; k < nbm; k += 32) h[k] = 0.0;
   __syncwarp();
-  const double sa = sc[2 * a], ca = sc[2 * a + 1], Xmin = xp[2 * a], t = xp[2 * a + 1];
+  const double sa = sc[2 * a], ca = sc[2 * a + 1], Xmin = xp[3 * a], t = xp[3 * a + 1], inv_t = xp[3 * a + 2];
   const double tiny = (double)1E-10f;  // F90:1449
   const int gw = blockIdx.x * kXWarps + warp;
   const int r0 = (int)((long long)gw * nb / nwarps), r1 = (int)((long long)(gw + 1) * nb / nwarps);
   bool bad = false;
   for (int i = r0; i < r1; ++i) {
+    const int wlo = rowext[2 * i], whi = rowext[2 * i + 1];
+    if (whi < wlo) continue;
     const double* row = grid + (size_t)i * nb;
-    for (int w0 = 0; w0 < nb; w0 += 32) {
+    const double es = __dmul_rn(__dadd_rn(Emin, __dmul_rn((double)i + 0.5, dE)), sa);
+    for (int w0 = wlo; w0 <= whi; w0 += 32) {
       const int w = w0 + lane;
-      const double g = w < nb ? row[w] : 0.0;
-      const double X = mixed_x(i, w, Emin, dE, Dmin, dD, sa, ca);
-      const double tq = trunc(__ddiv_rn(__dsub_rn(X, Xmin), t));  // int() of F90:1446
+      const double g = w <= whi ? row[w] : 0.0;
+      const double X = __dadd_rn(es, __dmul_rn(__dadd_rn(Dmin, __dmul_rn((double)w + 0.5, dD)), ca));
+      const double num = __dsub_rn(X, Xmin);
+      const double tq = mixed_bin(num, t, inv_t);
       const bool in = tq >= 0.0 && tq < (double)nbm;
       int key = (int)fmin(fmax(tq, 0.0), (double)(nbm - 1));
       double v = 0.0;
       if (g > 0) {
-        if (in || fabs(__dsub_rn(X, Xmin)) < tiny) v = g;
+        if (in || fabs(num) < tiny) v = g;
         else bad = true;
-        if (!in && fabs(__dsub_rn(X, Xmin)) < tiny) key = 0;
+        if (!in && fabs(num) < tiny) key = 0;
       }
       for (int d = 1; d < 32; d <<= 1) {
         const double ov = __shfl_up_sync(0xffffffffu, v, d);
@@ -368,23 +407,26 @@ __global__ void __launch_bounds__(32 * kXWarps) k_h2d_xhist(const double* __rest
   for (int k = lane; k < nbm; k += 32) wpart[((size_t)a * nwarps + gw) * nbm + k] = h[k];
 }
 
-// Sum of the warps' histograms in warp order: q[a][k].
+// Sum of the warps' histograms, one warp per (bin k, angle a): lane l adds the partials of warps
+// l, l + 32, ... in order, then a fixed shuffle tree: q[a][k].
 __global__ void k_h2d_xsum(const double* __restrict__ wpart, int nwarps, int nbm, double* __restrict__ q) {
-  const int a = blockIdx.y, k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int a = blockIdx.y, k = blockIdx.x * (kT / 32) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (k >= nbm) return;
   double s = 0.0;
-  for (int g = 0; g < nwarps; ++g) s = __dadd_rn(s, wpart[((size_t)a * nwarps + g) * nbm + k]);
-  q[(size_t)a * nbm + k] = s;
+  for (int g = lane; g < nwarps; g += 32) s = __dadd_rn(s, wpart[((size_t)a * nwarps + g) * nbm + k]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s = __dadd_rn(s, __shfl_xor_sync(0xffffffffu, s, o));
+  if (lane == 0) q[(size_t)a * nbm + k] = s;
 }
 
-// Raw mixed-parameter histograms of n <= kMaxAngles angles: qraw (n x nbm) and xp (Xmin, width).
+// Raw mixed-parameter histograms of n <= kMaxAngles angles: qraw (n x nbm) and xp (Xmin, width,
+// 1 / width) of the last reweighted grid (its row extents come with it).
 int bin_mixed(cvf_h2d* H, const double* alpha, int n, std::vector<double>& qraw, std::vector<double>& xp) {
   const int nb = H->nb, nbm = H->nbm;
   if (nbm < 3) return h2d_fail(CVF_EINVAL, "too few mixed-parameter bins");
   HK(cudaSetDevice(H->device));
   const int nwb = std::max(1, std::min(128, (nb + kXWarps - 1) / kXWarps)), nwarps = nwb * kXWarps;
-  const size_t need = 2 * (size_t)n + 2 * (size_t)n * H->nblk + 2 * (size_t)n + (size_t)n * nwarps * nbm +
-                      (size_t)n * nbm + 1;
+  const size_t need = 2 * (size_t)n + 3 * (size_t)n + (size_t)n * nwarps * nbm + (size_t)n * nbm + 1;
   if (need > H->scratch_n) {
     if (H->d_scratch) cudaFree(H->d_scratch);
     H->d_scratch = nullptr;
@@ -393,9 +435,8 @@ int bin_mixed(cvf_h2d* H, const double* alpha, int n, std::vector<double>& qraw,
     H->scratch_n = need;
   }
   double* d_sc = H->d_scratch;
-  double* d_part = d_sc + 2 * (size_t)n;
-  double* d_xp = d_part + 2 * (size_t)n * H->nblk;
-  double* d_w = d_xp + 2 * (size_t)n;
+  double* d_xp = d_sc + 2 * (size_t)n;
+  double* d_w = d_xp + 3 * (size_t)n;
   double* d_q = d_w + (size_t)n * nwarps * nbm;
   int* d_err = reinterpret_cast<int*>(d_q + (size_t)n * nbm);
   std::vector<double> sc(2 * (size_t)n);
@@ -405,15 +446,13 @@ int bin_mixed(cvf_h2d* H, const double* alpha, int n, std::vector<double>& qraw,
   }
   HK(cudaMemcpyAsync(d_sc, sc.data(), sc.size() * sizeof(double), cudaMemcpyHostToDevice, H->s));
   HK(cudaMemsetAsync(d_err, 0, sizeof(int), H->s));
-  k_h2d_xrange<<<dim3(H->nblk, n), kT, 0, H->s>>>(H->d_grid, nb, H->Emin, H->dE, H->Dmin, H->dD, d_sc, H->nblk,
-                                                  d_part);
-  k_h2d_xparams<<<(n + 31) / 32, 32, 0, H->s>>>(d_part, H->nblk, n, nbm, d_xp, d_err);
+  k_h2d_xrange<<<n, kT, 0, H->s>>>(H->d_rowext, nb, H->Emin, H->dE, H->Dmin, H->dD, d_sc, nbm, d_xp, d_err);
   k_h2d_xhist<<<dim3(nwb, n), 32 * kXWarps, (size_t)kXWarps * nbm * sizeof(double), H->s>>>(
-      H->d_grid, nb, H->Emin, H->dE, H->Dmin, H->dD, d_sc, d_xp, nbm, nwarps, d_w, d_err);
-  k_h2d_xsum<<<dim3((nbm + 127) / 128, n), 128, 0, H->s>>>(d_w, nwarps, nbm, d_q);
+      H->d_grid, H->d_rowext, nb, H->Emin, H->dE, H->Dmin, H->dD, d_sc, d_xp, nbm, nwarps, d_w, d_err);
+  k_h2d_xsum<<<dim3((nbm + kT / 32 - 1) / (kT / 32), n), kT, 0, H->s>>>(d_w, nwarps, nbm, d_q);
   HK(cudaGetLastError());
   qraw.resize((size_t)n * nbm);
-  xp.resize(2 * (size_t)n);
+  xp.resize(3 * (size_t)n);
   int err = 0;
   HK(cudaMemcpyAsync(qraw.data(), d_q, qraw.size() * sizeof(double), cudaMemcpyDeviceToHost, H->s));
   HK(cudaMemcpyAsync(xp.data(), d_xp, xp.size() * sizeof(double), cudaMemcpyDeviceToHost, H->s));
@@ -598,8 +637,9 @@ void destroy(cvf_h2d* H) {
   if (!H) return;
   cudaSetDevice(H->device);
   if (H->s) cudaStreamSynchronize(H->s);
-  for (double* p : {H->d_hsum, H->d_logp, H->d_run, H->d_tgt, H->d_part, H->d_grid, H->d_scratch})
+  for (double* p : {H->d_hsum, H->d_logp, H->d_run, H->d_tgt, H->d_part, H->d_grid, H->d_scratch, H->d_colpart})
     if (p) cudaFree(p);
+  if (H->d_rowext) cudaFree(H->d_rowext);
   if (H->s) cudaStreamDestroy(H->s);
   delete H;
 }
@@ -718,7 +758,9 @@ int cvf_h2d_create(int device, const double* h, const double* rho, const int* ru
       cudaMalloc(&H->d_run, 4 * (size_t)R * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&H->d_tgt, 2 * (size_t)R * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&H->d_part, ((size_t)R * H->nblk + R + 2 * (size_t)nb) * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&H->d_grid, (size_t)nb2 * sizeof(double)) != cudaSuccess)
+      cudaMalloc(&H->d_grid, (size_t)nb2 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&H->d_colpart, (size_t)kColChunks * nb * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&H->d_rowext, 2 * (size_t)nb * sizeof(int)) != cudaSuccess)
     return bail(CVF_ENOMEM, "cudaMalloc");
   cudaMemsetAsync(d_counts, 0, (size_t)R * nb2 * sizeof(unsigned int), H->s);
   cudaMemcpyAsync(d_cell, cell.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, H->s);
@@ -785,7 +827,9 @@ int cvf_h2d_reweight(cvf_h2d* H, double T_hat, double P_hat, double* grid, doubl
   norma = norma * H->dE * H->dD;
   k_h2d_scale<<<(nb2 + kT - 1) / kT, kT, 0, H->s>>>(H->d_grid, nb2, norma);
   double* d_marg = H->d_part + (size_t)H->R * H->nblk + H->R;
-  k_h2d_marginals<<<(2 * nb + kT - 1) / kT, kT, 0, H->s>>>(H->d_hsum, H->d_grid, nb, d_marg);
+  k_h2d_rows<<<(nb + kT / 32 - 1) / (kT / 32), kT, 0, H->s>>>(H->d_grid, nb, d_marg, H->d_rowext);
+  k_h2d_cols_part<<<dim3((nb + kT - 1) / kT, kColChunks), kT, 0, H->s>>>(H->d_grid, nb, H->d_colpart);
+  k_h2d_cols<<<(nb + kT - 1) / kT, kT, 0, H->s>>>(H->d_colpart, nb, d_marg);
   HK(cudaGetLastError());
   std::vector<double> marg(2 * (size_t)nb);
   HK(cudaMemcpyAsync(marg.data(), d_marg, marg.size() * sizeof(double), cudaMemcpyDeviceToHost, H->s));
@@ -828,7 +872,7 @@ int cvf_h2d_mixed_batch(cvf_h2d* H, const double* alpha, int n, double* x_out, d
     if (int rc = bin_mixed(H, alpha + c0, c, qraw, xp)) return rc;
     for (int k = 0; k < c; ++k) {
       const int a = c0 + k;
-      if (int rc = mixed_1d(nbm, xp[2 * k], xp[2 * k + 1], qraw.data() + (size_t)k * nbm, x, q, a1, media)) return rc;
+      if (int rc = mixed_1d(nbm, xp[3 * k], xp[3 * k + 1], qraw.data() + (size_t)k * nbm, x, q, a1, media)) return rc;
       if (x_out) std::copy(x.begin(), x.end(), x_out + (size_t)a * nbm);
       if (q_out) std::copy(q.begin(), q.end(), q_out + (size_t)a * nbm);
       if (binder_m) binder_m[a] = binder_of(x, q, a1, media);
@@ -882,7 +926,7 @@ int cvf_h2d_scan(cvf_h2d* H, const double* T_hat, int n_T, const double* P_hat, 
         std::vector<double> qraw, xp;
         if (int rc = bin_mixed(H, S + c0, c, qraw, xp)) return rc;
         for (int k = 0; k < c; ++k) {
-          if (int rc = mixed_1d(nbm, xp[2 * k], xp[2 * k + 1], qraw.data() + (size_t)k * nbm, x, q, a1, media))
+          if (int rc = mixed_1d(nbm, xp[3 * k], xp[3 * k + 1], qraw.data() + (size_t)k * nbm, x, q, a1, media))
             return rc;
           const long long r = tp * n_S + c0 + k;
           double v[7];

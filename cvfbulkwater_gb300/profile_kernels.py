@@ -15,13 +15,14 @@ import argparse
 import ctypes as C
 
 KINDS = {"sweep": 0, "cube": 1, "volume": 2, "measure": 3}
+ANALYSIS = ("h2d_scan",)
 STEPS = {"step": (1, 0), "step_sw": (0, 1)}  # full MC steps: (Metropolis sweeps, SW steps)
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--L", type=int, default=256)
-    ap.add_argument("--kind", default="sweep", choices=sorted(KINDS) + sorted(STEPS))
+    ap.add_argument("--kind", default="sweep", choices=sorted(KINDS) + sorted(STEPS) + list(ANALYSIS))
     ap.add_argument("--launches", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--start", type=int, default=2)
@@ -36,6 +37,8 @@ def main():
     from . import abi, build
     from .engine import Lattice, Params
     build.build()
+    if a.kind == "h2d_scan":
+        return h2d_scan(a)
     lat = Lattice(Params(L=a.L, T=a.T, P=a.P, seed=44648604, start=a.start))
     if a.mode is not None:
         lat.launch_mode = a.mode
@@ -59,6 +62,40 @@ def main():
           f"ms/rep={e0.elapsed_time(e1) / max(a.launches, 1):.4f}")
     lat.synchronize()
     lat.close()
+
+
+def h2d_scan(a):
+    """The 2-D reweighting search on 8 chains of L=--L lattices at T = 0.70 .. 0.77 (20,000 records
+    each, bin_factor 1, 1500 constant iterations), then --launches searches over 5 temperatures x
+    21 angles."""
+    import time
+
+    import numpy as np
+
+    from .analysis import Histogram2D, f90_range
+    from .engine import Lattice, Params
+    That = np.array([float(np.float32(0.70 + 0.01 * j)) for j in range(8)])
+    lat = Lattice([Params(L=a.L, T=float(t), P=a.P, seed=900 + j, start=0, replica=j) for j, t in enumerate(That)])
+    lat.run(2000, 1, 0)
+    lat.run_sampled(20000, 1, 0, 1)
+    N = float(a.L) ** 3
+    h, rho, run = [], [], []
+    for j in range(8):
+        for smp in lat.samples(j):
+            ob = lat.sample_observables(smp, j)
+            h.append(ob.enthalpy / N)
+            rho.append(N / ob.v_total)
+            run.append(j)
+    lat.close()
+    H = Histogram2D(np.array(h), np.array(rho), np.array(run), That, np.full(8, float(np.float32(a.P))), a.L,
+                    bin_factor=1.0, steps=1500)
+    T, P, S = f90_range(0.72, 0.76, 0.01), np.array([a.P]), f90_range(-0.5, 0.5, 0.05, inclusive=False)
+    t0 = time.perf_counter()
+    for _ in range(max(a.launches, 1)):
+        H.scan(T, P, S)
+    dt = (time.perf_counter() - t0) / max(a.launches, 1)
+    print(f"h2d_scan L={a.L} grid={H.n_bin2d}^2 rows={len(T) * len(S)} ms/search={dt * 1e3:.2f}")
+    H.close()
 
 
 if __name__ == "__main__":
