@@ -23,20 +23,29 @@ __device__ __forceinline__ void cell_xyz(uint32_t c, uint32_t L, int lgL, uint32
 
 // One thread per cell: checks sigma in [0,5] and eta in {0,1} (GW:776-790), packs sigma into the
 // colour-split word and the six eta bits into eta6[c]; the smallest offending cell goes to *bad.
+// kVec (a 16-byte aligned array): the block's 256 cells (12 KB) are read with fully coalesced
+// 16-byte loads into shared memory first, so every line of host memory crosses the link once.
+constexpr int kCfgCells = 256;  // cells per block = threads per block
 template <bool kVec>
-__global__ void k_pack_cells(const int* __restrict__ c12, uint32_t L, uint32_t H, int lgL, uint32_t N,
-                             uint32_t* __restrict__ cells0, uint32_t* __restrict__ cells1, uint8_t* __restrict__ eta6,
-                             unsigned long long* bad) {
-  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= N) return;
+__global__ void __launch_bounds__(kCfgCells) k_pack_cells(const int* __restrict__ c12, uint32_t L, uint32_t H, int lgL,
+                                                          uint32_t N, uint32_t* __restrict__ cells0,
+                                                          uint32_t* __restrict__ cells1, uint8_t* __restrict__ eta6,
+                                                          unsigned long long* bad) {
+  __shared__ int4 s_in[3 * kCfgCells];
+  const uint32_t c0 = blockIdx.x * kCfgCells, c = c0 + threadIdx.x;
   int v[12];
   if (kVec) {
-    const int4* p = reinterpret_cast<const int4*>(c12) + 3ull * c;
-    const int4 a = p[0], b = p[1], d = p[2];
+    const uint32_t n4 = 3u * min((uint32_t)kCfgCells, N - c0);
+    const int4* src = reinterpret_cast<const int4*>(c12) + 3ull * c0;
+    for (uint32_t i = threadIdx.x; i < n4; i += kCfgCells) s_in[i] = src[i];
+    __syncthreads();
+    if (c >= N) return;
+    const int4 a = s_in[3 * threadIdx.x], b = s_in[3 * threadIdx.x + 1], d = s_in[3 * threadIdx.x + 2];
     v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
     v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
     v[8] = d.x; v[9] = d.y; v[10] = d.z; v[11] = d.w;
   } else {
+    if (c >= N) return;
 #pragma unroll
     for (int i = 0; i < 12; ++i) v[i] = c12[12ull * c + i];
   }
@@ -56,6 +65,47 @@ __global__ void k_pack_cells(const int* __restrict__ c12, uint32_t L, uint32_t H
   cell_xyz(c, L, lgL, x, y, z);
   ((x + y + z) & 1u ? cells1 : cells0)[(x >> 1) + H * (y + L * z)] = w;
   eta6[c] = (uint8_t)e;
+}
+
+// The reverse for cvf_get_config: one thread per cell builds its twelve values (sigma from the
+// colour-split word, eta from the even and the odd cube containing the cell, as the host unpack
+// does) in shared memory, then the block writes its 12 KB to the caller's 16-byte aligned array
+// with fully coalesced 16-byte stores.
+__global__ void __launch_bounds__(kCfgCells) k_unpack_cells(const uint32_t* __restrict__ cells0,
+                                                            const uint32_t* __restrict__ cells1,
+                                                            const uint8_t* __restrict__ ce,
+                                                            const uint8_t* __restrict__ co, uint32_t L, uint32_t H,
+                                                            int lgL, uint32_t N, int* __restrict__ c12) {
+  __shared__ int4 s_out[3 * kCfgCells];
+  __shared__ uint8_t s_tab[72];
+  if (threadIdx.x < 72) s_tab[threadIdx.x] = (uint8_t)cube_eta_bits(threadIdx.x >> 3, threadIdx.x & 7);
+  __syncthreads();
+  const uint32_t c0 = blockIdx.x * kCfgCells, c = c0 + threadIdx.x;
+  if (c < N) {
+    uint32_t x, y, z;
+    cell_xyz(c, L, lgL, x, y, z);
+    const uint32_t w = ((x + y + z) & 1u ? cells1 : cells0)[(x >> 1) + H * (y + L * z)];
+    const uint32_t xo = (x & 1u) ? x : (x == 0 ? L - 1 : x - 1);
+    const uint32_t yo = (y & 1u) ? y : (y == 0 ? L - 1 : y - 1);
+    const uint32_t zo = (z & 1u) ? z : (z == 0 ? L - 1 : z - 1);
+    const uint32_t p = (x & 1u) | ((y & 1u) << 1) | ((z & 1u) << 2);
+    const uint32_t se = ce[(x >> 1) + H * ((y >> 1) + H * (z >> 1))];
+    const uint32_t so = co[(xo >> 1) + H * ((yo >> 1) + H * (zo >> 1))];
+    const uint32_t eta = (uint32_t)s_tab[se * 8 + p] | (uint32_t)s_tab[so * 8 + (p ^ 7u)];
+    int v[12];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+      v[a] = (int)((w >> (3 * a)) & 7u);
+      v[6 + a] = (int)((eta >> a) & 1u);
+    }
+    s_out[3 * threadIdx.x] = make_int4(v[0], v[1], v[2], v[3]);
+    s_out[3 * threadIdx.x + 1] = make_int4(v[4], v[5], v[6], v[7]);
+    s_out[3 * threadIdx.x + 2] = make_int4(v[8], v[9], v[10], v[11]);
+  }
+  __syncthreads();
+  const uint32_t n4 = 3u * min((uint32_t)kCfgCells, N - c0);
+  int4* dst = reinterpret_cast<int4*>(c12) + 3ull * c0;
+  for (uint32_t i = threadIdx.x; i < n4; i += kCfgCells) dst[i] = s_out[i];
 }
 
 // One thread per cube: the cube state from the eta of its vertices with the decision tree of
@@ -96,9 +146,17 @@ cudaError_t launch_pack_config(const ReplicaDesc& R, const int* c12, uint32_t* c
                                uint8_t* ce, uint8_t* co, unsigned long long* bad, cudaStream_t s) {
   const uint32_t L = (uint32_t)R.L, H = (uint32_t)R.H, N = L * L * L;
   const bool vec = ((uintptr_t)c12 & 15u) == 0;
-  if (vec) k_pack_cells<true><<<grid_of(N), kThreads, 0, s>>>(c12, L, H, R.lgL, N, cells0, cells1, eta6, bad);
-  else k_pack_cells<false><<<grid_of(N), kThreads, 0, s>>>(c12, L, H, R.lgL, N, cells0, cells1, eta6, bad);
+  static_assert(kCfgCells == kThreads, "one cell per thread");
+  if (vec) k_pack_cells<true><<<grid_of(N), kCfgCells, 0, s>>>(c12, L, H, R.lgL, N, cells0, cells1, eta6, bad);
+  else k_pack_cells<false><<<grid_of(N), kCfgCells, 0, s>>>(c12, L, H, R.lgL, N, cells0, cells1, eta6, bad);
   k_pack_cubes<<<grid_of(2ull * H * H * H), kThreads, 0, s>>>(eta6, L, H, ce, co);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_config(const ReplicaDesc& R, int* c12, cudaStream_t s) {
+  const uint32_t L = (uint32_t)R.L, H = (uint32_t)R.H, N = L * L * L;
+  if (((uintptr_t)c12 & 15u) != 0) return cudaErrorInvalidValue;
+  k_unpack_cells<<<grid_of(N), kCfgCells, 0, s>>>(R.cells[0], R.cells[1], R.cubes[0], R.cubes[1], L, H, R.lgL, N, c12);
   return cudaGetLastError();
 }
 

@@ -160,6 +160,10 @@ cudaError_t launch_run_stats(const BatchDev& b, double* out, cudaStream_t s);
 // cell).
 cudaError_t launch_pack_config(const ReplicaDesc& R, const int* c12, uint32_t* cells0, uint32_t* cells1, uint8_t* eta6,
                                uint8_t* ce, uint8_t* co, unsigned long long* bad, cudaStream_t s);
+// cvf_get_config on the GPU: the replica's lattice written as cells12 straight into the caller's
+// 16-byte aligned array in host memory (pageable-memory access); cudaErrorInvalidValue if the
+// array is not aligned.
+cudaError_t launch_unpack_config(const ReplicaDesc& R, int* c12, cudaStream_t s);
 void launch_cluster_stats_impl(const BatchDev& b, unsigned long long* blocktop, int record, cudaStream_t s);
 
 }  // namespace cvf

@@ -62,8 +62,9 @@ struct cvf_handle {
   int launch_mode = 0;
   void* staging = nullptr;  // pinned host buffer for configuration transfers (lazily allocated)
   size_t staging_bytes = 0;
-  // cvf_set_config: 1 = a kernel reads and packs the caller's array in host memory (the GPU
-  // accesses pageable memory through the host page tables), 0 = host packing + copies.
+  // cvf_set_config / cvf_get_config: 1 = kernels read and pack, or unpack and write, the
+  // caller's array in host memory (the GPU accesses pageable memory through the host page
+  // tables), 0 = host packing and unpacking + copies.
   int io_mode = 0;
   bool io_capable = false;
   void* io_scratch = nullptr;  // device: packed cells, eta bytes and cube states of one replica
@@ -624,8 +625,14 @@ int cvf_get_config(cvf_handle* h, int r, int* c12, long long n_cells) {
   if (!c12 || n_cells != R.N) return fail(CVF_EINVAL, "cells12 must hold 12 ints for each of the N cells");
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
-  // always the packed copy + threaded host unpack: GPU stores into pageable host memory ran at
-  // ~55 GB/s on GB300 (14.5 ms for L=256 against 6.2 ms this way, far more into untouched pages)
+  if (h->io_mode == 1 && ((uintptr_t)c12 & 15u) == 0) {
+    // the GPU writes the caller's array in place, block by block with coalesced 16-byte stores,
+    // into pages that host threads have made present first
+    touch_pages(c12, (size_t)R.N * 12 * sizeof(int));
+    CK(launch_unpack_config(R.desc, c12, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return 0;
+  }
   if (int rc = ensure_staging(h, R)) return rc;
   const size_t half = (size_t)(R.N / 2), nc = (size_t)R.H * R.H * R.H;
   uint32_t* c0 = (uint32_t*)h->staging;

@@ -7,6 +7,9 @@
 #include <algorithm>
 #include <atomic>
 #include <thread>
+#include <vector>
+#include <sys/mman.h>
+#include <unistd.h>
 
 #include "cvf_spec.cuh"
 
@@ -114,6 +117,27 @@ static void parallel_for(long long n, long long work, F body) {
     th.emplace_back([=]() { body(b, e); });
   }
   for (auto& t : th) t.join();
+}
+
+void touch_pages(void* p, size_t bytes) {
+  if (!bytes) return;
+  long ps = sysconf(_SC_PAGESIZE);
+  if (ps <= 0) ps = 4096;
+  const uintptr_t lo = (uintptr_t)p & ~((uintptr_t)ps - 1), hi = (uintptr_t)p + bytes;
+  const long long n = (long long)((hi - lo + ps - 1) / ps);
+  std::vector<unsigned char> in(n, 0);
+  if (mincore((void*)lo, hi - lo, in.data()) != 0) std::fill(in.begin(), in.end(), 0);
+  long long missing = 0;
+  for (unsigned char v : in) missing += (v & 1) ? 0 : 1;
+  if (!missing) return;
+  parallel_for(n, missing * 64, [&](long long b, long long e) {
+    for (long long k = b; k < e; ++k) {
+      if (in[k] & 1) continue;
+      // the first byte of the page that lies inside the range
+      const uintptr_t a = std::max(lo + (uintptr_t)k * ps, (uintptr_t)p);
+      *reinterpret_cast<volatile char*>(a) = 0;
+    }
+  });
 }
 
 std::string config_value_error(const int* c12, long long c) {

@@ -36,6 +36,10 @@ bool pack_config(int L, const int* cells12, uint32_t* cells0, uint32_t* cells1, 
                  uint8_t* cubes_odd, std::string& err);
 // The reader's message (GW:776-790) for the first invalid value of cell c.
 std::string config_value_error(const int* c12, long long c);
+// Writes a zero into every page of [p, p + bytes) that is not resident (mincore), from host
+// threads, so that the pages exist before a GPU writes the range (a GPU's first write to a
+// pageable page faults far more slowly than a host thread's).
+void touch_pages(void* p, size_t bytes);
 void unpack_config(int L, const uint32_t* cells0, const uint32_t* cells1, const uint8_t* cubes_even,
                    const uint8_t* cubes_odd, int* cells12);
 

@@ -146,7 +146,8 @@ class Lattice:
 
     @property
     def io_mode(self) -> int:
-        """1: set_config reads the caller's array in host memory from the GPU; 0: host packing."""
+        """1: set_config / get_config read and write the caller's array in host memory from the
+        GPU; 0: host packing and unpacking."""
         m = C.c_int()
         check(lib().cvf_get_io_mode(self._h, C.byref(m)))
         return m.value

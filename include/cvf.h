@@ -307,14 +307,15 @@ int cvf_get_launch_mode(const cvf_handle* h, int* mode);
 int cvf_set_replica_groups(cvf_handle* h, int groups);
 int cvf_get_replica_groups(const cvf_handle* h, int* groups);
 
-/* Transfer mode of cvf_set_config. 1: kernels read and pack the caller's cells12 array where it
- * lies in host memory (the GPU accesses pageable host memory through the host page tables, as
- * over NVLink-C2C on GB300); the default when the device reports
- * cudaDevAttrPageableMemoryAccess. 0: host threads pack into pinned memory, then one copy (the
- * only mode on other systems; cvf_set_io_mode(h, 1) then fails with CVF_EINVAL). Both modes give
- * the same lattice and the same error for an invalid value (the lattice is left unchanged).
- * cvf_get_config always copies the packed lattice and unpacks it with host threads, which is the
- * faster direction on GB300. No reference counterpart. */
+/* Transfer mode of cvf_set_config and cvf_get_config. 1: kernels read and pack, or unpack and
+ * write, the caller's cells12 array where it lies in host memory (the GPU accesses pageable host
+ * memory through the host page tables, as over NVLink-C2C on GB300); the default when the device
+ * reports cudaDevAttrPageableMemoryAccess. cvf_get_config first has host threads touch the
+ * array's pages that are not resident, and uses the mode only for a 16-byte aligned array. 0:
+ * host threads pack into pinned memory and unpack from it, with one copy each way (the only mode
+ * on other systems; cvf_set_io_mode(h, 1) then fails with CVF_EINVAL). Both modes give the same
+ * lattice and array and the same error for an invalid value (the lattice is left unchanged).
+ * No reference counterpart. */
 int cvf_set_io_mode(cvf_handle* h, int mode);
 int cvf_get_io_mode(const cvf_handle* h, int* mode);
 
