@@ -22,7 +22,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libcvf_gb300.so")
 EXE = os.path.join(BUILD, "gpu_water3D")
 
-CU = ["cvf_mc.cu", "cvf_sw.cu", "cvf_reweight.cu", "cvf_noalloc.cu", "cvf_config.cu", "cvf_stats.cu", "cvf_corr.cu", "cvf_hist2d.cu"]
+CU = ["cvf_mc.cu", "cvf_sw.cu", "cvf_reweight.cu", "cvf_noalloc.cu", "cvf_config.cu", "cvf_stats.cu", "cvf_corr.cu", "cvf_hist2d.cu", "cvf_nhb.cu"]
 CPP = ["cvf_engine.cpp", "cvf_host.cpp", "cvf_io.cpp", "cvf_isobar.cpp"]
 DRIVER = ["gpu_water3D.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

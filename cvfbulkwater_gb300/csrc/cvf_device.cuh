@@ -25,6 +25,13 @@ struct ReplicaDesc {
   int32_t* cand;      // 6N: percolation candidate id by root (-1 none)
   uint32_t* cover;    // max_cand * 3 * W: coordinate coverage bitmaps
   int max_cand;       // capacity of cover
+  // Flag_chessboard = 0 (null otherwise): eta of every cell as 6 bits, the bond count of every
+  // cell, and the greedy measurement's work arrays (cells with 5 or more matched bonds, their
+  // counts); cells indexed x + L*(y + L*z)
+  uint8_t* eta6;
+  uint8_t* nhb;
+  uint8_t* sat;
+  uint8_t* cnt;
   // vdW shells (device copies)
   const float* dist;
   const int* freq;
@@ -121,6 +128,7 @@ struct BatchDev {
   int* blk_site4;       // one thread per 4 arm sites
   int* blk_cell4;       // one thread per 4 cell words
   int nblk_sweep, nblk_cube, nblk_cubev, nblk_cell, nblk_site, nblk_site4, nblk_cell4;
+  int max_L;            // largest edge among the replicas
   GridSync* gsync;      // device barrier state of the persistent step kernel
   CorrState* corr;      // device array [nrep] of correlators (null until enabled)
 };
@@ -147,6 +155,14 @@ void launch_measure_end(const BatchDev& b, int record, cudaStream_t s);
 // interval > 0. Same lattice, counters and samples as the per-phase kernels.
 cudaError_t launch_run(const BatchDev& b, int nsteps, int nmet, int interval, cudaStream_t s);
 void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s);
+// Flag_chessboard = 0: bond counts from the lattice and eta6 (GW:841-862; one replica, or all for
+// only_replica < 0), one Metropolis sweep
+// (12 launches: colour 0 arms 0..5, colour 1 arms 0..5) and the measurement with the greedy
+// bond count of GW:2064-2099 into the replicas' last record (appended to the sample stream when
+// record is set).
+void launch_nhb_init(const BatchDev& b, int only_replica, cudaStream_t s);
+void launch_nhb_sweep(const BatchDev& b, int jsweep, cudaStream_t s);
+void launch_nhb_measure(const BatchDev& b, int record, cudaStream_t s);
 // One correlator step of every replica: the sigma histogram of the lattice, then the add of the
 // most-populated fraction to the replica's correlator (b.corr must be allocated).
 cudaError_t launch_corr_step(const BatchDev& b, cudaStream_t s);

@@ -76,6 +76,9 @@ struct cvf_handle {
   // kernels per group of consecutive replicas, on parallel branches of the graph, so that one
   // group's blocks fill the tails of another group's kernels. 0 = automatic.
   int group_setting = 0;
+  // Flag_chessboard = 0 for every replica: the nhb<=4 compatibility mode (no cube moves, bond
+  // counts per cell, per-arm sweep launches, greedy bond count in the measurement)
+  bool nhb_mode = false;
   struct Group {
     BatchDev b;
     cudaStream_t s = nullptr;
@@ -199,6 +202,8 @@ static int fill_tables(cvf_handle* h, int r0, int r1, int vec, BatchDev& b) {
   b.nblk_cube = tc[n];
   b.nblk_cell = tl[n];
   b.nblk_site = tsi[n];
+  b.max_L = 0;
+  for (int i = r0; i < r1; ++i) b.max_L = std::max(b.max_L, h->reps[i].L);
   return 0;
 }
 
@@ -340,7 +345,7 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     return 0;
   }
   cudaGraph_t g;
-  if (h->launch_mode == 1 && ncl == 0 && !h->corr_on) {
+  if (h->launch_mode == 1 && ncl == 0 && !h->corr_on && !h->nhb_mode) {
     // one persistent launch; a driver that cannot capture a cooperative launch leaves the
     // handle on the per-phase kernels
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -361,7 +366,7 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     cudaGetLastError();
     h->launch_mode = 0;
   }
-  if (ncl == 0 && group_count(h) > 1) {
+  if (ncl == 0 && group_count(h) > 1 && !h->nhb_mode) {
     if (int rc = build_groups(h)) return rc;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     CK(cudaEventRecord(h->fork, h->stream));
@@ -382,7 +387,15 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     return 0;
   }
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  for (int i = 0; i < steps; ++i) {
+  for (int i = 0; i < steps && h->nhb_mode; ++i) {
+    // Flag_chessboard = 0: volume move, nmet per-arm sweeps, no cube move (GW:1348-1384)
+    launch_step_begin(h->b, nmet, 0, 0, 1, h->stream);
+    launch_cube_volume(h->b, 0, 1, h->stream);
+    for (int j = 0; j < nmet; ++j) launch_nhb_sweep(h->b, j, h->stream);
+    if (i == 0 && record) launch_nhb_measure(h->b, 1, h->stream);
+    if (h->corr_on) launch_corr_step(h->b, h->stream);
+  }
+  for (int i = 0; i < steps && !h->nhb_mode; ++i) {
     if (i == 0 && record && ncl == 0 && nmet > 0) {
       enqueue_recorded_metropolis_step(h, nmet);
     } else {
@@ -441,8 +454,9 @@ int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
     const cvf_params& p = params[i];
     if (p.L < 4 || (p.L & 1)) return fail(CVF_EINVAL, "L must be even and >= 4");
     if ((long long)p.L * p.L * p.L * 6 >= (1LL << 31)) return fail(CVF_EINVAL, "L too large (6 L^3 must fit int32)");
-    if (p.flag_chessboard != 1)
-      return fail(CVF_EINVAL, "Flag_chessboard=0 (nhb<=4 mode) is not supported; use Flag_chessboard=1");
+    if (p.flag_chessboard != 0 && p.flag_chessboard != 1) return fail(CVF_EINVAL, "Flag_chessboard must be 0 or 1");
+    if (p.flag_chessboard != params[0].flag_chessboard)
+      return fail(CVF_EINVAL, "all replicas of a handle share Flag_chessboard");
     if (!(p.T > 0.0f)) return fail(CVF_EINVAL, "T must be > 0");
     if (!(p.R_cutoff > 0.0f)) return fail(CVF_EINVAL, "R_cutoff must be > 0");
     if (p.start < 0 || p.start > 2) return fail(CVF_EINVAL, "Flag_config must be 0, 1 or 2");
@@ -456,6 +470,7 @@ int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
   init_device_tables();
   cvf_handle* h = new cvf_handle();
   h->device = params[0].device;
+  h->nhb_mode = params[0].flag_chessboard == 0;
   {
     int pageable = 0;
     if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, h->device) == cudaSuccess && pageable) {
@@ -487,6 +502,13 @@ int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
     if ((rc = dev_alloc(h, (void**)&d.cells[0], half_cells * 4)) || (rc = dev_alloc(h, (void**)&d.cells[1], half_cells * 4)) ||
         (rc = dev_alloc(h, (void**)&d.cubes[0], ncubes)) || (rc = dev_alloc(h, (void**)&d.cubes[1], ncubes)))
       return bail(rc);
+    if (h->nhb_mode) {
+      const size_t nc = (size_t)r.N;
+      if ((rc = dev_alloc(h, (void**)&d.eta6, nc)) || (rc = dev_alloc(h, (void**)&d.nhb, nc)) ||
+          (rc = dev_alloc(h, (void**)&d.sat, nc)) || (rc = dev_alloc(h, (void**)&d.cnt, nc)))
+        return bail(rc);
+      if (cudaMemset(d.eta6, 63, nc) != cudaSuccess) return bail(fail(CVF_ECUDA, "eta reset failed"));  // GW:721-724
+    }
     float* dd;
     int* df;
     if ((rc = dev_alloc(h, (void**)&dd, kMaxShells * sizeof(float))) || (rc = dev_alloc(h, (void**)&df, kMaxShells * sizeof(int))))
@@ -546,6 +568,7 @@ int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
   if ((rc = upload_descs(h)) || (rc = build_tables(h))) return bail(rc);
   // start 1 leaves sigma at zero until cvf_set_config; cubes always start random (GW:700-708)
   launch_init_lattice(h->b, h->stream);
+  if (h->nhb_mode) launch_nhb_init(h->b, -1, h->stream);
   cudaError_t e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return bail(fail(CVF_ECUDA, std::string("init: ") + cudaGetErrorString(e)));
   *out = h;
@@ -582,7 +605,7 @@ int cvf_set_config(cvf_handle* h, int r, const int* c12, long long n_cells) {
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
   const size_t half = (size_t)(R.N / 2), nc = (size_t)R.H * R.H * R.H;
-  if (h->io_mode == 1) {
+  if (h->io_mode == 1 && !h->nhb_mode) {
     // pack on the GPU straight from the caller's array into scratch; the lattice changes only
     // when every value is valid
     if (int rc = ensure_io_scratch(h, R)) return rc;
@@ -615,6 +638,19 @@ int cvf_set_config(cvf_handle* h, int r, const int* c12, long long n_cells) {
   CK(cudaMemcpyAsync(R.desc.cells[1], c1, half * 4, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(R.desc.cubes[0], ce, nc, cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(R.desc.cubes[1], co, nc, cudaMemcpyHostToDevice, h->stream));
+  if (h->nhb_mode) {
+    // Flag_chessboard = 0 keeps the file's eta (GW:751-756) and counts the bonds from it
+    // (GW:841-862); the cube states stay unused
+    std::vector<uint8_t> e6((size_t)R.N);
+    for (long long c = 0; c < R.N; ++c) {
+      uint32_t e = 0;
+      for (int a = 0; a < 6; ++a) e |= (uint32_t)(c12[c * 12 + 6 + a] & 1) << a;
+      e6[c] = (uint8_t)e;
+    }
+    CK(cudaMemcpyAsync(R.desc.eta6, e6.data(), e6.size(), cudaMemcpyHostToDevice, h->stream));
+    launch_nhb_init(h->b, r, h->stream);
+    CK(cudaGetLastError());
+  }
   CK(cudaStreamSynchronize(h->stream));  // the staging buffer is reused by the next call
   return 0;
 }
@@ -625,7 +661,7 @@ int cvf_get_config(cvf_handle* h, int r, int* c12, long long n_cells) {
   if (!c12 || n_cells != R.N) return fail(CVF_EINVAL, "cells12 must hold 12 ints for each of the N cells");
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
-  if (h->io_mode == 1 && ((uintptr_t)c12 & 15u) == 0) {
+  if (h->io_mode == 1 && !h->nhb_mode && ((uintptr_t)c12 & 15u) == 0) {
     // the GPU writes the caller's array in place, block by block with coalesced 16-byte stores,
     // into pages that host threads have made present first
     touch_pages(c12, (size_t)R.N * 12 * sizeof(int));
@@ -643,8 +679,16 @@ int cvf_get_config(cvf_handle* h, int r, int* c12, long long n_cells) {
   CK(cudaMemcpyAsync(c1, R.desc.cells[1], half * 4, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaMemcpyAsync(ce, R.desc.cubes[0], nc, cudaMemcpyDeviceToHost, h->stream));
   CK(cudaMemcpyAsync(co, R.desc.cubes[1], nc, cudaMemcpyDeviceToHost, h->stream));
+  std::vector<uint8_t> e6;
+  if (h->nhb_mode) {
+    e6.resize((size_t)R.N);
+    CK(cudaMemcpyAsync(e6.data(), R.desc.eta6, e6.size(), cudaMemcpyDeviceToHost, h->stream));
+  }
   CK(cudaStreamSynchronize(h->stream));
   unpack_config(R.L, c0, c1, ce, co, c12);
+  if (h->nhb_mode)  // Flag_chessboard = 0: eta as read (GW:1296-1305 writes active_bond)
+    for (long long c = 0; c < R.N; ++c)
+      for (int a = 0; a < 6; ++a) c12[c * 12 + 6 + a] = (e6[c] >> a) & 1;
   return 0;
 }
 
@@ -682,6 +726,8 @@ int cvf_get_distances(const cvf_handle* h, int r, float* dist, int* freq, int ca
 static int run_impl(cvf_handle* h, int n_steps, int nmet, int ncl, int interval) {
   if (!h) return fail(CVF_EINVAL, "null handle");
   if (n_steps < 0 || nmet < 0 || ncl < 0) return fail(CVF_EINVAL, "negative step counts");
+  if (ncl > 0 && h->nhb_mode)
+    return fail(CVF_EINVAL, "Cluster_Steps > 0 needs Flag_chessboard = 1 (the nhb<=4 mode has no cluster move here)");
   CK(cudaSetDevice(h->device));
   if (ncl > 0) {
     if (int rc = ensure_sw(h)) return rc;
@@ -733,7 +779,8 @@ int cvf_observables(cvf_handle* h, int r, cvf_obs* out) {
   if (int rc = check_rep(h, r)) return rc;
   if (!out) return fail(CVF_EINVAL, "null out");
   CK(cudaSetDevice(h->device));
-  launch_measure(h->b, 0, h->stream);
+  if (h->nhb_mode) launch_nhb_measure(h->b, 0, h->stream);
+  else launch_measure(h->b, 0, h->stream);
   SampleRec last;  // only the 32-byte measurement record crosses to the host
   CK(cudaMemcpyAsync(&last, (char*)(h->b.st + r) + offsetof(ReplicaState, last), sizeof(SampleRec),
                      cudaMemcpyDeviceToHost, h->stream));
@@ -880,6 +927,10 @@ int cvf_set_state(cvf_handle* h, int r, const cvf_state* in) {
 
 int cvf_autotune(cvf_handle* h, int* vec_out) {
   if (!h) return fail(CVF_EINVAL, "null handle");
+  if (h->nhb_mode) {  // the per-arm sweep of Flag_chessboard = 0 has no tile to choose
+    if (vec_out) *vec_out = h->b.vec;
+    return 0;
+  }
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
   std::vector<int> cands;
@@ -965,6 +1016,7 @@ int cvf_get_stream(cvf_handle* h, void** stream) {
 
 int cvf_profile_launch(cvf_handle* h, int kind, int n) {
   if (!h || n < 0 || kind < 0 || kind > 3) return fail(CVF_EINVAL, "bad profile request");
+  if (h->nhb_mode) return fail(CVF_EINVAL, "kernel profiling covers the Flag_chessboard = 1 kernels");
   CK(cudaSetDevice(h->device));
   for (int i = 0; i < n; ++i) {
     switch (kind) {

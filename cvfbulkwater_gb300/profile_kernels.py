@@ -29,6 +29,10 @@ def main():
     ap.add_argument("--T", type=float, default=0.70)
     ap.add_argument("--P", type=float, default=0.45)
     ap.add_argument("--mode", type=int, default=None, help="launch mode of the step kinds (0 per phase, 1 persistent)")
+    ap.add_argument("--nhb", action="store_true",
+                    help="step kinds in the nhb<=4 compatibility mode (Flag_chessboard = 0)")
+    ap.add_argument("--measure", action="store_true",
+                    help="step kinds followed by one observables read per repetition")
     ap.add_argument("--correlation", action="store_true",
                     help="step kinds with the multi-tau correlator on (Flag_correlation = 1)")
     a = ap.parse_args()
@@ -39,7 +43,7 @@ def main():
     build.build()
     if a.kind == "h2d_scan":
         return h2d_scan(a)
-    lat = Lattice(Params(L=a.L, T=a.T, P=a.P, seed=44648604, start=a.start))
+    lat = Lattice(Params(L=a.L, T=a.T, P=a.P, seed=44648604, start=a.start, flag_chessboard=0 if a.nhb else 1))
     if a.mode is not None:
         lat.launch_mode = a.mode
     if a.correlation:
@@ -52,7 +56,11 @@ def main():
     s = torch.cuda.ExternalStream(sp.value)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(s)
-    if a.kind in STEPS:
+    if a.kind in STEPS and a.measure:
+        for _ in range(a.launches):
+            lat.run(1, nmet, ncl)
+            lat.observables()
+    elif a.kind in STEPS:
         lat.run(a.launches, nmet, ncl)
     else:
         abi.check(abi.lib().cvf_profile_launch(lat._h, KINDS[a.kind], a.launches))

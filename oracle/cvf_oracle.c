@@ -86,6 +86,8 @@ struct oracle {
     int freq[512];
     uint64_t thr_sweep[33], thr_cube[9], thr_sw[2];
     int nthreads;
+    int chess;    /* Flag_chessboard: 1 cube moves, 0 the nhb<=4 mode */
+    uint8_t* nhb; /* Flag_chessboard = 0: dev_nhb of GW:1974-2007, one byte per cell */
 };
 
 static void rng(const oracle_t* o, uint32_t c0, uint32_t c1, uint32_t c2, uint32_t out[4])
@@ -369,7 +371,17 @@ static void random_cubes(oracle_t* o)
     }
 }
 
+static void nhb_init(oracle_t* o);
+
 oracle_t* oracle_create(int L, float T, float P, int64_t seed, float Rc, uint32_t replica, int start)
+{
+    return oracle_create_mode(L, T, P, seed, Rc, replica, start, 1);
+}
+
+/* flag_chessboard = 0: every eta is 1 (GW:721-724), no cube moves, and the bond count per cell
+ * (GW:841-862) drives the nhb<=4 dynamics. */
+oracle_t* oracle_create_mode(int L, float T, float P, int64_t seed, float Rc, uint32_t replica, int start,
+                             int flag_chessboard)
 {
     if (L < 4 || (L & 1)) return NULL;
     oracle_t* o = (oracle_t*)calloc(1, sizeof(oracle_t));
@@ -413,6 +425,12 @@ oracle_t* oracle_create(int L, float T, float P, int64_t seed, float Rc, uint32_
     } else {
         random_cubes(o);
     }
+    o->chess = flag_chessboard != 0;
+    o->nhb = (uint8_t*)calloc((size_t)o->N, 1);
+    if (!o->chess) {
+        memset(o->eta, 1, (size_t)(ARMS * o->N));
+        nhb_init(o);
+    }
     return o;
 }
 
@@ -423,6 +441,7 @@ void oracle_destroy(oracle_t* o)
     free(o->eta);
     free(o->cube);
     free(o->label);
+    free(o->nhb);
     free(o);
 }
 
@@ -440,6 +459,10 @@ int oracle_set_config(oracle_t* o, const int32_t* c12, int64_t n_cells)
             o->s[a * o->N + c] = (uint8_t)sv;
             o->eta[a * o->N + c] = (uint8_t)ev;
         }
+    if (!o->chess) { /* GW:791-806 infers cube states only with Flag_chessboard = 1 */
+        nhb_init(o);
+        return 0;
+    }
     int L = o->L;
     int64_t ncubes = o->N / 4;
     for (int64_t i = 0; i < ncubes; ++i) {
@@ -607,10 +630,80 @@ static void sweep_cell(oracle_t* o, int64_t cell, uint32_t t)
     }
 }
 
+/* GW:841-862: bonds of each cell whose two arms agree, counted only where eta = 1. */
+static void nhb_init(oracle_t* o)
+{
+    int64_t N = o->N;
+    for (int64_t c = 0; c < N; ++c) {
+        int acc = 0;
+        for (int a = 0; a < ARMS; ++a)
+            acc += o->eta[a * N + c] * (o->s[a * N + c] == o->s[(int64_t)(a ^ 1) * N + neighbour(o->L, c, a)]);
+        o->nhb[c] = (uint8_t)acc;
+    }
+}
+
+/* Flag_chessboard = 0 (GW:1964-2007, non-chessboard branch): arm a of one cell with the same
+ * random numbers as the checkerboard sweep (proposal digit a of word 0, acceptance uniform chunk
+ * a), and the hydrogen-bond term theta(nhb_i + d <= 4) theta(nhb_j + d <= 4) delta(new, s') minus
+ * theta(nhb_i <= 4) theta(nhb_j <= 4) delta(old, s'), with d = delta(new, s') - delta(old, s').
+ * On acceptance both cells' counts move by d, as bytes. */
+static void sweep_cell_arm_nhb(oracle_t* o, int64_t cell, int a, uint32_t t)
+{
+    int64_t N = o->N;
+    uint32_t r[4];
+    rng(o, (uint32_t)cell, t, ST_SWEEP, r);
+    static const uint32_t pow6[ARMS] = {7776, 1296, 216, 36, 6, 1};
+    uint32_t d = draw_below(o, 46656u, r, 1, (uint32_t)cell, t, ST_SWEEP);
+    int nw = (int)((d / pow6[a]) % 6);
+    int old = o->s[a * N + cell];
+    if (nw == old) return;
+    int64_t j = neighbour(o->L, cell, a);
+    int nb = o->s[(int64_t)(a ^ 1) * N + j];
+    int dn = (nw == nb) - (old == nb);
+    int ni = o->nhb[cell], nj = o->nhb[j];
+    int hbn = (ni + dn <= 4) * (nj + dn <= 4) * (nw == nb);
+    int hbo = (ni <= 4) * (nj <= 4) * (old == nb);
+    int dhb = hbn - hbo;
+    int dns = 0;
+    for (int b = 0; b < ARMS; ++b) {
+        if (b == a) continue;
+        int sb = o->s[b * N + cell];
+        dns += (nw == sb) - (old == sb);
+    }
+    uint64_t T = o->thr_sweep[(dhb + 1) * 11 + dns + 5];
+    uint32_t hU = (r[1 + a / 2] >> (16 * (a & 1))) & 0xffffu;
+    int acc;
+    if (hU != (uint32_t)(T >> 16)) {
+        acc = hU < (T >> 16);
+    } else {
+        uint32_t rf[4];
+        rng(o, (uint32_t)cell, t, ST_SWEEP_REFINE, rf);
+        uint32_t lU = (rf[a / 2] >> (16 * (a & 1))) & 0xffffu;
+        acc = ((((uint64_t)hU) << 16) | lU) < T;
+    }
+    if (acc) {
+        o->s[a * N + cell] = (uint8_t)nw;
+        o->nhb[cell] = (uint8_t)(ni + dn);
+        o->nhb[j] = (uint8_t)(nj + dn);
+    }
+}
+
 void oracle_sweep(oracle_t* o)
 {
     int L = o->L;
     uint32_t t = o->ctr[0];
+    if (!o->chess) {
+        /* colour 0 arms 0..5, then colour 1 arms 0..5: in one (colour, arm) pass no two cells
+         * share a neighbour along the arm, so the cells are independent */
+        for (int colour = 0; colour < 2; ++colour)
+            for (int a = 0; a < ARMS; ++a)
+                for (int64_t zy = 0; zy < (int64_t)L * L; ++zy) {
+                    int y = (int)(zy % L), z = (int)(zy / L);
+                    for (int x = (y + z + colour) & 1; x < L; x += 2) sweep_cell_arm_nhb(o, cell_of(L, x, y, z), a, t);
+                }
+        o->ctr[0]++;
+        return;
+    }
     for (int colour = 0; colour < 2; ++colour) {
 #pragma omp parallel for schedule(static) num_threads(o->nthreads)
         for (int64_t zy = 0; zy < (int64_t)L * L; ++zy) {
@@ -688,6 +781,11 @@ void oracle_sw_step(oracle_t* o)
 
 void oracle_step(oracle_t* o, int nmet, int ncl)
 {
+    if (!o->chess) { /* GW:1348-1384 and GW:1556: no cube move; cluster moves are not restated */
+        oracle_volume_move(o);
+        for (int j = 0; j < nmet; ++j) oracle_sweep(o);
+        return;
+    }
     oracle_cube_move(o);
     oracle_volume_move(o);
     for (int j = 0; j < nmet; ++j) oracle_sweep(o);
@@ -701,15 +799,34 @@ void oracle_measure(const oracle_t* o, oracle_obs_t* out)
     int L = o->L;
     int64_t N = o->N;
     int64_t hb2 = 0, ns = 0;
+    if (!o->chess) {
+        /* GW:2064-2099: bonds in typewriter order (cell, then x+, y+, z+), each counted for both
+         * cells while both have fewer than NHBMAX = 4; hb2 = sum of the counts = 2 N_hb */
+        uint8_t* cnt = (uint8_t*)calloc((size_t)N, 1);
+        for (int64_t c = 0; c < N; ++c)
+            for (int d = 0; d < 3; ++d) {
+                int64_t nb = neighbour(L, c, 2 * d);
+                if (o->s[(int64_t)(2 * d) * N + c] == o->s[(int64_t)(2 * d + 1) * N + nb] && cnt[c] < 4 && cnt[nb] < 4) {
+                    cnt[c]++;
+                    cnt[nb]++;
+                    hb2 += 2;
+                }
+            }
+        free(cnt);
+        for (int64_t c = 0; c < N; ++c)
+            for (int a = 0; a < ARMS - 1; ++a)
+                for (int b = a + 1; b < ARMS; ++b) ns += o->s[a * N + c] == o->s[b * N + c];
+    } else {
 #pragma omp parallel for schedule(static) reduction(+ : hb2, ns) num_threads(o->nthreads)
-    for (int64_t c = 0; c < N; ++c) {
-        for (int d = 0; d < 3; ++d) {
-            int64_t nb = neighbour(L, c, 2 * d);
-            if (o->s[(int64_t)(2 * d) * N + c] == o->s[(int64_t)(2 * d + 1) * N + nb])
-                hb2 += o->eta[(int64_t)(2 * d) * N + c] + o->eta[(int64_t)(2 * d + 1) * N + nb];
+        for (int64_t c = 0; c < N; ++c) {
+            for (int d = 0; d < 3; ++d) {
+                int64_t nb = neighbour(L, c, 2 * d);
+                if (o->s[(int64_t)(2 * d) * N + c] == o->s[(int64_t)(2 * d + 1) * N + nb])
+                    hb2 += o->eta[(int64_t)(2 * d) * N + c] + o->eta[(int64_t)(2 * d + 1) * N + nb];
+            }
+            for (int a = 0; a < ARMS - 1; ++a)
+                for (int b = a + 1; b < ARMS; ++b) ns += o->s[a * N + c] == o->s[b * N + c];
         }
-        for (int a = 0; a < ARMS - 1; ++a)
-            for (int b = a + 1; b < ARMS; ++b) ns += o->s[a * N + c] == o->s[b * N + c];
     }
     out->n_hb2 = hb2;
     out->n_sigma = ns;
@@ -813,3 +930,5 @@ void oracle_get_thresholds(const oracle_t* o, uint64_t* s33, uint64_t* c9, uint6
     memcpy(c9, o->thr_cube, sizeof(o->thr_cube));
     memcpy(sw2, o->thr_sw, sizeof(o->thr_sw));
 }
+
+void oracle_get_nhb(const oracle_t* o, uint8_t* nhb) { memcpy(nhb, o->nhb, (size_t)o->N); }

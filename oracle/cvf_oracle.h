@@ -50,6 +50,11 @@ int oracle_distances(int L, float Rc, float* dist, int* freq, int cap);
 
 /* start: 0 random, 1 caller sets config, 2 ordered (GW:730-833). */
 oracle_t* oracle_create(int L, float T, float P, int64_t seed, float Rc, uint32_t replica, int start);
+/* flag_chessboard = 0: the nhb<=4 mode (every eta 1, no cube moves, bond counts per cell). */
+oracle_t* oracle_create_mode(int L, float T, float P, int64_t seed, float Rc, uint32_t replica, int start,
+                             int flag_chessboard);
+/* Flag_chessboard = 0: the per-cell bond counts that drive the dynamics (N bytes). */
+void oracle_get_nhb(const oracle_t* o, uint8_t* nhb);
 void oracle_destroy(oracle_t* o);
 void oracle_set_threads(oracle_t* o, int n_threads);
 

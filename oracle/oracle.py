@@ -36,6 +36,10 @@ def lib():
         P = C.c_void_p
         L.oracle_create.restype = P
         L.oracle_create.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int64, C.c_float, C.c_uint32, C.c_int]
+        L.oracle_create_mode.restype = P
+        L.oracle_create_mode.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int64, C.c_float, C.c_uint32, C.c_int,
+                                         C.c_int]
+        L.oracle_get_nhb.argtypes = [P, P]
         L.oracle_destroy.argtypes = [P]
         L.oracle_set_threads.argtypes = [P, C.c_int]
         L.oracle_set_config.argtypes = [P, P, C.c_int64]
@@ -88,10 +92,10 @@ def distances(L: int, Rc: float):
 class Oracle:
     """One lattice of the CPU oracle."""
 
-    def __init__(self, L, T, P, seed, Rc=6.0, replica=0, start=0, threads=1):
+    def __init__(self, L, T, P, seed, Rc=6.0, replica=0, start=0, threads=1, flag_chessboard=1):
         self.L = L
         self.N = L ** 3
-        self._h = lib().oracle_create(L, T, P, seed, Rc, replica, start)
+        self._h = lib().oracle_create_mode(L, T, P, seed, Rc, replica, start, flag_chessboard)
         if not self._h:
             raise ValueError("oracle_create failed")
         lib().oracle_set_threads(self._h, threads)
@@ -111,6 +115,12 @@ class Oracle:
         rc = lib().oracle_set_config(self._h, _ptr(a), a.size // 12)
         if rc:
             raise ValueError(f"oracle_set_config rc={rc}")
+
+    def nhb(self) -> np.ndarray:
+        """Flag_chessboard = 0: the bond count of every cell (cell = x + L*(y + L*z))."""
+        a = np.zeros(self.N, dtype=np.uint8)
+        lib().oracle_get_nhb(self._h, _ptr(a))
+        return a
 
     def get_config(self) -> np.ndarray:
         a = np.zeros((self.N, 12), dtype=np.int32)

@@ -29,7 +29,7 @@ def test_version_string(engine_lib):
 @pytest.mark.parametrize("field,value,msg", [
     ("L", 7, b"even"),
     ("L", 2, b"even"),
-    ("flag_chessboard", 0, b"Flag_chessboard"),
+    ("flag_chessboard", 2, b"Flag_chessboard"),
     ("start", 3, b"Flag_config"),
     ("T", 0.0, b"T must"),
 ])

@@ -1,4 +1,4 @@
-"""Configuration uploads in both modes: kernels reading the caller's cells12 array in host memory
+"""Configuration transfers in both modes: kernels reading and writing the caller's cells12 array in host memory
 (io_mode 1, GPUs with pageable-memory access) and host packing with a copy (io_mode 0).
 Lattices, read-back cells12 arrays and error reports must be identical, for power-of-two and
 other edges, aligned and unaligned caller arrays."""

@@ -58,9 +58,23 @@ def test_driver_rejects_bad_input(engine_lib, tmp_path):
     open(tmp_path / "input_data", "w").write("Pressure 0.45\nTemperature\n")
     r = subprocess.run([EXE], cwd=tmp_path, capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "Error [Temperature]" in r.stderr
-    write_input(tmp_path, L=16, Flag_chessboard=0)
+    write_input(tmp_path, L=16, Flag_chessboard=2)
     r = subprocess.run([EXE], cwd=tmp_path, capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "Flag_chessboard" in r.stderr
+    write_input(tmp_path, L=16, Flag_chessboard=0, Cluster_Steps=1)
+    r = subprocess.run([EXE], cwd=tmp_path, capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "Flag_chessboard" in r.stderr
+
+
+def test_driver_non_chessboard_mode(engine_lib, tmp_path):
+    """Flag_chessboard = 0: every eta stays 1, data.out carries the capped bond count."""
+    write_input(tmp_path, L=8, Flag_chessboard=0, Equilibrium_Steps=20, Sampling_Steps=200)
+    run(tmp_path)
+    data = np.loadtxt(tmp_path / "data.out")
+    assert data.shape == (20, 7)
+    assert np.all(data[:, 4] <= 2 * 512)  # at most 4 counted bonds per cell
+    cfg = np.loadtxt(tmp_path / "config.out", dtype=np.int64)
+    assert cfg.shape == (512, 12) and np.all(cfg[:, 6:] == 1)
 
 
 def test_driver_reproduces_reference_statistics(engine_lib, tmp_path):
