@@ -388,11 +388,17 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
   }
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   for (int i = 0; i < steps && h->nhb_mode; ++i) {
-    // Flag_chessboard = 0: volume move, nmet per-arm sweeps, no cube move (GW:1348-1384)
-    launch_step_begin(h->b, nmet, 0, 0, 1, h->stream);
+    // Flag_chessboard = 0: volume move, nmet per-arm sweeps, ncl SW steps, no cube move
+    // (GW:1348-1384, GW:1480-1555); the SW steps leave the bond counts as they are, as the
+    // reference's cluster update does (GW:2531-2542)
+    launch_step_begin(h->b, nmet, ncl, 0, 1, h->stream);
     launch_cube_volume(h->b, 0, 1, h->stream);
     for (int j = 0; j < nmet; ++j) launch_nhb_sweep(h->b, j, h->stream);
-    if (i == 0 && record) launch_nhb_measure(h->b, 1, h->stream);
+    for (int j = 0; j < ncl; ++j) launch_sw_step(h->b, j, h->stream);
+    if (i == 0 && record) {
+      launch_nhb_measure(h->b, 1, h->stream);
+      if (ncl > 0) enqueue_cstats(h, 1);
+    }
     if (h->corr_on) launch_corr_step(h->b, h->stream);
   }
   for (int i = 0; i < steps && !h->nhb_mode; ++i) {
@@ -726,8 +732,6 @@ int cvf_get_distances(const cvf_handle* h, int r, float* dist, int* freq, int ca
 static int run_impl(cvf_handle* h, int n_steps, int nmet, int ncl, int interval) {
   if (!h) return fail(CVF_EINVAL, "null handle");
   if (n_steps < 0 || nmet < 0 || ncl < 0) return fail(CVF_EINVAL, "negative step counts");
-  if (ncl > 0 && h->nhb_mode)
-    return fail(CVF_EINVAL, "Cluster_Steps > 0 needs Flag_chessboard = 1 (the nhb<=4 mode has no cluster move here)");
   CK(cudaSetDevice(h->device));
   if (ncl > 0) {
     if (int rc = ensure_sw(h)) return rc;

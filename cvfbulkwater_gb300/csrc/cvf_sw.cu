@@ -53,8 +53,10 @@ __device__ __forceinline__ uint32_t word_at(const ReplicaDesc& R, int x, int y, 
   return R.cells[(x + y + z) & 1][(uint32_t)(x >> 1) + (uint32_t)R.H * ((uint32_t)y + (uint32_t)R.L * (uint32_t)z)];
 }
 
+// eta of the cell's six arms: from its two cubes, or (Flag_chessboard = 0) as stored.
 __device__ __forceinline__ uint32_t eta_of_cell(const ReplicaDesc& R, int x, int y, int z) {
   const int L = R.L, H = R.H;
+  if (R.eta6) return R.eta6[(size_t)x + (size_t)L * ((size_t)y + (size_t)L * z)];
   const int xo = (x & 1) ? x : (x == 0 ? L - 1 : x - 1);
   const int yo = (y & 1) ? y : (y == 0 ? L - 1 : y - 1);
   const int zo = (z & 1) ? z : (z == 0 ? L - 1 : z - 1);

@@ -46,8 +46,9 @@ typedef struct cvf_params {
   int start;             /* Flag_config: 0 disordered, 1 caller loads cells12, 2 ordered (GW:730-833) */
   int flag_chessboard;   /* 1: eta moves by 2x2x2 cubes (GW:639-724). 0: the nhb<=4 compatibility
                             mode (GW:721-724, GW:1964-2007, GW:2064-2099): eta fixed (all 1, or
-                            as set by cvf_set_config), no cube move, Metropolis steps only. All
-                            replicas of a handle share the value. */
+                            as set by cvf_set_config), no cube move; SW steps leave the bond
+                            counts as they are, as in the reference. All replicas of a handle
+                            share the value. */
   unsigned int replica;  /* replica id, counter word 3 of every Philox draw */
   int device;            /* CUDA device ordinal (Device_ID, GW:457-468) */
   int sample_capacity;   /* samples kept on the device per replica; 0 selects 65536 */

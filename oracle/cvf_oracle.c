@@ -781,9 +781,10 @@ void oracle_sw_step(oracle_t* o)
 
 void oracle_step(oracle_t* o, int nmet, int ncl)
 {
-    if (!o->chess) { /* GW:1348-1384 and GW:1556: no cube move; cluster moves are not restated */
+    if (!o->chess) { /* GW:1348-1384: no cube move; SW leaves the bond counts stale (GW:2531-2542) */
         oracle_volume_move(o);
         for (int j = 0; j < nmet; ++j) oracle_sweep(o);
+        for (int j = 0; j < ncl; ++j) oracle_sw_step(o);
         return;
     }
     oracle_cube_move(o);

@@ -61,14 +61,11 @@ def test_driver_rejects_bad_input(engine_lib, tmp_path):
     write_input(tmp_path, L=16, Flag_chessboard=2)
     r = subprocess.run([EXE], cwd=tmp_path, capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "Flag_chessboard" in r.stderr
-    write_input(tmp_path, L=16, Flag_chessboard=0, Cluster_Steps=1)
-    r = subprocess.run([EXE], cwd=tmp_path, capture_output=True, text=True, timeout=60)
-    assert r.returncode == 1 and "Flag_chessboard" in r.stderr
 
 
 def test_driver_non_chessboard_mode(engine_lib, tmp_path):
     """Flag_chessboard = 0: every eta stays 1, data.out carries the capped bond count."""
-    write_input(tmp_path, L=8, Flag_chessboard=0, Equilibrium_Steps=20, Sampling_Steps=200)
+    write_input(tmp_path, L=8, Flag_chessboard=0, Cluster_Steps=1, Equilibrium_Steps=20, Sampling_Steps=200)
     run(tmp_path)
     data = np.loadtxt(tmp_path / "data.out")
     assert data.shape == (20, 7)

@@ -1,8 +1,8 @@
 """Flag_chessboard = 0 (the nhb<=4 compatibility mode) on the GPU against the oracle, bit for
 bit: lattice, eta, r_cell / volume, move counters and the exact counts of the measurement,
 whose N_hb is the reference's greedy typewriter-order count with the cap of 4 (GW:2064-2099);
-recorded samples, configurations with arbitrary eta, batches of replicas, and the rejections
-(cluster steps, mixed flags)."""
+recorded samples, configurations with arbitrary eta, batches of replicas, Swendsen-Wang steps
+(which leave the bond counts stale, as the reference's do) and the rejections (mixed flags)."""
 import numpy as np
 import pytest
 
@@ -112,11 +112,23 @@ def test_batch_of_replicas(engine_lib, oracle_mod):
     eng.close()
 
 
-def test_rejections(engine_lib):
-    eng = Lattice(Params(L=4, T=0.6, P=0.45, seed=1, start=0, flag_chessboard=0))
-    with pytest.raises(CvfError):
-        eng.run(1, 1, 1)  # cluster steps need the chessboard mode
+@pytest.mark.parametrize("L,T", [(6, 0.6), (8, 0.45)])
+def test_cluster_steps_leave_counts_stale(engine_lib, oracle_mod, L, T):
+    # Swendsen-Wang with Flag_chessboard = 0: bonds from the stored eta, counts untouched
+    eng, ora = pair(oracle_mod, L, T, 0.45, 40 + L, 0)
+    eng.run(5, 1, 1)
+    for _ in range(5):
+        ora.step(1, 1)
+    assert_same(eng, ora)
+    assert np.array_equal(eng.labels(), ora.labels())
+    eng.run_sampled(4, 1, 1, 2)
+    for _ in range(4):
+        ora.step(1, 1)
+    assert_same(eng, ora)
     eng.close()
+
+
+def test_rejections(engine_lib):
     with pytest.raises(CvfError):
         Lattice([Params(L=4, T=0.6, P=0.45, seed=1, flag_chessboard=0), Params(L=4, T=0.6, P=0.45, seed=2)])
     with pytest.raises(CvfError):
