@@ -147,6 +147,8 @@ def lib():
         "cvf_isobar_point_from_stats": (I, [C.POINTER(RunStats), C.POINTER(IsobarPoint)]),
         "cvf_isobar_point_to_si": (I, [C.POINTER(IsobarPoint), D, C.POINTER(IsobarPointSI)]),
         "cvf_alpha_p_derivative": (I, [P, P, P, P, I, P, P, P, C.POINTER(I)]),
+        "cvf_cp_derivative": (I, [P, P, P, P, I, P, P, P, C.POINTER(I)]),
+        "cvf_kt_derivative": (I, [P, P, P, P, I, P, P]),
         "cvf_reweight_forward": (I, [I, P, P, LL, P, I, P, I, D, D, P, P, I, P]),
         "cvf_reweight_adjoint": (I, [I, P, P, LL, P, I, P, D, P, P, I, P, P]),
     }

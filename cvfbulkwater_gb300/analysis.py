@@ -58,6 +58,32 @@ def alpha_p_derivative(T, V, V2, n):
     return tuple(o[: k.value] for o in outs)
 
 
+def cp_derivative(T, H, H2, n):
+    """CPderivate.c: arrays of one isobar (any order) -> (T, C_P, error) for the sorted points
+    2 .. m-3."""
+    T, H, H2 = (np.ascontiguousarray(a, dtype=np.float64) for a in (T, H, H2))
+    n = np.ascontiguousarray(n, dtype=np.int64)
+    m = len(T)
+    outs = [np.zeros(max(m, 1)) for _ in range(3)]
+    k = C.c_int()
+    check(lib().cvf_cp_derivative(_ptr(T), _ptr(H), _ptr(H2), _ptr(n), m, _ptr(outs[0]), _ptr(outs[1]),
+                                  _ptr(outs[2]), C.byref(k)))
+    return tuple(o[: k.value] for o in outs)
+
+
+KT_NOT_VALUE = -10.0
+
+
+def kt_derivative(T, P, rho, Erho):
+    """KTderivate.c: points (T in K, P in MPa, rho and its error in kg/m^3, any order) ->
+    (K_T, error) per point in MPa^-1, KT_NOT_VALUE where the reference gives none."""
+    T, P, rho, Erho = (np.ascontiguousarray(a, dtype=np.float64) for a in (T, P, rho, Erho))
+    m = len(T)
+    kt, ekt = np.zeros(max(m, 1)), np.zeros(max(m, 1))
+    check(lib().cvf_kt_derivative(_ptr(T), _ptr(P), _ptr(rho), _ptr(Erho), m, _ptr(kt), _ptr(ekt)))
+    return kt[:m], ekt[:m]
+
+
 def _ptr(a):
     return a.ctypes.data_as(C.c_void_p)
 

@@ -125,4 +125,122 @@ int cvf_alpha_p_derivative(const double* T, const double* V, const double* V2, c
   return 0;
 }
 
+// CPderivate.c:56-124: C_P = dH/dT along an isobar by central differences (one-sided at the
+// ends), the error from the third derivative and the neighbours' sqrt(3 var / n); only points
+// 2 .. n-3 are written.
+int cvf_cp_derivative(const double* T, const double* H, const double* H2, const long long* n, int m, double* T_out,
+                      double* cp_out, double* err_out, int* m_out) {
+  if (!T || !H || !H2 || !n || !T_out || !cp_out || !err_out || !m_out || m < 0)
+    return iso_fail("null array or negative count");
+  *m_out = 0;
+  if (m < 2) return 0;
+  for (int j = 0; j < m; ++j)
+    if (n[j] < 1) return iso_fail("a point without samples");
+  std::vector<int> o((size_t)m);
+  std::iota(o.begin(), o.end(), 0);
+  std::stable_sort(o.begin(), o.end(), [&](int a, int b) { return T[a] < T[b]; });
+  std::vector<double> t(m), h(m), cp(m), eh(m);
+  for (int j = 0; j < m; ++j) {
+    t[j] = T[o[j]];
+    h[j] = H[o[j]];
+  }
+  for (int j = 0; j < m; ++j) {
+    if (j == 0) cp[j] = (h[j + 1] - h[j]) / (t[j + 1] - t[j]);
+    else if (j == m - 1) cp[j] = (h[j] - h[j - 1]) / (t[j] - t[j - 1]);
+    else cp[j] = (h[j + 1] - h[j - 1]) / (t[j + 1] - t[j - 1]);
+    eh[j] = sqrt((H2[o[j]] / (double)n[o[j]]) * 3);
+  }
+  int k = 0;
+  for (int j = 2; j < m - 2; ++j) {
+    const double dT = (t[j + 1] - t[j - 1]) / 2.0;
+    double der = fabs(h[j + 2] / 2.0 - h[j + 1] + h[j - 1] - h[j - 2] / 2.0) / (dT * dT * dT);
+    der *= dT * dT / 6.0;
+    const double est = (eh[j + 1] + eh[j - 1]) / (2.0 * dT);
+    T_out[k] = t[j];
+    cp_out[k] = cp[j];
+    err_out[k] = sqrt(der * der + est * est);
+    ++k;
+  }
+  *m_out = k;
+  return 0;
+}
+
+// KTderivate.c:345-563 (compresibilidad_log, error_compresibilidad_log): for every point, K_T =
+// d ln(rho) / dP along its isotherm (points whose T agrees within 1e-8) from the nearest
+// pressures above and below (one-sided at the ends), with the error from the neighbours' density
+// errors plus a third-derivative term (from the second neighbours when both exist, else from the
+// neighbours' K_T). Points in the gas (rho < 500), alone on their isotherm or next to a gas point
+// get CVF_KT_NOT_VALUE (-10) in both outputs.
+int cvf_kt_derivative(const double* T, const double* P, const double* rho, const double* Erho, int m, double* KT,
+                      double* EKT) {
+  if (!T || !P || !rho || !Erho || !KT || !EKT || m < 0) return iso_fail("null array or negative count");
+  const double kNot = -10.0, kGas = 500;
+  struct Nb {
+    int up = -1, dn = -1, up2 = -1, dn2 = -1;
+    double Pup = 1E12, Pdn = -1E12, Pup2 = 1E12, Pdn2 = -1E12;
+  };
+  std::vector<Nb> nb((size_t)m);
+  for (int j = 0; j < m; ++j) {
+    Nb& b = nb[j];
+    for (int i = 0; i < m; ++i) {
+      if (i == j || !(fabs(T[i] - T[j]) < 1E-8)) continue;
+      if (P[i] > P[j] && P[i] < b.Pup) {
+        b.Pup = P[i];
+        b.up = i;
+      }
+      if (P[i] < P[j] && P[i] > b.Pdn) {
+        b.Pdn = P[i];
+        b.dn = i;
+      }
+    }
+    for (int i = 0; i < m; ++i) {
+      if (i == j || !(fabs(T[i] - T[j]) < 1E-8)) continue;
+      if (P[i] > b.Pup && P[i] < b.Pup2) {
+        b.Pup2 = P[i];
+        b.up2 = i;
+      }
+      if (P[i] < b.Pdn && P[i] > b.Pdn2) {
+        b.Pdn2 = P[i];
+        b.dn2 = i;
+      }
+    }
+  }
+  for (int j = 0; j < m; ++j) {
+    const Nb& b = nb[j];
+    const double d = rho[j], p = P[j];
+    KT[j] = EKT[j] = kNot;
+    if (d < kGas || (b.up == -1 && b.dn == -1)) continue;
+    if (b.up == -1) {
+      if (rho[b.dn] < kGas) continue;
+      KT[j] = (log(d) - log(rho[b.dn])) / (p - b.Pdn);
+      EKT[j] = fabs(Erho[j] / d + Erho[b.dn] / rho[b.dn]) / (p - b.Pdn);
+    } else if (b.dn == -1) {
+      if (rho[b.up] < kGas) continue;
+      KT[j] = (log(rho[b.up]) - log(d)) / (b.Pup - p);
+      EKT[j] = fabs(Erho[j] / d + Erho[b.up] / rho[b.up]) / (b.Pup - p);
+    } else {
+      if (rho[b.up] < kGas || rho[b.dn] < kGas) continue;
+      KT[j] = (log(rho[b.up]) - log(rho[b.dn])) / (b.Pup - b.Pdn);
+      EKT[j] = fabs(Erho[b.dn] / rho[b.dn] + Erho[b.up] / rho[b.up]) / (b.Pup - b.Pdn);
+    }
+  }
+  for (int j = 0; j < m; ++j) {
+    const Nb& b = nb[j];
+    if (KT[j] == kNot || EKT[j] == kNot) continue;
+    double der;
+    if (b.up2 != -1 && b.dn2 != -1) {
+      if (rho[b.up2] < kGas || rho[b.up] < kGas || rho[b.dn2] < kGas || rho[b.dn] < kGas) continue;
+      const double dP2 = (b.Pup2 - b.Pdn2) / 4.0;
+      der = fabs(0.5 * log(rho[b.up2]) - log(rho[b.up]) + log(rho[b.dn]) - 0.5 * log(rho[b.dn2])) / (6.0 * dP2);
+    } else if (b.up != -1 && b.dn != -1) {
+      if (KT[b.up] == kNot || KT[b.dn] == kNot) continue;
+      der = fabs(KT[b.dn] - 2 * KT[j] + KT[b.up]) / (6.0);
+    } else {
+      continue;
+    }
+    EKT[j] = sqrt(EKT[j] * EKT[j] + der * der);
+  }
+  return 0;
+}
+
 }  // extern "C"

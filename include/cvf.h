@@ -276,6 +276,15 @@ int cvf_isobar_point_to_si(const cvf_isobar_point* p, double P, cvf_isobar_point
  * K_T and C_P without finite differences. */
 int cvf_alpha_p_derivative(const double* T, const double* V, const double* V2, const long long* n, int m,
                            double* T_out, double* ap_out, double* err_out, int* m_out);
+/* CPderivate.c:56-124: C_P = dH/dT of one isobar (H = <H>/N, H2 = var(H)/N^2, n samples per
+ * point, any order); writes the points 2 .. m-3 of the T-sorted isobar as the reference does. */
+int cvf_cp_derivative(const double* T, const double* H, const double* H2, const long long* n, int m, double* T_out,
+                      double* cp_out, double* err_out, int* m_out);
+/* KTderivate.c:345-563: K_T = d ln(rho) / dP along isotherms for m points (T in K, P in MPa, rho
+ * and its error in kg/m^3, any order), KT and EKT per point, -10 where the reference gives no
+ * value (gas, rho < 500; a point alone on its isotherm; a gas neighbour). */
+int cvf_kt_derivative(const double* T, const double* P, const double* rho, const double* Erho, int m, double* KT,
+                      double* EKT);
 
 /* Autotuner: times the checkerboard sweep kernel on this handle's replicas for every supported
  * cells-per-thread tile (1, 2, 4 or 8 consecutive colour cells: 32-, 64-, 128- or 2x128-bit accesses) and

@@ -15,9 +15,16 @@ GPU and the library's host functions; nothing in the library calls it.
                  only points 2 .. n-3 are written)
   alpha_p_text   conversor.sh:54-66 as a text pipeline: awk's %.6g output between the stages,
                  AlphaPderivate's "%lf", the x1000 conversion and the nan/inf filter
+  cp_derivative  CPderivate.c:56-124 (as alpha_p without the 1/V factor; error from the third
+                 derivative and the neighbours' sqrt(3 var / n))
+  kt_derivative  KTderivate.c:345-563 (compresibilidad_log, error_compresibilidad_log)
+  kt_text        conversor.sh:84-119 as a text pipeline: the KT_input fields as awk prints them,
+                 KTderivate's per-isobar "%lf %lf %e %lf" lines, the x1000 conversion, sort -g
 
 Pinned by tests/golden/isobars_L32*.txt (the reference's own L32_P*_density.dat,
-L32_P*_density.dat.SI and L32_P*_AlphaPderivate.dat.SI for all 47 isobars).
+L32_P*_density.dat.SI and L32_P*_AlphaPderivate.dat.SI for all 47 isobars, and the 47
+L32_P*_KTderivate.dat.SI files, whose inputs the fixtures hold only to the 6 digits of the
+density files).
 """
 from __future__ import annotations
 
@@ -144,4 +151,118 @@ def alpha_p_text(si_lines, n=1, derivative=alpha_p):
         if as_ in ("-nan", "nan", "inf", "-inf") or es == "inf":
             continue
         out.append((ts, awk_g(float(as_) * 1000), awk_g(float(es) * 1000)))
+    return out
+
+
+def cp_derivative(T, H, H2, n):
+    """CPderivate.c on arrays (any order): the rows (T, C_P, error) it writes."""
+    T, H, H2, n = (np.asarray(a, dtype=np.float64) for a in (T, H, H2, n))
+    o = np.argsort(T, kind="stable")
+    T, H, H2, n = T[o], H[o], H2[o], n[o]
+    m = len(T)
+    if m < 2:
+        return []
+    cp = np.empty(m)
+    eh = np.empty(m)
+    for j in range(m):
+        if j == 0:
+            cp[j] = (H[j + 1] - H[j]) / (T[j + 1] - T[j])
+        elif j == m - 1:
+            cp[j] = (H[j] - H[j - 1]) / (T[j] - T[j - 1])
+        else:
+            cp[j] = (H[j + 1] - H[j - 1]) / (T[j + 1] - T[j - 1])
+        eh[j] = math.sqrt((H2[j] / n[j]) * 3)
+    rows = []
+    for j in range(2, m - 2):
+        dT = (T[j + 1] - T[j - 1]) / 2.0
+        der = abs(H[j + 2] / 2.0 - H[j + 1] + H[j - 1] - H[j - 2] / 2.0) / (dT * dT * dT)
+        der *= dT * dT / 6.0
+        est = (eh[j + 1] + eh[j - 1]) / (2.0 * dT)
+        rows.append((T[j], cp[j], math.sqrt(der * der + est * est)))
+    return rows
+
+
+KT_NOT_VALUE, GAS_DENS = -10.0, 500
+
+
+def kt_derivative(T, P, rho, Erho):
+    """KTderivate.c's K_T and its error for every point (lists), KT_NOT_VALUE where none."""
+    m = len(T)
+
+    def near(j, lo, hi):
+        up = dn = -1
+        Pup, Pdn = 1e12, -1e12
+        for i in range(m):
+            if i == j or not abs(T[i] - T[j]) < 1e-8:
+                continue
+            if P[i] > hi and P[i] < Pup:
+                Pup, up = P[i], i
+            if P[i] < lo and P[i] > Pdn:
+                Pdn, dn = P[i], i
+        return up, dn, Pup, Pdn
+
+    nb = []
+    for j in range(m):
+        up, dn, Pup, Pdn = near(j, P[j], P[j])
+        up2, dn2, Pup2, Pdn2 = near(j, Pdn, Pup)
+        nb.append((up, dn, Pup, Pdn, up2, dn2, Pup2, Pdn2))
+    KT, EKT = [KT_NOT_VALUE] * m, [KT_NOT_VALUE] * m
+    for j in range(m):
+        up, dn, Pup, Pdn = nb[j][:4]
+        d, p = rho[j], P[j]
+        if d < GAS_DENS or (up == -1 and dn == -1):
+            continue
+        if up == -1:
+            if rho[dn] < GAS_DENS:
+                continue
+            KT[j] = (math.log(d) - math.log(rho[dn])) / (p - Pdn)
+            EKT[j] = abs(Erho[j] / d + Erho[dn] / rho[dn]) / (p - Pdn)
+        elif dn == -1:
+            if rho[up] < GAS_DENS:
+                continue
+            KT[j] = (math.log(rho[up]) - math.log(d)) / (Pup - p)
+            EKT[j] = abs(Erho[j] / d + Erho[up] / rho[up]) / (Pup - p)
+        else:
+            if rho[up] < GAS_DENS or rho[dn] < GAS_DENS:
+                continue
+            KT[j] = (math.log(rho[up]) - math.log(rho[dn])) / (Pup - Pdn)
+            EKT[j] = abs(Erho[dn] / rho[dn] + Erho[up] / rho[up]) / (Pup - Pdn)
+    for j in range(m):
+        up, dn, Pup, Pdn, up2, dn2, Pup2, Pdn2 = nb[j]
+        if KT[j] == KT_NOT_VALUE or EKT[j] == KT_NOT_VALUE:
+            continue
+        if up2 != -1 and dn2 != -1:
+            if min(rho[up2], rho[up], rho[dn2], rho[dn]) < GAS_DENS:
+                continue
+            dP2 = (Pup2 - Pdn2) / 4.0
+            der = abs(0.5 * math.log(rho[up2]) - math.log(rho[up]) + math.log(rho[dn]) - 0.5 * math.log(rho[dn2])) / (6.0 * dP2)
+        elif up != -1 and dn != -1:
+            if KT[up] == KT_NOT_VALUE or KT[dn] == KT_NOT_VALUE:
+                continue
+            der = abs(KT[dn] - 2 * KT[j] + KT[up]) / 6.0
+        else:
+            continue
+        EKT[j] = math.sqrt(EKT[j] * EKT[j] + der * der)
+    return KT, EKT
+
+
+def kt_text(points, isobars, derivative=kt_derivative):
+    """conversor.sh:84-119 on the KT_input points [(T_K, P_MPa, rho, err) as the awk text] and the
+    isobar list (MPa, as awk prints it): {isobar name "%lf": printed lines (T, K_T, error, P)}."""
+    T = [float(t) for t, _, _, _ in points]
+    P = [float(p) for _, p, _, _ in points]
+    rho = [float(r) for _, _, r, _ in points]
+    err = [float(e) for _, _, _, e in points]
+    KT, EKT = derivative(T, P, rho, err)
+    out = {}
+    for iso in isobars:
+        pv = float(iso)
+        lines = []
+        for k in range(len(points)):
+            if KT[k] == KT_NOT_VALUE or not abs(P[k] - pv) < 1e-5:
+                continue
+            t, kt, ekt, p = "%f" % T[k], "%f" % KT[k], "%e" % EKT[k], "%f" % P[k]
+            lines.append((t, awk_g(float(kt) * 1000), awk_g(float(ekt) * 1000), p))
+        lines.sort(key=lambda r: (float(r[0]), r))  # sort -g
+        out["%f" % pv] = lines
     return out

@@ -19,6 +19,8 @@ to what the tests need:
   isobars_L32_si.txt        P T_K rho_SI err_SI (L32_P*_density.dat.SI, conversor.sh:20)
   isobars_L32_alphap_si.txt P T_K alpha_P err (L32_P*_AlphaPderivate.dat.SI, conversor.sh:54-66
                             with AlphaPderivate.c), the printed text kept as it is
+  isobars_L32_kt_si.txt     P_MPa T_K K_T err P_MPa (L32_P*_KTderivate.dat.SI, conversor.sh:84-119
+                            with KTderivate.c, isobars named by their pressure in MPa), as printed
   correlator_ref.json       the reference's own multi-tau correlator (initialize/add/evaluate of
                             SOURCE/gpu_water3D.cu, built by oracle/build_ref.py) on a seeded
                             random walk of 20000 values: the evaluated (t, f), as hex floats
@@ -67,7 +69,7 @@ def main(ref: str):
         data = t.extractfile(m).read().decode()
     open(os.path.join(HERE, "isobar_P0.45_density.txt"), "w").write(data)
     kinds = [("density.dat", "isobars_L32.txt"), ("density.dat.SI", "isobars_L32_si.txt"),
-             ("AlphaPderivate.dat.SI", "isobars_L32_alphap_si.txt")]
+             ("AlphaPderivate.dat.SI", "isobars_L32_alphap_si.txt"), ("KTderivate.dat.SI", "isobars_L32_kt_si.txt")]
     with tarfile.open(os.path.join(ref, "PROCESSED_DATA", "CVF_isobars.tar.gz")) as t:
         names = t.getnames()
         for suffix, out in kinds:

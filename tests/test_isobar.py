@@ -134,3 +134,72 @@ def test_run_stats_oracle_formula():
     assert n == 3
     assert np.allclose(mean, x.mean(0)) and np.allclose(var, x.var(0))
     assert math.isclose(var[0], (1 + 4 + 16) / 3 - (7 / 3) ** 2)
+
+
+def kt_points(golden_si):
+    """The KT_input points rebuilt from the density.dat.SI fixture (conversor.sh:94 prints T, P in
+    MPa, rho, err with awk's %.6g; the reference built them from full-precision run averages, the
+    fixture holds the 6-digit densities) and the isobar list in MPa (conversor.sh:96-100)."""
+    pts, isobars = [], []
+    for P, rows in golden_si.items():
+        p = I.awk_g(float(P) * I.PS + I.PI)
+        isobars.append(p)
+        for t, rho, err in rows:
+            pts.append((t, p, rho, err))
+    return pts, isobars
+
+
+@pytest.fixture(scope="module")
+def kt_golden():
+    out = collections.OrderedDict()
+    for line in open(os.path.join(GOLD, "isobars_L32_kt_si.txt")):
+        f = line.split()
+        out.setdefault(f[0], []).append(tuple(f[1:]))
+    return out
+
+
+def test_oracle_kt_matches_reference(golden, kt_golden):
+    pts, isobars = kt_points(golden[1])
+    got = I.kt_text(pts, isobars)
+    assert set(kt_golden) <= set(got)
+    n = exact = 0
+    for name, want in kt_golden.items():
+        mine = got[name]
+        assert len(mine) == len(want), name
+        for a, b in zip(want, mine):
+            n += 1
+            assert a[0] == b[0] and a[3] == b[3]  # T and P as KTderivate prints them
+            # K_T to the printed digit; the 6-digit densities of the fixture move the last digit of
+            # 24 of the 1614 values and the third-derivative part of the error by up to 5.5 %
+            assert abs(float(a[1]) - float(b[1])) <= 0.0010001
+            assert abs(float(a[2]) - float(b[2])) <= 0.06 * float(a[2])
+            exact += a[1] == b[1]
+    assert n == 1614 and exact >= 1590
+
+
+def test_library_kt_equals_oracle(golden, ana):
+    pts, _ = kt_points(golden[1])
+    T, P, rho, err = (np.array([float(p[k]) for p in pts]) for k in range(4))
+    kt, ekt = ana.kt_derivative(T, P, rho, err)
+    kto, ekto = I.kt_derivative(list(T), list(P), list(rho), list(err))
+    assert np.array_equal(kt, np.array(kto)) and np.array_equal(ekt, np.array(ekto))
+    # gas points and single-point isotherms give no value
+    kt, ekt = ana.kt_derivative([300.0, 300.0, 310.0], [0.1, 10.0, 0.1], [400.0, 990.0, 995.0], [1.0, 1.0, 1.0])
+    assert list(kt) == [ana.KT_NOT_VALUE] * 3 and list(ekt) == [ana.KT_NOT_VALUE] * 3
+
+
+def test_library_cp_equals_oracle(ana):
+    rng = np.random.default_rng(4)
+    T = rng.permutation(np.linspace(0.3, 1.2, 19))
+    H = -2.0 + 1.7 * T + 0.05 * np.sin(7 * T)
+    H2 = rng.uniform(1e-4, 1e-3, 19)
+    n = rng.integers(1000, 5000, 19)
+    got = ana.cp_derivative(T, H, H2, n)
+    want = I.cp_derivative(T, H, H2, n)
+    assert len(got[0]) == len(want) == 15
+    for k, (t, cp, e) in enumerate(want):
+        assert (got[0][k], got[1][k], got[2][k]) == (t, cp, e)
+    # linear enthalpy: the central difference is the slope
+    Tl = np.linspace(0.5, 1.0, 11)
+    _, cp, _ = ana.cp_derivative(Tl, 3.0 * Tl, np.full(11, 1e-4), np.full(11, 100))
+    assert np.allclose(cp, 3.0, rtol=1e-12)
