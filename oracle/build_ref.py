@@ -1,9 +1,16 @@
-"""Build recipe for oracle/_ref/ (test infrastructure only): the reference's own multi-tau
-correlator, compiled from SOURCE/gpu_water3D.cu and SOURCE/mersenne_inline.cu where they lie in
-the reference checkout (main renamed, nothing else changed), linked with oracle/ref_correlator.cpp, which calls its
-initialize / add / evaluate. Run where the reference checkout exists (argument: its path);
-elsewhere the tests that need the library skip. Nothing from the reference is copied into the
-repository; the output stays in the git-ignored oracle/_ref/.
+"""Build recipe for oracle/_ref/ (test infrastructure only):
+
+  libref_correlator.so  the reference's own multi-tau correlator, compiled from
+                        SOURCE/gpu_water3D.cu and SOURCE/mersenne_inline.cu where they lie in the
+                        reference checkout (main renamed, nothing else changed), linked with
+                        oracle/ref_correlator.cpp, which calls its initialize / add / evaluate;
+  AlphaPderivate, CPderivate, KTderivate
+                        the reference's finite-difference programs of
+                        CVF_ThermodynamicAnalysis/*.c, compiled as they are with gcc (tools()).
+
+Run where the reference checkout exists (argument: its path); elsewhere the tests that need
+them skip. Nothing from the reference is copied into the repository; the output stays in the
+git-ignored oracle/_ref/.
 """
 from __future__ import annotations
 
@@ -39,5 +46,28 @@ def build(ref: str = "/root/reference", force: bool = False):
     return LIB
 
 
+TOOLS = ("AlphaPderivate", "CPderivate", "KTderivate")
+
+
+def tools(ref: str = "/root/reference"):
+    """{name: path} of the three analysis programs, built from the reference's own .c files with
+    gcc -O2 (empty where the checkout is absent)."""
+    src_dir = os.path.join(ref, "CVF_ThermodynamicAnalysis")
+    out = {}
+    for name in TOOLS:
+        src = os.path.join(src_dir, name + ".c")
+        if not os.path.exists(src):
+            return {}
+        exe = os.path.join(OUT, name)
+        if not os.path.exists(exe) or os.path.getmtime(exe) < os.path.getmtime(src):
+            os.makedirs(OUT, exist_ok=True)
+            tmp = exe + f".tmp{os.getpid()}"
+            subprocess.run(["gcc", "-O2", "-w", "-o", tmp, src, "-lm"], check=True)
+            os.replace(tmp, exe)
+        out[name] = exe
+    return out
+
+
 if __name__ == "__main__":
     print(build(*(sys.argv[1:2])))
+    print(tools(*(sys.argv[1:2])))

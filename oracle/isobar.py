@@ -24,7 +24,8 @@ GPU and the library's host functions; nothing in the library calls it.
 Pinned by tests/golden/isobars_L32*.txt (the reference's own L32_P*_density.dat,
 L32_P*_density.dat.SI and L32_P*_AlphaPderivate.dat.SI for all 47 isobars, and the 47
 L32_P*_KTderivate.dat.SI files, whose inputs the fixtures hold only to the 6 digits of the
-density files).
+density files), and where the reference checkout exists by its AlphaPderivate, CPderivate and
+KTderivate programs compiled from their .c files (oracle/build_ref.py), output for output.
 """
 from __future__ import annotations
 
@@ -246,9 +247,9 @@ def kt_derivative(T, P, rho, Erho):
     return KT, EKT
 
 
-def kt_text(points, isobars, derivative=kt_derivative):
-    """conversor.sh:84-119 on the KT_input points [(T_K, P_MPa, rho, err) as the awk text] and the
-    isobar list (MPa, as awk prints it): {isobar name "%lf": printed lines (T, K_T, error, P)}."""
+def kt_files(points, isobars, derivative=kt_derivative):
+    """KTderivate.c:77-123 on the KT_input points [(T_K, P_MPa, rho, err) as text] and the isobar
+    list (MPa, as text): {"%lf" of the isobar: the lines it writes to P%lf_KTderivate.dat}."""
     T = [float(t) for t, _, _, _ in points]
     P = [float(p) for _, p, _, _ in points]
     rho = [float(r) for _, _, r, _ in points]
@@ -257,12 +258,20 @@ def kt_text(points, isobars, derivative=kt_derivative):
     out = {}
     for iso in isobars:
         pv = float(iso)
-        lines = []
-        for k in range(len(points)):
-            if KT[k] == KT_NOT_VALUE or not abs(P[k] - pv) < 1e-5:
-                continue
-            t, kt, ekt, p = "%f" % T[k], "%f" % KT[k], "%e" % EKT[k], "%f" % P[k]
-            lines.append((t, awk_g(float(kt) * 1000), awk_g(float(ekt) * 1000), p))
-        lines.sort(key=lambda r: (float(r[0]), r))  # sort -g
-        out["%f" % pv] = lines
+        out["%f" % pv] = ["%f %f %e %f" % (T[k], KT[k], EKT[k], P[k]) for k in range(len(points))
+                          if KT[k] != KT_NOT_VALUE and abs(P[k] - pv) < 1e-5]
+    return out
+
+
+def kt_text(points, isobars, derivative=kt_derivative):
+    """conversor.sh:84-119: the KTderivate files of kt_files after awk '{print $1, $2*1000,
+    $3*1000, $4}' and sort -g: {isobar "%lf": [(T, K_T, error, P) as printed]}."""
+    out = {}
+    for name, lines in kt_files(points, isobars, derivative).items():
+        rows = []
+        for line in lines:
+            t, kt, ekt, p = line.split()
+            rows.append((t, awk_g(float(kt) * 1000), awk_g(float(ekt) * 1000), p))
+        rows.sort(key=lambda r: (float(r[0]), r))  # sort -g
+        out[name] = rows
     return out

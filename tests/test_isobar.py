@@ -203,3 +203,71 @@ def test_library_cp_equals_oracle(ana):
     Tl = np.linspace(0.5, 1.0, 11)
     _, cp, _ = ana.cp_derivative(Tl, 3.0 * Tl, np.full(11, 1e-4), np.full(11, 100))
     assert np.allclose(cp, 3.0, rtol=1e-12)
+
+
+@pytest.fixture(scope="module")
+def ref_tools():
+    from oracle import build_ref
+    t = build_ref.tools()
+    if not t:
+        pytest.skip("the reference checkout is not here to build its analysis programs")
+    return t
+
+
+def run_tool(exe, cwd, files):
+    import subprocess
+    for name, text in files.items():
+        open(os.path.join(cwd, name), "w").write(text)
+    subprocess.run([exe], cwd=cwd, check=True, capture_output=True, timeout=120)
+
+
+def synthetic_kt_points(seed=1):
+    """Isotherms of 2 to 9 points, some in the gas (rho < 500), one isotherm of a single point."""
+    rng = np.random.default_rng(seed)
+    pts = []
+    for t in np.round(np.linspace(190.0, 260.0, 12), 3):
+        k = int(rng.integers(2, 10))
+        for p in np.sort(rng.choice(np.round(np.linspace(-300, 300, 25), 3), k, replace=False)):
+            rho = 900 + 0.2 * p - 0.5 * (t - 220) + rng.normal(0, 2) if rng.random() > 0.1 else 300.0
+            pts.append((I.awk_g(t), I.awk_g(p), I.awk_g(rho), I.awk_g(abs(rng.normal(0.3, 0.1)))))
+    pts.append(("300.5", "0", "950", "0.2"))
+    return pts
+
+
+def test_reference_kt_program_equals_oracle(golden, ref_tools, tmp_path):
+    """KTderivate.c built from the reference's source, on the points rebuilt from the fixture and
+    on synthetic isotherms with gas points: every P*_KTderivate.dat line the oracle's, text for text."""
+    for pts, isobars in [kt_points(golden[1]), (synthetic_kt_points(), None)]:
+        if isobars is None:
+            isobars = sorted({p for _, p, _, _ in pts}, key=float)
+        d = tmp_path / ("kt%d" % len(pts))
+        d.mkdir()
+        run_tool(ref_tools["KTderivate"], d, {
+            "KT_input": "".join(" ".join(p) + "\n" for p in pts),
+            "KT_list_isobars": "".join(p + "\n" for p in isobars),
+            "KT_list_isotherms": "300.5\n"})
+        want = I.kt_files(pts, isobars)
+        for name, lines in want.items():
+            got = open(d / f"P{name}_KTderivate.dat").read().splitlines()
+            assert got == lines, name
+
+
+def test_reference_cp_and_alpha_programs_equal_oracle(ref_tools, tmp_path):
+    rng = np.random.default_rng(8)
+    T = rng.permutation(np.round(np.linspace(0.3, 1.2, 19), 4))
+    H = -2.0 + 1.7 * T + 0.05 * np.sin(7 * T)
+    V = 1.2 + 0.1 * T - 0.02 * np.cos(5 * T)
+    H2, V2 = rng.uniform(1e-4, 1e-3, 19), rng.uniform(1e-5, 1e-4, 19)
+    n = rng.integers(1000, 5000, 19)
+    rows = lambda X, X2: "".join("%s %s %s %d\n" % (I.awk_g(t), I.awk_g(x), I.awk_g(x2), k)  # noqa: E731
+                                  for t, x, x2, k in zip(T, X, X2, n))
+    for tool, inp, outf, fn, X, X2 in [("CPderivate", "CP_input", "CP_derivate.out", I.cp_derivative, H, H2),
+                                       ("AlphaPderivate", "AlphaP_input", "AlphaP_derivate.out", I.alpha_p, V, V2)]:
+        d = tmp_path / tool
+        d.mkdir()
+        text = rows(X, X2)
+        run_tool(ref_tools[tool], d, {inp: text})
+        vals = [line.split() for line in text.splitlines()]
+        cols = [np.array([float(v[c]) for v in vals]) for c in range(4)]
+        want = ["%f %f %f" % r for r in fn(*cols)]
+        assert open(d / outf).read().splitlines() == want, tool
