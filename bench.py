@@ -378,8 +378,9 @@ def run_engine(args):
            "h2d_bytes_per_step": int(round(packed / args.steps)),
            "d2h_bytes_per_step": int(round(packed / args.steps)) + 32,
            "note": "per step: cvf_run_steps(1 step) + cvf_observables (measurement, 32 B D2H, sync); "
-                   "lattice upload (cvf_set_config from the caller's cells12 array, packed on the host "
-                   "into pinned memory) and download (cvf_get_config) amortised over the K steps"}
+                   "lattice upload (cvf_set_config: the caller's 805 MB cells12 array read and packed "
+                   "by the GPU in host memory, io_mode 1) and download (cvf_get_config: unpacked by the "
+                   "GPU into the caller's array) amortised over the K steps"}
     del out_cfg
     # the drop-in driver's production loop: one sampled run call recording a sample after every
     # step on the device, the K records read back afterwards
