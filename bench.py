@@ -227,6 +227,128 @@ def bench_batch64(steps, warmup, local, flush, verify=4):
             "l2": "256 MB write before every timed step in both arms"}
 
 
+def sample_columns(lat, smp, r=0):
+    """E, V and N_hb of every record from the sample fields, vectorised with the engine's own
+    formulas (GW:2014-2160; E_vdW summed over the shells in their order, each operation rounded
+    as in the library)."""
+    d, f = lat.get_distances(r)
+    Rc = float(np.float32(6.0))
+    rr = smp["r_cell"].astype(np.float64)
+    t = 1.0 / Rc
+    t = t * t * t
+    att = t * t
+    shift = att * att - att
+    ev = np.zeros_like(rr)
+    for di, fi in zip(d.astype(np.float64), f.astype(np.float64)):
+        rd = rr * di
+        m = rd < Rc
+        tmp = np.where(m, 1.0 / np.where(m, rd, 1.0), 0.0)
+        tmp = tmp * tmp * tmp
+        a = tmp * tmp
+        ev = np.where(m, ev + fi * ((a * a - a) - shift), ev)
+    nhb = smp["n_hb2"].astype(np.float64) * 0.5
+    e = (ev + (-float(np.float32(0.5))) * nhb) + (-float(np.float32(0.08))) * smp["n_sigma"].astype(np.float64)
+    v = smp["volume"].astype(np.float64) + float(np.float32(0.6)) * nhb
+    return e, v, nhb
+
+
+def bench_differentiation(local):
+    """Differentiable reweighting (survey config 5): 32 replicas of L=32 along P=0.45 at T uniform
+    in [0.60, 0.90], 100,000 recorded steps each (3.2 M samples); FP64 WHAM forward and adjoint;
+    alpha_P, K_T, C_P at T = 0.75 from the adjoint against finite differences and the fluctuation
+    formulas; the reweighted density against the reference's L32 P=0.45 isobar."""
+    import ctypes as C
+    from cvfbulkwater_gb300 import abi
+    from cvfbulkwater_gb300.engine import Lattice, Params
+    L, N, P0, R, K = 32, 32 ** 3, 0.45, 32, 100000
+    temps = np.linspace(0.60, 0.90, R)
+    lat = Lattice([Params(L=L, T=float(t), P=P0, seed=SEED + 500 + i, start=0, replica=i, device=local,
+                          sample_capacity=K) for i, t in enumerate(temps)])
+    lat.run(3000, 1, 0)
+    lat.synchronize()
+    t0 = time.perf_counter()
+    lat.run_sampled(K, 1, 0, 1)
+    lat.synchronize()
+    t_sample = time.perf_counter() - t0
+    cols, run_of = [], []
+    for r in range(R):
+        smp = lat.samples(r)
+        e, v, nhb = sample_columns(lat, smp, r)
+        cols.append(np.stack([e, v, nhb, smp["n_sigma"].astype(np.float64)], axis=1))
+        run_of.append(np.full(len(smp), r, dtype=np.int32))
+    lat.close()
+    s = np.ascontiguousarray(np.concatenate(cols))
+    ro = np.ascontiguousarray(np.concatenate(run_of))
+    runs = np.ascontiguousarray([[1.0 / float(np.float32(t)), float(np.float32(P0))] for t in temps])
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    ids = {"E": 0, "V": 1, "NHB": 2, "NSIG": 3, "H": 4, "RHO": 5, "H2": 6, "V2": 7, "VH": 8}
+
+    def forward(theta, obs, f, n_iter):
+        o = np.ascontiguousarray([ids[k] for k in obs], dtype=np.int32)
+        out = np.zeros(len(obs) + 1)
+        th = np.ascontiguousarray(theta, dtype=np.float64)
+        abi.check(abi.lib().cvf_reweight_forward(local, ptr(s), ptr(ro), len(s), ptr(runs), R, ptr(f), n_iter, 1e-10,
+                                                 float(N), ptr(th), ptr(o), len(obs), ptr(out)))
+        return out[:-1]
+
+    def adjoint(theta, obs, f, g):
+        o = np.ascontiguousarray([ids[k] for k in obs], dtype=np.int32)
+        th = np.ascontiguousarray(theta, dtype=np.float64)
+        gg = np.ascontiguousarray(g, dtype=np.float64)
+        out = np.zeros(5)
+        abi.check(abi.lib().cvf_reweight_adjoint(local, ptr(s), ptr(ro), len(s), ptr(runs), R, ptr(f), float(N),
+                                                 ptr(th), ptr(o), len(obs), ptr(gg), ptr(out)))
+        return out
+
+    P = float(np.float32(P0))
+    th = lambda t, p=P: [1.0 / t, p, 0.0, 0.0, 0.0]  # noqa: E731
+    f = np.zeros(R)
+    n_it = 200
+    t0 = time.perf_counter()
+    forward(th(0.75), ["V"], f, n_it)
+    t_wham = time.perf_counter() - t0
+    f_next = f.copy()
+    forward(th(0.75), ["V"], f_next, 1)
+    wham_change = float(np.max(np.abs(f_next - f)))
+    t0 = time.perf_counter()
+    V, H, V2, H2, VH = forward(th(0.75), ["V", "H", "V2", "H2", "VH"], f, 0)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    gV = adjoint(th(0.75), ["V"], f, [1.0])
+    t_adj = time.perf_counter() - t0
+    gH = adjoint(th(0.75), ["H"], f, [1.0])
+    t = 0.75
+    ap_adj = -gV[0] / (t * t) / V  # d/dT = -beta^2 d/dbeta
+    kt_adj = -gV[1] / V
+    cp_adj = -gH[0] / (t * t) / N
+    vp, vm = forward(th(0.755), ["V"], f, 0)[0], forward(th(0.745), ["V"], f, 0)[0]
+    hp, hm = forward(th(0.755), ["H"], f, 0)[0], forward(th(0.745), ["H"], f, 0)[0]
+    vpp, vpm = forward(th(0.75, P + 0.005), ["V"], f, 0)[0], forward(th(0.75, P - 0.005), ["V"], f, 0)[0]
+    gold = {round(a, 3): (b, c) for a, b, c in np.loadtxt(os.path.join(ROOT, "tests", "golden", "isobar_P0.45_density.txt"))}
+    cmp = []
+    for tt in sorted(k for k in gold if 0.6 <= k <= 0.9):
+        rho = forward(th(tt), ["RHO"], f, 0)[0]
+        want, err = gold[tt]
+        cmp.append([tt, round(float(rho), 6), want, round(float((rho - want) / err), 2)])
+    return {"workload": f"{R} replicas, L={L}, P=0.45, T uniform in [0.60, 0.90], {K} recorded steps each "
+                        f"({len(s)} samples, {len(s) * 32 / 1e6:.0f} MB of records on the device)",
+            "sampling_s": round(t_sample, 3),
+            "sampling_site_updates_per_ns": round(R * N * K / t_sample / 1e9, 2),
+            "wham_ms_per_iteration": round(t_wham / n_it * 1e3, 3),
+            "wham_last_change": wham_change,
+            "fp64_exp_per_s_in_wham": round(len(s) * R * n_it / t_wham / 1e9, 2),
+            "forward_ms": round(t_fwd * 1e3, 3), "adjoint_ms": round(t_adj * 1e3, 3),
+            "response_T0.75": {
+                "alpha_P": {"adjoint": ap_adj, "finite_difference": (vp - vm) / 0.01 / V,
+                            "fluctuation": (VH - V * H) / (t * t * V)},
+                "K_T": {"adjoint": kt_adj, "finite_difference": -(vpp - vpm) / 0.01 / V,
+                        "fluctuation": (V2 - V * V) / (t * V)},
+                "C_P": {"adjoint": cp_adj, "finite_difference": (hp - hm) / 0.01 / N,
+                        "fluctuation": (H2 - H * H) / (t * t * N)}},
+            "rho_vs_reference_isobar": {"columns": ["T", "reweighted", "reference", "(rw - ref) / ref_err"],
+                                        "rows": cmp}}
+
+
 def bench_plain_l16(steps, warmup, local, flush):
     """Plain small run: L=16, disordered start, T=0.815, P=0.45, 1 sweep + volume + cube per step.
     Launch-latency bound, so the per-step time inside a 32-step graph replay is reported too."""
@@ -245,9 +367,26 @@ def bench_plain_l16(steps, warmup, local, flush):
     torch.cuda.synchronize()
     replay_us = e0.elapsed_time(e1) * 1e3 / 640
     lat.close()
+    # the survey's protocol: 1000 equilibration + 10000 sampling steps, a record every 10
+    lat = Lattice(Params(L=16, T=0.815, P=0.45, seed=SEED, start=0, device=local))
+    t0 = time.perf_counter()
+    lat.run(1000, 1, 0)
+    lat.run_sampled(10000, 1, 0, 10)
+    smp = lat.samples()
+    wall = time.perf_counter() - t0
+    e, v, nhb = sample_columns(lat, smp)
+    lat.close()
+
+    def mean_err(x):
+        b = x[: len(x) // 20 * 20].reshape(20, -1).mean(1)
+        return [round(float(x.mean()), 6), round(float(b.std(ddof=1) / np.sqrt(20)), 6)]
     return {"workload": "L=16 disordered start, T=0.815, P=0.45, 1 cube + 1 volume move + 1 sweep per step",
             "steps_per_s": round(steps / (ms / 1e3), 1), "site_updates_per_ns": round(4096 * steps / (ms * 1e6), 4),
-            "graph_replay_us_per_step": round(replay_us, 3)}
+            "graph_replay_us_per_step": round(replay_us, 3),
+            "sampled_run": {"steps": 11000, "records": int(len(smp)), "wall_s": round(wall, 3),
+                            "per_cell_mean_and_20_block_error": {
+                                "E": mean_err(e / 4096), "V": mean_err(v / 4096), "rho": mean_err(4096 / v),
+                                "N_hb": mean_err(nhb / 4096)}}}
 
 
 def bench_sw(steps, warmup, local, flush):
@@ -264,6 +403,8 @@ def bench_sw(steps, warmup, local, flush):
             cs = lat.cluster_stats()
             out.append({"L": L, "T": T, "sw_steps_per_s": round(steps / (ms / 1e3), 1),
                         "site_updates_per_ns": round(L ** 3 * steps / (ms * 1e6), 4),
+                        "labelling_passes_per_step": 1,
+                        "algorithmic_GBps": round(68 * L ** 3 * steps / (ms / 1e3) / 1e9, 1),
                         "largest_cluster": int(cs.largest), "n_clusters": int(cs.n_clusters)})
             lat.close()
     return out
@@ -402,6 +543,7 @@ def run_engine(args):
         extras["batched"] = bench_batch64(max(10, min(args.steps, 50)), args.warmup, local, flush)
         extras["swendsen_wang"] = bench_sw(max(10, min(args.steps, 30)), args.warmup, local, flush)
         extras["plain_l16"] = bench_plain_l16(max(10, min(args.steps, 50)), args.warmup, local, flush)
+        extras["differentiation"] = bench_differentiation(local)
         if not args.no_cpu_baseline:
             extras["cpu_baseline_1thread"] = cpu_baseline_oracle(steps_cap=1, budget_s=10.0, threads=1)
 

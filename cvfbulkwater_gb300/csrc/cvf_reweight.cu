@@ -11,8 +11,11 @@
 // The adjoint returns sum_m g_m d<A_m>/d theta = <g.dA> + <s dlogw> - <s><dlogw>, s = g.A.
 #include <cuda_runtime.h>
 #include <math.h>
+
+#include <cmath>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -73,6 +76,53 @@ __global__ void __launch_bounds__(kRwThreads) k_rw_logD(const double* __restrict
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nr; i += blockDim.x) atomicAdd(&s_out[i], s_acc[i]);
+}
+
+// The same sums in log space, for runs whose sum underflowed: pass 0 takes every run's maximum
+// of a_ik = f_i - beta_i H_i(k) - log D_k into mx (order bits), pass 1 adds exp(a_ik - max_i).
+__global__ void __launch_bounds__(kRwThreads) k_rw_runlse(const double* __restrict__ samp, long long n,
+                                                          const double* __restrict__ runs,
+                                                          const double* __restrict__ f, int nr,
+                                                          const double* __restrict__ logD, int pass,
+                                                          unsigned long long* __restrict__ mx,
+                                                          double* __restrict__ s_out) {
+  __shared__ double s_b[kRwMaxRuns], s_p[kRwMaxRuns], s_f[kRwMaxRuns], s_m[kRwMaxRuns], s_acc[kRwMaxRuns];
+  __shared__ unsigned long long s_mx[kRwMaxRuns];
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+    s_b[i] = runs[2 * i];
+    s_p[i] = runs[2 * i + 1];
+    s_f[i] = f[i];
+    s_mx[i] = 0ull;
+    s_acc[i] = 0.0;
+    if (pass == 1) {
+      const unsigned long long b = mx[i];
+      s_m[i] = __longlong_as_double((long long)((b >> 63) ? (b & 0x7fffffffffffffffull) : ~b));
+    }
+  }
+  __syncthreads();
+  for (long long k0 = (long long)blockIdx.x * blockDim.x; k0 < n; k0 += (long long)gridDim.x * blockDim.x) {
+    const long long k = k0 + threadIdx.x;
+    const bool ok = k < n;
+    const double E = ok ? samp[4 * k] : 0.0, V = ok ? samp[4 * k + 1] : 0.0, ld = ok ? logD[k] : 0.0;
+    for (int i = 0; i < nr; ++i) {
+      const double a = s_f[i] - s_b[i] * (E + s_p[i] * V) - ld;
+      if (pass == 0) {
+        double m = ok ? a : -INFINITY;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if ((threadIdx.x & 31) == 0) atomicMax(&s_mx[i], order_bits(m));
+      } else {
+        double u = ok ? exp(a - s_m[i]) : 0.0;
+        u = warp_sum(u);
+        if ((threadIdx.x & 31) == 0) atomicAdd(&s_acc[i], u);
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+    if (pass == 0) atomicMax(&mx[i], s_mx[i]);
+    else atomicAdd(&s_out[i], s_acc[i]);
+  }
 }
 
 struct Target {
@@ -245,7 +295,7 @@ int rw_fail(int code, const std::string& m) {
   } while (0)
 
 struct RwSetup {
-  DevBuf samp, logD, runs, logn, f, acc, mx, ids, g;
+  DevBuf samp, logD, runs, logn, f, acc, mx, ids, g, runmx;
   long long n;
   int nr, grid;
 };
@@ -280,6 +330,7 @@ int rw_prepare(RwSetup& S, int device, const double* samples, const int* run_of,
   RWCK(cudaMalloc(&S.logn.p, (size_t)n_runs * sizeof(double)));
   RWCK(cudaMalloc(&S.f.p, (size_t)n_runs * sizeof(double)));
   RWCK(cudaMalloc(&S.acc.p, (size_t)(kRwMaxRuns + 32) * sizeof(double)));
+  RWCK(cudaMalloc(&S.runmx.p, (size_t)kRwMaxRuns * sizeof(unsigned long long)));
   RWCK(cudaMalloc(&S.mx.p, sizeof(unsigned long long)));
   RWCK(cudaMalloc(&S.ids.p, kRwMaxObs * sizeof(int)));
   RWCK(cudaMalloc(&S.g.p, kRwMaxObs * sizeof(double)));
@@ -299,16 +350,43 @@ int rw_pass(RwSetup& S, double* f_host, bool update, double* max_change) {
                                      (double*)S.acc.p);
   RWCK(cudaGetLastError());
   if (!update) return 0;
-  std::vector<double> s(S.nr);
+  std::vector<double> s(S.nr), logs(S.nr);
   RWCK(cudaMemcpy(s.data(), S.acc.p, S.nr * sizeof(double), cudaMemcpyDeviceToHost));
+  bool under = false;
+  for (int i = 0; i < S.nr; ++i) {
+    under = under || !(s[i] > 0.0) || !std::isfinite(s[i]);
+    logs[i] = log(s[i]);
+  }
+  if (under) {
+    // a run far from every sample (free energies still far from converged): the same sums in
+    // log space, max_i + log sum_k exp(a_ik - max_i)
+    RWCK(cudaMemset(S.runmx.p, 0, S.nr * sizeof(unsigned long long)));
+    RWCK(cudaMemset(S.acc.p, 0, S.nr * sizeof(double)));
+    for (int pass = 0; pass < 2; ++pass)
+      k_rw_runlse<<<S.grid, kRwThreads>>>((const double*)S.samp.p, S.n, (const double*)S.runs.p,
+                                           (const double*)S.f.p, S.nr, (const double*)S.logD.p, pass,
+                                           (unsigned long long*)S.runmx.p, (double*)S.acc.p);
+    RWCK(cudaGetLastError());
+    std::vector<unsigned long long> mb(S.nr);
+    RWCK(cudaMemcpy(mb.data(), S.runmx.p, S.nr * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    RWCK(cudaMemcpy(s.data(), S.acc.p, S.nr * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < S.nr; ++i) {
+      const unsigned long long raw = (mb[i] >> 63) ? (mb[i] & 0x7fffffffffffffffull) : ~mb[i];
+      double m;
+      memcpy(&m, &raw, 8);
+      logs[i] = m + log(s[i]);
+    }
+  }
   std::vector<double> nf(S.nr);
-  for (int i = 0; i < S.nr; ++i) nf[i] = f_host[i] - log(s[i]);
+  for (int i = 0; i < S.nr; ++i) nf[i] = f_host[i] - logs[i];
   double c = nf[0], mc = 0.0;
   for (int i = 0; i < S.nr; ++i) {
     nf[i] -= c;
-    mc = fmax(mc, fabs(nf[i] - f_host[i]));
+    const double d = fabs(nf[i] - f_host[i]);
+    mc = d > mc || d != d ? d : mc;  // a NaN change never reads as converged
     f_host[i] = nf[i];
   }
+  if (!std::isfinite(mc)) return rw_fail(CVF_ELIMIT, "reweight: the free energies are not finite");
   *max_change = mc;
   RWCK(cudaMemcpy(S.f.p, f_host, S.nr * sizeof(double), cudaMemcpyHostToDevice));
   return 0;
@@ -348,11 +426,55 @@ double host_max(RwSetup& S) {
 }
 }  // namespace
 
+// Starting free energies when the caller gives none (all zero): thermodynamic integration of
+// d f = <E> d beta + <V> d(beta P) between consecutive runs in (beta, beta P) order, trapezoids
+// of the runs' own means, made relative to run 0. WHAM then refines them.
+static void ti_start(const double* samples, const int* run_of, long long n, const double* runs, int nr, double* f) {
+  std::vector<double> se(nr, 0.0), sv(nr, 0.0);
+  std::vector<long long> c(nr, 0);
+  for (long long k = 0; k < n; ++k) {
+    se[run_of[k]] += samples[4 * k];
+    sv[run_of[k]] += samples[4 * k + 1];
+    c[run_of[k]]++;
+  }
+  std::vector<int> o(nr);
+  for (int i = 0; i < nr; ++i) {
+    o[i] = i;
+    se[i] /= (double)c[i];
+    sv[i] /= (double)c[i];
+  }
+  std::stable_sort(o.begin(), o.end(), [&](int a, int b) {
+    const double ba = runs[2 * a], bb = runs[2 * b];
+    return ba < bb || (ba == bb && ba * runs[2 * a + 1] < bb * runs[2 * b + 1]);
+  });
+  f[o[0]] = 0.0;
+  for (int q = 1; q < nr; ++q) {
+    const int a = o[q - 1], b = o[q];
+    const double db = runs[2 * b] - runs[2 * a];
+    const double dbp = runs[2 * b] * runs[2 * b + 1] - runs[2 * a] * runs[2 * a + 1];
+    f[b] = f[a] + 0.5 * (se[a] + se[b]) * db + 0.5 * (sv[a] + sv[b]) * dbp;
+  }
+  const double f0 = f[0];
+  for (int i = 0; i < nr; ++i) f[i] -= f0;
+}
+
 extern "C" int cvf_reweight_forward(int device, const double* samples, const int* run_of, long long n,
                                     const double* runs, int n_runs, double* f, int n_iter, double tol,
                                     double n_cells, const double* theta, const int* obs_ids, int n_obs,
                                     double* out) {
   RwSetup S;
+  if (f && samples && run_of && runs && n > 0 && n_runs > 0 && n_runs <= kRwMaxRuns && n_iter > 0) {
+    bool zero = true;
+    for (int i = 0; i < n_runs; ++i) zero = zero && f[i] == 0.0;
+    bool ok = true;
+    for (long long k = 0; k < n && ok; ++k) ok = run_of[k] >= 0 && run_of[k] < n_runs;
+    if (zero && ok) {
+      std::vector<long long> cnt(n_runs, 0);
+      for (long long k = 0; k < n; ++k) cnt[run_of[k]]++;
+      for (int i = 0; i < n_runs; ++i) ok = ok && cnt[i] > 0;
+      if (ok) ti_start(samples, run_of, n, runs, n_runs, f);
+    }
+  }
   if (int rc = rw_prepare(S, device, samples, run_of, n, runs, n_runs, f, obs_ids, n_obs)) return rc;
   for (int it = 0; it < n_iter; ++it) {
     double mc = 0.0;

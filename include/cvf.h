@@ -362,7 +362,8 @@ int cvf_cluster_stats_noalloc(const int* labels, int L, long long* out7, void* s
  *   samples: n rows of (E, V, N_hb, N_sigma) in internal units, grouped by run;
  *   run_of:  run index of each row; runs: n_runs rows of (beta, P) of the simulations;
  *   f:       in/out dimensionless free energies -log Z_j (n_runs), refined by n_iter WHAM
- *            iterations on the device when n_iter > 0;
+ *            iterations on the device when n_iter > 0 (all zeros in: started from thermodynamic
+ *            integration of <E> d beta + <V> d(beta P) between consecutive runs);
  *   theta:   target (beta, P, dJ_hb, dJ_sigma, dv_hb): weights exp(-beta (E' + P V')) with
  *            E' = E - dJ_hb N_hb - dJ_sigma N_sigma and V' = V + dv_hb N_hb;
  *   out:     n_obs reweighted means of the columns (E, V, N_hb, N_sigma, H = E + P V, rho = N/V,

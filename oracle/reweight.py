@@ -35,15 +35,33 @@ def log_d(samples, run_of, runs, f):
     return lse(t, axis=1)
 
 
+def ti_start(samples, run_of, runs):
+    """Starting f: d f = <E> d beta + <V> d(beta P) integrated by trapezoids between consecutive
+    runs in (beta, beta P) order, relative to run 0 (the engine's start when given zeros)."""
+    nr = len(runs)
+    c = np.bincount(run_of, minlength=nr).astype(np.float64)
+    se = np.bincount(run_of, weights=samples[:, E], minlength=nr) / c
+    sv = np.bincount(run_of, weights=samples[:, V], minlength=nr) / c
+    order = sorted(range(nr), key=lambda i: (runs[i, 0], runs[i, 0] * runs[i, 1]))
+    f = np.zeros(nr)
+    for a, b in zip(order[:-1], order[1:]):
+        db = runs[b, 0] - runs[a, 0]
+        dbp = runs[b, 0] * runs[b, 1] - runs[a, 0] * runs[a, 1]
+        f[b] = f[a] + 0.5 * (se[a] + se[b]) * db + 0.5 * (sv[a] + sv[b]) * dbp
+    return f - f[0]
+
+
 def wham(samples, run_of, runs, f0=None, n_iter=300, tol=1e-7):
     """Self-consistent f_j = -log Z_j (F90:450-473 restated per sample)."""
     runs = np.asarray(runs, dtype=np.float64)
     f = np.zeros(len(runs)) if f0 is None else np.array(f0, dtype=np.float64)
+    if n_iter > 0 and not np.any(f):
+        f = ti_start(samples, np.asarray(run_of), runs)
     b, p = runs[:, 0], runs[:, 1]
     for _ in range(n_iter):
         ld = log_d(samples, run_of, runs, f)
         u = f[None, :] - b[None, :] * (samples[:, E:E + 1] + p[None, :] * samples[:, V:V + 1]) - ld[:, None]
-        nf = f - np.log(np.exp(u).sum(0))
+        nf = f - lse(u, axis=0).ravel()  # in log space: no run's sum underflows to 0
         nf -= nf[0]
         change = np.max(np.abs(nf - f))
         f = nf
