@@ -78,6 +78,18 @@ def test_forward_matches_numpy(engine_lib):
     assert logz == pytest.approx(logz_ref, rel=1e-10)
 
 
+def test_far_start_underflow_recovers(engine_lib):
+    """A start far from the solution makes whole runs' WHAM sums underflow to zero; the log-space
+    sums must carry the iteration to the same free energies (none NaN)."""
+    s, ro, runs = synthetic(5)
+    f_ref = RW.wham(s, ro, runs, n_iter=3000, tol=1e-12)
+    far = np.array([0.0, 900.0, -800.0, 1500.0])
+    _, _, f = gpu_forward(s, ro, runs, far, [1.32, 0.46, 0, 0, 0], ["E"], 512.0, n_iter=3000, tol=1e-12)
+    assert np.all(np.isfinite(f)) and np.allclose(f, f_ref, atol=1e-7)
+    # the oracle's log-space update from the same start agrees too
+    assert np.allclose(RW.wham(s, ro, runs, f0=far, n_iter=3000, tol=1e-12), f_ref, atol=1e-7)
+
+
 def test_adjoint_matches_numpy_and_finite_differences(engine_lib):
     s, ro, runs = synthetic(11)
     f = RW.wham(s, ro, runs, n_iter=2000, tol=1e-12)
