@@ -85,6 +85,10 @@ struct ReplicaState {
   CStatsRec* cstats;    // device cluster-statistics stream
   SampleRec last;
   CStatsRec last_cstats;
+  // Running counts for cvf_observables: the counts of the last full measurement plus the
+  // changes the counting kernels added since (two's complement in slot block % 32)
+  long long base_hb2, base_ns;
+  unsigned long long dlt_slot[2][32];
 };
 
 // Multi-tau correlator of one replica (GW:165-181, GW:2983-3128): kCorrLevels levels of kCorrP
@@ -143,8 +147,14 @@ void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do
                        int zero_slots = 0);
 // Cube moves of all replicas (do_cubes) and, in extra blocks of the same launch, their volume
 // moves (do_volume): the two moves are independent, so the volume move hides under the cubes.
-void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s);
-void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s);
+// count: the counting variants also add the changes of N_hb and N_sigma they make to the
+// replicas' running counts (dlt_slot).
+void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, bool count = false);
+void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, bool count = false);
+// The running counts into every replica's last record (with its r_cell and volume), and the
+// re-basing after a full measurement (base = last record, changes zeroed).
+void launch_count_read(const BatchDev& b, cudaStream_t s);
+void launch_count_rebase(const BatchDev& b, cudaStream_t s);
 void launch_measure(const BatchDev& b, int record, cudaStream_t s);
 // Colour-1 sweep jsweep fused with the measurement of the step (slots zeroed by the step's
 // launch_step_begin), and the summation of the slots into the replica's record.

@@ -79,6 +79,12 @@ struct cvf_handle {
   // Flag_chessboard = 0 for every replica: the nhb<=4 compatibility mode (no cube moves, bond
   // counts per cell, per-arm sweep launches, greedy bond count in the measurement)
   bool nhb_mode = false;
+  // Running counts for cvf_observables: a run right after cvf_observables uses the counting
+  // kernels, which add the changes of N_hb and N_sigma they make to the counts of the last full
+  // measurement; while every step since then counted, cvf_observables reads those counts
+  // instead of measuring the lattice again.
+  bool count_valid = false;
+  bool obs_since_run = false;
   struct Group {
     BatchDev b;
     cudaStream_t s = nullptr;
@@ -279,12 +285,12 @@ static int ensure_sw(cvf_handle* h) {
   return upload_descs(h);
 }
 
-static void enqueue_step(cvf_handle* h, int nmet, int ncl) {
+static void enqueue_step(cvf_handle* h, int nmet, int ncl, bool count = false) {
   launch_step_begin(h->b, nmet, ncl, 1, 1, h->stream);
-  launch_cube_volume(h->b, 1, 1, h->stream);
+  launch_cube_volume(h->b, 1, 1, h->stream, count);
   for (int j = 0; j < nmet; ++j) {
-    launch_sweep(h->b, 0, j, h->stream);
-    launch_sweep(h->b, 1, j, h->stream);
+    launch_sweep(h->b, 0, j, h->stream, count);
+    launch_sweep(h->b, 1, j, h->stream, count);
   }
   for (int j = 0; j < ncl; ++j) launch_sw_step(h->b, j, h->stream);
 }
@@ -337,15 +343,17 @@ static void enqueue_cstats(cvf_handle* h, int record) {
 
 // Graph of `steps` MC steps; when record is set, the first step is followed by a recorded
 // measurement (and cluster statistics when ncl > 0).
-static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cudaGraphExec_t* out) {
-  auto key = std::make_tuple(steps, nmet, ncl, record);
+// count: plain steps with the counting kernels (ungrouped per-phase capture; record must be 0).
+static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cudaGraphExec_t* out,
+                     bool count = false) {
+  auto key = std::make_tuple(steps, nmet, ncl, record | (count ? 2 : 0));
   auto it = h->graphs.find(key);
   if (it != h->graphs.end()) {
     *out = it->second;
     return 0;
   }
   cudaGraph_t g;
-  if (h->launch_mode == 1 && ncl == 0 && !h->corr_on && !h->nhb_mode) {
+  if (h->launch_mode == 1 && ncl == 0 && !h->corr_on && !h->nhb_mode && !count) {
     // one persistent launch; a driver that cannot capture a cooperative launch leaves the
     // handle on the per-phase kernels
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -366,7 +374,7 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     cudaGetLastError();
     h->launch_mode = 0;
   }
-  if (ncl == 0 && group_count(h) > 1 && !h->nhb_mode) {
+  if (ncl == 0 && group_count(h) > 1 && !h->nhb_mode && !count) {
     if (int rc = build_groups(h)) return rc;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     CK(cudaEventRecord(h->fork, h->stream));
@@ -405,7 +413,7 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     if (i == 0 && record && ncl == 0 && nmet > 0) {
       enqueue_recorded_metropolis_step(h, nmet);
     } else {
-      enqueue_step(h, nmet, ncl);
+      enqueue_step(h, nmet, ncl, count);
       if (i == 0 && record) {
         launch_measure(h->b, 1, h->stream);
         if (ncl > 0) enqueue_cstats(h, 1);
@@ -606,6 +614,7 @@ int cvf_num_replicas(const cvf_handle* h) { return h ? (int)h->reps.size() : 0; 
 
 int cvf_set_config(cvf_handle* h, int r, const int* c12, long long n_cells) {
   if (int rc = check_rep(h, r)) return rc;
+  h->count_valid = false;
   ReplicaHost& R = h->reps[r];
   if (!c12 || n_cells != R.N) return fail(CVF_EINVAL, "cells12 must hold 12 ints for each of the N cells");
   CK(cudaSetDevice(h->device));
@@ -732,6 +741,8 @@ int cvf_get_distances(const cvf_handle* h, int r, float* dist, int* freq, int ca
 static int run_impl(cvf_handle* h, int n_steps, int nmet, int ncl, int interval) {
   if (!h) return fail(CVF_EINVAL, "null handle");
   if (n_steps < 0 || nmet < 0 || ncl < 0) return fail(CVF_EINVAL, "negative step counts");
+  const bool want_count = h->obs_since_run;
+  h->obs_since_run = false;
   CK(cudaSetDevice(h->device));
   if (ncl > 0) {
     if (int rc = ensure_sw(h)) return rc;
@@ -739,17 +750,21 @@ static int run_impl(cvf_handle* h, int n_steps, int nmet, int ncl, int interval)
   if (n_steps == 0) return 0;
   const int chunk_plain = 32;
   if (interval <= 0) {
+    // the counting kernels run where the per-phase capture of one group serves the handle
+    const bool count = want_count && h->count_valid && ncl == 0 && !h->nhb_mode && group_count(h) <= 1;
+    if (!count) h->count_valid = false;
     int full = n_steps / chunk_plain, rem = n_steps % chunk_plain;
     cudaGraphExec_t g;
     if (full) {
-      if (int rc = get_graph(h, chunk_plain, nmet, ncl, 0, &g)) return rc;
+      if (int rc = get_graph(h, chunk_plain, nmet, ncl, 0, &g, count)) return rc;
       for (int i = 0; i < full; ++i) CK(cudaGraphLaunch(g, h->stream));
     }
     if (rem) {
-      if (int rc = get_graph(h, rem, nmet, ncl, 0, &g)) return rc;
+      if (int rc = get_graph(h, rem, nmet, ncl, 0, &g, count)) return rc;
       CK(cudaGraphLaunch(g, h->stream));
     }
   } else {
+    h->count_valid = false;
     int full = n_steps / interval, rem = n_steps % interval;
     cudaGraphExec_t g;
     if (full) {
@@ -783,8 +798,16 @@ int cvf_observables(cvf_handle* h, int r, cvf_obs* out) {
   if (int rc = check_rep(h, r)) return rc;
   if (!out) return fail(CVF_EINVAL, "null out");
   CK(cudaSetDevice(h->device));
-  if (h->nhb_mode) launch_nhb_measure(h->b, 0, h->stream);
-  else launch_measure(h->b, 0, h->stream);
+  h->obs_since_run = true;
+  if (h->count_valid) {
+    launch_count_read(h->b, h->stream);  // every step since the last measurement counted
+  } else if (h->nhb_mode) {
+    launch_nhb_measure(h->b, 0, h->stream);
+  } else {
+    launch_measure(h->b, 0, h->stream);
+    launch_count_rebase(h->b, h->stream);
+    h->count_valid = true;
+  }
   SampleRec last;  // only the 32-byte measurement record crosses to the host
   CK(cudaMemcpyAsync(&last, (char*)(h->b.st + r) + offsetof(ReplicaState, last), sizeof(SampleRec),
                      cudaMemcpyDeviceToHost, h->stream));
@@ -931,6 +954,7 @@ int cvf_set_state(cvf_handle* h, int r, const cvf_state* in) {
 
 int cvf_autotune(cvf_handle* h, int* vec_out) {
   if (!h) return fail(CVF_EINVAL, "null handle");
+  h->count_valid = false;
   if (h->nhb_mode) {  // the per-arm sweep of Flag_chessboard = 0 has no tile to choose
     if (vec_out) *vec_out = h->b.vec;
     return 0;
@@ -1020,6 +1044,7 @@ int cvf_get_stream(cvf_handle* h, void** stream) {
 
 int cvf_profile_launch(cvf_handle* h, int kind, int n) {
   if (!h || n < 0 || kind < 0 || kind > 3) return fail(CVF_EINVAL, "bad profile request");
+  h->count_valid = false;
   if (h->nhb_mode) return fail(CVF_EINVAL, "kernel profiling covers the Flag_chessboard = 1 kernels");
   CK(cudaSetDevice(h->device));
   for (int i = 0; i < n; ++i) {

@@ -348,7 +348,7 @@ __device__ __forceinline__ void fill_cube_tables(const ReplicaDesc& R, CubeTable
 // wrote earlier in the same launch.
 template <int VC>
 __device__ __forceinline__ void cube_move_v(const ReplicaDesc& R, const CubeTables* ct, const int* __restrict__ blk,
-                                            int r, int vb, uint32_t t) {
+                                            int r, int vb, uint32_t t, int& cdh) {
   const uint32_t L = R.L, H = R.H, cpr = H / VC;
   const int b0 = __ldg(blk + r), half = (__ldg(blk + r + 1) - b0) >> 1;
   const int lb = vb - b0;
@@ -405,6 +405,7 @@ __device__ __forceinline__ void cube_move_v(const ReplicaDesc& R, const CubeTabl
     if ((unsigned long long)rr.y < ct->thr[dhb + 4] && nw != old) {
       st[k] = nw;
       changed = true;
+      cdh += dhb;
     }
   }
   if (changed) {
@@ -417,16 +418,29 @@ __device__ __forceinline__ void cube_move_v(const ReplicaDesc& R, const CubeTabl
   }
 }
 
+// cdh receives the change of N_hb the thread's accepted cube moves make.
 __device__ __forceinline__ void cube_move(const ReplicaDesc& R, const CubeTables* ct, const int* __restrict__ blk,
-                                          int r, int vb, uint32_t t) {
-  if (R.cvec == 4) cube_move_v<4>(R, ct, blk, r, vb, t);
-  else if (R.cvec == 2) cube_move_v<2>(R, ct, blk, r, vb, t);
-  else cube_move_v<1>(R, ct, blk, r, vb, t);
+                                          int r, int vb, uint32_t t, int& cdh) {
+  if (R.cvec == 4) cube_move_v<4>(R, ct, blk, r, vb, t, cdh);
+  else if (R.cvec == 2) cube_move_v<2>(R, ct, blk, r, vb, t, cdh);
+  else cube_move_v<1>(R, ct, blk, r, vb, t, cdh);
+}
+
+// Warp sums of the threads' count changes (dn in N_hb units, ds in N_sigma units) added to one
+// of the replica's 32 running-count slots (no block barrier). Every lane of the warp calls it.
+__device__ __forceinline__ void count_accumulate(ReplicaState& S, int vb, int dn, int ds) {
+  const int wn = __reduce_add_sync(0xffffffffu, dn), wsum = __reduce_add_sync(0xffffffffu, ds);
+  if ((threadIdx.x & 31) == 0 && (wn | wsum)) {
+    const int slot = (vb * (kThreads / 32) + (int)(threadIdx.x >> 5)) & 31;
+    atomicAdd(&S.dlt_slot[0][slot], (unsigned long long)(long long)wn);
+    atomicAdd(&S.dlt_slot[1][slot], (unsigned long long)(long long)wsum);
+  }
 }
 
 // Cube moves of every replica, then (blocks at and after nblk_cube) the volume move of replica
 // (block - nblk_cube), both with the counters of the current step.
-__global__ void __launch_bounds__(kThreads) k_cube_volume(const ReplicaDesc* __restrict__ reps,
+template <bool kCount>
+__global__ void __launch_bounds__(kThreads, 4) k_cube_volume(const ReplicaDesc* __restrict__ reps,
                                                           ReplicaState* __restrict__ st,
                                                           const int* __restrict__ blk, int nrep, int nblk_cube) {
   if ((int)blockIdx.x >= nblk_cube) {
@@ -440,7 +454,9 @@ __global__ void __launch_bounds__(kThreads) k_cube_volume(const ReplicaDesc* __r
   CubeTables* ct = s_ct + (threadIdx.x >> 5);
   fill_cube_tables(R, ct, threadIdx.x & 31);
   __syncwarp();
-  cube_move(R, ct, blk, r, blockIdx.x, st[r].cur[1]);
+  int cdh = 0;
+  cube_move(R, ct, blk, r, blockIdx.x, st[r].cur[1], cdh);
+  if (kCount) count_accumulate(st[r], blockIdx.x, cdh, 0);
 }
 
 // ------------------------------------------------------------------ checkerboard sweep
@@ -557,12 +573,15 @@ __device__ __noinline__ uint32_t sweep_proposal_retry(uint32_t c0, uint32_t t, u
 
 // Exact update of one cell with the full 32-bit uniforms (high halves from the sweep block,
 // low halves from the refinement block). Taken only when a 16-bit comparison tied.
-__device__ __noinline__ uint32_t sweep_cell_exact(uint32_t w, uint32_t nbs, uint32_t eta, uint32_t u,
-                                                  uint32_t a1, uint32_t a2, uint32_t a3, uint32_t c0, uint32_t t,
-                                                  const ReplicaDesc* R) {
+// Returns the new word in the low 32 bits and the packed count changes of the accepted arms,
+// 65536 dN_hb + dN_sigma, in the high 32 bits.
+__device__ __noinline__ unsigned long long sweep_cell_exact(uint32_t w, uint32_t nbs, uint32_t eta, uint32_t u,
+                                                            uint32_t a1, uint32_t a2, uint32_t a3, uint32_t c0,
+                                                            uint32_t t, const ReplicaDesc* R) {
   const U4 rf = philox(c0, t, kStSweepRefine, R->replica, R->key0, R->key1);
   uint32_t h = sigma_histogram(w);
   uint32_t f = u;
+  int32_t acc = 0;
   for (int a = 0; a < 6; ++a) {
     unsigned long long m = (unsigned long long)f * 6ull;
     const uint32_t n = (uint32_t)(m >> 32);
@@ -580,9 +599,10 @@ __device__ __noinline__ uint32_t sweep_cell_exact(uint32_t w, uint32_t nbs, uint
     if (U < T) {
       w = (w & ~(7u << (3 * a))) | (n << (3 * a));
       h += (1u << (4 * n)) - (1u << (4 * o));
+      acc += dhb * 65536 + dns;
     }
   }
-  return w;
+  return ((unsigned long long)(uint32_t)acc << 32) | w;
 }
 
 // Byte select: byte i of the result is byte ((sel >> 4i) & 7) of the eight bytes {hi:lo}. Every
@@ -608,12 +628,23 @@ struct EtaTables {
 //   nbw[v]  44 at byte v (v = 0..5), zero for v = 6, 7 (7 marks an arm with eta = 0)
 //   tv[i]   2*(T_i >> 16) + ((T_i & 0xffff) != 0) for the threshold T_i of entry
 //           i = 11*dN_hb + (h_new - h_old) + 17
+//   pk[i]   65536 dN_hb + dN_sigma of entry i (dN_sigma = h_new - h_old + 1): the change of the
+//           counts an accepted arm makes, for the running counts of cvf_observables
 struct SweepTables {
   uint2 cnt[8];
   uint2 nbw[8];
   uint32_t tv[33];
+  int32_t pk[33];
   EtaTables et;
 };
+
+// 65536 dN_hb + dN_sigma for table entry i = 11 dN_hb + (h_new - h_old) + 17 (h_new - h_old in
+// [-6, 4], so the split is unique).
+__device__ __forceinline__ int32_t entry_delta(int i) {
+  const int v = i - 17;
+  const int dn = v + 6 >= 11 ? 1 : (v + 6 < 0 ? -1 : 0);
+  return dn * 65536 + (v - 11 * dn + 1);
+}
 
 __device__ __forceinline__ uint2 count_bytes(uint32_t v, uint32_t b) {
   return v < 4 ? make_uint2(b << (8 * v), 0u) : (v < 6 ? make_uint2(0u, b << (8 * (v - 4))) : make_uint2(0u, 0u));
@@ -635,7 +666,11 @@ __device__ __forceinline__ const EtaTables* warp_eta_tables(const ReplicaDesc& R
 __device__ __forceinline__ void fill_sweep_tables(const ReplicaDesc& R, SweepTables* wt, uint32_t lane) {
   fill_eta_tables(R, &wt->et, lane);
   wt->tv[lane] = R.tv[lane];
-  if (lane == 0) wt->tv[32] = R.tv[32];
+  wt->pk[lane] = entry_delta((int)lane);
+  if (lane == 0) {
+    wt->tv[32] = R.tv[32];
+    wt->pk[32] = entry_delta(32);
+  }
   if (lane < 8) {
     wt->cnt[lane] = count_bytes(lane, 4u);
     wt->nbw[lane] = count_bytes(lane, 44u);
@@ -662,8 +697,11 @@ __device__ __forceinline__ const SweepTables* warp_sweep_tables(const ReplicaDes
 // zero; a product that wraps to zero without a tie only sends the cell through the exact path
 // as well, which decides every arm from the full 32-bit uniforms. A proposal equal to the old
 // value lands on entry 17 (dN = 0), which always accepts and changes nothing.
+// kCount: dacc also receives the packed count changes (pk) of the accepted arms that change a value.
+template <bool kCount>
 __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32_t nbe, uint32_t eta, const U4& rr,
-                                                uint32_t c0, uint32_t t, const ReplicaDesc& R, const SweepTables* wt) {
+                                                uint32_t c0, uint32_t t, const ReplicaDesc& R, const SweepTables* wt,
+                                                int32_t& dacc) {
   uint32_t u = rr.x;
   if (u * 46656u < 2560u) u = sweep_proposal_retry(c0, t, R.replica, R.key0, R.key1);
   const uint32_t w0 = w;
@@ -675,7 +713,9 @@ __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32
     hy += c.y;
   }
   const char* tvb = reinterpret_cast<const char*>(wt->tv) + 68;
+  const char* pkb = reinterpret_cast<const char*>(wt->pk) + 68;
   uint32_t f = u, tprod = 1u;
+  int32_t cacc = 0;
 #pragma unroll
   for (int a = 0; a < 6; ++a) {
     const unsigned long long m = (unsigned long long)f * 6ull + (0x7770ull << 32);
@@ -692,12 +732,26 @@ __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32
     tprod *= (uint32_t)(d - 1);
     const uint2 cn = wt->cnt[sn - 0x7770u], co = wt->cnt[o];
     const uint32_t dw = (sn - 0x7770u - o) << (3 * a);
-    asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %3, 2;\n\t@p add.u32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;"
-        "\n\t@p sub.u32 %1, %1, %6;\n\t@p add.u32 %2, %2, %7;\n\t@p sub.u32 %2, %2, %8;\n\t}"
-        : "+r"(w), "+r"(hx), "+r"(hy)
-        : "r"(d), "r"(dw), "r"(cn.x), "r"(co.x), "r"(cn.y), "r"(co.y));
+    if (kCount) {
+      const int32_t pk = dw ? *reinterpret_cast<const int32_t*>(pkb + off) : 0;
+      asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %4, 2;\n\t@p add.u32 %0, %0, %5;\n\t@p add.u32 %1, %1, %6;"
+          "\n\t@p sub.u32 %1, %1, %7;\n\t@p add.u32 %2, %2, %8;\n\t@p sub.u32 %2, %2, %9;"
+          "\n\t@p add.u32 %3, %3, %10;\n\t}"
+          : "+r"(w), "+r"(hx), "+r"(hy), "+r"(cacc)
+          : "r"(d), "r"(dw), "r"(cn.x), "r"(co.x), "r"(cn.y), "r"(co.y), "r"(pk));
+    } else {
+      asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %3, 2;\n\t@p add.u32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;"
+          "\n\t@p sub.u32 %1, %1, %6;\n\t@p add.u32 %2, %2, %7;\n\t@p sub.u32 %2, %2, %8;\n\t}"
+          : "+r"(w), "+r"(hx), "+r"(hy)
+          : "r"(d), "r"(dw), "r"(cn.x), "r"(co.x), "r"(cn.y), "r"(co.y));
+    }
   }
-  if (tprod == 0u) w = sweep_cell_exact(w0, nbs, eta, u, rr.y, rr.z, rr.w, c0, t, &R);
+  if (tprod == 0u) {
+    const unsigned long long x = sweep_cell_exact(w0, nbs, eta, u, rr.y, rr.z, rr.w, c0, t, &R);
+    w = (uint32_t)x;
+    cacc = (int32_t)(uint32_t)(x >> 32);
+  }
+  if (kCount) dacc += cacc;
   return w;
 }
 
@@ -716,9 +770,9 @@ struct SweepMinBlocks {
 // colour-1 cells count all bonds (delta of the facing sigmas times the bond's eta, twice), and
 // each colour-1 cell adds the sigma pairs of itself and of the colour-0 cell with the same word
 // index (the x-neighbour the segment loads anyway).
-template <int V, bool kMeasure>
+template <int V, bool kMeasure, bool kCount = false>
 __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepTables* wt, uint32_t q, int colour,
-                                              uint32_t t, uint32_t& hb2, uint32_t& ns) {
+                                              uint32_t t, uint32_t& hb2, uint32_t& ns, int32_t* dacc = nullptr) {
   int hc, y, z;
   if (!segment_of<V>(R, q, hc, y, z)) return;
   uint32_t out[V], nbs[V], nbe[V], eta[V];
@@ -744,7 +798,8 @@ __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepT
   for (int k = 0; k < V; ++k) {
     const uint32_t c0 = cbase + 2u * k;
     const U4 rr = philox(c0, t, kStSweep, R.replica, R.key0, R.key1);
-    out[k] = update_cell(out[k], nbs[k], nbe[k], eta[k], rr, c0, t, R, wt);
+    int32_t dummy = 0;
+    out[k] = update_cell<kCount>(out[k], nbs[k], nbe[k], eta[k], rr, c0, t, R, wt, kCount ? *dacc : dummy);
   }
   VecLoad<V>::st(own_ptr, out);
   if (kMeasure) {
@@ -758,17 +813,22 @@ __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepT
   }
 }
 
-template <int V>
+template <int V, bool kCount>
 __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const ReplicaDesc* __restrict__ reps,
-                                                    const ReplicaState* __restrict__ st,
+                                                    ReplicaState* __restrict__ st,
                                                     const int* __restrict__ blk, int nrep, int colour, int jsweep) {
   __shared__ SweepTables s_tab[kThreads / 32];
   const int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   const SweepTables* wt = warp_sweep_tables(R, s_tab);
   uint32_t hb2 = 0, ns = 0;
-  sweep_segment<V, false>(R, wt, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
-                          st[r].cur[0] + (uint32_t)jsweep, hb2, ns);
+  int32_t dacc = 0;
+  sweep_segment<V, false, kCount>(R, wt, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
+                                  st[r].cur[0] + (uint32_t)jsweep, hb2, ns, &dacc);
+  if (kCount) {
+    const int ds = (int)(int16_t)(dacc & 0xffff);  // |dN_sigma| per thread <= 8 cells x 30
+    count_accumulate(st[r], blockIdx.x, (dacc - ds) / 65536, ds);
+  }
 }
 
 // Colour-1 sweep of a recorded step fused with its measurement: the counts go to the slots
@@ -946,7 +1006,8 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_run(BatchDev
           const int r = find_replica(b.blk_cubev, b.nrep, vb);
           StepTables* wt = s_tab + (threadIdx.x >> 5);
           ensure_tables(b.reps, r, wt, s_held[threadIdx.x >> 5]);
-          cube_move(b.reps[r], &wt->cube, b.blk_cubev, r, vb, b.st[r].ctr[1] + (uint32_t)s);
+          int cdh = 0;
+          cube_move(b.reps[r], &wt->cube, b.blk_cubev, r, vb, b.st[r].ctr[1] + (uint32_t)s, cdh);
         } else if (threadIdx.x < 32) {
           const int r = vb - b.nblk_cubev;
           ReplicaState& S = b.st[r];
@@ -1024,20 +1085,58 @@ void launch_measure_end(const BatchDev& b, int record, cudaStream_t s) {
   k_measure_end<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, record);
 }
 
-void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s) {
+void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, bool count) {
   const int cube_blocks = do_cubes ? b.nblk_cubev : 0;
   const int vol_blocks = do_volume ? b.nrep : 0;
   if (cube_blocks + vol_blocks == 0) return;
-  k_cube_volume<<<cube_blocks + vol_blocks, kThreads, 0, s>>>(b.reps, b.st, b.blk_cubev, b.nrep, cube_blocks);
+  if (count) k_cube_volume<true><<<cube_blocks + vol_blocks, kThreads, 0, s>>>(b.reps, b.st, b.blk_cubev, b.nrep, cube_blocks);
+  else k_cube_volume<false><<<cube_blocks + vol_blocks, kThreads, 0, s>>>(b.reps, b.st, b.blk_cubev, b.nrep, cube_blocks);
 }
 
-void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s) {
+template <bool kCount>
+static void launch_sweep_t(const BatchDev& b, int colour, int jsweep, cudaStream_t s) {
   switch (b.vec) {
-    case 8: k_sweep<8><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    case 4: k_sweep<4><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    case 2: k_sweep<2><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    default: k_sweep<1><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    case 8: k_sweep<8, kCount><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    case 4: k_sweep<4, kCount><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    case 2: k_sweep<2, kCount><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    default: k_sweep<1, kCount><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
   }
+}
+
+void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, bool count) {
+  if (count) launch_sweep_t<true>(b, colour, jsweep, s);
+  else launch_sweep_t<false>(b, colour, jsweep, s);
+}
+
+__global__ void k_count_read(ReplicaState* __restrict__ st, int nrep) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrep) return;
+  ReplicaState& S = st[r];
+  long long dn = 0, ds = 0;
+  for (int i = 0; i < 32; ++i) {
+    dn += (long long)S.dlt_slot[0][i];
+    ds += (long long)S.dlt_slot[1][i];
+  }
+  SampleRec rec;
+  rec.n_hb2 = S.base_hb2 + 2 * dn;
+  rec.n_sigma = S.base_ns + ds;
+  rec.r_cell = S.r_cell;
+  rec.volume = S.volume;
+  S.last = rec;
+}
+
+__global__ void k_count_rebase(ReplicaState* __restrict__ st, int nrep) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrep) return;
+  ReplicaState& S = st[r];
+  S.base_hb2 = S.last.n_hb2;
+  S.base_ns = S.last.n_sigma;
+  for (int i = 0; i < 32; ++i) S.dlt_slot[0][i] = S.dlt_slot[1][i] = 0ull;
+}
+
+void launch_count_read(const BatchDev& b, cudaStream_t s) { k_count_read<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep); }
+void launch_count_rebase(const BatchDev& b, cudaStream_t s) {
+  k_count_rebase<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep);
 }
 
 void launch_measure(const BatchDev& b, int record, cudaStream_t s) {
