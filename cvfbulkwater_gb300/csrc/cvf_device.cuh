@@ -151,9 +151,10 @@ void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do
 // replicas' running counts (dlt_slot).
 void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, bool count = false);
 void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, bool count = false);
-// The running counts into every replica's last record (with its r_cell and volume), and the
-// re-basing after a full measurement (base = last record, changes zeroed).
-void launch_count_read(const BatchDev& b, cudaStream_t s);
+// The running counts into every replica's last record (with its r_cell and volume; appended to
+// the sample stream when record is set), and the re-basing after a full measurement (base =
+// last record, changes zeroed).
+void launch_count_read(const BatchDev& b, cudaStream_t s, int record);
 void launch_count_rebase(const BatchDev& b, cudaStream_t s);
 void launch_measure(const BatchDev& b, int record, cudaStream_t s);
 // Colour-1 sweep jsweep fused with the measurement of the step (slots zeroed by the step's

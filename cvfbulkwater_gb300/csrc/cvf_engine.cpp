@@ -410,7 +410,11 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     if (h->corr_on) launch_corr_step(h->b, h->stream);
   }
   for (int i = 0; i < steps && !h->nhb_mode; ++i) {
-    if (i == 0 && record && ncl == 0 && nmet > 0) {
+    if (count) {
+      // the record of a counting step is the running counts
+      enqueue_step(h, nmet, ncl, true);
+      if (i == 0 && record) launch_count_read(h->b, h->stream, 1);
+    } else if (i == 0 && record && ncl == 0 && nmet > 0) {
       enqueue_recorded_metropolis_step(h, nmet);
     } else {
       enqueue_step(h, nmet, ncl, count);
@@ -764,15 +768,22 @@ static int run_impl(cvf_handle* h, int n_steps, int nmet, int ncl, int interval)
       CK(cudaGraphLaunch(g, h->stream));
     }
   } else {
-    h->count_valid = false;
+    // sampled runs record from running counts (one full measurement first when they are not
+    // current) wherever the plain per-phase capture serves the handle
+    const bool count = ncl == 0 && nmet > 0 && !h->nhb_mode && group_count(h) <= 1 && h->launch_mode == 0;
+    if (count && !h->count_valid) {
+      launch_measure(h->b, 0, h->stream);
+      launch_count_rebase(h->b, h->stream);
+    }
+    h->count_valid = count;
     int full = n_steps / interval, rem = n_steps % interval;
     cudaGraphExec_t g;
     if (full) {
-      if (int rc = get_graph(h, interval, nmet, ncl, 1, &g)) return rc;
+      if (int rc = get_graph(h, interval, nmet, ncl, 1, &g, count)) return rc;
       for (int i = 0; i < full; ++i) CK(cudaGraphLaunch(g, h->stream));
     }
     if (rem) {
-      if (int rc = get_graph(h, rem, nmet, ncl, 1, &g)) return rc;
+      if (int rc = get_graph(h, rem, nmet, ncl, 1, &g, count)) return rc;
       CK(cudaGraphLaunch(g, h->stream));
     }
   }
@@ -800,7 +811,7 @@ int cvf_observables(cvf_handle* h, int r, cvf_obs* out) {
   CK(cudaSetDevice(h->device));
   h->obs_since_run = true;
   if (h->count_valid) {
-    launch_count_read(h->b, h->stream);  // every step since the last measurement counted
+    launch_count_read(h->b, h->stream, 0);  // every step since the last measurement counted
   } else if (h->nhb_mode) {
     launch_nhb_measure(h->b, 0, h->stream);
   } else {

@@ -1108,7 +1108,7 @@ void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, boo
   else launch_sweep_t<false>(b, colour, jsweep, s);
 }
 
-__global__ void k_count_read(ReplicaState* __restrict__ st, int nrep) {
+__global__ void k_count_read(ReplicaState* __restrict__ st, int nrep, int record) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrep) return;
   ReplicaState& S = st[r];
@@ -1123,6 +1123,8 @@ __global__ void k_count_read(ReplicaState* __restrict__ st, int nrep) {
   rec.r_cell = S.r_cell;
   rec.volume = S.volume;
   S.last = rec;
+  if (record && S.samples && S.n_samples < S.cap_samples) S.samples[S.n_samples] = rec;
+  if (record) S.n_samples++;
 }
 
 __global__ void k_count_rebase(ReplicaState* __restrict__ st, int nrep) {
@@ -1134,7 +1136,9 @@ __global__ void k_count_rebase(ReplicaState* __restrict__ st, int nrep) {
   for (int i = 0; i < 32; ++i) S.dlt_slot[0][i] = S.dlt_slot[1][i] = 0ull;
 }
 
-void launch_count_read(const BatchDev& b, cudaStream_t s) { k_count_read<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep); }
+void launch_count_read(const BatchDev& b, cudaStream_t s, int record) {
+  k_count_read<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, record);
+}
 void launch_count_rebase(const BatchDev& b, cudaStream_t s) {
   k_count_rebase<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep);
 }
