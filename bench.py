@@ -253,7 +253,7 @@ def sample_columns(lat, smp, r=0):
 
 
 def bench_differentiation(local):
-    """Differentiable reweighting (survey config 5): 32 replicas of L=32 along P=0.45 at T uniform
+    """Differentiable reweighting workload: 32 replicas of L=32 along P=0.45 at T uniform
     in [0.60, 0.90], 100,000 recorded steps each (3.2 M samples); FP64 WHAM forward and adjoint;
     alpha_P, K_T, C_P at T = 0.75 from the adjoint against finite differences and the fluctuation
     formulas; the reweighted density against the reference's L32 P=0.45 isobar."""
@@ -367,7 +367,8 @@ def bench_plain_l16(steps, warmup, local, flush):
     torch.cuda.synchronize()
     replay_us = e0.elapsed_time(e1) * 1e3 / 640
     lat.close()
-    # the survey's protocol: 1000 equilibration + 10000 sampling steps, a record every 10
+    # the small plain workload's protocol: 1000 equilibration + 10000 sampling steps, a record
+    # every 10
     lat = Lattice(Params(L=16, T=0.815, P=0.45, seed=SEED, start=0, device=local))
     t0 = time.perf_counter()
     lat.run(1000, 1, 0)
