@@ -101,6 +101,7 @@ def lib():
         "cvf_set_distances": (I, [P, I, P, P, I]),
         "cvf_get_distances": (I, [P, I, P, P, I, C.POINTER(I)]),
         "cvf_run_steps": (I, [P, I, I, I]),
+        "cvf_batch_run": (I, [P, I, I, I]),
         "cvf_run_sampled": (I, [P, I, I, I, I]),
         "cvf_synchronize": (I, [P]),
         "cvf_observables": (I, [P, I, C.POINTER(Obs)]),
@@ -108,6 +109,7 @@ def lib():
         "cvf_get_labels": (I, [P, I, P, LL]),
         "cvf_sample_count": (I, [P, I, C.POINTER(LL)]),
         "cvf_get_samples": (I, [P, I, P, LL, C.POINTER(LL)]),
+        "cvf_sample_stream": (I, [P, I, P, LL, C.POINTER(LL)]),
         "cvf_get_cstats_stream": (I, [P, I, P, LL, C.POINTER(LL)]),
         "cvf_clear_samples": (I, [P]),
         "cvf_sample_observables": (I, [P, I, C.POINTER(Sample), C.POINTER(Obs)]),

@@ -794,6 +794,8 @@ static int run_impl(cvf_handle* h, int n_steps, int nmet, int ncl, int interval)
 
 int cvf_run_steps(cvf_handle* h, int n_steps, int nmet, int ncl) { return run_impl(h, n_steps, nmet, ncl, 0); }
 
+int cvf_batch_run(cvf_handle* h, int n_steps, int nmet, int ncl) { return run_impl(h, n_steps, nmet, ncl, 0); }
+
 int cvf_run_sampled(cvf_handle* h, int n_steps, int nmet, int ncl, int interval) {
   if (interval < 1) return fail(CVF_EINVAL, "interval must be >= 1");
   return run_impl(h, n_steps, nmet, ncl, interval);
@@ -902,6 +904,10 @@ int cvf_get_samples(cvf_handle* h, int r, cvf_sample* out, long long max, long l
   if (n_out) *n_out = n;
   if (s.n_samples > s.cap_samples) return fail(CVF_ELIMIT, "sample stream overflowed its capacity");
   return 0;
+}
+
+int cvf_sample_stream(cvf_handle* h, int r, cvf_sample* out, long long max, long long* n_out) {
+  return cvf_get_samples(h, r, out, max, n_out);
 }
 
 int cvf_get_cstats_stream(cvf_handle* h, int r, cvf_cstats* out, long long max, long long* n_out) {

@@ -120,6 +120,8 @@ int cvf_get_distances(const cvf_handle* h, int replica, float* dist, int* freq, 
 /* Replaces n_steps calls of MonteCarlo_Step (GW:1346-1733) for every replica: one cube move,
  * one volume move, n_metropolis checkerboard sweeps, n_cluster Swendsen-Wang steps per step. */
 int cvf_run_steps(cvf_handle* h, int n_steps, int n_metropolis, int n_cluster);
+/* The same for a handle made by cvf_batch_create (every replica steps; one graph per chunk). */
+int cvf_batch_run(cvf_handle* h, int n_steps, int n_metropolis, int n_cluster);
 /* The production loop GW:1204-1244: after step i (0-based within the call) with
  * i % interval == 0, a sample (and, when n_cluster > 0, a cluster-statistics record) is
  * appended on the device. No host synchronisation inside. */
@@ -137,6 +139,9 @@ int cvf_get_labels(cvf_handle* h, int replica, int* labels, long long n_sites);
 /* Device sample stream: number of samples recorded since the last clear, and a copy. */
 int cvf_sample_count(cvf_handle* h, int replica, long long* count);
 int cvf_get_samples(cvf_handle* h, int replica, cvf_sample* out, long long max, long long* n_out);
+/* cvf_get_samples under the name of the sample-stream export: the (N_hb2, N_sigma, r_cell, V)
+ * records, from which cvf_sample_observables gives E, V, N_hb and N_sigma. */
+int cvf_sample_stream(cvf_handle* h, int replica, cvf_sample* out, long long max, long long* n_out);
 int cvf_get_cstats_stream(cvf_handle* h, int replica, cvf_cstats* out, long long max, long long* n_out);
 int cvf_clear_samples(cvf_handle* h);
 /* Observables of one sample (host FP64 formulas of GW:2138-2159). */

@@ -42,3 +42,29 @@ def test_groupings_identical(engine_lib, corr):
             assert len(a[2]) == len(b[2]) and all(x == y for x, y in zip(a[2], b[2])), (g, r)
             if corr:
                 assert np.array_equal(a[3][0], b[3][0]) and np.array_equal(a[3][1], b[3][1]), (g, r)
+
+
+def test_batch_run_and_sample_stream_exports(engine_lib):
+    """cvf_batch_run steps a batch as cvf_run_steps does; cvf_sample_stream returns the records of
+    cvf_get_samples."""
+    import ctypes as C
+    from cvfbulkwater_gb300 import abi
+    specs = [(8, 0.6), (12, 0.8)]
+    a = Lattice([Params(L=L, T=T, P=0.45, seed=70 + i, start=0, replica=i) for i, (L, T) in enumerate(specs)])
+    b = Lattice([Params(L=L, T=T, P=0.45, seed=70 + i, start=0, replica=i) for i, (L, T) in enumerate(specs)])
+    a.run(5, 1, 0)
+    abi.check(abi.lib().cvf_batch_run(b._h, 5, 1, 0))
+    for r in range(2):
+        assert np.array_equal(a.get_config(r), b.get_config(r))
+    a.run_sampled(6, 1, 0, 2)
+    n = C.c_longlong()
+    abi.check(abi.lib().cvf_sample_count(a._h, 1, C.byref(n)))
+    buf = (abi.Sample * n.value)()
+    got = C.c_longlong()
+    abi.check(abi.lib().cvf_sample_stream(a._h, 1, buf, n.value, C.byref(got)))
+    want = a.samples(1)
+    assert got.value == len(want) == 3
+    for k in range(3):
+        assert (buf[k].n_hb2, buf[k].n_sigma, buf[k].r_cell, buf[k].volume) == tuple(want[k].tolist())
+    a.close()
+    b.close()
