@@ -85,6 +85,7 @@ struct cvf_handle {
   // instead of measuring the lattice again.
   bool count_valid = false;
   bool obs_since_run = false;
+  cudaGraphExec_t nhb_read = nullptr;  // Flag_chessboard = 0: the read's 3L + 1 launches, captured once
   struct Group {
     BatchDev b;
     cudaStream_t s = nullptr;
@@ -95,6 +96,14 @@ struct cvf_handle {
   int groups_vec = 0;
   cudaEvent_t fork = nullptr;
 };
+
+// Drops every cached graph (kernel arguments such as the block tables change).
+static void drop_graphs(cvf_handle* h) {
+  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+  h->graphs.clear();
+  if (h->nhb_read) cudaGraphExecDestroy(h->nhb_read);
+  h->nhb_read = nullptr;
+}
 
 // A correlator in its initial state (GW:2983-3008): empty channels hold -2e10.
 static CorrState corr_initial() {
@@ -280,8 +289,7 @@ static int ensure_sw(cvf_handle* h) {
   }
   if (int rc = dev_alloc(h, (void**)&h->blocktop, (size_t)h->b.nblk_site * 2 * sizeof(unsigned long long))) return rc;
   h->sw_alloc = true;
-  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
-  h->graphs.clear();
+  drop_graphs(h);
   return upload_descs(h);
 }
 
@@ -599,7 +607,7 @@ int cvf_destroy(cvf_handle* h) {
   if (!h) return 0;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
-  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
+  drop_graphs(h);
   for (auto& g : h->groups) {
     if (g.s) cudaStreamDestroy(g.s);
     if (g.done) cudaEventDestroy(g.done);
@@ -815,7 +823,19 @@ int cvf_observables(cvf_handle* h, int r, cvf_obs* out) {
   if (h->count_valid) {
     launch_count_read(h->b, h->stream, 0);  // every step since the last measurement counted
   } else if (h->nhb_mode) {
-    launch_nhb_measure(h->b, 0, h->stream);
+    if (!h->nhb_read) {
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      launch_nhb_measure(h->b, 0, h->stream);
+      CK(cudaStreamEndCapture(h->stream, &g));
+      cudaError_t e = cudaGraphInstantiate(&h->nhb_read, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) {
+        h->nhb_read = nullptr;
+        return fail(CVF_ECUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+      }
+    }
+    CK(cudaGraphLaunch(h->nhb_read, h->stream));
   } else {
     launch_measure(h->b, 0, h->stream);
     launch_count_rebase(h->b, h->stream);
@@ -1035,8 +1055,7 @@ int cvf_autotune(cvf_handle* h, int* vec_out) {
   cudaEventDestroy(e1);
   if (e != cudaSuccess) return fail(CVF_ECUDA, std::string("autotune: ") + cudaGetErrorString(e));
   // the sweep blocks depend on the tile: rebuild the block tables and drop captured graphs
-  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
-  h->graphs.clear();
+  drop_graphs(h);
   if (int rc = build_tables(h, best)) return rc;
   if (vec_out) *vec_out = best;
   return 0;
@@ -1046,8 +1065,7 @@ int cvf_set_sweep_tile(cvf_handle* h, int vec, int* vec_out) {
   if (!h || !(vec == 1 || vec == 2 || vec == 4 || vec == 8)) return fail(CVF_EINVAL, "tile must be 1, 2, 4 or 8");
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
-  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
-  h->graphs.clear();
+  drop_graphs(h);
   if (int rc = build_tables(h, vec)) return rc;
   if (vec_out) *vec_out = h->b.vec;
   return 0;
@@ -1090,8 +1108,7 @@ int cvf_set_launch_mode(cvf_handle* h, int mode) {
   if (mode == h->launch_mode) return 0;
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
-  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
-  h->graphs.clear();
+  drop_graphs(h);
   h->launch_mode = mode;
   return 0;
 }
@@ -1121,8 +1138,7 @@ int cvf_set_replica_groups(cvf_handle* h, int groups) {
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
   h->group_setting = groups;
-  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
-  h->graphs.clear();
+  drop_graphs(h);
   return 0;
 }
 
@@ -1145,8 +1161,7 @@ int cvf_set_correlation(cvf_handle* h, int enable) {
     CK(cudaMemcpy(h->b.corr, init.data(), init.size() * sizeof(CorrState), cudaMemcpyHostToDevice));
   }
   h->corr_on = enable != 0;
-  for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);
-  h->graphs.clear();
+  drop_graphs(h);
   return 0;
 }
 
