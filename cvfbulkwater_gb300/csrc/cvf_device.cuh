@@ -26,8 +26,9 @@ struct ReplicaDesc {
   uint32_t* cover;    // max_cand * 3 * W: coordinate coverage bitmaps
   int max_cand;       // capacity of cover
   // Flag_chessboard = 0 (null otherwise): eta of every cell as 6 bits, the bond count of every
-  // cell, and the greedy measurement's work arrays (cells with 5 or more matched bonds, their
-  // counts); cells indexed x + L*(y + L*z)
+  // cell, and the greedy measurement's work arrays (per cell: bits 0..2 its matched x+, y+, z+
+  // bonds and bit 3 set when 5 or more of its arms are matched; the counts of those cells);
+  // cells indexed x + L*(y + L*z)
   uint8_t* eta6;
   uint8_t* nhb;
   uint8_t* sat;

@@ -167,9 +167,10 @@ __device__ __forceinline__ uint32_t pairs6(uint32_t w) {
   return zero_fields6(w ^ r1) + zero_fields6(w ^ r2) + (zero_fields6(w ^ r3) >> 1);
 }
 
-// Per cell: the number of its six arms that agree with the arm they face (eta plays no part,
-// GW:2064-2099), marked when 5 or more; the matched forward bonds (x+, y+, z+) and the sigma
-// pairs summed per block into slot block % 32.
+// Per cell: which of its six arms agree with the arm they face (eta plays no part,
+// GW:2064-2099), stored as the matched forward bonds (bits 0..2: x+, y+, z+) and a mark (bit 3)
+// when 5 or more agree; the matched forward bonds and the sigma pairs summed per block into slot
+// block % 32.
 __global__ void k_nhb_mark(const ReplicaDesc* __restrict__ reps, ReplicaState* __restrict__ st,
                            const int* __restrict__ blk, int nrep) {
   __shared__ unsigned long long s_acc[2];
@@ -181,15 +182,16 @@ __global__ void k_nhb_mark(const ReplicaDesc* __restrict__ reps, ReplicaState* _
   if (c < N) {
     const Cell p = cell_xyz(c, L);
     const uint32_t w = word_at(R, p.x, p.y, p.z);
-    uint32_t m = 0;
+    uint32_t m = 0, bits = 0;
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
       const Cell q = step_arm(p, a, L);
       const uint32_t e = field(w, a) == field(word_at(R, q.x, q.y, q.z), a ^ 1);
       m += e;
-      if ((a & 1) == 0) fwd += e;
+      if ((a & 1) == 0) bits |= e << (a >> 1);
     }
-    R.sat[c] = m >= 5;
+    fwd = __popc(bits);
+    R.sat[c] = (uint8_t)(bits | (uint32_t)(m >= 5) << 3);
     R.cnt[c] = 0;
     ns = pairs6(w);
   }
@@ -208,6 +210,42 @@ __global__ void k_nhb_mark(const ReplicaDesc* __restrict__ reps, ReplicaState* _
   }
 }
 
+// One cell's turn in the greedy count (GW:2064-2099): its x+, y+ and z+ bonds in that order.
+// m: bits 0..2 the matched bonds, bit 3 the cell is marked; own: its count so far (including the
+// x bond from the cell before it); nx/y/z: mark and count of the cell at the other end. Returns
+// what the x+ bond adds to the next cell's count (1 when accepted and that cell is marked).
+__device__ __forceinline__ uint32_t nhb_turn(uint32_t m, uint32_t& own, uint32_t nx_sat, uint32_t nx_cnt,
+                                             uint32_t y_sat, uint32_t& y_cnt, uint32_t z_sat,
+                                             uint32_t& z_cnt, uint32_t& refused) {
+  const uint32_t si = (m >> 3) & 1u;
+  uint32_t out = 0;
+  if (m & 1u) {
+    if ((!si || own < 4) && (!nx_sat || nx_cnt < 4)) {
+      own += si;
+      out = nx_sat;
+    } else {
+      ++refused;
+    }
+  }
+  if (m & 2u) {
+    if ((!si || own < 4) && (!y_sat || y_cnt < 4)) {
+      own += si;
+      y_cnt += y_sat;
+    } else {
+      ++refused;
+    }
+  }
+  if (m & 4u) {
+    if ((!si || own < 4) && (!z_sat || z_cnt < 4)) {
+      own += si;
+      z_cnt += z_sat;
+    } else {
+      ++refused;
+    }
+  }
+  return out;
+}
+
 // The greedy count in typewriter order as a wavefront over rows. Row (y, z) touches the cells
 // of rows (y, z), (y+1, z) and (y, z+1) (mod L). Wave t holds the rows with y + 2z = t: rows of
 // one wave share no row they touch, and of two bonds that share a cell the one earlier in the
@@ -215,9 +253,16 @@ __global__ void k_nhb_mark(const ReplicaDesc* __restrict__ reps, ReplicaState* _
 // bond comes from wave t-1 or, wrapped, a later wave; its backward z bond from wave t-2 or,
 // wrapped, a later wave). So 3L - 2 waves, each row replayed along x, give exactly the
 // sequential result. One warp per row: the lanes load the row's matched forward bonds, the
-// marks and the counts of the three rows it touches into shared memory, lane 0 replays the
-// row, the lanes store the counts back. Refused bonds are subtracted from the replica's slots
-// (modulo 2^64, exact).
+// marks and the counts of the three rows it touches into shared memory, replay the row, and
+// store the counts back. Refused bonds are subtracted from the replica's slots (modulo 2^64,
+// exact).
+//
+// Along the row only the x bonds chain the cells: what cell x's x+ bond adds to cell x+1's count
+// (0 or 1) is a function of what cell x-1's added to cell x's, and the y and z partners are
+// distinct cells. So each lane takes ceil(L/32) consecutive cells, evaluates that function for
+// both inputs over its cells, a warp scan composes the functions (exclusive, from 0 at x = 0),
+// and each lane replays its cells with the true input. The wrapped bond of x = L-1 meets cell 0
+// after cell 0's own turn, whose outcome does not depend on the chain.
 constexpr int kWaveWarps = 4;
 __global__ void __launch_bounds__(32 * kWaveWarps) k_nhb_wave(const ReplicaDesc* __restrict__ reps,
                                                              ReplicaState* __restrict__ st, int nrep, int t) {
@@ -239,49 +284,69 @@ __global__ void __launch_bounds__(32 * kWaveWarps) k_nhb_wave(const ReplicaDesc*
   uint8_t* cnt0 = satZ + L;
   uint8_t* cntY = cnt0 + L;
   uint8_t* cntZ = cntY + L;
+  const uint32_t o0 = Lu * ((uint32_t)y + Lu * z), oY = Lu * (yp + Lu * z), oZ = Lu * ((uint32_t)y + Lu * zp);
+#pragma unroll 4
   for (int x = lane; x < L; x += 32) {
-    const uint32_t xu = (uint32_t)x, xn = x + 1 == L ? 0u : xu + 1;
-    const uint32_t w = word_at(R, xu, y, z);
-    uint32_t m = (uint32_t)(field(w, 0) == field(word_at(R, xn, y, z), 1)) |
-                 ((uint32_t)(field(w, 2) == field(word_at(R, xu, yp, z), 3)) << 1) |
-                 ((uint32_t)(field(w, 4) == field(word_at(R, xu, y, zp), 5)) << 2);
-    const uint32_t c = xu + Lu * ((uint32_t)y + Lu * z), cy = xu + Lu * (yp + Lu * z), cz = xu + Lu * ((uint32_t)y + Lu * zp);
-    m |= (uint32_t)R.sat[c] << 3;
-    msk[x] = (uint8_t)m;
-    satY[x] = R.sat[cy];
-    satZ[x] = R.sat[cz];
-    cnt0[x] = R.cnt[c];
-    cntY[x] = R.cnt[cy];
-    cntZ[x] = R.cnt[cz];
+    msk[x] = R.sat[o0 + x];
+    satY[x] = R.sat[oY + x] >> 3;
+    satZ[x] = R.sat[oZ + x] >> 3;
+    cnt0[x] = R.cnt[o0 + x];
+    cntY[x] = R.cnt[oY + x];
+    cntZ[x] = R.cnt[oZ + x];
   }
   __syncwarp();
-  if (lane == 0) {
-    unsigned long long refused = 0;
-    for (int x = 0; x < L; ++x) {
-      const uint32_t m = msk[x];
-      if (!(m & 7u)) continue;
-      const bool si = (m >> 3) & 1u;
-      for (int d = 0; d < 3; ++d) {
-        if (!((m >> d) & 1u)) continue;
-        const int xn = x + 1 == L ? 0 : x + 1;
-        const bool sj = d == 0 ? ((msk[xn] >> 3) & 1u) : (d == 1 ? satY[x] != 0 : satZ[x] != 0);
-        uint8_t* cj = d == 0 ? cnt0 + xn : (d == 1 ? cntY + x : cntZ + x);
-        if ((!si || cnt0[x] < 4) && (!sj || *cj < 4)) {
-          if (si) cnt0[x] = cnt0[x] + 1;
-          if (sj) *cj = *cj + 1;
-        } else {
-          ++refused;
-        }
-      }
+  const int per = (L + 31) >> 5;
+  const int x0 = min(L, lane * per), x1 = min(L, x0 + per);
+  uint32_t refused = 0, scratch = 0;
+  // cell 0 after its own turn, which the wrapped bond of x = L-1 meets
+  uint32_t c0 = cnt0[0];
+  if (L > 1) {
+    uint32_t yc = cntY[0], zc = cntZ[0];
+    nhb_turn(msk[0], c0, msk[1] >> 3, cnt0[1], satY[0], yc, satZ[0], zc, scratch);
+  }
+  // the count of cell x1 before the chain reaches it (lane + 1 overwrites it in the replay)
+  const uint32_t next_init = x1 < L ? cnt0[x1] : c0;
+  // this lane's cells as a function of the input: bit i = output for input i
+  uint32_t f = 0;
+#pragma unroll
+  for (uint32_t in = 0; in < 2; ++in) {
+    uint32_t cur = in;
+    for (int x = x0; x < x1; ++x) {
+      uint32_t own = cnt0[x] + cur, yc = cntY[x], zc = cntZ[x];
+      const bool last = x + 1 == L;
+      cur = nhb_turn(msk[x], own, msk[last ? 0 : x + 1] >> 3, last ? c0 : cnt0[x + 1], satY[x], yc,
+                     satZ[x], zc, scratch);
     }
-    if (refused) atomicAdd(&st[r].acc_slot[0][z & 31], 0ull - refused);
+    f |= cur << in;
   }
+  if (x0 == x1) f = 2u;  // no cells: the identity
+  // inclusive scan of the composition (earlier lanes' function applied first)
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t g = __shfl_up_sync(0xffffffffu, f, off);
+    if (lane >= off) f = ((f >> (g & 1u)) & 1u) | (((f >> ((g >> 1) & 1u)) & 1u) << 1);
+  }
+  const uint32_t before = __shfl_up_sync(0xffffffffu, f, 1);
+  uint32_t cur = lane == 0 ? 0u : (before & 1u);
+  __syncwarp();
+  for (int x = x0; x < x1; ++x) {
+    uint32_t own = cnt0[x] + cur, yc = cntY[x], zc = cntZ[x];
+    const bool last = x + 1 == L;
+    const uint32_t nc = last ? c0 : (x + 1 == x1 ? next_init : cnt0[x + 1]);
+    cur = nhb_turn(msk[x], own, msk[last ? 0 : x + 1] >> 3, nc, satY[x], yc, satZ[x], zc, refused);
+    cnt0[x] = (uint8_t)own;
+    cntY[x] = (uint8_t)yc;
+    cntZ[x] = (uint8_t)zc;
+  }
+  const uint32_t wrap = __shfl_sync(0xffffffffu, cur, (L - 1) / per);
+  if (lane == 0 && L > 1) cnt0[0] = (uint8_t)(cnt0[0] + wrap);
+  refused = __reduce_add_sync(0xffffffffu, refused);
+  if (lane == 0 && refused) atomicAdd(&st[r].acc_slot[0][z & 31], 0ull - (unsigned long long)refused);
   __syncwarp();
   for (int x = lane; x < L; x += 32) {
-    const uint32_t xu = (uint32_t)x;
-    R.cnt[xu + Lu * ((uint32_t)y + Lu * z)] = cnt0[x];
-    R.cnt[xu + Lu * (yp + Lu * z)] = cntY[x];
-    R.cnt[xu + Lu * ((uint32_t)y + Lu * zp)] = cntZ[x];
+    R.cnt[o0 + x] = cnt0[x];
+    R.cnt[oY + x] = cntY[x];
+    R.cnt[oZ + x] = cntZ[x];
   }
 }
 

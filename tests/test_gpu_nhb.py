@@ -62,6 +62,20 @@ def test_ordered_start_low_temperature(engine_lib, oracle_mod):
     eng.close()
 
 
+@pytest.mark.parametrize("L,T,start", [(34, 0.2, 2), (66, 0.5, 0), (96, 0.3, 2), (130, 0.4, 0)])
+def test_long_rows(engine_lib, oracle_mod, L, T, start):
+    # rows of more than 32 cells: each lane replays several cells (ragged at 34, 66, 130) and the
+    # chain of x bonds crosses lanes; the ordered starts mark most cells
+    eng, ora = pair(oracle_mod, L, T, 0.45, 77 + L, start)
+    assert_same(eng, ora)
+    for _ in range(2):
+        eng.run(2, 1, 0)
+        for _ in range(2):
+            ora.step(1, 0)
+        assert_same(eng, ora)
+    eng.close()
+
+
 def test_sampled_run_records(engine_lib, oracle_mod):
     eng, ora = pair(oracle_mod, 6, 0.5, 0.45, 4, 0)
     eng.run_sampled(12, 1, 0, 3)
