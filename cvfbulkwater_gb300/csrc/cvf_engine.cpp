@@ -61,6 +61,7 @@ struct cvf_handle {
   // cooperative launch per graph.
   int launch_mode = 0;
   void* staging = nullptr;  // pinned host buffer for configuration transfers (lazily allocated)
+  SampleRec* rec_pin = nullptr;  // pinned landing place of the record cvf_observables reads
   size_t staging_bytes = 0;
   // cvf_set_config / cvf_get_config: 1 = kernels read and pack, or unpack and write, the
   // caller's array in host memory (the GPU accesses pageable memory through the host page
@@ -617,6 +618,7 @@ int cvf_destroy(cvf_handle* h) {
   if (h->io_scratch) cudaFree(h->io_scratch);
   if (h->io_bad) cudaFree(h->io_bad);
   if (h->staging) cudaFreeHost(h->staging);
+  if (h->rec_pin) cudaFreeHost(h->rec_pin);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return 0;
@@ -841,10 +843,18 @@ int cvf_observables(cvf_handle* h, int r, cvf_obs* out) {
     launch_count_rebase(h->b, h->stream);
     h->count_valid = true;
   }
-  SampleRec last;  // only the 32-byte measurement record crosses to the host
-  CK(cudaMemcpyAsync(&last, (char*)(h->b.st + r) + offsetof(ReplicaState, last), sizeof(SampleRec),
+  if (!h->rec_pin) {
+    cudaError_t e = cudaHostAlloc((void**)&h->rec_pin, sizeof(SampleRec), cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+      h->rec_pin = nullptr;
+      return fail(CVF_ENOMEM, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+    }
+  }
+  // only the 32-byte measurement record crosses to the host, into page-locked memory
+  CK(cudaMemcpyAsync(h->rec_pin, (char*)(h->b.st + r) + offsetof(ReplicaState, last), sizeof(SampleRec),
                      cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  const SampleRec last = *h->rec_pin;
   const ReplicaHost& R = h->reps[r];
   fill_obs(out, last.n_hb2, last.n_sigma, last.r_cell, last.volume,
            host_evdw(last.r_cell, R.dist, R.freq, R.p.R_cutoff), R.N, R.p.P);
