@@ -46,7 +46,7 @@ struct ReplicaDesc {
   double beta, Jeff;
   unsigned long long thr_sweep[33];  // U < T, T in [0, 2^32]; index (dN_hb+1)*11 + dN_s+5
   // Sweep fast-path tables, read through L1 by the kernels:
-  //   tv[i] = 2*(T_i >> 16) + ((T_i & 0xffff) != 0) for the same index i;
+  //   tv[i] = 2*(T_i >> 16) + ((T_i & 0xffff) != 0) - 1 for the same index i (modulo 2^32);
   //   eta_tab[s*8 + p] = eta bits a cube in state s gives its vertex at offset p;
   //   nbmask[m] = 7 in every 3-bit field a whose bit a of the 6-bit mask m is set.
   uint32_t tv[33];

@@ -561,7 +561,8 @@ int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
     d.beta = r.thr.beta;
     d.Jeff = r.thr.Jeff;
     memcpy(d.thr_sweep, r.thr.sweep, sizeof(d.thr_sweep));
-    for (int i = 0; i < 33; ++i) d.tv[i] = 2u * (uint32_t)(r.thr.sweep[i] >> 16) + ((r.thr.sweep[i] & 0xffffull) != 0);
+    for (int i = 0; i < 33; ++i)
+      d.tv[i] = 2u * (uint32_t)(r.thr.sweep[i] >> 16) + ((r.thr.sweep[i] & 0xffffull) != 0) - 1u;
     for (int m = 0; m < 64; ++m) {
       uint32_t v = 0;
       for (int a = 0; a < 6; ++a)

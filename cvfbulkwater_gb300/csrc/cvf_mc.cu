@@ -626,7 +626,7 @@ struct EtaTables {
 // a warp's random lookups never conflict in a shared-memory bank.
 //   cnt[v]  4 at byte v (v = 0..5), zero for v = 6, 7: one arm of value v
 //   nbw[v]  44 at byte v (v = 0..5), zero for v = 6, 7 (7 marks an arm with eta = 0)
-//   tv[i]   2*(T_i >> 16) + ((T_i & 0xffff) != 0) for the threshold T_i of entry
+//   tv[i]   2*(T_i >> 16) + ((T_i & 0xffff) != 0) - 1 for the threshold T_i of entry
 //           i = 11*dN_hb + (h_new - h_old) + 17
 //   pk[i]   65536 dN_hb + dN_sigma of entry i (dN_sigma = h_new - h_old + 1): the change of the
 //           counts an accepted arm makes, for the running counts of cvf_observables
@@ -692,10 +692,10 @@ __device__ __forceinline__ const SweepTables* warp_sweep_tables(const ReplicaDes
 // terms come from byte selects on G = 4h + 44*[v == nb]: the selector v + 0x7770 picks byte v
 // with zeros above it, so G[new] - G[old] + 68 is the byte offset 4i into tv. The proposal's
 // selector is the high word of u*6 + (0x7770 << 32).
-// Accept is 2*hu + 2 <= tv for the 16-bit high half hu of the acceptance uniform; a tie
-// 2*hu + 1 == tv needs the low half. A tie makes the product of (tv - 2*hu - 1) over the six arms
-// zero; a product that wraps to zero without a tie only sends the cell through the exact path
-// as well, which decides every arm from the full 32-bit uniforms. A proposal equal to the old
+// With d = tv - 2*hu for the 16-bit high half hu of the acceptance uniform, accept is d >= 1; a
+// tie d == 0 needs the low half. A tie makes the product of d over the six arms zero; a product
+// that wraps to zero without a tie only sends the cell through the exact path as well, which
+// decides every arm from the full 32-bit uniforms. A proposal equal to the old
 // value lands on entry 17 (dN = 0), which always accepts and changes nothing.
 // kCount: dacc also receives the packed count changes (pk) of the accepted arms that change a value.
 template <bool kCount>
@@ -729,18 +729,18 @@ __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32
     const uint32_t word = a < 2 ? rr.y : (a < 4 ? rr.z : rr.w);
     const uint32_t hu = (a & 1) ? (word >> 16) : (word & 0xffffu);
     const int d = (int)(tv - 2u * hu);
-    tprod *= (uint32_t)(d - 1);
+    tprod *= (uint32_t)d;
     const uint2 cn = wt->cnt[sn - 0x7770u], co = wt->cnt[o];
     const uint32_t dw = (sn - 0x7770u - o) << (3 * a);
     if (kCount) {
       const int32_t pk = dw ? *reinterpret_cast<const int32_t*>(pkb + off) : 0;
-      asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %4, 2;\n\t@p add.u32 %0, %0, %5;\n\t@p add.u32 %1, %1, %6;"
+      asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %4, 1;\n\t@p add.u32 %0, %0, %5;\n\t@p add.u32 %1, %1, %6;"
           "\n\t@p sub.u32 %1, %1, %7;\n\t@p add.u32 %2, %2, %8;\n\t@p sub.u32 %2, %2, %9;"
           "\n\t@p add.u32 %3, %3, %10;\n\t}"
           : "+r"(w), "+r"(hx), "+r"(hy), "+r"(cacc)
           : "r"(d), "r"(dw), "r"(cn.x), "r"(co.x), "r"(cn.y), "r"(co.y), "r"(pk));
     } else {
-      asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %3, 2;\n\t@p add.u32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;"
+      asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %3, 1;\n\t@p add.u32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;"
           "\n\t@p sub.u32 %1, %1, %6;\n\t@p add.u32 %2, %2, %7;\n\t@p sub.u32 %2, %2, %8;\n\t}"
           : "+r"(w), "+r"(hx), "+r"(hy)
           : "r"(d), "r"(dw), "r"(cn.x), "r"(co.x), "r"(cn.y), "r"(co.y));
