@@ -509,9 +509,11 @@ def run_engine(args):
     dist.barrier()
     t0 = time.perf_counter()
     lat2.set_config(host_cfg)
+    ta = time.perf_counter()
     for _ in range(args.steps):
         lat2.run(1, 1, 0)
         lat2.observables()
+    tb = time.perf_counter()
     out_cfg = lat2.get_config(out=out_buf)
     t1 = time.perf_counter()
     e2e_s = dist.max(t1 - t0)
@@ -519,6 +521,8 @@ def run_engine(args):
     e2e = {"value": round(world * N * args.steps / (e2e_s * 1e9), 4), "unit": "site-updates/ns",
            "h2d_bytes_per_step": int(round(packed / args.steps)),
            "d2h_bytes_per_step": int(round(packed / args.steps)) + 32,
+           "upload_ms": round(1e3 * (ta - t0), 3), "steps_ms": round(1e3 * (tb - ta), 3),
+           "download_ms": round(1e3 * (t1 - tb), 3),
            "note": "per step: cvf_run_steps(1 step) + cvf_observables (measurement, 32 B D2H, sync); "
                    "lattice upload (cvf_set_config: the caller's 805 MB cells12 array read and packed "
                    "by the GPU in host memory, io_mode 1) and download (cvf_get_config: unpacked by the "

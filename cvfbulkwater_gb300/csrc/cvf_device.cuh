@@ -133,6 +133,9 @@ struct BatchDev {
   int* blk_site4;       // one thread per 4 arm sites
   int* blk_cell4;       // one thread per 4 cell words
   int nblk_sweep, nblk_cube, nblk_cubev, nblk_cell, nblk_site, nblk_site4, nblk_cell4;
+  int vec_count;        // tile of the counting sweep: vec, at most 4 (8 would spill registers)
+  int* blk_sweep_count; // its block prefix table
+  int nblk_sweep_count;
   int max_L;            // largest edge among the replicas
   GridSync* gsync;      // device barrier state of the persistent step kernel
   CorrState* corr;      // device array [nrep] of correlators (null until enabled)

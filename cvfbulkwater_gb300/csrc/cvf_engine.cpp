@@ -179,8 +179,9 @@ static int build_tables(cvf_handle* h, int force_vec = 0) {
 // Block prefix tables of replicas [r0, r1) (a new device allocation) into b.
 static int fill_tables(cvf_handle* h, int r0, int r1, int vec, BatchDev& b) {
   const int n = r1 - r0;
-  std::vector<int> ts(n + 1), tc(n + 1), tcv(n + 1), tl(n + 1), tsi(n + 1), ts4(n + 1), tl4(n + 1);
-  ts[0] = tc[0] = tcv[0] = tl[0] = tsi[0] = ts4[0] = tl4[0] = 0;
+  const int vec_count = vec < 4 ? vec : 4;
+  std::vector<int> ts(n + 1), tc(n + 1), tcv(n + 1), tl(n + 1), tsi(n + 1), ts4(n + 1), tl4(n + 1), tsc(n + 1);
+  ts[0] = tc[0] = tcv[0] = tl[0] = tsi[0] = ts4[0] = tl4[0] = tsc[0] = 0;
   auto blocks = [](long long threads) { return (int)((threads + kThreads - 1) / kThreads); };
   for (int i = 0; i < n; ++i) {
     const auto& r = h->reps[r0 + i];
@@ -192,9 +193,10 @@ static int fill_tables(cvf_handle* h, int r0, int r1, int vec, BatchDev& b) {
     tsi[i + 1] = tsi[i] + blocks(6 * r.N);
     ts4[i + 1] = ts4[i] + blocks(6 * r.N / 4);
     tl4[i + 1] = tl4[i] + blocks(r.N / 4);
+    tsc[i + 1] = tsc[i] + blocks((H / vec_count) * L * L);
   }
   int* d;
-  if (int rc = dev_alloc(h, (void**)&d, sizeof(int) * 7 * (n + 1))) return rc;
+  if (int rc = dev_alloc(h, (void**)&d, sizeof(int) * 8 * (n + 1))) return rc;
   std::vector<int> all;
   all.insert(all.end(), ts.begin(), ts.end());
   all.insert(all.end(), tc.begin(), tc.end());
@@ -203,6 +205,7 @@ static int fill_tables(cvf_handle* h, int r0, int r1, int vec, BatchDev& b) {
   all.insert(all.end(), ts4.begin(), ts4.end());
   all.insert(all.end(), tcv.begin(), tcv.end());
   all.insert(all.end(), tl4.begin(), tl4.end());
+  all.insert(all.end(), tsc.begin(), tsc.end());
   CK(cudaMemcpy(d, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
   b.blk_sweep = d;
   b.blk_cube = d + (n + 1);
@@ -211,6 +214,9 @@ static int fill_tables(cvf_handle* h, int r0, int r1, int vec, BatchDev& b) {
   b.blk_site4 = d + 4 * (n + 1);
   b.blk_cubev = d + 5 * (n + 1);
   b.blk_cell4 = d + 6 * (n + 1);
+  b.blk_sweep_count = d + 7 * (n + 1);
+  b.vec_count = vec_count;
+  b.nblk_sweep_count = tsc[n];
   b.nblk_cell4 = tl4[n];
   b.nblk_cubev = tcv[n];
   b.nblk_site4 = ts4[n];

@@ -1093,19 +1093,25 @@ void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStre
   else k_cube_volume<false><<<cube_blocks + vol_blocks, kThreads, 0, s>>>(b.reps, b.st, b.blk_cubev, b.nrep, cube_blocks);
 }
 
-template <bool kCount>
-static void launch_sweep_t(const BatchDev& b, int colour, int jsweep, cudaStream_t s) {
-  switch (b.vec) {
-    case 8: k_sweep<8, kCount><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    case 4: k_sweep<4, kCount><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    case 2: k_sweep<2, kCount><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    default: k_sweep<1, kCount><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-  }
-}
-
+// The counting sweep runs at most 4 cells per thread (its 8-cell tile spills registers under
+// the 3-blocks-per-SM bound and ran 2 us per step slower at L=256).
 void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, bool count) {
-  if (count) launch_sweep_t<true>(b, colour, jsweep, s);
-  else launch_sweep_t<false>(b, colour, jsweep, s);
+  if (count) {
+    const int n = b.nblk_sweep_count;
+    const int* blk = b.blk_sweep_count;
+    switch (b.vec_count) {
+      case 4: k_sweep<4, true><<<n, kThreads, 0, s>>>(b.reps, b.st, blk, b.nrep, colour, jsweep); break;
+      case 2: k_sweep<2, true><<<n, kThreads, 0, s>>>(b.reps, b.st, blk, b.nrep, colour, jsweep); break;
+      default: k_sweep<1, true><<<n, kThreads, 0, s>>>(b.reps, b.st, blk, b.nrep, colour, jsweep); break;
+    }
+    return;
+  }
+  switch (b.vec) {
+    case 8: k_sweep<8, false><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    case 4: k_sweep<4, false><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    case 2: k_sweep<2, false><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    default: k_sweep<1, false><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+  }
 }
 
 __global__ void k_count_read(ReplicaState* __restrict__ st, int nrep, int record) {

@@ -38,6 +38,24 @@ def test_read_after_every_step(engine_lib, oracle_mod, L, T, start):
     eng.close()
 
 
+@pytest.mark.parametrize("L", [32, 48])
+def test_eight_cell_tile(engine_lib, oracle_mod, L):
+    # a handle on the 8-cell sweep tile counts with the 4-cell tile and its own block table
+    eng, ora = pair(oracle_mod, L, 0.7, 0.45, 40 + L, 2)
+    assert eng.set_sweep_tile(8) == 8
+    for _ in range(12):
+        eng.run(1, 1, 0)
+        ora.step(1, 0)
+        same_counts(eng, ora)
+    eng.run(3, 1, 0)  # plain 8-cell steps between reads
+    eng.run(2, 1, 0)
+    for _ in range(5):
+        ora.step(1, 0)
+    same_counts(eng, ora)
+    assert np.array_equal(eng.get_config(), ora.get_config())
+    eng.close()
+
+
 def test_through_the_exact_path(engine_lib, oracle_mod):
     # L=16 x 6 arms x 400 steps: some 150 arm decisions need the low half of the uniform
     eng, ora = pair(oracle_mod, 16, 0.6, 0.45, 77)
