@@ -1034,32 +1034,41 @@ int cvf_autotune(cvf_handle* h, int* vec_out) {
     cudaMemcpyAsync((char*)p + bytes / 2, r.desc.cells[1], bytes / 2, cudaMemcpyDeviceToDevice, h->stream);
     saved.push_back(p);
   }
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  int best = h->b.vec;
-  float best_ms = 1e30f;
+  // block tables of every candidate (block counts depend on the tile)
+  std::vector<BatchDev> tabs;
   for (int v : cands) {
-    if (int rc = build_tables(h, v)) {  // block counts depend on the tile
+    if (int rc = build_tables(h, v)) {
       for (void* q : saved) cudaFree(q);
       return rc;
     }
-    launch_sweep(h->b, 0, 0, h->stream);  // warm-up
-    launch_sweep(h->b, 1, 0, h->stream);
-    cudaEventRecord(e0, h->stream);
-    for (int i = 0; i < 5; ++i) {
-      launch_sweep(h->b, 0, i, h->stream);
-      launch_sweep(h->b, 1, i, h->stream);
-    }
-    cudaEventRecord(e1, h->stream);
-    cudaEventSynchronize(e1);
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms < best_ms) {
-      best_ms = ms;
-      best = v;
+    tabs.push_back(h->b);
+  }
+  // three interleaved rounds, the best time of each candidate: tiles within a few per cent of
+  // each other are not told apart by one timing taken after another
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  std::vector<float> cand_ms(cands.size(), 1e30f);
+  for (int round = 0; round < 3; ++round) {
+    for (size_t c = 0; c < cands.size(); ++c) {
+      launch_sweep(tabs[c], 0, 0, h->stream);  // warm-up
+      launch_sweep(tabs[c], 1, 0, h->stream);
+      cudaEventRecord(e0, h->stream);
+      for (int i = 0; i < 5; ++i) {
+        launch_sweep(tabs[c], 0, i, h->stream);
+        launch_sweep(tabs[c], 1, i, h->stream);
+      }
+      cudaEventRecord(e1, h->stream);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      cand_ms[c] = std::min(cand_ms[c], ms);
     }
   }
+  size_t bi = 0;
+  for (size_t c = 1; c < cands.size(); ++c)
+    if (cand_ms[c] < cand_ms[bi]) bi = c;
+  const int best = cands.empty() ? h->b.vec : cands[bi];
   for (size_t i = 0; i < h->reps.size(); ++i) {
     auto& r = h->reps[i];
     size_t bytes = (size_t)r.N * sizeof(uint32_t);
@@ -1071,9 +1080,9 @@ int cvf_autotune(cvf_handle* h, int* vec_out) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (e != cudaSuccess) return fail(CVF_ECUDA, std::string("autotune: ") + cudaGetErrorString(e));
-  // the sweep blocks depend on the tile: rebuild the block tables and drop captured graphs
+  // the sweep blocks depend on the tile: keep the chosen tables and drop captured graphs
   drop_graphs(h);
-  if (int rc = build_tables(h, best)) return rc;
+  if (!tabs.empty()) h->b = tabs[bi];
   if (vec_out) *vec_out = best;
   return 0;
 }
