@@ -541,12 +541,16 @@ def run_engine(args):
     t0 = time.perf_counter()
     lat2.set_config(host_cfg)
     lat2.clear_samples()
+    ta = time.perf_counter()
     lat2.run_sampled(args.steps, 1, 0, 1)
     smp = lat2.samples()
+    tb = time.perf_counter()
     out_cfg = lat2.get_config(out=out_buf)
     t1 = time.perf_counter()
     e2e_sampled = {"value": round(world * N * args.steps / (dist.max(t1 - t0) * 1e9), 4),
                    "unit": "site-updates/ns", "records": int(len(smp)),
+                   "upload_ms": round(1e3 * (ta - t0), 3), "steps_ms": round(1e3 * (tb - ta), 3),
+                   "download_ms": round(1e3 * (t1 - tb), 3),
                    "note": "cvf_set_config, cvf_run_sampled(K steps, a record after every step), "
                            "cvf_get_samples, cvf_get_config"}
     del out_cfg

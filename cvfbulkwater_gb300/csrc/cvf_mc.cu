@@ -338,8 +338,10 @@ __device__ __forceinline__ void fill_cube_tables(const ReplicaDesc& R, CubeTable
 
 // GW:3374-3466. One thread per VC consecutive cubes along x of one parity (both parities in one
 // launch: cubes share no edge and sigma is frozen, so all cube decisions are independent). The
-// block's half of the replica's blocks in the table blk (blk_cubev) gives the parity: even
-// origins (2a,2b,2c) first, then odd origins (2a+1,2b+1,2c+1). Vertex p = dx | dy<<1 | dz<<2 of
+// parity of the block's index among the replica's blocks in the table blk (blk_cubev) is the
+// cubes' parity, even origins (2a,2b,2c) or odd origins (2a+1,2b+1,2c+1), and block pairs 2i,
+// 2i+1 take the same chunk of each: the two reads of every cell (one per cube containing it)
+// come close together, the second from L2. Vertex p = dx | dy<<1 | dz<<2 of
 // cube (a,b,c) has colour (parity + popc(p)) & 1 and word (x>>1) + H*(y + L*z), which is a for
 // every vertex except dx = 1 of an odd cube (a + 1, wrapping at the row end): the VC cubes read
 // each vertex row with one VC-word access, the odd dx = 1 rows with one more word. Their VC state
@@ -350,10 +352,9 @@ template <int VC>
 __device__ __forceinline__ void cube_move_v(const ReplicaDesc& R, const CubeTables* ct, const int* __restrict__ blk,
                                             int r, int vb, uint32_t t, int& cdh) {
   const uint32_t L = R.L, H = R.H, cpr = H / VC;
-  const int b0 = __ldg(blk + r), half = (__ldg(blk + r + 1) - b0) >> 1;
-  const int lb = vb - b0;
-  const uint32_t par = lb >= half;
-  const uint32_t qi = (uint32_t)(lb - (int)par * half) * blockDim.x + threadIdx.x;
+  const int lb = vb - __ldg(blk + r);
+  const uint32_t par = (uint32_t)lb & 1u;
+  const uint32_t qi = (uint32_t)(lb >> 1) * blockDim.x + threadIdx.x;
   if (qi >= cpr * H * H) return;
   uint32_t seg, bc, b, c;
   divmod32(qi, cpr, R.lgH >= 0 ? R.lgH - Log2V<VC>::v : -1, bc, seg);
@@ -437,26 +438,28 @@ __device__ __forceinline__ void count_accumulate(ReplicaState& S, int vb, int dn
   }
 }
 
-// Cube moves of every replica, then (blocks at and after nblk_cube) the volume move of replica
-// (block - nblk_cube), both with the counters of the current step.
+// The volume move of replica b for the first nvol blocks b (one warp each: scheduled first, they
+// run beside the cube blocks), then the cube moves of every replica, both with the counters of the
+// current step.
 template <bool kCount>
 __global__ void __launch_bounds__(kThreads, 4) k_cube_volume(const ReplicaDesc* __restrict__ reps,
                                                           ReplicaState* __restrict__ st,
-                                                          const int* __restrict__ blk, int nrep, int nblk_cube) {
-  if ((int)blockIdx.x >= nblk_cube) {
-    const int r = blockIdx.x - nblk_cube;
+                                                          const int* __restrict__ blk, int nrep, int nvol) {
+  if ((int)blockIdx.x < nvol) {
+    const int r = blockIdx.x;
     if (threadIdx.x < 32 && r < nrep) volume_move_warp(reps[r], st[r], st[r].cur[2]);
     return;
   }
   __shared__ CubeTables s_ct[kThreads / 32];
-  const int r = find_replica(blk, nrep, blockIdx.x);
+  const int vb = (int)blockIdx.x - nvol;
+  const int r = find_replica(blk, nrep, vb);
   const ReplicaDesc& R = reps[r];
   CubeTables* ct = s_ct + (threadIdx.x >> 5);
   fill_cube_tables(R, ct, threadIdx.x & 31);
   __syncwarp();
   int cdh = 0;
-  cube_move(R, ct, blk, r, blockIdx.x, st[r].cur[1], cdh);
-  if (kCount) count_accumulate(st[r], blockIdx.x, cdh, 0);
+  cube_move(R, ct, blk, r, vb, st[r].cur[1], cdh);
+  if (kCount) count_accumulate(st[r], vb, cdh, 0);
 }
 
 // ------------------------------------------------------------------ checkerboard sweep
@@ -1089,8 +1092,8 @@ void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStre
   const int cube_blocks = do_cubes ? b.nblk_cubev : 0;
   const int vol_blocks = do_volume ? b.nrep : 0;
   if (cube_blocks + vol_blocks == 0) return;
-  if (count) k_cube_volume<true><<<cube_blocks + vol_blocks, kThreads, 0, s>>>(b.reps, b.st, b.blk_cubev, b.nrep, cube_blocks);
-  else k_cube_volume<false><<<cube_blocks + vol_blocks, kThreads, 0, s>>>(b.reps, b.st, b.blk_cubev, b.nrep, cube_blocks);
+  if (count) k_cube_volume<true><<<cube_blocks + vol_blocks, kThreads, 0, s>>>(b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks);
+  else k_cube_volume<false><<<cube_blocks + vol_blocks, kThreads, 0, s>>>(b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks);
 }
 
 // The counting sweep runs at most 4 cells per thread (its 8-cell tile spills registers under
