@@ -46,6 +46,15 @@ __device__ __forceinline__ int find_replica(const int* __restrict__ blk, int nre
   return lo;
 }
 
+// Programmatic dependent launch: the step's kernels are launched so that the next one may start
+// while the previous drains (launch_pdl). Each lets its dependents launch as soon as its own
+// blocks have started (pdl_trigger), and waits for the previous kernel's completion and memory
+// (pdl_wait) before it touches the state that kernel writes; what it does before the wait reads
+// only the descriptors and tables, which no kernel writes. Without a programmatic predecessor
+// the wait returns at once.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // n / d and n % d; shift >= 0 means d = 2^shift.
 __device__ __forceinline__ void divmod32(uint32_t n, uint32_t d, int shift, uint32_t& q, uint32_t& r) {
   if (shift >= 0) {
@@ -180,6 +189,8 @@ __global__ void k_init_cubes(const ReplicaDesc* __restrict__ reps, const int* __
 // One thread per replica: snapshot the move counters that this step's kernels use.
 __global__ void k_step_begin(ReplicaState* __restrict__ st, int nrep, int nmet, int ncl, int do_cube,
                              int do_volume, int zero_slots) {
+  pdl_trigger();
+  pdl_wait();
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrep) return;
   ReplicaState& S = st[r];
@@ -445,7 +456,9 @@ template <bool kCount>
 __global__ void __launch_bounds__(kThreads, 4) k_cube_volume(const ReplicaDesc* __restrict__ reps,
                                                           ReplicaState* __restrict__ st,
                                                           const int* __restrict__ blk, int nrep, int nvol) {
+  pdl_trigger();
   if ((int)blockIdx.x < nvol) {
+    pdl_wait();
     const int r = blockIdx.x;
     if (threadIdx.x < 32 && r < nrep) volume_move_warp(reps[r], st[r], st[r].cur[2]);
     return;
@@ -457,6 +470,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_cube_volume(const ReplicaDesc* 
   CubeTables* ct = s_ct + (threadIdx.x >> 5);
   fill_cube_tables(R, ct, threadIdx.x & 31);
   __syncwarp();
+  pdl_wait();
   int cdh = 0;
   cube_move(R, ct, blk, r, vb, st[r].cur[1], cdh);
   if (kCount) count_accumulate(st[r], vb, cdh, 0);
@@ -820,10 +834,12 @@ template <int V, bool kCount>
 __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const ReplicaDesc* __restrict__ reps,
                                                     ReplicaState* __restrict__ st,
                                                     const int* __restrict__ blk, int nrep, int colour, int jsweep) {
+  pdl_trigger();
   __shared__ SweepTables s_tab[kThreads / 32];
   const int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   const SweepTables* wt = warp_sweep_tables(R, s_tab);
+  pdl_wait();
   uint32_t hb2 = 0, ns = 0;
   int32_t dacc = 0;
   sweep_segment<V, false, kCount>(R, wt, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
@@ -1065,6 +1081,21 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_run(BatchDev
 // ------------------------------------------------------------------ launchers
 static inline dim3 grid1(int n) { return dim3((unsigned)((n + kThreads - 1) / kThreads)); }
 
+// Launch that may overlap the previous kernel in the stream (programmatic dependent launch).
+template <typename... P, typename... A>
+static void launch_pdl(void (*kernel)(P...), dim3 grid, cudaStream_t s, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(kThreads);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, ((P)args)...);
+}
+
 void launch_init_lattice(const BatchDev& b, cudaStream_t s) {
   k_init_sigma<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.blk_cell, b.nrep);
   k_init_cubes<<<b.nblk_cube, kThreads, 0, s>>>(b.reps, b.blk_cube, b.nrep);
@@ -1072,7 +1103,7 @@ void launch_init_lattice(const BatchDev& b, cudaStream_t s) {
 
 void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do_volume, cudaStream_t s,
                        int zero_slots) {
-  k_step_begin<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, nmet, ncl, do_cube, do_volume, zero_slots);
+  launch_pdl(k_step_begin, grid1(b.nrep), s, b.st, b.nrep, nmet, ncl, do_cube, do_volume, zero_slots);
 }
 
 void launch_sweep_measure(const BatchDev& b, int jsweep, cudaStream_t s) {
@@ -1092,8 +1123,9 @@ void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStre
   const int cube_blocks = do_cubes ? b.nblk_cubev : 0;
   const int vol_blocks = do_volume ? b.nrep : 0;
   if (cube_blocks + vol_blocks == 0) return;
-  if (count) k_cube_volume<true><<<cube_blocks + vol_blocks, kThreads, 0, s>>>(b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks);
-  else k_cube_volume<false><<<cube_blocks + vol_blocks, kThreads, 0, s>>>(b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks);
+  const dim3 grid((unsigned)(cube_blocks + vol_blocks));
+  if (count) launch_pdl(k_cube_volume<true>, grid, s, b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks);
+  else launch_pdl(k_cube_volume<false>, grid, s, b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks);
 }
 
 // The counting sweep runs at most 4 cells per thread (its 8-cell tile spills registers under
@@ -1102,18 +1134,20 @@ void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, boo
   if (count) {
     const int n = b.nblk_sweep_count;
     const int* blk = b.blk_sweep_count;
+    const dim3 g((unsigned)n);
     switch (b.vec_count) {
-      case 4: k_sweep<4, true><<<n, kThreads, 0, s>>>(b.reps, b.st, blk, b.nrep, colour, jsweep); break;
-      case 2: k_sweep<2, true><<<n, kThreads, 0, s>>>(b.reps, b.st, blk, b.nrep, colour, jsweep); break;
-      default: k_sweep<1, true><<<n, kThreads, 0, s>>>(b.reps, b.st, blk, b.nrep, colour, jsweep); break;
+      case 4: launch_pdl(k_sweep<4, true>, g, s, b.reps, b.st, blk, b.nrep, colour, jsweep); break;
+      case 2: launch_pdl(k_sweep<2, true>, g, s, b.reps, b.st, blk, b.nrep, colour, jsweep); break;
+      default: launch_pdl(k_sweep<1, true>, g, s, b.reps, b.st, blk, b.nrep, colour, jsweep); break;
     }
     return;
   }
+  const dim3 g((unsigned)b.nblk_sweep);
   switch (b.vec) {
-    case 8: k_sweep<8, false><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    case 4: k_sweep<4, false><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    case 2: k_sweep<2, false><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    default: k_sweep<1, false><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    case 8: launch_pdl(k_sweep<8, false>, g, s, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    case 4: launch_pdl(k_sweep<4, false>, g, s, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    case 2: launch_pdl(k_sweep<2, false>, g, s, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    default: launch_pdl(k_sweep<1, false>, g, s, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
   }
 }
 
