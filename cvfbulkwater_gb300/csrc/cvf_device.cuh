@@ -137,6 +137,7 @@ struct BatchDev {
   int* blk_sweep_count; // its block prefix table
   int nblk_sweep_count;
   int max_L;            // largest edge among the replicas
+  int pdl;              // launch the step's kernels as programmatic dependents (launch_pdl)
   GridSync* gsync;      // device barrier state of the persistent step kernel
   CorrState* corr;      // device array [nrep] of correlators (null until enabled)
 };
@@ -196,5 +197,32 @@ cudaError_t launch_pack_config(const ReplicaDesc& R, const int* c12, uint32_t* c
 // array is not aligned.
 cudaError_t launch_unpack_config(const ReplicaDesc& R, int* c12, cudaStream_t s);
 void launch_cluster_stats_impl(const BatchDev& b, unsigned long long* blocktop, int record, cudaStream_t s);
+
+#ifdef __CUDACC__
+// Programmatic dependent launch: kernels of a chain are launched so that the next one may start
+// while the previous drains (launch_pdl). Each lets its dependents launch as soon as its own
+// blocks have started (pdl_trigger), and waits for the previous kernel's completion and memory
+// (pdl_wait) before it touches the state that kernel writes; what it does before the wait reads
+// only the descriptors and tables, which no kernel writes. Without a programmatic predecessor
+// the wait returns at once.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// With pdl = 0 (chains captured on parallel branches, where blocks waiting early would hold SM
+// slots that the other branches' kernels could use) the launch is an ordinary one.
+template <typename... P, typename... A>
+static inline void launch_pdl(void (*kernel)(P...), dim3 grid, cudaStream_t s, int pdl, A... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(kThreads);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, ((P)args)...);
+}
+#endif
 
 }  // namespace cvf

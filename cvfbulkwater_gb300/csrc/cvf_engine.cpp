@@ -226,6 +226,7 @@ static int fill_tables(cvf_handle* h, int r0, int r1, int vec, BatchDev& b) {
   b.nblk_site = tsi[n];
   b.max_L = 0;
   for (int i = r0; i < r1; ++i) b.max_L = std::max(b.max_L, h->reps[i].L);
+  b.pdl = 1;
   return 0;
 }
 
@@ -268,6 +269,7 @@ static int build_groups(cvf_handle* h) {
       g.r1 = cut[k + 1];
       g.b = h->b;
       if (int rc = fill_tables(h, g.r0, g.r1, h->b.vec, g.b)) return rc;
+      g.b.pdl = 0;  // the groups' chains run side by side
       g.b.reps = h->b.reps + g.r0;
       g.b.st = h->b.st + g.r0;
       g.b.nrep = g.r1 - g.r0;

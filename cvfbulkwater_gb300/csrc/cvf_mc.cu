@@ -46,15 +46,6 @@ __device__ __forceinline__ int find_replica(const int* __restrict__ blk, int nre
   return lo;
 }
 
-// Programmatic dependent launch: the step's kernels are launched so that the next one may start
-// while the previous drains (launch_pdl). Each lets its dependents launch as soon as its own
-// blocks have started (pdl_trigger), and waits for the previous kernel's completion and memory
-// (pdl_wait) before it touches the state that kernel writes; what it does before the wait reads
-// only the descriptors and tables, which no kernel writes. Without a programmatic predecessor
-// the wait returns at once.
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-
 // n / d and n % d; shift >= 0 means d = 2^shift.
 __device__ __forceinline__ void divmod32(uint32_t n, uint32_t d, int shift, uint32_t& q, uint32_t& r) {
   if (shift >= 0) {
@@ -1081,21 +1072,6 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_run(BatchDev
 // ------------------------------------------------------------------ launchers
 static inline dim3 grid1(int n) { return dim3((unsigned)((n + kThreads - 1) / kThreads)); }
 
-// Launch that may overlap the previous kernel in the stream (programmatic dependent launch).
-template <typename... P, typename... A>
-static void launch_pdl(void (*kernel)(P...), dim3 grid, cudaStream_t s, A... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = dim3(kThreads);
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kernel, ((P)args)...);
-}
-
 void launch_init_lattice(const BatchDev& b, cudaStream_t s) {
   k_init_sigma<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.blk_cell, b.nrep);
   k_init_cubes<<<b.nblk_cube, kThreads, 0, s>>>(b.reps, b.blk_cube, b.nrep);
@@ -1103,7 +1079,7 @@ void launch_init_lattice(const BatchDev& b, cudaStream_t s) {
 
 void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do_volume, cudaStream_t s,
                        int zero_slots) {
-  launch_pdl(k_step_begin, grid1(b.nrep), s, b.st, b.nrep, nmet, ncl, do_cube, do_volume, zero_slots);
+  launch_pdl(k_step_begin, grid1(b.nrep), s, b.pdl, b.st, b.nrep, nmet, ncl, do_cube, do_volume, zero_slots);
 }
 
 void launch_sweep_measure(const BatchDev& b, int jsweep, cudaStream_t s) {
@@ -1124,8 +1100,8 @@ void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStre
   const int vol_blocks = do_volume ? b.nrep : 0;
   if (cube_blocks + vol_blocks == 0) return;
   const dim3 grid((unsigned)(cube_blocks + vol_blocks));
-  if (count) launch_pdl(k_cube_volume<true>, grid, s, b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks);
-  else launch_pdl(k_cube_volume<false>, grid, s, b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks);
+  if (count) launch_pdl(k_cube_volume<true>, grid, s, b.pdl, b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks);
+  else launch_pdl(k_cube_volume<false>, grid, s, b.pdl, b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks);
 }
 
 // The counting sweep runs at most 4 cells per thread (its 8-cell tile spills registers under
@@ -1136,18 +1112,18 @@ void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, boo
     const int* blk = b.blk_sweep_count;
     const dim3 g((unsigned)n);
     switch (b.vec_count) {
-      case 4: launch_pdl(k_sweep<4, true>, g, s, b.reps, b.st, blk, b.nrep, colour, jsweep); break;
-      case 2: launch_pdl(k_sweep<2, true>, g, s, b.reps, b.st, blk, b.nrep, colour, jsweep); break;
-      default: launch_pdl(k_sweep<1, true>, g, s, b.reps, b.st, blk, b.nrep, colour, jsweep); break;
+      case 4: launch_pdl(k_sweep<4, true>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep); break;
+      case 2: launch_pdl(k_sweep<2, true>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep); break;
+      default: launch_pdl(k_sweep<1, true>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep); break;
     }
     return;
   }
   const dim3 g((unsigned)b.nblk_sweep);
   switch (b.vec) {
-    case 8: launch_pdl(k_sweep<8, false>, g, s, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    case 4: launch_pdl(k_sweep<4, false>, g, s, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    case 2: launch_pdl(k_sweep<2, false>, g, s, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    default: launch_pdl(k_sweep<1, false>, g, s, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    case 8: launch_pdl(k_sweep<8, false>, g, s, b.pdl, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    case 4: launch_pdl(k_sweep<4, false>, g, s, b.pdl, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    case 2: launch_pdl(k_sweep<2, false>, g, s, b.pdl, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    default: launch_pdl(k_sweep<1, false>, g, s, b.pdl, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
   }
 }
 

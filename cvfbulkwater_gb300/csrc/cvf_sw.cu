@@ -72,6 +72,7 @@ __device__ __forceinline__ uint32_t eta_of_cell(const ReplicaDesc& R, int x, int
 __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __restrict__ reps,
                                                        const ReplicaState* __restrict__ st,
                                                        const int* __restrict__ blk, int nrep, int jsw) {
+  pdl_trigger();
   const int r = find_replica_sw(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   const int L = R.L;
@@ -80,6 +81,7 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
   if (c >= N) return;
   int x, y, z;
   cell_xyz(R, c, x, y, z);
+  pdl_wait();
   const uint32_t t = st[r].cur[3] + (uint32_t)jsw;
   const uint32_t w = word_at(R, x, y, z);
   uint32_t rw[20];
@@ -169,12 +171,14 @@ __device__ __forceinline__ bool uf_unite(int32_t* p, int32_t a, int32_t b) {
 __global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __restrict__ reps,
                                                        ReplicaState* __restrict__ st,
                                                        const int* __restrict__ blk, int nrep) {
+  pdl_trigger();
   const int r = find_replica_sw(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   const uint32_t L = R.L;
   const uint32_t N = L * L * L;
   const uint32_t c = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
   if (c >= N) return;
+  pdl_wait();
   uint32_t hb = R.hbmask[c];
   if (!hb) return;
   int xi, yi, zi;
@@ -197,12 +201,14 @@ __global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __rest
 __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __restrict__ reps,
                                                         const ReplicaState* __restrict__ st,
                                                         const int* __restrict__ blk, int nrep, int jsw) {
+  pdl_trigger();
   const int r = find_replica_sw(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   const int L = R.L;
   const uint32_t N = (uint32_t)L * L * L;
   const uint32_t c = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
   if (c >= N) return;
+  pdl_wait();
   const uint32_t t = st[r].cur[3] + (uint32_t)jsw;
   int32_t roots[6];
 #pragma unroll
@@ -419,9 +425,10 @@ __global__ void k_cs_begin(ReplicaState* __restrict__ st, int nrep) {
 
 // ---------------------------------------------------------------- launchers
 void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s) {
-  k_sw_local<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.st, b.blk_cell, b.nrep, jsw);
-  k_sw_union<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.st, b.blk_cell, b.nrep);
-  k_sw_finish<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.st, b.blk_cell, b.nrep, jsw);
+  const dim3 g((unsigned)b.nblk_cell);
+  launch_pdl(k_sw_local, g, s, b.pdl, b.reps, b.st, b.blk_cell, b.nrep, jsw);
+  launch_pdl(k_sw_union, g, s, b.pdl, b.reps, b.st, b.blk_cell, b.nrep);
+  launch_pdl(k_sw_finish, g, s, b.pdl, b.reps, b.st, b.blk_cell, b.nrep, jsw);
 }
 
 // Needs csize zeroed and cover zeroed by the caller (memset nodes); blocktop sized 2*nblk_site.
