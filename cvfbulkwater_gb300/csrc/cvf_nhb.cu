@@ -86,15 +86,9 @@ __global__ void k_nhb_init(const ReplicaDesc* __restrict__ reps, const int* __re
   R.nhb[c] = (uint8_t)acc;
 }
 
-// One (colour, arm) pass of the sweep; thread = colour word q (N/2 per replica).
-__global__ void k_nhb_sweep(const ReplicaDesc* __restrict__ reps, const ReplicaState* __restrict__ st,
-                            const int* __restrict__ blk, int nrep, int colour, int a, int jsweep) {
-  const int r = rep_of(blk, nrep, blockIdx.x);
-  const ReplicaDesc& R = reps[r];
-  const uint32_t L = R.L, H = R.H, half = L * L * H;
-  const uint32_t q = (uint32_t)(blockIdx.x - __ldg(blk + r)) * blockDim.x + threadIdx.x;
-  if (q >= half) return;
-  const uint32_t t = st[r].cur[0] + (uint32_t)jsweep;
+// Arm a of colour word q of replica R with sweep counter t.
+__device__ __forceinline__ void nhb_update(const ReplicaDesc& R, uint32_t q, int colour, int a, uint32_t t) {
+  const uint32_t L = R.L, H = R.H;
   const uint32_t hx = q % H, yz = q / H, y = yz % L, z = yz / L;
   const Cell p{2 * hx + ((y + z + (uint32_t)colour) & 1u), y, z};
   const uint32_t c0 = nat(p, L);
@@ -145,6 +139,20 @@ __global__ void k_nhb_sweep(const ReplicaDesc* __restrict__ reps, const ReplicaS
     R.nhb[c0] = (uint8_t)(ni + dn);
     R.nhb[j] = (uint8_t)(nj + dn);
   }
+}
+
+// One (colour, arm) pass of the sweep: thread = colour words q and q + N/4 of its replica (the
+// N/2 words of the colour; blk is the table of N/4 threads per replica).
+__global__ void k_nhb_sweep(const ReplicaDesc* __restrict__ reps, const ReplicaState* __restrict__ st,
+                            const int* __restrict__ blk, int nrep, int colour, int a, int jsweep) {
+  const int r = rep_of(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  const uint32_t quarter = (uint32_t)R.L * R.L * R.H / 2;
+  const uint32_t q = (uint32_t)(blockIdx.x - __ldg(blk + r)) * blockDim.x + threadIdx.x;
+  if (q >= quarter) return;
+  const uint32_t t = st[r].cur[0] + (uint32_t)jsweep;
+  nhb_update(R, q, colour, a, t);
+  nhb_update(R, q + quarter, colour, a, t);
 }
 
 __global__ void k_nhb_begin(ReplicaState* __restrict__ st, int nrep) {
@@ -267,6 +275,7 @@ constexpr int kWaveWarps = 4;
 __global__ void __launch_bounds__(32 * kWaveWarps) k_nhb_wave(const ReplicaDesc* __restrict__ reps,
                                                              ReplicaState* __restrict__ st, int nrep, int t) {
   extern __shared__ uint8_t sm[];
+  pdl_trigger();
   const int r = blockIdx.y;
   if (r >= nrep) return;
   const ReplicaDesc& R = reps[r];
@@ -285,6 +294,7 @@ __global__ void __launch_bounds__(32 * kWaveWarps) k_nhb_wave(const ReplicaDesc*
   uint8_t* cntY = cnt0 + L;
   uint8_t* cntZ = cntY + L;
   const uint32_t o0 = Lu * ((uint32_t)y + Lu * z), oY = Lu * (yp + Lu * z), oZ = Lu * ((uint32_t)y + Lu * zp);
+  pdl_wait();
 #pragma unroll 4
   for (int x = lane; x < L; x += 32) {
     msk[x] = R.sat[o0 + x];
@@ -381,7 +391,7 @@ void launch_nhb_init(const BatchDev& b, int only, cudaStream_t s) {
 void launch_nhb_sweep(const BatchDev& b, int jsweep, cudaStream_t s) {
   for (int colour = 0; colour < 2; ++colour)
     for (int a = 0; a < 6; ++a)
-      k_nhb_sweep<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.st, b.blk_cell, b.nrep, colour, a, jsweep);
+      k_nhb_sweep<<<b.nblk_cell4, kThreads, 0, s>>>(b.reps, b.st, b.blk_cell4, b.nrep, colour, a, jsweep);
 }
 
 void launch_nhb_measure(const BatchDev& b, int record, cudaStream_t s) {
@@ -391,7 +401,19 @@ void launch_nhb_measure(const BatchDev& b, int record, cudaStream_t s) {
   const int rows = b.max_L / 2 + 1;
   const dim3 grid((rows + kWaveWarps - 1) / kWaveWarps, b.nrep);
   const size_t smem = (size_t)kWaveWarps * 6 * b.max_L;
-  for (int t = 0; t <= 3 * b.max_L - 3; ++t) k_nhb_wave<<<grid, 32 * kWaveWarps, smem, s>>>(b.reps, b.st, b.nrep, t);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(32 * kWaveWarps);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  for (int t = 0; t <= 3 * b.max_L - 3; ++t) {
+    cfg.numAttrs = t > 0 && b.pdl ? 1 : 0;  // each wave a programmatic dependent of the one before
+    cudaLaunchKernelEx(&cfg, k_nhb_wave, (const ReplicaDesc*)b.reps, b.st, b.nrep, t);
+  }
   k_nhb_finish<<<(b.nrep + 127) / 128, 128, 0, s>>>(b.st, b.nrep, record);
 }
 
