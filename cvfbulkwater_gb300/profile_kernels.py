@@ -7,7 +7,9 @@ and then --launches profiled repetitions of the chosen kind: a single kernel kin
 cvf_profile_launch (sweep = 2 launches per repetition), or whole steps (kind "step": cube +
 volume + sweep; kind "step_sw": cube + volume + one Swendsen-Wang step; --correlation adds
 the multi-tau correlator's histogram and update to every step).
-Prints the mean time per repetition measured with CUDA events on the engine's stream.
+Prints the mean time per repetition measured with CUDA events on the engine's stream. Kind
+"c2c" times the configuration transfers against plain copies over the host link, kind
+"h2d_scan" the 2-D reweighting search.
 """
 from __future__ import annotations
 
@@ -15,7 +17,7 @@ import argparse
 import ctypes as C
 
 KINDS = {"sweep": 0, "cube": 1, "volume": 2, "measure": 3}
-ANALYSIS = ("h2d_scan",)
+ANALYSIS = ("h2d_scan", "c2c")
 STEPS = {"step": (1, 0), "step_sw": (0, 1)}  # full MC steps: (Metropolis sweeps, SW steps)
 
 
@@ -43,6 +45,8 @@ def main():
     build.build()
     if a.kind == "h2d_scan":
         return h2d_scan(a)
+    if a.kind == "c2c":
+        return c2c(a)
     lat = Lattice(Params(L=a.L, T=a.T, P=a.P, seed=44648604, start=a.start, flag_chessboard=0 if a.nhb else 1))
     if a.mode is not None:
         lat.launch_mode = a.mode
@@ -104,6 +108,45 @@ def h2d_scan(a):
     dt = (time.perf_counter() - t0) / max(a.launches, 1)
     print(f"h2d_scan L={a.L} grid={H.n_bin2d}^2 rows={len(T) * len(S)} ms/search={dt * 1e3:.2f}")
     H.close()
+
+
+def c2c(a):
+    """The host link under the configuration transfers: a plain copy of an (L^3, 12) int32 array in
+    pageable host memory to and from the device (cudaMemcpy through torch), against
+    cvf_set_config / cvf_get_config of the same array (the GPU packing and unpacking it in place),
+    each the best of --launches repetitions after one untimed pass."""
+    import time
+
+    import numpy as np
+    import torch
+
+    from .engine import Lattice, Params
+    lat = Lattice(Params(L=a.L, T=a.T, P=a.P, seed=44648604, start=1))
+    cfg = lat.get_config()
+    buf = np.empty_like(cfg)
+    buf.fill(0)
+    nbytes = cfg.nbytes
+    host = torch.from_numpy(buf.reshape(-1))
+    dev = torch.empty(host.numel(), dtype=torch.int32, device="cuda")
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(max(a.launches, 1)):
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        return best
+
+    h2d = timed(lambda: dev.copy_(host))
+    d2h = timed(lambda: host.copy_(dev))
+    up = timed(lambda: lat.set_config(cfg))
+    down = timed(lambda: lat.get_config(out=buf))
+    for name, t in (("copy H2D", h2d), ("copy D2H", d2h), ("cvf_set_config", up), ("cvf_get_config", down)):
+        print(f"c2c L={a.L} {name}: {t * 1e3:.3f} ms, {nbytes / t / 1e9:.1f} GB/s of the {nbytes / 1e6:.0f} MB array")
+    lat.close()
 
 
 if __name__ == "__main__":
