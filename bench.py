@@ -132,15 +132,19 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(name):
-    """DRAM bytes per launch from a committed ncu summary under profiles/, if there is one."""
+def ncu_traffic(name, tile=None):
+    """DRAM bytes per launch from a committed ncu summary under profiles/ (the entry of the sweep
+    tile when the summary has one per tile), if there is one."""
     p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     try:
-        return json.load(open(p)).get("dram_bytes_per_launch")
+        d = json.load(open(p))
     except (ValueError, OSError):
         return None
+    if tile is not None and "by_tile" in d:
+        return d["by_tile"].get(str(tile), {}).get("dram_bytes_per_launch")
+    return d.get("dram_bytes_per_launch")
 
 
 def cpu_baseline_oracle(steps_cap=3, budget_s=30.0, threads=None):
@@ -566,7 +570,7 @@ def run_engine(args):
 
     peak, peak_kind = peaks()
     achieved = alg_bytes_launch / launch_s / 1e9
-    traffic = ncu_traffic("sweep_l256_traffic.json")
+    traffic = ncu_traffic("sweep_l256_traffic.json", tile)
     line = {
         "metric": "site-updates/ns at L=256", "value": round(value, 4), "unit": "site-updates/ns",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 5),
