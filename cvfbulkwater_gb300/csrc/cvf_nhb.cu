@@ -287,49 +287,49 @@ __global__ void __launch_bounds__(32 * kWaveWarps) k_nhb_wave(const ReplicaDesc*
   if (z > zhi) return;
   const int y = t - 2 * z;
   const uint32_t Lu = (uint32_t)L, yp = y + 1 == L ? 0 : y + 1, zp = z + 1 == L ? 0 : z + 1;
-  uint8_t* msk = sm + (size_t)warp * 6 * L;  // bits 0..2 matched x+, y+, z+ bonds, bit 3 marked
-  uint8_t* satY = msk + L;
-  uint8_t* satZ = satY + L;
-  uint8_t* cnt0 = satZ + L;
-  uint8_t* cntY = cnt0 + L;
-  uint8_t* cntZ = cntY + L;
+  // the warp's six rows of L bytes in shared memory, indexed from sm itself: bits 0..2 matched
+  // x+, y+, z+ bonds and bit 3 the mark of row (y, z); the marks of rows (y+1, z) and (y, z+1);
+  // the counts of the three rows
+  const int bM = warp * 6 * L, bSY = bM + L, bSZ = bSY + L, bC0 = bSZ + L, bCY = bC0 + L, bCZ = bCY + L;
+  const uint8_t* __restrict__ gsat = R.sat;
+  uint8_t* __restrict__ gcnt = R.cnt;
   const uint32_t o0 = Lu * ((uint32_t)y + Lu * z), oY = Lu * (yp + Lu * z), oZ = Lu * ((uint32_t)y + Lu * zp);
   pdl_wait();
 #pragma unroll 4
   for (int x = lane; x < L; x += 32) {
-    msk[x] = R.sat[o0 + x];
-    satY[x] = R.sat[oY + x] >> 3;
-    satZ[x] = R.sat[oZ + x] >> 3;
-    cnt0[x] = R.cnt[o0 + x];
-    cntY[x] = R.cnt[oY + x];
-    cntZ[x] = R.cnt[oZ + x];
+    const uint8_t m = gsat[o0 + x], sy = gsat[oY + x], sz = gsat[oZ + x];
+    const uint8_t c0v = __ldcg(gcnt + o0 + x), cyv = __ldcg(gcnt + oY + x), czv = __ldcg(gcnt + oZ + x);
+    sm[bM + x] = m;
+    sm[bSY + x] = sy >> 3;
+    sm[bSZ + x] = sz >> 3;
+    sm[bC0 + x] = c0v;
+    sm[bCY + x] = cyv;
+    sm[bCZ + x] = czv;
   }
   __syncwarp();
   const int per = (L + 31) >> 5;
   const int x0 = min(L, lane * per), x1 = min(L, x0 + per);
   uint32_t refused = 0, scratch = 0;
   // cell 0 after its own turn, which the wrapped bond of x = L-1 meets
-  uint32_t c0 = cnt0[0];
+  uint32_t c0 = sm[bC0];
   if (L > 1) {
-    uint32_t yc = cntY[0], zc = cntZ[0];
-    nhb_turn(msk[0], c0, msk[1] >> 3, cnt0[1], satY[0], yc, satZ[0], zc, scratch);
+    uint32_t yc = sm[bCY], zc = sm[bCZ];
+    nhb_turn(sm[bM], c0, sm[bM + 1] >> 3, sm[bC0 + 1], sm[bSY], yc, sm[bSZ], zc, scratch);
   }
   // the count of cell x1 before the chain reaches it (lane + 1 overwrites it in the replay)
-  const uint32_t next_init = x1 < L ? cnt0[x1] : c0;
-  // this lane's cells as a function of the input: bit i = output for input i
-  uint32_t f = 0;
-#pragma unroll
-  for (uint32_t in = 0; in < 2; ++in) {
-    uint32_t cur = in;
-    for (int x = x0; x < x1; ++x) {
-      uint32_t own = cnt0[x] + cur, yc = cntY[x], zc = cntZ[x];
-      const bool last = x + 1 == L;
-      cur = nhb_turn(msk[x], own, msk[last ? 0 : x + 1] >> 3, last ? c0 : cnt0[x + 1], satY[x], yc,
-                     satZ[x], zc, scratch);
-    }
-    f |= cur << in;
+  const uint32_t next_init = x1 < L ? sm[bC0 + x1] : c0;
+  // this lane's cells as a function of the input, both inputs side by side: bit i = output for
+  // input i
+  uint32_t cur0 = 0, cur1 = 1;
+  for (int x = x0; x < x1; ++x) {
+    const bool last = x + 1 == L;
+    const uint32_t m = sm[bM + x], nsat = sm[bM + (last ? 0 : x + 1)] >> 3, ncnt = last ? c0 : sm[bC0 + x + 1];
+    const uint32_t sy = sm[bSY + x], sz = sm[bSZ + x], cy = sm[bCY + x], cz = sm[bCZ + x], cc = sm[bC0 + x];
+    uint32_t own0 = cc + cur0, own1 = cc + cur1, y0 = cy, y1 = cy, z0 = cz, z1 = cz;
+    cur0 = nhb_turn(m, own0, nsat, ncnt, sy, y0, sz, z0, scratch);
+    cur1 = nhb_turn(m, own1, nsat, ncnt, sy, y1, sz, z1, scratch);
   }
-  if (x0 == x1) f = 2u;  // no cells: the identity
+  uint32_t f = x0 == x1 ? 2u : (cur0 | (cur1 << 1));  // no cells: the identity
   // inclusive scan of the composition (earlier lanes' function applied first)
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
@@ -340,23 +340,24 @@ __global__ void __launch_bounds__(32 * kWaveWarps) k_nhb_wave(const ReplicaDesc*
   uint32_t cur = lane == 0 ? 0u : (before & 1u);
   __syncwarp();
   for (int x = x0; x < x1; ++x) {
-    uint32_t own = cnt0[x] + cur, yc = cntY[x], zc = cntZ[x];
+    uint32_t own = sm[bC0 + x] + cur, yc = sm[bCY + x], zc = sm[bCZ + x];
     const bool last = x + 1 == L;
-    const uint32_t nc = last ? c0 : (x + 1 == x1 ? next_init : cnt0[x + 1]);
-    cur = nhb_turn(msk[x], own, msk[last ? 0 : x + 1] >> 3, nc, satY[x], yc, satZ[x], zc, refused);
-    cnt0[x] = (uint8_t)own;
-    cntY[x] = (uint8_t)yc;
-    cntZ[x] = (uint8_t)zc;
+    const uint32_t nc = last ? c0 : (x + 1 == x1 ? next_init : sm[bC0 + x + 1]);
+    cur = nhb_turn(sm[bM + x], own, sm[bM + (last ? 0 : x + 1)] >> 3, nc, sm[bSY + x], yc, sm[bSZ + x], zc,
+                   refused);
+    sm[bC0 + x] = (uint8_t)own;
+    sm[bCY + x] = (uint8_t)yc;
+    sm[bCZ + x] = (uint8_t)zc;
   }
   const uint32_t wrap = __shfl_sync(0xffffffffu, cur, (L - 1) / per);
-  if (lane == 0 && L > 1) cnt0[0] = (uint8_t)(cnt0[0] + wrap);
+  if (lane == 0 && L > 1) sm[bC0] = (uint8_t)(sm[bC0] + wrap);
   refused = __reduce_add_sync(0xffffffffu, refused);
   if (lane == 0 && refused) atomicAdd(&st[r].acc_slot[0][z & 31], 0ull - (unsigned long long)refused);
   __syncwarp();
   for (int x = lane; x < L; x += 32) {
-    R.cnt[o0 + x] = cnt0[x];
-    R.cnt[oY + x] = cntY[x];
-    R.cnt[oZ + x] = cntZ[x];
+    gcnt[o0 + x] = sm[bC0 + x];
+    gcnt[oY + x] = sm[bCY + x];
+    gcnt[oZ + x] = sm[bCZ + x];
   }
 }
 
