@@ -159,7 +159,8 @@ void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, boo
 // The running counts into every replica's last record (with its r_cell and volume; appended to
 // the sample stream when record is set), and the re-basing after a full measurement (base =
 // last record, changes zeroed).
-void launch_count_read(const BatchDev& b, cudaStream_t s, int record);
+void launch_count_read(const BatchDev& b, cudaStream_t s, int record, SampleRec* host_out = nullptr,
+                       int host_r = -1);
 void launch_count_rebase(const BatchDev& b, cudaStream_t s);
 void launch_measure(const BatchDev& b, int record, cudaStream_t s);
 // Colour-1 sweep jsweep fused with the measurement of the step (slots zeroed by the step's

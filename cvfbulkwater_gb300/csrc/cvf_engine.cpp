@@ -61,7 +61,8 @@ struct cvf_handle {
   // cooperative launch per graph.
   int launch_mode = 0;
   void* staging = nullptr;  // pinned host buffer for configuration transfers (lazily allocated)
-  SampleRec* rec_pin = nullptr;  // pinned landing place of the record cvf_observables reads
+  SampleRec* rec_pin = nullptr;  // mapped page-locked landing place of the record cvf_observables reads
+  SampleRec* rec_dev = nullptr;  // its device address
   size_t staging_bytes = 0;
   // cvf_set_config / cvf_get_config: 1 = kernels read and pack, or unpack and write, the
   // caller's array in host memory (the GPU accesses pageable memory through the host page
@@ -831,8 +832,21 @@ int cvf_observables(cvf_handle* h, int r, cvf_obs* out) {
   if (!out) return fail(CVF_EINVAL, "null out");
   CK(cudaSetDevice(h->device));
   h->obs_since_run = true;
+  if (!h->rec_pin) {
+    cudaError_t e = cudaHostAlloc((void**)&h->rec_pin, sizeof(SampleRec), cudaHostAllocMapped);
+    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&h->rec_dev, h->rec_pin, 0);
+    if (e != cudaSuccess) {
+      if (h->rec_pin) cudaFreeHost(h->rec_pin);
+      h->rec_pin = nullptr;
+      return fail(CVF_ENOMEM, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+    }
+  }
+  bool landed = false;  // the record already written to rec_pin by the kernel
   if (h->count_valid) {
-    launch_count_read(h->b, h->stream, 0);  // every step since the last measurement counted
+    // every step since the last measurement counted: the read kernel writes the record
+    // straight into the mapped page-locked buffer
+    launch_count_read(h->b, h->stream, 0, h->rec_dev, r);
+    landed = true;
   } else if (h->nhb_mode) {
     if (!h->nhb_read) {
       cudaGraph_t g;
@@ -852,16 +866,10 @@ int cvf_observables(cvf_handle* h, int r, cvf_obs* out) {
     launch_count_rebase(h->b, h->stream);
     h->count_valid = true;
   }
-  if (!h->rec_pin) {
-    cudaError_t e = cudaHostAlloc((void**)&h->rec_pin, sizeof(SampleRec), cudaHostAllocDefault);
-    if (e != cudaSuccess) {
-      h->rec_pin = nullptr;
-      return fail(CVF_ENOMEM, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
-    }
-  }
   // only the 32-byte measurement record crosses to the host, into page-locked memory
-  CK(cudaMemcpyAsync(h->rec_pin, (char*)(h->b.st + r) + offsetof(ReplicaState, last), sizeof(SampleRec),
-                     cudaMemcpyDeviceToHost, h->stream));
+  if (!landed)
+    CK(cudaMemcpyAsync(h->rec_pin, (char*)(h->b.st + r) + offsetof(ReplicaState, last), sizeof(SampleRec),
+                       cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
   const SampleRec last = *h->rec_pin;
   const ReplicaHost& R = h->reps[r];

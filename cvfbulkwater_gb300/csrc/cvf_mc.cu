@@ -1127,23 +1127,36 @@ void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, boo
   }
 }
 
-__global__ void k_count_read(ReplicaState* __restrict__ st, int nrep, int record) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+// One warp per replica: the 32 slots of each count summed across the lanes (modulo 2^64, so in
+// any order), the record stored as the replica's last measurement (and appended to the sample
+// stream when record is set); replica host_r's record is also written to host_out, page-locked
+// host memory mapped for the device, when that is given.
+__global__ void k_count_read(ReplicaState* __restrict__ st, int nrep, int record, SampleRec* host_out, int host_r) {
+  pdl_trigger();
+  const int r = blockIdx.x * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  pdl_wait();
   if (r >= nrep) return;
   ReplicaState& S = st[r];
-  long long dn = 0, ds = 0;
-  for (int i = 0; i < 32; ++i) {
-    dn += (long long)S.dlt_slot[0][i];
-    ds += (long long)S.dlt_slot[1][i];
+  unsigned long long dn = S.dlt_slot[0][lane], ds = S.dlt_slot[1][lane];
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    dn += __shfl_xor_sync(0xffffffffu, dn, off);
+    ds += __shfl_xor_sync(0xffffffffu, ds, off);
   }
+  if (lane != 0) return;
   SampleRec rec;
-  rec.n_hb2 = S.base_hb2 + 2 * dn;
-  rec.n_sigma = S.base_ns + ds;
+  rec.n_hb2 = S.base_hb2 + 2 * (long long)dn;
+  rec.n_sigma = S.base_ns + (long long)ds;
   rec.r_cell = S.r_cell;
   rec.volume = S.volume;
   S.last = rec;
   if (record && S.samples && S.n_samples < S.cap_samples) S.samples[S.n_samples] = rec;
   if (record) S.n_samples++;
+  if (host_out && r == host_r) {
+    *host_out = rec;
+    __threadfence_system();
+  }
 }
 
 __global__ void k_count_rebase(ReplicaState* __restrict__ st, int nrep) {
@@ -1155,8 +1168,9 @@ __global__ void k_count_rebase(ReplicaState* __restrict__ st, int nrep) {
   for (int i = 0; i < 32; ++i) S.dlt_slot[0][i] = S.dlt_slot[1][i] = 0ull;
 }
 
-void launch_count_read(const BatchDev& b, cudaStream_t s, int record) {
-  k_count_read<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, record);
+void launch_count_read(const BatchDev& b, cudaStream_t s, int record, SampleRec* host_out, int host_r) {
+  launch_pdl(k_count_read, dim3((unsigned)((b.nrep + kThreads / 32 - 1) / (kThreads / 32))), s, b.pdl, b.st, b.nrep,
+             record, host_out, host_r);
 }
 void launch_count_rebase(const BatchDev& b, cudaStream_t s) {
   k_count_rebase<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep);
