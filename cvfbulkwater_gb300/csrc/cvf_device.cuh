@@ -155,6 +155,7 @@ void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do
 // count: the counting variants also add the changes of N_hb and N_sigma they make to the
 // replicas' running counts (dlt_slot).
 void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, bool count = false);
+void launch_volume_chain(const BatchDev& b, int steps, cudaStream_t s);
 void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, bool count = false);
 // The running counts into every replica's last record (with its r_cell and volume; appended to
 // the sample stream when record is set), and the re-basing after a full measurement (base =

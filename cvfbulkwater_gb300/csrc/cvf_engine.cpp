@@ -97,6 +97,8 @@ struct cvf_handle {
   std::vector<Group> groups;
   int groups_vec = 0;
   cudaEvent_t fork = nullptr;
+  cudaStream_t vstream = nullptr;  // side branch of a chunk's volume moves
+  cudaEvent_t vfork = nullptr, vdone = nullptr;
 };
 
 // Drops every cached graph (kernel arguments such as the block tables change).
@@ -303,9 +305,11 @@ static int ensure_sw(cvf_handle* h) {
   return upload_descs(h);
 }
 
-static void enqueue_step(cvf_handle* h, int nmet, int ncl, bool count = false) {
-  launch_step_begin(h->b, nmet, ncl, 1, 1, h->stream);
-  launch_cube_volume(h->b, 1, 1, h->stream, count);
+// volume: the step's volume move in the cube kernel (false when a side branch runs the chunk's
+// volume moves).
+static void enqueue_step(cvf_handle* h, int nmet, int ncl, bool count = false, bool volume = true) {
+  launch_step_begin(h->b, nmet, ncl, 1, volume ? 1 : 0, h->stream);
+  launch_cube_volume(h->b, 1, volume ? 1 : 0, h->stream, count);
   for (int j = 0; j < nmet; ++j) {
     launch_sweep(h->b, 0, j, h->stream, count);
     launch_sweep(h->b, 1, j, h->stream, count);
@@ -427,8 +431,26 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     }
     if (h->corr_on) launch_corr_step(h->b, h->stream);
   }
+  // a chunk without records of a handle up to 2^22 cells runs its volume moves on a side branch,
+  // beside the cube moves and sweeps, and joins it at the end: there the one-warp FP64 volume
+  // move (about 15 us) outlasts the cube moves it otherwise runs beside (L=16 step 16.1 -> 9.8
+  // us); on larger lattices the cube moves hide it and the branch only adds its fork and join
+  long long cells = 0;
+  for (const auto& r : h->reps) cells += r.N;
+  const bool side = !h->nhb_mode && !record && steps > 0 && cells <= (1ll << 22);
+  if (side) {
+    if (!h->vstream) CK(cudaStreamCreateWithFlags(&h->vstream, cudaStreamNonBlocking));
+    if (!h->vfork) CK(cudaEventCreateWithFlags(&h->vfork, cudaEventDisableTiming));
+    if (!h->vdone) CK(cudaEventCreateWithFlags(&h->vdone, cudaEventDisableTiming));
+    CK(cudaEventRecord(h->vfork, h->stream));
+    CK(cudaStreamWaitEvent(h->vstream, h->vfork, 0));
+    launch_volume_chain(h->b, steps, h->vstream);
+    CK(cudaEventRecord(h->vdone, h->vstream));
+  }
   for (int i = 0; i < steps && !h->nhb_mode; ++i) {
-    if (count) {
+    if (side) {
+      enqueue_step(h, nmet, ncl, count, false);
+    } else if (count) {
       // the record of a counting step is the running counts
       enqueue_step(h, nmet, ncl, true);
       if (i == 0 && record) launch_count_read(h->b, h->stream, 1);
@@ -443,6 +465,7 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     }
     if (h->corr_on) launch_corr_step(h->b, h->stream);  // after the step's measurement, as GW:1245
   }
+  if (side) CK(cudaStreamWaitEvent(h->stream, h->vdone, 0));
   CK(cudaStreamEndCapture(h->stream, &g));
   cudaGraphExec_t ex;
   cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
@@ -624,6 +647,9 @@ int cvf_destroy(cvf_handle* h) {
     if (g.done) cudaEventDestroy(g.done);
   }
   if (h->fork) cudaEventDestroy(h->fork);
+  if (h->vfork) cudaEventDestroy(h->vfork);
+  if (h->vdone) cudaEventDestroy(h->vdone);
+  if (h->vstream) cudaStreamDestroy(h->vstream);
   for (void* p : h->allocs) cudaFree(p);
   if (h->io_scratch) cudaFree(h->io_scratch);
   if (h->io_bad) cudaFree(h->io_bad);

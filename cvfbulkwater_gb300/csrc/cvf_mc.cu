@@ -190,8 +190,10 @@ __global__ void k_step_begin(ReplicaState* __restrict__ st, int nrep, int nmet, 
   S.ctr[0] += (uint32_t)nmet;
   S.cur[1] = S.ctr[1];
   S.ctr[1] += (uint32_t)do_cube;
-  S.cur[2] = S.ctr[2];
-  S.ctr[2] += (uint32_t)do_volume;
+  if (do_volume) {  // otherwise a side branch may be moving the volume counter
+    S.cur[2] = S.ctr[2];
+    S.ctr[2] += 1u;
+  }
   S.cur[3] = S.ctr[3];
   S.ctr[3] += (uint32_t)ncl;
 }
@@ -257,6 +259,24 @@ __device__ void volume_move_warp(const ReplicaDesc& R, ReplicaState& S, uint32_t
     S.volume = tV;
     S.e_vdw = tE;
   }
+}
+
+// The volume moves of `steps` consecutive steps of replica blockIdx.x (one warp), with the volume
+// counters ctr[2], ctr[2] + 1, ...; the counter advances by `steps` at the end. The volume chain
+// reads and writes only r_cell, volume and e_vdw, which the cube moves and sweeps neither read
+// nor write (the acceptance of sigma and eta moves does not depend on the volume), so a chunk's
+// volume moves can run beside its other kernels.
+__global__ void __launch_bounds__(32) k_volume_chain(const ReplicaDesc* __restrict__ reps,
+                                                    ReplicaState* __restrict__ st, int nrep, int steps) {
+  const int r = blockIdx.x;
+  if (r >= nrep) return;
+  ReplicaState& S = st[r];
+  const uint32_t t0 = S.ctr[2];
+  for (int i = 0; i < steps; ++i) {
+    volume_move_warp(reps[r], S, t0 + (uint32_t)i);
+    __syncwarp();
+  }
+  if (threadIdx.x == 0) S.ctr[2] = t0 + (uint32_t)steps;
 }
 
 // ------------------------------------------------------------------ vector access helpers
@@ -1075,6 +1095,10 @@ static inline dim3 grid1(int n) { return dim3((unsigned)((n + kThreads - 1) / kT
 void launch_init_lattice(const BatchDev& b, cudaStream_t s) {
   k_init_sigma<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.blk_cell, b.nrep);
   k_init_cubes<<<b.nblk_cube, kThreads, 0, s>>>(b.reps, b.blk_cube, b.nrep);
+}
+
+void launch_volume_chain(const BatchDev& b, int steps, cudaStream_t s) {
+  k_volume_chain<<<b.nrep, 32, 0, s>>>(b.reps, b.st, b.nrep, steps);
 }
 
 void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do_volume, cudaStream_t s,
