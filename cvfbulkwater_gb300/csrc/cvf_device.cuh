@@ -43,6 +43,7 @@ struct ReplicaDesc {
   int cvec;           // consecutive cubes per thread in the cube move: 4, 2 or 1 (divides H)
   uint32_t key0, key1, replica;
   float T, P, Rc;
+  double vdw_shift;   // vdw_shift(Rc), computed once on the host
   double beta, Jeff;
   unsigned long long thr_sweep[33];  // U < T, T in [0, 2^32]; index (dN_hb+1)*11 + dN_s+5
   // Sweep fast-path tables, read through L1 by the kernels:

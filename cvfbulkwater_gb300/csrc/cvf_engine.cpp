@@ -590,6 +590,7 @@ int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
     d.T = r.p.T;
     d.P = r.p.P;
     d.Rc = r.p.R_cutoff;
+    d.vdw_shift = vdw_shift(d.Rc);
     d.beta = r.thr.beta;
     d.Jeff = r.thr.Jeff;
     memcpy(d.thr_sweep, r.thr.sweep, sizeof(d.thr_sweep));

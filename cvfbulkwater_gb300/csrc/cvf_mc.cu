@@ -220,11 +220,7 @@ __device__ void volume_move_warp(const ReplicaDesc& R, ReplicaState& S, uint32_t
   }
   __syncwarp();
   const double trial = s_trial;
-  double tmp = 1.0 / (double)R.Rc;
-  tmp = CVF_DMUL(CVF_DMUL(tmp, tmp), tmp);
-  double att = CVF_DMUL(tmp, tmp);
-  double rep = CVF_DMUL(att, att);
-  const double shift = CVF_DSUB(rep, att);
+  const double shift = R.vdw_shift;  // the same expression, evaluated once on the host
   for (int i = lane; i < R.n_shells; i += 32) {
     double rd = CVF_DMUL(trial, (double)R.dist[i]);
     double term;
@@ -254,7 +250,9 @@ __device__ void volume_move_warp(const ReplicaDesc& R, ReplicaState& S, uint32_t
   double dE = CVF_DSUB(CVF_DSUB(tE, S.e_vdw), CVF_DMUL(NT, own_log(tV / S.volume)));
   double u2 = u53(q.z, q.w);
   double arg = CVF_DMUL(-R.beta, CVF_DADD(dE, CVF_DMUL((double)R.P, dV)));
-  if (u2 < own_exp(arg)) {
+  // own_exp(arg) >= 1 > u2 for arg >= 0 (the last Horner step adds a non-negative product to
+  // 1.0, or the power of two is at least 2), so the exponential is needed only below zero
+  if (arg >= 0.0 || u2 < own_exp(arg)) {
     S.r_cell = trial;
     S.volume = tV;
     S.e_vdw = tE;

@@ -245,12 +245,18 @@ CVF_HD double own_log(double x) {
 }
 
 // van der Waals lattice energy E(r) = sum_i f_i [(r d_i)^-12 - (r d_i)^-6 - shift], GW:1784-1805.
-CVF_HD double evdw(double r, const float* dist, const int* freq, int n, float Rc) {
+// The cut-off shift (1/Rc)^12 - (1/Rc)^6 of E_vdW (GW:1790-1794).
+CVF_HD double vdw_shift(float Rc) {
   double tmp = 1.0 / (double)Rc;
   tmp = CVF_DMUL(CVF_DMUL(tmp, tmp), tmp);
-  double att = CVF_DMUL(tmp, tmp);
-  double rep = CVF_DMUL(att, att);
-  double shift = CVF_DSUB(rep, att);
+  const double att = CVF_DMUL(tmp, tmp);
+  const double rep = CVF_DMUL(att, att);
+  return CVF_DSUB(rep, att);
+}
+
+CVF_HD double evdw(double r, const float* dist, const int* freq, int n, float Rc) {
+  const double shift = vdw_shift(Rc);
+  double tmp, att, rep;
   double ret = 0.0;
   for (int i = 0; i < n; ++i) {
     double rd = CVF_DMUL(r, (double)dist[i]);
