@@ -157,6 +157,7 @@ void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do
 // replicas' running counts (dlt_slot).
 void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, bool count = false);
 void launch_volume_chain(const BatchDev& b, int steps, cudaStream_t s);
+cudaError_t launch_chunk_cluster(const BatchDev& b, int steps, int nmet, cudaStream_t s);
 void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, bool count = false);
 // The running counts into every replica's last record (with its r_cell and volume; appended to
 // the sample stream when record is set), and the re-basing after a full measurement (base =

@@ -859,6 +859,70 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const 
   }
 }
 
+// A chunk of Metropolis-only steps of a small replica on one thread-block cluster of kClusterCtas
+// blocks (cluster c = replica c): each block takes every kClusterCtas-th cube block and row
+// segment of the replica, and a cluster barrier (release / acquire, so the cells and cube states
+// written before it are seen after it) separates the cube moves and the two colours of every
+// sweep. The step counters are those the per-phase kernels get from k_step_begin: cube move
+// ctr[1] + s, sweep j of step s ctr[0] + s * nmet + j; block 0 advances them after the last step.
+// The volume moves run on a side branch (k_volume_chain). The same cells, draws and decisions as
+// the per-phase kernels, with kClusterCtas blocks instead of one launch per phase: a step of
+// an L=16 lattice is a few microseconds of work spread over launches of a few blocks.
+constexpr int kClusterCtas = 8;
+
+__device__ __forceinline__ void cluster_barrier() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+template <int V>
+__global__ void __launch_bounds__(kThreads) k_chunk_cluster(const ReplicaDesc* __restrict__ reps,
+                                                            ReplicaState* __restrict__ st,
+                                                            const int* __restrict__ blk_cubev, int nrep,
+                                                            int steps, int nmet) {
+  __shared__ SweepTables s_tab[kThreads / 32];
+  __shared__ CubeTables s_ct[kThreads / 32];
+  uint32_t rank;
+  asm("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+  const int r = (int)(blockIdx.x / kClusterCtas);
+  const bool live = r < nrep;  // every block of the cluster reaches every barrier
+  const ReplicaDesc& R = reps[live ? r : 0];
+  const SweepTables* wt = warp_sweep_tables(R, s_tab);
+  CubeTables* ct = s_ct + (threadIdx.x >> 5);
+  fill_cube_tables(R, ct, threadIdx.x & 31);
+  __syncwarp();
+  ReplicaState& S = st[live ? r : 0];
+  const uint32_t c0 = S.ctr[0], c1 = S.ctr[1];
+  const uint32_t nseg = (uint32_t)(R.H / V) * (uint32_t)R.L * (uint32_t)R.L;
+  const int vb0 = __ldg(blk_cubev + (live ? r : 0)), vb1 = __ldg(blk_cubev + (live ? r : 0) + 1);
+  uint32_t hb2 = 0, ns = 0;
+  cluster_barrier();  // every block has read the counters before block 0 moves them
+  for (int s = 0; s < steps; ++s) {
+    int cdh = 0;
+    if (live)
+      for (int vb = vb0 + (int)rank; vb < vb1; vb += kClusterCtas)
+        cube_move(R, ct, blk_cubev, r, vb, c1 + (uint32_t)s, cdh);
+    cluster_barrier();
+    for (int j = 0; j < nmet; ++j) {
+      const uint32_t t = c0 + (uint32_t)(s * nmet + j);
+      for (int colour = 0; colour < 2; ++colour) {
+        if (live)
+          for (uint32_t q = rank * kThreads + threadIdx.x; q < nseg; q += kClusterCtas * kThreads)
+            sweep_segment<V, false>(R, wt, q, colour, t, hb2, ns);
+        cluster_barrier();
+      }
+    }
+  }
+  if (live && rank == 0 && threadIdx.x == 0 && steps > 0) {
+    // the counters as the last step's k_step_begin leaves them (the volume counter belongs to
+    // the volume branch)
+    S.cur[0] = c0 + (uint32_t)((steps - 1) * nmet);
+    S.ctr[0] = c0 + (uint32_t)(steps * nmet);
+    S.cur[1] = c1 + (uint32_t)(steps - 1);
+    S.ctr[1] = c1 + (uint32_t)steps;
+    S.cur[3] = S.ctr[3];
+  }
+}
+
 // Colour-1 sweep of a recorded step fused with its measurement: the counts go to the slots
 // that k_step_begin zeroed, k_measure_end sums them after the step.
 template <int V>
@@ -1093,6 +1157,26 @@ static inline dim3 grid1(int n) { return dim3((unsigned)((n + kThreads - 1) / kT
 void launch_init_lattice(const BatchDev& b, cudaStream_t s) {
   k_init_sigma<<<b.nblk_cell, kThreads, 0, s>>>(b.reps, b.blk_cell, b.nrep);
   k_init_cubes<<<b.nblk_cube, kThreads, 0, s>>>(b.reps, b.blk_cube, b.nrep);
+}
+
+cudaError_t launch_chunk_cluster(const BatchDev& b, int steps, int nmet, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(b.nrep * kClusterCtas));
+  cfg.blockDim = dim3(kThreads);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kClusterCtas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  switch (b.vec) {
+    case 8: return cudaLaunchKernelEx(&cfg, k_chunk_cluster<8>, (const ReplicaDesc*)b.reps, b.st, (const int*)b.blk_cubev, b.nrep, steps, nmet);
+    case 4: return cudaLaunchKernelEx(&cfg, k_chunk_cluster<4>, (const ReplicaDesc*)b.reps, b.st, (const int*)b.blk_cubev, b.nrep, steps, nmet);
+    case 2: return cudaLaunchKernelEx(&cfg, k_chunk_cluster<2>, (const ReplicaDesc*)b.reps, b.st, (const int*)b.blk_cubev, b.nrep, steps, nmet);
+    default: return cudaLaunchKernelEx(&cfg, k_chunk_cluster<1>, (const ReplicaDesc*)b.reps, b.st, (const int*)b.blk_cubev, b.nrep, steps, nmet);
+  }
 }
 
 void launch_volume_chain(const BatchDev& b, int steps, cudaStream_t s) {

@@ -68,3 +68,27 @@ def test_batch_run_and_sample_stream_exports(engine_lib):
         assert (buf[k].n_hb2, buf[k].n_sigma, buf[k].r_cell, buf[k].volume) == tuple(want[k].tolist())
     a.close()
     b.close()
+
+
+SMALL = [(6, 0.6, 0.0), (16, 0.9, 0.6), (24, 0.75, 0.3), (12, 0.55, 0.45), (8, 0.7, 0.45)]
+
+
+def test_cluster_chunks_match_grouped_chains(engine_lib):
+    """An ungrouped batch whose lattices all hold at most 2^14 cells runs each chunk of plain
+    steps as one thread-block cluster per replica, with the volume moves on a side branch; a
+    grouped batch runs the per-phase kernels. Both leave the same lattices, counters and volume
+    chains, across chunks of several sweeps and a sampled run between them."""
+    outs = []
+    for groups in (1, 2):
+        lat = Lattice([Params(L=L, T=T, P=P, seed=500 + i, start=0, replica=i) for i, (L, T, P) in enumerate(SMALL)])
+        lat.replica_groups = groups
+        lat.run(37, 1, 0)
+        lat.run(5, 2, 0)
+        lat.run_sampled(6, 1, 0, 3)
+        lat.run(33, 1, 0)
+        outs.append([(lat.get_config(r), lat.state(r), lat.samples(r)) for r in range(len(SMALL))])
+        lat.close()
+    for r, (a, b) in enumerate(zip(*outs)):
+        assert np.array_equal(a[0], b[0]), r
+        assert a[1][0] == b[1][0] and a[1][1] == b[1][1] and list(a[1][3]) == list(b[1][3]), r
+        assert len(a[2]) == len(b[2]) and all(x == y for x, y in zip(a[2], b[2])), r
