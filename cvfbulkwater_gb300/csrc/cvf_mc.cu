@@ -860,8 +860,9 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const 
 }
 
 // A chunk of Metropolis-only steps of a small replica on one thread-block cluster of kClusterCtas
-// blocks (cluster c = replica c): each block takes every kClusterCtas-th cube block and row
-// segment of the replica, and a cluster barrier (release / acquire, so the cells and cube states
+// blocks (cluster c = replica c): each block takes every kClusterCtas-th cube block (one cube per
+// thread with cube1 and the table of one thread per cube, else the replica's cube tile and its
+// table) and row segment (V cells per thread) of the replica, and a cluster barrier (release / acquire, so the cells and cube states
 // written before it are seen after it) separates the cube moves and the two colours of every
 // sweep. The step counters are those the per-phase kernels get from k_step_begin: cube move
 // ctr[1] + s, sweep j of step s ctr[0] + s * nmet + j; block 0 advances them after the last step.
@@ -877,8 +878,8 @@ __device__ __forceinline__ void cluster_barrier() {
 template <int V>
 __global__ void __launch_bounds__(kThreads) k_chunk_cluster(const ReplicaDesc* __restrict__ reps,
                                                             ReplicaState* __restrict__ st,
-                                                            const int* __restrict__ blk_cubev, int nrep,
-                                                            int steps, int nmet) {
+                                                            const int* __restrict__ blk_cube, int cube1,
+                                                            int nrep, int steps, int nmet) {
   __shared__ SweepTables s_tab[kThreads / 32];
   __shared__ CubeTables s_ct[kThreads / 32];
   uint32_t rank;
@@ -893,14 +894,15 @@ __global__ void __launch_bounds__(kThreads) k_chunk_cluster(const ReplicaDesc* _
   ReplicaState& S = st[live ? r : 0];
   const uint32_t c0 = S.ctr[0], c1 = S.ctr[1];
   const uint32_t nseg = (uint32_t)(R.H / V) * (uint32_t)R.L * (uint32_t)R.L;
-  const int vb0 = __ldg(blk_cubev + (live ? r : 0)), vb1 = __ldg(blk_cubev + (live ? r : 0) + 1);
+  const int vb0 = __ldg(blk_cube + (live ? r : 0)), vb1 = __ldg(blk_cube + (live ? r : 0) + 1);
   uint32_t hb2 = 0, ns = 0;
   cluster_barrier();  // every block has read the counters before block 0 moves them
   for (int s = 0; s < steps; ++s) {
     int cdh = 0;
     if (live)
       for (int vb = vb0 + (int)rank; vb < vb1; vb += kClusterCtas)
-        cube_move(R, ct, blk_cubev, r, vb, c1 + (uint32_t)s, cdh);
+        if (cube1) cube_move_v<1>(R, ct, blk_cube, r, vb, c1 + (uint32_t)s, cdh);
+        else cube_move(R, ct, blk_cube, r, vb, c1 + (uint32_t)s, cdh);
     cluster_barrier();
     for (int j = 0; j < nmet; ++j) {
       const uint32_t t = c0 + (uint32_t)(s * nmet + j);
@@ -1171,11 +1173,18 @@ cudaError_t launch_chunk_cluster(const BatchDev& b, int steps, int nmet, cudaStr
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  switch (b.vec) {
-    case 8: return cudaLaunchKernelEx(&cfg, k_chunk_cluster<8>, (const ReplicaDesc*)b.reps, b.st, (const int*)b.blk_cubev, b.nrep, steps, nmet);
-    case 4: return cudaLaunchKernelEx(&cfg, k_chunk_cluster<4>, (const ReplicaDesc*)b.reps, b.st, (const int*)b.blk_cubev, b.nrep, steps, nmet);
-    case 2: return cudaLaunchKernelEx(&cfg, k_chunk_cluster<2>, (const ReplicaDesc*)b.reps, b.st, (const int*)b.blk_cubev, b.nrep, steps, nmet);
-    default: return cudaLaunchKernelEx(&cfg, k_chunk_cluster<1>, (const ReplicaDesc*)b.reps, b.st, (const int*)b.blk_cubev, b.nrep, steps, nmet);
+  // the phases are short and latency-bound: the fewest cells (cubes) per thread that still cover
+  // the largest replica in one pass of the cluster's threads
+  const long long pass = (long long)kClusterCtas * kThreads, L = b.max_L, H = L / 2;
+  int v = 1;
+  while (v < b.vec && (H / v) * L * L > pass) v *= 2;
+  const int cube1 = 2 * ((H * H * H + kThreads - 1) / kThreads) <= kClusterCtas;
+  const int* blk = cube1 ? b.blk_cube : b.blk_cubev;
+  switch (v) {
+    case 8: return cudaLaunchKernelEx(&cfg, k_chunk_cluster<8>, (const ReplicaDesc*)b.reps, b.st, blk, cube1, b.nrep, steps, nmet);
+    case 4: return cudaLaunchKernelEx(&cfg, k_chunk_cluster<4>, (const ReplicaDesc*)b.reps, b.st, blk, cube1, b.nrep, steps, nmet);
+    case 2: return cudaLaunchKernelEx(&cfg, k_chunk_cluster<2>, (const ReplicaDesc*)b.reps, b.st, blk, cube1, b.nrep, steps, nmet);
+    default: return cudaLaunchKernelEx(&cfg, k_chunk_cluster<1>, (const ReplicaDesc*)b.reps, b.st, blk, cube1, b.nrep, steps, nmet);
   }
 }
 
