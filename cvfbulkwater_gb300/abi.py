@@ -125,6 +125,7 @@ def lib():
         "cvf_get_io_mode": (I, [P, C.POINTER(I)]),
         "cvf_profile_launch": (I, [P, I, I]),
         "cvf_cluster_stats_noalloc": (I, [P, I, P, P]),
+        "cvf_set_wait_limits": (I, [P, C.c_longlong, C.c_longlong]),
         "cvf_read_input_data": (I, [C.c_char_p, C.POINTER(Input)]),
         "cvf_read_config_file": (I, [C.c_char_p, P, LL]),
         "cvf_write_config_file": (I, [C.c_char_p, P, LL]),

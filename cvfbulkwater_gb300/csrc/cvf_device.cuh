@@ -25,6 +25,7 @@ struct ReplicaDesc {
   int32_t* cand;      // 6N: percolation candidate id by root (-1 none)
   uint32_t* cover;    // max_cand * 3 * W: coordinate coverage bitmaps
   int max_cand;       // capacity of cover
+  uint32_t union_iters;  // attempts of one Swendsen-Wang union before it gives up (error code 1)
   // Flag_chessboard = 0 (null otherwise): eta of every cell as 6 bits, the bond count of every
   // cell, and the greedy measurement's work arrays (per cell: bits 0..2 its matched x+, y+, z+
   // bonds and bit 3 set when 5 or more of its arms are matched; the counts of those cells);
@@ -140,10 +141,16 @@ struct BatchDev {
   int max_L;            // largest edge among the replicas
   int pdl;              // launch the step's kernels as programmatic dependents (launch_pdl)
   GridSync* gsync;      // device barrier state of the persistent step kernel
+  unsigned int barrier_polls;  // polls of one grid-barrier wait before it gives up (error code 3)
   CorrState* corr;      // device array [nrep] of correlators (null until enabled)
 };
 
 constexpr int kThreads = 256;
+// Default bounds of the device waits: a grid-barrier wait polls at most kBarrierPolls times
+// (with a short sleep between polls, about a second in all), a union gives up after
+// kUnionIters attempts. cvf_set_wait_limits lowers them for tests of the error path.
+constexpr unsigned int kBarrierPolls = 1u << 24;
+constexpr unsigned int kUnionIters = 1u << 24;
 
 void launch_init_lattice(const BatchDev& b, cudaStream_t s);
 void init_device_tables();

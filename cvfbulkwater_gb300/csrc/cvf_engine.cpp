@@ -522,7 +522,9 @@ int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
   for (int i = 0; i < n; ++i) {
     const cvf_params& p = params[i];
     if (p.L < 4 || (p.L & 1)) return fail(CVF_EINVAL, "L must be even and >= 4");
-    if ((long long)p.L * p.L * p.L * 6 >= (1LL << 31)) return fail(CVF_EINVAL, "L too large (6 L^3 must fit int32)");
+    // L is bounded first so that 6 L^3 is formed without overflow (largest even L: 710)
+    if (p.L > 1024 || (long long)p.L * p.L * p.L * 6 >= (1LL << 31))
+      return fail(CVF_EINVAL, "L too large (6 L^3 must fit int32)");
     if (p.flag_chessboard != 0 && p.flag_chessboard != 1) return fail(CVF_EINVAL, "Flag_chessboard must be 0 or 1");
     if (p.flag_chessboard != params[0].flag_chessboard)
       return fail(CVF_EINVAL, "all replicas of a handle share Flag_chessboard");
@@ -616,6 +618,7 @@ int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
       for (int pp = 0; pp < 8; ++pp) d.eta_tab[st * 8 + pp] = (uint8_t)cube_eta_bits(st, pp);
     memcpy(d.thr_cube, r.thr.cube, sizeof(d.thr_cube));
     memcpy(d.thr_sw, r.thr.sw, sizeof(d.thr_sw));
+    d.union_iters = kUnionIters;
     ReplicaState& s = st[i];
     memset(&s, 0, sizeof(s));
     s.r_cell = kRcell0;
@@ -628,6 +631,7 @@ int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
       return bail(rc);
   }
   h->b.nrep = n;
+  h->b.barrier_polls = kBarrierPolls;
   int rc;
   if ((rc = dev_alloc(h, (void**)&h->b.reps, n * sizeof(ReplicaDesc))) ||
       (rc = dev_alloc(h, (void**)&h->b.st, n * sizeof(ReplicaState))) ||
@@ -1197,6 +1201,23 @@ int cvf_set_io_mode(cvf_handle* h, int mode) {
 int cvf_get_io_mode(const cvf_handle* h, int* mode) {
   if (!h || !mode) return fail(CVF_EINVAL, "null handle/out");
   *mode = h->io_mode;
+  return 0;
+}
+
+int cvf_set_wait_limits(cvf_handle* h, long long barrier_polls, long long union_iters) {
+  if (!h) return fail(CVF_EINVAL, "null handle");
+  const unsigned int polls = barrier_polls < 0 ? kBarrierPolls
+                             : (unsigned int)std::min<long long>(barrier_polls, (long long)kBarrierPolls);
+  const uint32_t iters = union_iters < 0 ? kUnionIters
+                         : (uint32_t)std::min<long long>(union_iters, (long long)kUnionIters);
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  for (auto& r : h->reps) r.desc.union_iters = iters;
+  if (int rc = upload_descs(h)) return rc;
+  // the persistent kernel takes the bound as a by-value argument of its captured launch
+  h->b.barrier_polls = polls;
+  for (auto& g : h->groups) g.b.barrier_polls = polls;
+  drop_graphs(h);
   return 0;
 }
 

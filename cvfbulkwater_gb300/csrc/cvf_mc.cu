@@ -994,12 +994,10 @@ __global__ void k_measure_end(ReplicaState* __restrict__ st, int nrep, int recor
 
 // ------------------------------------------------------------------ persistent step kernel
 // Grid barrier of the persistent kernel; every block of the cooperative launch is resident. A
-// waiting block polls the generation word at most kBarrierPolls times (with a short sleep
-// between polls, about a second in all); when the bound is reached it sets gs->err and error
-// code 3 of replica 0, and every block leaves the kernel at its next barrier.
-constexpr unsigned int kBarrierPolls = 1u << 24;
-
-__device__ __noinline__ bool grid_barrier(GridSync* gs, ReplicaState* st0) {
+// waiting block polls the generation word at most max_polls times (kBarrierPolls by default,
+// with a short sleep between polls, about a second in all); when the bound is reached it sets
+// gs->err and error code 3 of replica 0, and every block leaves the kernel at its next barrier.
+__device__ __noinline__ bool grid_barrier(GridSync* gs, ReplicaState* st0, unsigned int max_polls) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -1013,11 +1011,14 @@ __device__ __noinline__ bool grid_barrier(GridSync* gs, ReplicaState* st0) {
       __threadfence();
       atomicAdd(&gs->gen, 1u);
     } else {
-      for (unsigned int polls = 0; *gen == g; ++polls) {
-        if (*err != 0 || polls >= kBarrierPolls) {
+      // the bound is checked before each look at the generation word, so a bound of 0 makes
+      // every block that has to wait give up
+      for (unsigned int polls = 0;; ++polls) {
+        if (*err != 0 || polls >= max_polls) {
           ok = 0;
           break;
         }
+        if (*gen != g) break;
         __nanosleep(64);
       }
       if (!ok && atomicExch(&gs->err, 1) == 0) atomicExch(&st0->err, 3);
@@ -1136,7 +1137,7 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_run(BatchDev
         measure_accumulate(b.st[r], vb, hb2, ns, s_acc);
       });
     }
-    if (!grid_barrier(b.gsync, b.st)) return;
+    if (!grid_barrier(b.gsync, b.st, b.barrier_polls)) return;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) b.gsync->ticket = 0u;  // every ticket of the launch is taken
   const bool last_rec = interval > 0 && (nsteps - 1) % interval == 0;

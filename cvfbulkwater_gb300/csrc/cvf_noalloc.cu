@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <string>
 
 #include "../../include/cvf.h"
@@ -28,6 +29,7 @@ namespace {
 constexpr int kNaThreads = 256;
 constexpr long long kNaMaxSites = CVF_NOALLOC_MAX_SITES;
 constexpr int kNaMaxL = 54;                       // largest even L with 6 L^3 <= kNaMaxSites
+static_assert(6LL * kNaMaxL * kNaMaxL * kNaMaxL <= kNaMaxSites, "scratch limit");
 constexpr int kNaMaxCand = 3 * kNaMaxL * kNaMaxL;  // clusters of size >= 2L: at most 6N / 2L
 constexpr int kNaMaxW = (kNaMaxL + 31) / 32;
 constexpr int kNaMaxBlocks = (int)((kNaMaxSites + kNaThreads - 1) / kNaThreads);
@@ -188,7 +190,10 @@ __global__ void k_na_final(int nsites, int L, int nblocks, NaPtrs p, long long* 
   }
 }
 
-void* g_scratch_addr[64];  // device address of g_noalloc_scratch per device ordinal
+// Device address of g_noalloc_scratch per device ordinal. Several host threads may make their
+// first call on a device at once; they look up the same address, and the atomic slot makes
+// their concurrent stores and loads well defined.
+std::atomic<void*> g_scratch_addr[64];
 
 int na_fail(int code, const std::string& m) {
   cvf::set_last_error(m);
@@ -200,23 +205,24 @@ int na_fail(int code, const std::string& m) {
 extern "C" int cvf_cluster_stats_noalloc(const int* labels, int L, long long* out7, void* stream) {
   if (!labels || !out7) return na_fail(CVF_EINVAL, "cluster_stats_noalloc: null labels or out7");
   if (L < 4 || (L & 1)) return na_fail(CVF_EINVAL, "cluster_stats_noalloc: L must be even and >= 4");
-  const long long nsites = 6LL * L * L * L;
-  if (nsites > kNaMaxSites)
-    return na_fail(CVF_EINVAL, "cluster_stats_noalloc: 6*L^3 = " + std::to_string(nsites) +
-                                   " label sites exceed the fixed scratch limit of " +
+  // L is bounded before 6 L^3 is formed, so no product can overflow
+  if (L > kNaMaxL)
+    return na_fail(CVF_EINVAL, "cluster_stats_noalloc: L = " + std::to_string(L) +
+                                   ": its 6*L^3 label sites exceed the fixed scratch limit of " +
                                    std::to_string(kNaMaxSites) + " (even L <= 54)");
+  const long long nsites = 6LL * L * L * L;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return na_fail(CVF_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= 64) return na_fail(CVF_EINVAL, "cluster_stats_noalloc: device ordinal >= 64");
-  if (!g_scratch_addr[dev]) {
-    void* ptr = nullptr;
-    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess || !ptr)
+  void* addr = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!addr) {
+    e = cudaGetSymbolAddress(&addr, g_noalloc_scratch);
+    if (e != cudaSuccess || !addr)
       return na_fail(CVF_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_scratch_addr[dev] = ptr;
+    g_scratch_addr[dev].store(addr, std::memory_order_release);
   }
-  unsigned char* base = (unsigned char*)g_scratch_addr[dev];
+  unsigned char* base = (unsigned char*)addr;
   NaPtrs p;
   p.size = (int32_t*)(base + kOffSize);
   p.cand = (int32_t*)(base + kOffCand);

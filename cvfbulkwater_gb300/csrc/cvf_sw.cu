@@ -151,8 +151,9 @@ __device__ __forceinline__ int32_t uf_find(int32_t* p, int32_t x) {
   return x;
 }
 
-__device__ __forceinline__ bool uf_unite(int32_t* p, int32_t a, int32_t b) {
-  for (int it = 0; it < (1 << 24); ++it) {
+// Hooks the larger of the two roots under the smaller; gives up (false) after max_iters attempts.
+__device__ __forceinline__ bool uf_unite(int32_t* p, int32_t a, int32_t b, uint32_t max_iters) {
+  for (uint32_t it = 0; it < max_iters; ++it) {
     a = uf_find(p, a);
     b = uf_find(p, b);
     if (a == b) return true;
@@ -189,7 +190,8 @@ __global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __rest
 #pragma unroll
   for (int d = 0; d < 3; ++d)
     if ((hb >> d) & 1u)
-      if (!uf_unite(R.label, (int32_t)((2 * d) * N + c), (int32_t)((2 * d + 1) * N + nb[d]))) st[r].err = 1;
+      if (!uf_unite(R.label, (int32_t)((2 * d) * N + c), (int32_t)((2 * d + 1) * N + nb[d]), R.union_iters))
+        st[r].err = 1;
 }
 
 // Compression, cluster shift and update in one pass, one thread per cell: each of the cell's six

@@ -316,6 +316,16 @@ int cvf_set_sweep_tile(cvf_handle* h, int vec, int* vec_out);
 int cvf_set_launch_mode(cvf_handle* h, int mode);
 int cvf_get_launch_mode(const cvf_handle* h, int* mode);
 
+/* Bounds of the handle's device waits, for tests of the error path: a grid-barrier wait of the
+ * persistent launch (mode 1) polls at most barrier_polls times, one Swendsen-Wang union gives up
+ * after union_iters attempts; either sets the replica's error word and the kernel returns, and
+ * the next cvf_synchronize reports CVF_ELIMIT (code 3 and code 1). A value < 0 restores the
+ * default (2^24 each, about a second of barrier polling; values above it are clamped to it). The
+ * state of the replicas after a wait gave up is not a Markov chain state any more: discard the
+ * handle. Replaces the reference's unbounded host-polled convergence loop (GW:1480-1555), which
+ * has no bound to set. */
+int cvf_set_wait_limits(cvf_handle* h, long long barrier_polls, long long union_iters);
+
 /* Replica groups of a batch (0 = automatic: 4 groups for 8 or more replicas, 2 for 2 to 7).
  * Metropolis-only steps of a batch are captured as one chain of per-phase kernels per group of
  * consecutive replicas (groups of about equal cell counts), on parallel branches of the CUDA

@@ -29,6 +29,9 @@ def test_version_string(engine_lib):
 @pytest.mark.parametrize("field,value,msg", [
     ("L", 7, b"even"),
     ("L", 2, b"even"),
+    ("L", 712, b"too large"),       # 6 L^3 > 2^31 - 1
+    ("L", 1200000, b"too large"),   # 6 L^3 would overflow a signed 64-bit product of ints
+    ("L", 2147483646, b"too large"),
     ("flag_chessboard", 2, b"Flag_chessboard"),
     ("start", 3, b"Flag_config"),
     ("T", 0.0, b"T must"),

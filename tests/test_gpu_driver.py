@@ -92,5 +92,5 @@ def test_driver_reproduces_reference_statistics(engine_lib, tmp_path):
         b = x.reshape(20, -1).mean(1)
         err = b.std(ddof=1) / math.sqrt(20)
         z = (x.mean() - stats[name]["mean"]) / math.hypot(err, stats[name]["block_err"])
-        assert abs(z) < 4.0, (name, x.mean(), stats[name]["mean"], z)
+        assert abs(z) < 2.0, (name, x.mean(), stats[name]["mean"], z)
     assert "Energy:" in open(tmp_path / "water3D.log").read()

@@ -1,6 +1,6 @@
 """Statistical pin on the reference's processed results: the density of the L=32 lattice along the
 isobar P=0.45 (PROCESSED_DATA/CVF_isobars.tar.gz, L32_P0.45_density.dat: rho = N/<V> with its
-error) is reproduced by the engine at T = 0.78, 0.80 and 0.82 within 4 combined standard errors
+error) is reproduced by the engine at T = 0.78, 0.80 and 0.82 within 2 combined standard errors
 (blocking), from disordered starts run as one batch of replicas."""
 import math
 import os
@@ -28,5 +28,5 @@ def test_isobar_density(engine_lib):
         err = N * (b.std(ddof=1) / math.sqrt(20)) / v.mean() ** 2
         want, want_err = table[t]
         z = (rho - want) / math.hypot(err, want_err)
-        assert abs(z) < 4.0, (t, rho, want, err, want_err, z)
+        assert abs(z) < 2.0, (t, rho, want, err, want_err, z)
     lat.close()

@@ -159,7 +159,7 @@ def test_reweighting_reproduces_direct_simulation(engine_lib):
     for k, col in ((0, 0), (1, 1)):
         err = block_err(d[:, col])
         z = (mean[k] - d[:, col].mean()) / err
-        assert abs(z) < 4.0, (k, mean[k], d[:, col].mean(), err)
+        assert abs(z) < 2.0, (k, mean[k], d[:, col].mean(), err)
     # adjoint response vs finite differences of the reweighted curve at T = 0.75 +/- 0.005
     beta = 1.0 / 0.75
     th = [beta, float(np.float32(P_)), 0, 0, 0]
