@@ -415,6 +415,14 @@ def bench_sw(steps, warmup, local, flush):
     return out
 
 
+def workload_config(n_gpus):
+    """The `config` object both arms print: the same workload, so the lines compare one to one."""
+    return {"workload": "L=256 ordered start, T=0.70, P=0.45, Metropolis only; 1 cube move + "
+                        "1 volume move + 1 checkerboard sweep per step", "L": L_BENCH, "cells": L_BENCH ** 3,
+            "l2": "64 MB lattice < 129 MB L2: a 256 MB buffer is written before every timed step",
+            "replicas": n_gpus}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -424,9 +432,8 @@ def run_reference(args):
     line = {"impl": "reference", "metric": "site-updates/ns at L=256", "value": base["value"],
             "unit": "site-updates/ns", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-            "data": "synthetic (ordered start, Philox seed 44648604)",
-            "config": {"workload": "L=256 ordered start, T=0.70, P=0.45, Metropolis only; "
-                                   "1 cube + 1 volume move + 1 checkerboard sweep per step", "L": 256},
+            "data": "synthetic (ordered start, Philox seed 44648604 + rank)",
+            "config": workload_config(args.gpus),
             "cpu_baseline": base,
             "e2e": {"value": base["value"], "unit": "site-updates/ns", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -525,10 +532,10 @@ def run_engine(args):
     out_cfg = lat2.get_config(out=out_buf)
     t1 = time.perf_counter()
     e2e_s = dist.max(t1 - t0)
-    packed = 4 * N + 2 * (L // 2) ** 3
+    cells12_bytes = 12 * 4 * N  # what crosses the host link each way: the caller's int32 cells12 array
     e2e = {"value": round(world * N * args.steps / (e2e_s * 1e9), 4), "unit": "site-updates/ns",
-           "h2d_bytes_per_step": int(round(packed / args.steps)),
-           "d2h_bytes_per_step": int(round(packed / args.steps)) + 32,
+           "h2d_bytes_per_step": int(round(cells12_bytes / args.steps)),
+           "d2h_bytes_per_step": int(round(cells12_bytes / args.steps)) + 32,
            "upload_ms": round(1e3 * (ta - t0), 3), "steps_ms": round(1e3 * (tb - ta), 3),
            "download_ms": round(1e3 * (t1 - tb), 3),
            "note": "per step: cvf_run_steps(1 step) + cvf_observables (measurement, 32 B D2H, sync); "
@@ -536,6 +543,36 @@ def run_engine(args):
                    "by the GPU in host memory, io_mode 1) and download (cvf_get_config: unpacked by the "
                    "GPU into the caller's array) amortised over the K steps"}
     del out_cfg
+    # the same sequence with the compact checkpoint format: cvf_set_packed + cvf_set_state in,
+    # cvf_get_packed + cvf_get_state out (4.25 bytes per cell each way instead of 48)
+    pk = lat.get_packed()
+    st = lat.state()
+    pk_out = np.zeros_like(pk)
+    lat2.set_packed(pk)
+    lat2.set_state(st[0], st[1], st[3])
+    for _ in range(max(3, args.warmup)):
+        lat2.run(1, 1, 0)
+        lat2.observables()
+    lat2.get_packed(out=pk_out)
+    dist.barrier()
+    t0 = time.perf_counter()
+    lat2.set_packed(pk)
+    lat2.set_state(st[0], st[1], st[3])
+    ta = time.perf_counter()
+    for _ in range(args.steps):
+        lat2.run(1, 1, 0)
+        lat2.observables()
+    tb = time.perf_counter()
+    lat2.get_packed(out=pk_out)
+    lat2.state()
+    t1 = time.perf_counter()
+    e2e_packed = {"value": round(world * N * args.steps / (dist.max(t1 - t0) * 1e9), 4), "unit": "site-updates/ns",
+                  "h2d_bytes_per_step": int(round((pk.size + 40) / args.steps)),
+                  "d2h_bytes_per_step": int(round((pk.size + 40) / args.steps)) + 32,
+                  "upload_ms": round(1e3 * (ta - t0), 3), "steps_ms": round(1e3 * (tb - ta), 3),
+                  "download_ms": round(1e3 * (t1 - tb), 3),
+                  "note": "as e2e with the packed checkpoint format: cvf_set_packed + cvf_set_state, per step "
+                          "cvf_run_steps + cvf_observables, cvf_get_packed + cvf_get_state (71 MB each way)"}
     # the drop-in driver's production loop: one sampled run call recording a sample after every
     # step on the device, the K records read back afterwards (after an untimed short run of the
     # same calls)
@@ -559,7 +596,7 @@ def run_engine(args):
                            "cvf_get_samples, cvf_get_config"}
     del out_cfg
 
-    extras = {"e2e_sampled": e2e_sampled}
+    extras = {"e2e_sampled": e2e_sampled, "e2e_packed": e2e_packed}
     if rank == 0 and world == 1 and not args.no_extras:
         extras["batched"] = bench_batch64(max(10, min(args.steps, 50)), args.warmup, local, flush)
         extras["swendsen_wang"] = bench_sw(max(10, min(args.steps, 30)), args.warmup, local, flush)
@@ -576,10 +613,8 @@ def run_engine(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 5),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (ordered start, Philox seed 44648604 + rank)",
-        "config": {"workload": "L=256 ordered start, T=0.70, P=0.45, Metropolis only; 1 cube move + "
-                               "1 volume move + 1 checkerboard sweep per step", "L": L, "cells": N,
-                   "l2": "64 MB lattice < 129 MB L2: a 256 MB buffer is written before every timed step",
-                   "replicas": world, "sweep_tile": tile},
+        "config": workload_config(world),
+        "sweep_tile": tile,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "kernel": f"k_sweep<{tile}> (one colour of the checkerboard sweep)",

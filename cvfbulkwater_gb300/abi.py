@@ -126,6 +126,9 @@ def lib():
         "cvf_profile_launch": (I, [P, I, I]),
         "cvf_cluster_stats_noalloc": (I, [P, I, P, P]),
         "cvf_set_wait_limits": (I, [P, C.c_longlong, C.c_longlong]),
+        "cvf_packed_size": (I, [P, I, C.POINTER(LL)]),
+        "cvf_get_packed": (I, [P, I, P, LL]),
+        "cvf_set_packed": (I, [P, I, P, LL]),
         "cvf_read_input_data": (I, [C.c_char_p, C.POINTER(Input)]),
         "cvf_read_config_file": (I, [C.c_char_p, P, LL]),
         "cvf_write_config_file": (I, [C.c_char_p, P, LL]),

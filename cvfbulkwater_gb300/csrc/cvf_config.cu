@@ -142,6 +142,30 @@ __global__ void k_pack_cubes(const uint8_t* __restrict__ eta6, uint32_t L, uint3
 
 static inline unsigned grid_of(unsigned long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
 
+// Validation of a packed state (cvf_set_packed) already copied to the device: words words[0..nw)
+// must hold six sigma fields in 0..5 and zero bits 18..31, bytes cubes[0..ncb) cube states 0..8.
+// The smallest offending index goes to *bad (words first, then cube bytes at nw + i).
+__global__ void k_check_packed(const uint32_t* __restrict__ words, unsigned long long nw,
+                               const uint8_t* __restrict__ cubes, unsigned long long ncb, unsigned long long* bad) {
+  const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool ok = true;
+  if (i < nw) {
+    const uint32_t w = words[i];
+    // a 3-bit field is above 5 (6 or 7) when its bits 2 and 1 are both set
+    ok = (w >> 18) == 0u && (w & (w << 1) & 0x24924u) == 0u;
+  } else if (i < nw + ncb) {
+    ok = cubes[i - nw] < 9u;
+  }
+  if (!ok) atomicMin(bad, i);
+}
+
+cudaError_t launch_check_packed(const uint32_t* words, unsigned long long nw, const uint8_t* cubes,
+                                unsigned long long ncb, unsigned long long* bad, cudaStream_t s) {
+  const unsigned long long n = nw + ncb;
+  k_check_packed<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(words, nw, cubes, ncb, bad);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pack_config(const ReplicaDesc& R, const int* c12, uint32_t* cells0, uint32_t* cells1, uint8_t* eta6,
                                uint8_t* ce, uint8_t* co, unsigned long long* bad, cudaStream_t s) {
   const uint32_t L = (uint32_t)R.L, H = (uint32_t)R.H, N = L * L * L;

@@ -21,6 +21,7 @@ struct ReplicaDesc {
   // Swendsen-Wang work arrays (null until the first SW step)
   int32_t* label;     // 6N parents / labels
   uint8_t* hbmask;    // N: bits 0..2 = active x+, y+, z+ cluster bonds
+  uint32_t* flip;     // N: bits 3a..3a+2 = shift of the cluster whose root is arm site a of the cell
   int32_t* csize;     // 6N: cluster sizes by root
   int32_t* cand;      // 6N: percolation candidate id by root (-1 none)
   uint32_t* cover;    // max_cand * 3 * W: coordinate coverage bitmaps
@@ -207,6 +208,11 @@ cudaError_t launch_pack_config(const ReplicaDesc& R, const int* c12, uint32_t* c
 // 16-byte aligned array in host memory (pageable-memory access); cudaErrorInvalidValue if the
 // array is not aligned.
 cudaError_t launch_unpack_config(const ReplicaDesc& R, int* c12, cudaStream_t s);
+// Checks a packed state on the device (sigma fields in 0..5 with bits 18..31 zero in the nw
+// words, cube states 0..8 in the ncb bytes); *bad must start at nw + ncb and receives the smallest
+// offending index (cube byte i at nw + i).
+cudaError_t launch_check_packed(const uint32_t* words, unsigned long long nw, const uint8_t* cubes,
+                                unsigned long long ncb, unsigned long long* bad, cudaStream_t s);
 void launch_cluster_stats_impl(const BatchDev& b, unsigned long long* blocktop, int record, cudaStream_t s);
 
 #ifdef __CUDACC__

@@ -294,6 +294,7 @@ static int ensure_sw(cvf_handle* h) {
     r.desc.max_cand = 3 * r.L * r.L;  // at most 6N / 2L clusters of size >= 2L
     if (int rc = dev_alloc(h, (void**)&r.desc.label, NS * sizeof(int32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.hbmask, (size_t)r.N)) return rc;
+    if (int rc = dev_alloc(h, (void**)&r.desc.flip, (size_t)r.N * sizeof(uint32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.csize, NS * sizeof(int32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.cand, NS * sizeof(int32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.cover, (size_t)r.desc.max_cand * 3 * W * sizeof(uint32_t))) return rc;
@@ -769,6 +770,64 @@ int cvf_get_config(cvf_handle* h, int r, int* c12, long long n_cells) {
   if (h->nhb_mode)  // Flag_chessboard = 0: eta as read (GW:1296-1305 writes active_bond)
     for (long long c = 0; c < R.N; ++c)
       for (int a = 0; a < 6; ++a) c12[c * 12 + 6 + a] = (e6[c] >> a) & 1;
+  return 0;
+}
+
+// Packed state of one replica: the colour-0 words, the colour-1 words, the even-origin cube
+// states, the odd-origin cube states, exactly as the replica holds them on the device.
+static long long packed_bytes(const ReplicaHost& R) { return 4 * R.N + 2LL * R.H * R.H * R.H; }
+
+int cvf_packed_size(const cvf_handle* h, int r, long long* bytes) {
+  if (int rc = check_rep(h, r)) return rc;
+  if (!bytes) return fail(CVF_EINVAL, "null bytes");
+  *bytes = packed_bytes(h->reps[r]);
+  return 0;
+}
+
+int cvf_get_packed(cvf_handle* h, int r, void* buf, long long bytes) {
+  if (int rc = check_rep(h, r)) return rc;
+  if (h->nhb_mode) return fail(CVF_EINVAL, "the packed state holds cube states: Flag_chessboard = 1 only");
+  ReplicaHost& R = h->reps[r];
+  if (!buf || bytes != packed_bytes(R)) return fail(CVF_EINVAL, "packed buffer must hold 4 N + 2 (L/2)^3 bytes");
+  CK(cudaSetDevice(h->device));
+  const size_t half = (size_t)(R.N / 2), nc = (size_t)R.H * R.H * R.H;
+  uint8_t* p = (uint8_t*)buf;
+  CK(cudaMemcpyAsync(p, R.desc.cells[0], half * 4, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(p + half * 4, R.desc.cells[1], half * 4, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(p + half * 8, R.desc.cubes[0], nc, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(p + half * 8 + nc, R.desc.cubes[1], nc, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int cvf_set_packed(cvf_handle* h, int r, const void* buf, long long bytes) {
+  if (int rc = check_rep(h, r)) return rc;
+  if (h->nhb_mode) return fail(CVF_EINVAL, "the packed state holds cube states: Flag_chessboard = 1 only");
+  ReplicaHost& R = h->reps[r];
+  if (!buf || bytes != packed_bytes(R)) return fail(CVF_EINVAL, "packed buffer must hold 4 N + 2 (L/2)^3 bytes");
+  h->count_valid = false;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  // copied and checked in scratch first: the lattice changes only when every value is valid
+  if (int rc = ensure_io_scratch(h, R)) return rc;
+  const size_t half = (size_t)(R.N / 2), nc = (size_t)R.H * R.H * R.H;
+  uint8_t* d = (uint8_t*)h->io_scratch;
+  CK(cudaMemcpyAsync(d, buf, (size_t)bytes, cudaMemcpyHostToDevice, h->stream));
+  const unsigned long long nw = 2 * half, ncb = 2 * nc;
+  unsigned long long bad = nw + ncb;
+  CK(cudaMemcpyAsync(h->io_bad, &bad, sizeof(bad), cudaMemcpyHostToDevice, h->stream));
+  CK(launch_check_packed((const uint32_t*)d, nw, d + 4 * nw, ncb, h->io_bad, h->stream));
+  CK(cudaMemcpyAsync(&bad, h->io_bad, sizeof(bad), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (bad < nw)
+    return fail(CVF_ECONFIG, "packed state: word " + std::to_string(bad) + " holds a sigma above 5 or bits above 17");
+  if (bad < nw + ncb)
+    return fail(CVF_ECONFIG, "packed state: cube byte " + std::to_string(bad - nw) + " is not a state 0..8");
+  CK(cudaMemcpyAsync(R.desc.cells[0], d, half * 4, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(R.desc.cells[1], d + half * 4, half * 4, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(R.desc.cubes[0], d + half * 8, nc, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(R.desc.cubes[1], d + half * 8 + nc, nc, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
   return 0;
 }
 

@@ -356,6 +356,27 @@ __device__ __forceinline__ void fill_cube_tables(const ReplicaDesc& R, CubeTable
   }
 }
 
+// The accepted raw proposal word of a cube group when words 0 and 3 both fell in the rejected
+// range of the exact draw in [0, 9^4) (p ~ 1.3e-6 each).
+__device__ __noinline__ uint32_t cube_proposal_retry(uint32_t gid, uint32_t t, const ReplicaDesc* R) {
+  uint32_t w = 0;
+  for (uint32_t k = 0; k < 256; ++k) {
+    w = philox(gid, t, retry_tag(kStCube, k), R->replica, R->key0, R->key1).x;
+    if (w * 6561u >= 5476u) return w;
+  }
+  return w;
+}
+
+// Acceptance of cube kk of a group when the high half hu of its uniform tied with T >> 16: the
+// low half from the group's refinement block.
+__device__ __noinline__ bool cube_accept_exact(uint32_t gid, uint32_t t, uint32_t kk, uint32_t hu,
+                                               unsigned long long T, const ReplicaDesc* R) {
+  const U4 rf = philox(gid, t, kStCubeRefine, R->replica, R->key0, R->key1);
+  const uint32_t word = kk < 2 ? rf.y : rf.z;
+  const uint32_t lo = (kk & 1) ? (word >> 16) : (word & 0xffffu);
+  return ((((unsigned long long)hu) << 16) | lo) < T;
+}
+
 // GW:3374-3466. One thread per VC consecutive cubes along x of one parity (both parities in one
 // launch: cubes share no edge and sigma is frozen, so all cube decisions are independent). The
 // parity of the block's index among the replica's blocks in the table blk (blk_cubev) is the
@@ -403,7 +424,22 @@ __device__ __forceinline__ void cube_move_v(const ReplicaDesc& R, const CubeTabl
   else packed = *cs;
 #pragma unroll
   for (int k = 0; k < VC; ++k) st[k] = (packed >> (8 * k)) & 0xffu;
-  const uint32_t cid0 = 2 * a0 + par + L * (y0 + L * z0);
+  // one Philox block per group of four cubes along x (the thread's VC cubes lie in one group):
+  // words 0, 3 give the four proposals as base-9 digits of an exact uniform in [0, 9^4), words
+  // 1, 2 the high halves of the four acceptance uniforms
+  const uint32_t kk0 = a0 & 3u;
+  const uint32_t gid = 2 * (a0 - kk0) + par + L * (y0 + L * z0);
+  const U4 rr = philox(gid, t, kStCube, R.replica, R.key0, R.key1);
+  uint32_t u = rr.x;
+  if (u * 6561u < 5476u) u = rr.w;
+  if (u * 6561u < 5476u) u = cube_proposal_retry(gid, t, &R);
+  uint32_t dig[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const unsigned long long m = (unsigned long long)u * 9ull;
+    dig[j] = (uint32_t)(m >> 32);
+    u = (uint32_t)m;
+  }
   bool changed = false;
 #pragma unroll
   for (int k = 0; k < VC; ++k) {
@@ -416,14 +452,16 @@ __device__ __forceinline__ void cube_move_v(const ReplicaDesc& R, const CubeTabl
       const uint32_t x = ((w[p0][k] << 3) ^ w[p1][k]) & (7u << (6 * d + 3));
       D |= (x == 0u ? 1u : 0u) << e;
     }
-    const uint32_t cid = cid0 + 2u * k;
-    const U4 rr = philox(cid, t, kStCube, R.replica, R.key0, R.key1);
-    uint32_t nw;
-    if (!lemire_try(rr.x, 9, nw) && !lemire_try(rr.z, 9, nw) && !lemire_try(rr.w, 9, nw))
-      nw = lemire_retry(9, cid, t, kStCube, R.replica, R.key0, R.key1);
+    const uint32_t kk = VC == 4 ? (uint32_t)k : kk0 + (uint32_t)k;
+    const uint32_t nw = VC == 4 ? dig[k] : (kk == 0 ? dig[0] : (kk == 1 ? dig[1] : (kk == 2 ? dig[2] : dig[3])));
     const uint32_t old = st[k];
     const int dhb = __popc(ct->act[nw] & D) - __popc(ct->act[old] & D);
-    if ((unsigned long long)rr.y < ct->thr[dhb + 4] && nw != old) {
+    const unsigned long long T = ct->thr[dhb + 4];
+    const uint32_t word = kk < 2 ? rr.y : rr.z;
+    const uint32_t hu = (kk & 1) ? (word >> 16) : (word & 0xffffu);
+    const uint32_t th = (uint32_t)(T >> 16);
+    const bool acc = hu != th ? hu < th : cube_accept_exact(gid, t, kk, hu, T, &R);
+    if (acc && nw != old) {
       st[k] = nw;
       changed = true;
       cdh += dhb;

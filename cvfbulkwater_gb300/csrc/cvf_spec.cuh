@@ -50,13 +50,15 @@ constexpr int kMaxShells = 512;
 enum : uint32_t {
   kStSweep = 0x01u,        // per cell per sweep: w0 proposals, w1..w3 accept high halves
   kStSweepRefine = 0x02u,  // per cell per sweep, drawn only on a high-half tie
-  kStCube = 0x03u,         // per cube per cube move: w0,w2,w3 proposal, w1 accept
+  kStCube = 0x03u,         // per 4 cubes along x per cube move: w0,w3 proposals, w1,w2 accept high halves
   kStVolume = 0x04u,       // per volume move: (w0,w1) trial, (w2,w3) accept
-  kStSwFlip = 0x05u,       // per cluster root per SW step
+  kStSwFlip = 0x05u,       // retry streams of the cluster-shift digits (words 9, 10 of the bond blocks)
   kStInitSigma = 0x06u,
   kStInitCube = 0x07u,
   kStInitOrder = 0x08u,
-  kStSwBond = 0x10u,       // + 0..4: 20 words per cell per SW step, 18 used
+  kStCubeRefine = 0x09u,   // per 4 cubes per cube move, drawn only on a high-half tie
+  kStSwBond = 0x10u,       // + 0..2: 12 words per cell per SW step: 18 link high halves, shift digits
+  kStSwBondRefine = 0x18u, // + 0..2: the links' low halves, drawn only on a high-half tie
 };
 CVF_HD uint32_t retry_tag(uint32_t kind, uint32_t k) { return 0x1000u | (kind << 8) | k; }
 

@@ -67,8 +67,42 @@ __device__ __forceinline__ uint32_t eta_of_cell(const ReplicaDesc& R, int x, int
 }
 
 // ---------------------------------------------------------------- bonds + in-cell components
+// Random numbers of a cell per SW step: three Philox blocks (kStSwBond + 0..2, words 0..11).
+// Link l (0..17) is decided by the 32-bit uniform U whose high half is half (l & 1) of word
+// l >> 1; the low half, at the same position of the refinement blocks kStSwBondRefine + 0..2, is
+// drawn only when the high half equals T >> 16 (p ~ 2^-16 per link): U < T with T in [0, 2^32].
+// Words 9 and 10 (then the retry streams of kStSwFlip) give an exact uniform in [0, 6^6) whose
+// base-6 digits, most significant first, are the shifts of the clusters rooted at the cell's arm
+// sites 0..5 (GW:2531-2542 draws one shift per cluster).
+__device__ __noinline__ bool sw_link_exact(uint32_t c, uint32_t t, int l, uint32_t hi, unsigned long long T,
+                                           const ReplicaDesc* R) {
+  const U4 rf = philox(c, t, kStSwBondRefine + (uint32_t)(l >> 3), R->replica, R->key0, R->key1);
+  const int k = (l >> 1) & 3;
+  const uint32_t word = k == 0 ? rf.x : (k == 1 ? rf.y : (k == 2 ? rf.z : rf.w));
+  const uint32_t lo = (word >> (16 * (l & 1))) & 0xffffu;
+  return ((((unsigned long long)hi) << 16) | lo) < T;
+}
+
+// The accepted raw word of the shift digits when words 9 and 10 both fell in the rejected range.
+__device__ __noinline__ uint32_t sw_flip_retry(uint32_t c, uint32_t t, const ReplicaDesc* R) {
+  uint32_t w = 0;
+  for (uint32_t k = 0; k < 256; ++k) {
+    w = philox(c, t, retry_tag(kStSwFlip, k), R->replica, R->key0, R->key1).x;
+    if (w * 46656u >= 2560u) return w;
+  }
+  return w;
+}
+
+// U < T for link l from the high half of word `word`; th = T >> 16 (up to 65536).
+__device__ __forceinline__ bool sw_link(uint32_t word, int l, uint32_t th, unsigned long long T, uint32_t c,
+                                        uint32_t t, const ReplicaDesc& R) {
+  const uint32_t hi = (l & 1) ? (word >> 16) : (word & 0xffffu);
+  if (hi != th) return hi < th;
+  return sw_link_exact(c, t, l, hi, T, &R);
+}
+
 // GW:2383-2438: links 0..2 are the x+, y+, z+ hydrogen-bond links of the cell, links 3..17 the
-// intra-cell pairs (a<b) in row-major order. Each link draws word l of the cell's 20-word block.
+// intra-cell pairs (a<b) in row-major order.
 __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __restrict__ reps,
                                                        const ReplicaState* __restrict__ st,
                                                        const int* __restrict__ blk, int nrep, int jsw) {
@@ -84,9 +118,9 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
   pdl_wait();
   const uint32_t t = st[r].cur[3] + (uint32_t)jsw;
   const uint32_t w = word_at(R, x, y, z);
-  uint32_t rw[20];
+  uint32_t rw[12];
 #pragma unroll
-  for (int j = 0; j < 5; ++j) {
+  for (int j = 0; j < 3; ++j) {
     U4 q = philox((uint32_t)c, t, kStSwBond + j, R.replica, R.key0, R.key1);
     rw[4 * j] = q.x;
     rw[4 * j + 1] = q.y;
@@ -94,6 +128,7 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
     rw[4 * j + 3] = q.w;
   }
   const unsigned long long thb = R.thr_sw[0], ts = R.thr_sw[1];
+  const uint32_t thb_hi = (uint32_t)(thb >> 16), ts_hi = (uint32_t)(ts >> 16);
   uint32_t hb = 0;
   if (R.Jeff != 0.0) {
     const uint32_t eta = eta_of_cell(R, x, y, z);
@@ -101,11 +136,9 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
     const uint32_t wn[3] = {word_at(R, xn, y, z), word_at(R, x, yn, z), word_at(R, x, y, zn)};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      uint32_t sa = (w >> (6 * d)) & 7u, sb = (wn[d] >> (6 * d + 3)) & 7u;
-      bool b;
-      if (R.Jeff > 0.0) b = ((eta >> (2 * d)) & 1u) && sa == sb && (unsigned long long)rw[d] < thb;
-      else b = sa != sb && (unsigned long long)rw[d] < thb;
-      hb |= (uint32_t)b << d;
+      const uint32_t sa = (w >> (6 * d)) & 7u, sb = (wn[d] >> (6 * d + 3)) & 7u;
+      const bool cond = R.Jeff > 0.0 ? (((eta >> (2 * d)) & 1u) && sa == sb) : sa != sb;
+      if (cond && sw_link(rw[d >> 1], d, thb_hi, thb, c, t, R)) hb |= 1u << d;
     }
   }
   R.hbmask[c] = (uint8_t)hb;
@@ -116,9 +149,21 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
   for (int a = 0; a < 5; ++a)
 #pragma unroll
     for (int b = a + 1; b < 6; ++b, ++l) {
-      const bool bond = ((w >> (3 * a)) & 7u) == ((w >> (3 * b)) & 7u) && (unsigned long long)rw[l] < ts;
-      bm |= (uint32_t)bond << (l - 3);
+      if (((w >> (3 * a)) & 7u) == ((w >> (3 * b)) & 7u) && sw_link(rw[l >> 1], l, ts_hi, ts, c, t, R))
+        bm |= 1u << (l - 3);
     }
+  // shift digits of the clusters rooted at this cell's arm sites
+  uint32_t u = rw[9];
+  if (u * 46656u < 2560u) u = rw[10];
+  if (u * 46656u < 2560u) u = sw_flip_retry(c, t, &R);
+  uint32_t fw = 0;
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    const unsigned long long m = (unsigned long long)u * 6ull;
+    fw |= (uint32_t)(m >> 32) << (3 * a);
+    u = (uint32_t)m;
+  }
+  R.flip[c] = fw;
   // in-cell components: lab holds 3 bits per arm, the smallest arm of its component; merging
   // two components rewrites every field equal to the larger minimum with the smaller one
   const unsigned long long kPairA = 0x11b491248000ull, kPairB = 0x16cb1d8d58d1ull;  // e -> (a, b), 3 bits each
@@ -129,8 +174,8 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
     const uint32_t a = (uint32_t)(kPairA >> (3 * e)) & 7u, b = (uint32_t)(kPairB >> (3 * e)) & 7u;
     const uint32_t la = (lab >> (3 * a)) & 7u, lb = (lab >> (3 * b)) & 7u;
     const uint32_t lo = la < lb ? la : lb, hi = la < lb ? lb : la;
-    const uint32_t x = lab ^ (hi * 0x9249u);
-    const uint32_t m7 = (~(x | (x >> 1) | (x >> 2)) & 0x9249u) * 7u;
+    const uint32_t xx = lab ^ (hi * 0x9249u);
+    const uint32_t m7 = (~(xx | (xx >> 1) | (xx >> 2)) & 0x9249u) * 7u;
     lab = (lab & ~m7) | ((lo * 0x9249u) & m7);
   }
 #pragma unroll
@@ -196,10 +241,9 @@ __global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __rest
 
 // Compression, cluster shift and update in one pass, one thread per cell: each of the cell's six
 // sites walks to its root (the component's minimum site id) and stores it as its label, then
-// draws the root's shift itself -- GW:2531-2542 gives every cluster one uniform shift in 0..5;
-// here it is the exact uniform from word (root & 3) of the flip block of counter root >> 2
-// (retry streams of the root on a rejection), so every site of a cluster draws the same value --
-// and shifts its sigma. A repeated root reuses the previous arm's draw.
+// takes the root's shift -- GW:2531-2542 gives every cluster one uniform shift in 0..5; here it
+// is digit a of the shift word that k_sw_local drew for cell c, for the root site a*N + c -- and
+// shifts its sigma. A repeated root reuses the previous arm's shift.
 __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __restrict__ reps,
                                                         const ReplicaState* __restrict__ st,
                                                         const int* __restrict__ blk, int nrep, int jsw) {
@@ -211,7 +255,6 @@ __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __res
   const uint32_t c = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
   if (c >= N) return;
   pdl_wait();
-  const uint32_t t = st[r].cur[3] + (uint32_t)jsw;
   int32_t roots[6];
 #pragma unroll
   for (int a = 0; a < 6; ++a) {
@@ -229,16 +272,22 @@ __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __res
   cell_xyz(R, c, x, y, z);
   uint32_t* wp = R.cells[(x + y + z) & 1] + (uint32_t)(x >> 1) + (uint32_t)R.H * ((uint32_t)y + (uint32_t)L * (uint32_t)z);
   const uint32_t w = *wp;
+  const uint32_t own_flip = R.flip[c];
   uint32_t out = 0, sh = 0;
   int32_t last = -1;
 #pragma unroll
   for (int a = 0; a < 6; ++a) {
     const int32_t root = roots[a];
     if (root != last) {
-      const U4 qq = philox((uint32_t)root >> 2, t, kStSwFlip, R.replica, R.key0, R.key1);
-      const uint32_t k = (uint32_t)root & 3u;
-      const uint32_t word = k == 0 ? qq.x : (k == 1 ? qq.y : (k == 2 ? qq.z : qq.w));
-      if (!lemire_try(word, 6, sh)) sh = lemire_retry(6, (uint32_t)root, t, kStSwFlip, R.replica, R.key0, R.key1);
+      uint32_t rc = (uint32_t)root, ra = 0;
+#pragma unroll
+      for (int k = 0; k < 5; ++k)
+        if (rc >= N) {
+          rc -= N;
+          ++ra;
+        }
+      const uint32_t fw = rc == c ? own_flip : R.flip[rc];
+      sh = (fw >> (3 * ra)) & 7u;
       last = root;
     }
     uint32_t v = ((w >> (3 * a)) & 7u) + sh;

@@ -89,6 +89,25 @@ class Lattice:
         check(lib().cvf_get_config(self._h, r, _ptr(a), self.N(r)))
         return a
 
+    def packed_size(self, r: int = 0) -> int:
+        n = C.c_longlong()
+        check(lib().cvf_packed_size(self._h, r, C.byref(n)))
+        return n.value
+
+    def get_packed(self, r: int = 0, out: np.ndarray = None) -> np.ndarray:
+        """The replica's packed state (colour words, then cube states) as uint8; pass `out` to
+        reuse a buffer."""
+        n = self.packed_size(r)
+        a = np.empty(n, dtype=np.uint8) if out is None else out
+        if a.dtype != np.uint8 or a.size != n or not a.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous uint8 array of packed_size() bytes")
+        check(lib().cvf_get_packed(self._h, r, _ptr(a), n))
+        return a
+
+    def set_packed(self, buf: np.ndarray, r: int = 0):
+        a = np.ascontiguousarray(buf, dtype=np.uint8)
+        check(lib().cvf_set_packed(self._h, r, _ptr(a), a.size))
+
     def set_distances(self, dist, freq, r: int = 0):
         d = np.ascontiguousarray(dist, dtype=np.float32)
         f = np.ascontiguousarray(freq, dtype=np.int32)

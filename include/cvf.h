@@ -112,6 +112,22 @@ int cvf_set_config(cvf_handle* h, int replica, const int* cells12, long long n_c
 /* Replaces the config.out writer GW:1296-1305. */
 int cvf_get_config(cvf_handle* h, int replica, int* cells12, long long n_cells);
 
+/* Packed state of a replica, for checkpoint and resume without the text format: the engine's own
+ * device layout, 4 N + 2 (L/2)^3 bytes (about 4.25 bytes per cell against the 48 of cells12):
+ *   bytes [0, 2N):          the N/2 colour-0 words ((x+y+z) even), word (x>>1) + (L/2)*(y + L*z),
+ *                           bits 3a..3a+2 = sigma_a (arm a), bits 18..31 zero;
+ *   bytes [2N, 4N):         the N/2 colour-1 words, the same layout;
+ *   then (L/2)^3 bytes:     states 0..8 of the cubes with even origins (2i, 2j, 2k), index
+ *                           i + (L/2)*(j + (L/2)*k);
+ *   then (L/2)^3 bytes:     the cubes with odd origins (2i+1, 2j+1, 2k+1), the same index.
+ * eta of every arm follows from the two cube states (the cube numbering of SOURCE/chessboard.h).
+ * cvf_set_packed checks every value (CVF_ECONFIG, lattice unchanged) before it loads the state;
+ * with cvf_set_state it resumes a chain exactly. Flag_chessboard = 1 only. No reference
+ * counterpart (the reference's only state file is config.out, GW:1296-1305). */
+int cvf_packed_size(const cvf_handle* h, int replica, long long* bytes);
+int cvf_get_packed(cvf_handle* h, int replica, void* buf, long long bytes);
+int cvf_set_packed(cvf_handle* h, int replica, const void* buf, long long bytes);
+
 /* vdW shell table (GW:865-989). The library computes it at create (Flag_distances=0);
  * set_distances loads a table read from a distances file (Flag_distances=1). */
 int cvf_set_distances(cvf_handle* h, int replica, const float* dist, const int* freq, int n);

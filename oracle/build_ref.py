@@ -8,8 +8,10 @@
                         the reference's finite-difference programs of
                         CVF_ThermodynamicAnalysis/*.c, compiled as they are with gcc (tools()).
 
-Run where the reference checkout exists (argument: its path); elsewhere the tests that need
-them skip. Nothing from the reference is copied into the repository; the output stays in the
+Run where the reference checkout exists: its path is the argument, else the environment variable
+CVF_REFERENCE_DIR, else the checkout's location in the build container (DEFAULT_CHECKOUT, the one
+place the repository names it). Where none exists (the GPU box) every call returns None or {}
+and the tests that need these builds skip. Nothing from the reference is copied into the repository; the output stays in the
 git-ignored oracle/_ref/.
 """
 from __future__ import annotations
@@ -19,11 +21,23 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_CHECKOUT = "/root/reference"
+
+
+def checkout(ref: str | None = None) -> str | None:
+    """The reference checkout to build from, or None where there is none."""
+    for cand in (ref, os.environ.get("CVF_REFERENCE_DIR"), DEFAULT_CHECKOUT):
+        if cand and os.path.isdir(os.path.join(cand, "SOURCE")):
+            return cand
+    return None
 OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libref_correlator.so")
 
 
-def build(ref: str = "/root/reference", force: bool = False):
+def build(ref: str | None = None, force: bool = False):
+    ref = checkout(ref)
+    if ref is None:
+        return None
     src = os.path.join(ref, "SOURCE", "gpu_water3D.cu")
     if not os.path.exists(src):
         return None
@@ -49,9 +63,12 @@ def build(ref: str = "/root/reference", force: bool = False):
 TOOLS = ("AlphaPderivate", "CPderivate", "KTderivate")
 
 
-def tools(ref: str = "/root/reference"):
+def tools(ref: str | None = None):
     """{name: path} of the three analysis programs, built from the reference's own .c files with
     gcc -O2 (empty where the checkout is absent)."""
+    ref = checkout(ref)
+    if ref is None:
+        return {}
     src_dir = os.path.join(ref, "CVF_ThermodynamicAnalysis")
     out = {}
     for name in TOOLS:

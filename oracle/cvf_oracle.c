@@ -46,7 +46,9 @@
 #define ST_INIT_SIGMA 0x06u
 #define ST_INIT_CUBE 0x07u
 #define ST_INIT_ORDER 0x08u
-#define ST_SW_BOND 0x10u /* + 0..4 */
+#define ST_CUBE_REFINE 0x09u
+#define ST_SW_BOND 0x10u        /* + 0..2 */
+#define ST_SW_BOND_REFINE 0x18u /* + 0..2 */
 #define ST_RETRY(kind, k) (0x1000u | ((uint32_t)(kind) << 8) | (uint32_t)(k))
 
 /* ------------------------------------------------------------------ Philox */
@@ -526,31 +528,53 @@ void oracle_get_cubes(const oracle_t* o, uint8_t* ev, uint8_t* od)
 
 /* ------------------------------------------------------------ moves */
 /* Cube (chessboard) Metropolis move: GW:3374-3466, CPU twin CB:326-478. All cubes at once:
- * cubes share no edge and sigma is fixed, so the update order does not matter. */
+ * cubes share no edge and sigma is fixed, so the update order does not matter.
+ * Random numbers: the cubes of one parity are grouped by four consecutive along x (origins
+ * x = 2*hx + parity, hx = 4g .. 4g+3, same y and z; the last group of a row holds fewer when
+ * L/2 is not a multiple of 4). Group g draws one Philox block at the cell id of its first cube's
+ * origin: words 0 and 3 (then the retry streams of ST_CUBE) give an exact uniform in [0, 9^4)
+ * whose base-9 digit k (most significant first) is the proposed state of cube hx = 4g + k; the
+ * acceptance uniform of cube k is the 32-bit U with high half (k & 1) of word 1 + (k >> 1) and
+ * low half at the same position of the refinement block (ST_CUBE_REFINE), drawn only when the
+ * high half equals T >> 16. */
 void oracle_cube_move(oracle_t* o)
 {
     int L = o->L;
     int64_t N = o->N, ncubes = N / 4;
     uint32_t t = o->ctr[1];
+    static const uint32_t pow9[4] = {729, 81, 9, 1};
 #pragma omp parallel for schedule(static) num_threads(o->nthreads)
     for (int64_t i = 0; i < ncubes; ++i) {
         int x, y, z;
         cube_origin_from_index(L, i, &x, &y, &z);
-        uint32_t cid = (uint32_t)cell_of(L, x, y, z);
+        int hx = x / 2, k = hx & 3, odd = x & 1;
+        uint32_t gid = (uint32_t)cell_of(L, 2 * (hx - k) + odd, y, z);
         uint32_t r[4];
-        rng(o, cid, t, ST_CUBE, r);
-        uint32_t pw[3] = {r[0], r[2], r[3]};
-        int nw = (int)draw_below(o, NSOL, pw, 3, cid, t, ST_CUBE);
+        rng(o, gid, t, ST_CUBE, r);
+        uint32_t pw[2] = {r[0], r[3]};
+        uint32_t d = draw_below(o, 6561u, pw, 2, gid, t, ST_CUBE);
+        int nw = (int)((d / pow9[k]) % 9);
         int old = o->cube[i];
         int dhb = 0;
         for (int e = 0; e < EDGES; ++e) {
             int64_t v0, v1;
             edge_cells(L, x, y, z, e, &v0, &v1);
-            int d = edge_dir[e];
-            int same = o->s[(int64_t)(2 * d) * N + v0] == o->s[(int64_t)(2 * d + 1) * N + v1];
+            int dd = edge_dir[e];
+            int same = o->s[(int64_t)(2 * dd) * N + v0] == o->s[(int64_t)(2 * dd + 1) * N + v1];
             dhb += (sol_active(nw, e) - sol_active(old, e)) * same;
         }
-        if (!((uint64_t)r[1] < o->thr_cube[dhb + 4])) nw = old;
+        uint64_t T = o->thr_cube[dhb + 4];
+        uint32_t hU = (r[1 + (k >> 1)] >> (16 * (k & 1))) & 0xffffu;
+        int acc;
+        if ((uint64_t)hU != (T >> 16)) {
+            acc = (uint64_t)hU < (T >> 16);
+        } else {
+            uint32_t rf[4];
+            rng(o, gid, t, ST_CUBE_REFINE, rf);
+            uint32_t lU = (rf[1 + (k >> 1)] >> (16 * (k & 1))) & 0xffffu;
+            acc = ((((uint64_t)hU) << 16) | lU) < T;
+        }
+        if (!acc) nw = old;
         o->cube[i] = (uint8_t)nw;
         cube_write_eta(o, x, y, z, nw);
     }
@@ -735,45 +759,58 @@ static void uf_union(int32_t* p, int32_t a, int32_t b)
     else p[ra] = rb;
 }
 
+/* Bond decision of link l of a cell from its three bond blocks w[0..11]: U < T for the 32-bit
+ * uniform U whose high half is half (l & 1) of word l >> 1 and whose low half sits at the same
+ * position of the cell's refinement blocks (ST_SW_BOND_REFINE + 0..2), drawn only when the high
+ * half equals T >> 16. */
+static int sw_link(const oracle_t* o, const uint32_t* w, int l, uint64_t T, uint32_t c, uint32_t t)
+{
+    uint32_t hU = (w[l >> 1] >> (16 * (l & 1))) & 0xffffu;
+    if ((uint64_t)hU != (T >> 16)) return (uint64_t)hU < (T >> 16);
+    uint32_t rf[4];
+    rng(o, c, t, ST_SW_BOND_REFINE + (uint32_t)(l >> 3), rf);
+    uint32_t lU = (rf[(l >> 1) & 3] >> (16 * (l & 1))) & 0xffffu;
+    return ((((uint64_t)hU) << 16) | lU) < T;
+}
+
 /* Bonds GW:2383-2438 (18 links per cell: x+, y+, z+ hydrogen-bond links then the 15
  * intra-cell pairs a<b in row-major order), components over the 6N arm sites labelled by
- * their minimum site id (the fixed point of GW:2440-2529), cluster shift GW:2531-2542. */
+ * their minimum site id (the fixed point of GW:2440-2529), cluster shift GW:2531-2542.
+ * Random numbers per cell and SW step: three Philox blocks (ST_SW_BOND + 0..2, words w[0..11]);
+ * link l uses the 16-bit halves described at sw_link; words 9, 10 (then the retry streams of
+ * ST_SW_FLIP) give an exact uniform d in [0, 6^6) whose base-6 digit a (most significant first)
+ * is the shift of the cluster whose root is the cell's arm site a. */
 void oracle_sw_step(oracle_t* o)
 {
     int L = o->L;
     int64_t N = o->N, NS = ARMS * N;
     uint32_t t = o->ctr[3];
     int32_t* p = o->label;
+    static const uint32_t pow6[ARMS] = {7776, 1296, 216, 36, 6, 1};
+    uint8_t* shift = (uint8_t*)malloc(NS > 0 ? (size_t)NS : 1);
     for (int64_t i = 0; i < NS; ++i) p[i] = (int32_t)i;
     for (int64_t c = 0; c < N; ++c) {
-        uint32_t w[20];
-        for (uint32_t j = 0; j < 5; ++j) rng(o, (uint32_t)c, t, ST_SW_BOND + j, &w[4 * j]);
+        uint32_t w[12];
+        for (uint32_t j = 0; j < 3; ++j) rng(o, (uint32_t)c, t, ST_SW_BOND + j, &w[4 * j]);
         for (int d = 0; d < 3; ++d) {
             int64_t A = (int64_t)(2 * d) * N + c;
             int64_t B = (int64_t)(2 * d + 1) * N + neighbour(L, c, 2 * d);
             int bond = 0;
             if (o->Jeff > 0)
-                bond = o->eta[A] && o->s[A] == o->s[B] && (uint64_t)w[d] < o->thr_sw[0];
+                bond = o->eta[A] && o->s[A] == o->s[B] && sw_link(o, w, d, o->thr_sw[0], (uint32_t)c, t);
             else if (o->Jeff < 0)
-                bond = o->s[A] != o->s[B] && (uint64_t)w[d] < o->thr_sw[0];
+                bond = o->s[A] != o->s[B] && sw_link(o, w, d, o->thr_sw[0], (uint32_t)c, t);
             if (bond) uf_union(p, (int32_t)A, (int32_t)B);
         }
         int l = 3;
         for (int a = 0; a < ARMS - 1; ++a)
             for (int b = a + 1; b < ARMS; ++b, ++l)
-                if (o->s[a * N + c] == o->s[b * N + c] && (uint64_t)w[l] < o->thr_sw[1])
+                if (o->s[a * N + c] == o->s[b * N + c] && sw_link(o, w, l, o->thr_sw[1], (uint32_t)c, t))
                     uf_union(p, (int32_t)(a * N + c), (int32_t)(b * N + c));
+        uint32_t dsh = draw_below(o, 46656u, &w[9], 2, (uint32_t)c, t, ST_SW_FLIP);
+        for (int a = 0; a < ARMS; ++a) shift[a * N + c] = (uint8_t)((dsh / pow6[a]) % 6);
     }
     for (int64_t i = 0; i < NS; ++i) p[i] = uf_find(p, (int32_t)i);
-    /* the shift of root i is an exact uniform in [0,6) from word (i & 3) of the flip block of
-     * sites 4*(i>>2)..4*(i>>2)+3, falling back to the retry streams of site i */
-    uint8_t* shift = (uint8_t*)malloc(NS > 0 ? (size_t)NS : 1);
-    for (int64_t i = 0; i < NS; ++i) {
-        if (p[i] != i) continue;
-        uint32_t r[4];
-        rng(o, (uint32_t)(i >> 2), t, ST_SW_FLIP, r);
-        shift[i] = (uint8_t)draw_below(o, 6, &r[i & 3], 1, (uint32_t)i, t, ST_SW_FLIP);
-    }
     for (int64_t i = 0; i < NS; ++i) o->s[i] = (uint8_t)((o->s[i] + shift[p[i]]) % Q);
     free(shift);
     o->ctr[3]++;

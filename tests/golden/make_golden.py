@@ -110,4 +110,10 @@ def correlator_golden(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from oracle import build_ref
+
+    ref = build_ref.checkout(sys.argv[1] if len(sys.argv) > 1 else None)
+    if ref is None:
+        sys.exit("no reference checkout: pass its path or set CVF_REFERENCE_DIR")
+    main(ref)
