@@ -403,6 +403,23 @@ __device__ __forceinline__ void cube_move_v(const ReplicaDesc& R, const CubeTabl
   const uint32_t a0 = seg * VC;
   const uint32_t y0 = 2 * b + par, z0 = 2 * c + par;
   const uint32_t y1 = y0 + 1 == L ? 0 : y0 + 1, z1 = z0 + 1 == L ? 0 : z0 + 1;
+  // one Philox block per group of four cubes along x (the thread's VC cubes lie in one group):
+  // words 0, 3 give the four proposals as base-9 digits of an exact uniform in [0, 9^4), words
+  // 1, 2 the high halves of the four acceptance uniforms. Drawn before the vertex words are
+  // loaded, so the rare retry call holds few live registers.
+  const uint32_t kk0 = a0 & 3u;
+  const uint32_t gid = 2 * (a0 - kk0) + par + L * (y0 + L * z0);
+  const U4 rr = philox(gid, t, kStCube, R.replica, R.key0, R.key1);
+  uint32_t u = rr.x;
+  if (u * 6561u < 5476u) u = rr.w;
+  if (u * 6561u < 5476u) u = cube_proposal_retry(gid, t, &R);
+  uint32_t dig[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const unsigned long long m = (unsigned long long)u * 9ull;
+    dig[j] = (uint32_t)(m >> 32);
+    u = (uint32_t)m;
+  }
   const uint32_t rows[4] = {H * (y0 + L * z0), H * (y1 + L * z0), H * (y0 + L * z1), H * (y1 + L * z1)};
   const uint32_t anext = a0 + VC == H ? 0 : a0 + VC;
   uint32_t w[8][VC];
@@ -424,23 +441,11 @@ __device__ __forceinline__ void cube_move_v(const ReplicaDesc& R, const CubeTabl
   else packed = *cs;
 #pragma unroll
   for (int k = 0; k < VC; ++k) st[k] = (packed >> (8 * k)) & 0xffu;
-  // one Philox block per group of four cubes along x (the thread's VC cubes lie in one group):
-  // words 0, 3 give the four proposals as base-9 digits of an exact uniform in [0, 9^4), words
-  // 1, 2 the high halves of the four acceptance uniforms
-  const uint32_t kk0 = a0 & 3u;
-  const uint32_t gid = 2 * (a0 - kk0) + par + L * (y0 + L * z0);
-  const U4 rr = philox(gid, t, kStCube, R.replica, R.key0, R.key1);
-  uint32_t u = rr.x;
-  if (u * 6561u < 5476u) u = rr.w;
-  if (u * 6561u < 5476u) u = cube_proposal_retry(gid, t, &R);
-  uint32_t dig[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    const unsigned long long m = (unsigned long long)u * 9ull;
-    dig[j] = (uint32_t)(m >> 32);
-    u = (uint32_t)m;
-  }
-  bool changed = false;
+  // decisions from the 16-bit high halves; a tie (p ~ 2^-16 per cube) is settled after the loop,
+  // once the vertex words are dead
+  uint32_t nwk[VC];
+  int dhk[VC];
+  uint32_t acc_mask = 0, tie_mask = 0;
 #pragma unroll
   for (int k = 0; k < VC; ++k) {
     // edge e along d from p0 to p1: sigma_{2d}(p0) == sigma_{2d+1}(p1), compared in place by
@@ -454,17 +459,32 @@ __device__ __forceinline__ void cube_move_v(const ReplicaDesc& R, const CubeTabl
     }
     const uint32_t kk = VC == 4 ? (uint32_t)k : kk0 + (uint32_t)k;
     const uint32_t nw = VC == 4 ? dig[k] : (kk == 0 ? dig[0] : (kk == 1 ? dig[1] : (kk == 2 ? dig[2] : dig[3])));
-    const uint32_t old = st[k];
-    const int dhb = __popc(ct->act[nw] & D) - __popc(ct->act[old] & D);
-    const unsigned long long T = ct->thr[dhb + 4];
+    const int dhb = __popc(ct->act[nw] & D) - __popc(ct->act[st[k]] & D);
     const uint32_t word = kk < 2 ? rr.y : rr.z;
     const uint32_t hu = (kk & 1) ? (word >> 16) : (word & 0xffffu);
-    const uint32_t th = (uint32_t)(T >> 16);
-    const bool acc = hu != th ? hu < th : cube_accept_exact(gid, t, kk, hu, T, &R);
-    if (acc && nw != old) {
-      st[k] = nw;
+    const uint32_t th = (uint32_t)(ct->thr[dhb + 4] >> 16);
+    acc_mask |= (hu < th ? 1u : 0u) << k;
+    tie_mask |= (hu == th ? 1u : 0u) << k;
+    nwk[k] = nw;
+    dhk[k] = dhb;
+  }
+  if (tie_mask) {
+#pragma unroll
+    for (int k = 0; k < VC; ++k)
+      if ((tie_mask >> k) & 1u) {
+        const uint32_t kk = VC == 4 ? (uint32_t)k : kk0 + (uint32_t)k;
+        const uint32_t word = kk < 2 ? rr.y : rr.z;
+        const uint32_t hu = (kk & 1) ? (word >> 16) : (word & 0xffffu);
+        if (cube_accept_exact(gid, t, kk, hu, ct->thr[dhk[k] + 4], &R)) acc_mask |= 1u << k;
+      }
+  }
+  bool changed = false;
+#pragma unroll
+  for (int k = 0; k < VC; ++k) {
+    if (((acc_mask >> k) & 1u) && nwk[k] != st[k]) {
+      st[k] = nwk[k];
       changed = true;
-      cdh += dhb;
+      cdh += dhk[k];
     }
   }
   if (changed) {
@@ -748,6 +768,24 @@ __device__ __forceinline__ const SweepTables* warp_sweep_tables(const ReplicaDes
   return wt;
 }
 
+// One block-wide copy of the sweep tables of replica R (every block of the plain sweep kernels
+// serves one replica), filled by the first threads of the block; the caller synchronises the
+// block after it. A copy at a fixed shared-memory address lets the table reads of the decision
+// loop use constant offsets.
+__device__ __forceinline__ void fill_block_sweep_tables(const ReplicaDesc& R, SweepTables* t) {
+  const int i = threadIdx.x;
+  if (i < 64) t->et.nbmask[i] = R.nbmask[i];
+  if (i < 18) reinterpret_cast<uint32_t*>(t->et.eta)[i] = reinterpret_cast<const uint32_t*>(R.eta_tab)[i];
+  if (i < 33) {
+    t->tv[i] = R.tv[i];
+    t->pk[i] = entry_delta(i);
+  }
+  if (i < 8) {
+    t->cnt[i] = count_bytes((uint32_t)i, 4u);
+    t->nbw[i] = count_bytes((uint32_t)i, 44u);
+  }
+}
+
 // Metropolis update of the six arms of one cell, arms in order 0..5 (GW:1964-2007 energy change,
 // chessboard branch). Proposal of arm a: the a-th most significant base-6 digit of the uniform
 // word u (the high word of u*6 in a multiply chain). The threshold entry is
@@ -858,10 +896,11 @@ __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepT
   }
   const uint32_t L = R.L;
   const uint32_t cbase = L * ((uint32_t)y + L * (uint32_t)z) + (uint32_t)x0;
+  const PhiloxKeys rk = philox_keys(R.key0, R.key1);
 #pragma unroll
   for (int k = 0; k < V; ++k) {
     const uint32_t c0 = cbase + 2u * k;
-    const U4 rr = philox(c0, t, kStSweep, R.replica, R.key0, R.key1);
+    const U4 rr = philox_rk(c0, t, kStSweep, R.replica, rk);
     int32_t dummy = 0;
     out[k] = update_cell<kCount>(out[k], nbs[k], nbe[k], eta[k], rr, c0, t, R, wt, kCount ? *dacc : dummy);
   }
@@ -882,14 +921,15 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const 
                                                     ReplicaState* __restrict__ st,
                                                     const int* __restrict__ blk, int nrep, int colour, int jsweep) {
   pdl_trigger();
-  __shared__ SweepTables s_tab[kThreads / 32];
+  __shared__ SweepTables s_tab;
   const int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
-  const SweepTables* wt = warp_sweep_tables(R, s_tab);
+  fill_block_sweep_tables(R, &s_tab);
+  __syncthreads();
   pdl_wait();
   uint32_t hb2 = 0, ns = 0;
   int32_t dacc = 0;
-  sweep_segment<V, false, kCount>(R, wt, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
+  sweep_segment<V, false, kCount>(R, &s_tab, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
                                   st[r].cur[0] + (uint32_t)jsweep, hb2, ns, &dacc);
   if (kCount) {
     const int ds = (int)(int16_t)(dacc & 0xffff);  // |dN_sigma| per thread <= 8 cells x 30
@@ -918,17 +958,18 @@ __global__ void __launch_bounds__(kThreads) k_chunk_cluster(const ReplicaDesc* _
                                                             ReplicaState* __restrict__ st,
                                                             const int* __restrict__ blk_cube, int cube1,
                                                             int nrep, int steps, int nmet) {
-  __shared__ SweepTables s_tab[kThreads / 32];
+  __shared__ SweepTables s_tab;
   __shared__ CubeTables s_ct[kThreads / 32];
   uint32_t rank;
   asm("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
   const int r = (int)(blockIdx.x / kClusterCtas);
   const bool live = r < nrep;  // every block of the cluster reaches every barrier
   const ReplicaDesc& R = reps[live ? r : 0];
-  const SweepTables* wt = warp_sweep_tables(R, s_tab);
+  const SweepTables* wt = &s_tab;
+  fill_block_sweep_tables(R, &s_tab);
   CubeTables* ct = s_ct + (threadIdx.x >> 5);
   fill_cube_tables(R, ct, threadIdx.x & 31);
-  __syncwarp();
+  __syncthreads();
   ReplicaState& S = st[live ? r : 0];
   const uint32_t c0 = S.ctr[0], c1 = S.ctr[1];
   const uint32_t nseg = (uint32_t)(R.H / V) * (uint32_t)R.L * (uint32_t)R.L;
@@ -969,13 +1010,14 @@ template <int V>
 __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep_measure(
     const ReplicaDesc* __restrict__ reps, ReplicaState* __restrict__ st, const int* __restrict__ blk, int nrep,
     int jsweep) {
-  __shared__ SweepTables s_tab[kThreads / 32];
+  __shared__ SweepTables s_tab;
   __shared__ unsigned long long s_acc[2];
   const int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
-  const SweepTables* wt = warp_sweep_tables(R, s_tab);
+  fill_block_sweep_tables(R, &s_tab);
+  __syncthreads();
   uint32_t hb2 = 0, ns = 0;
-  sweep_segment<V, true>(R, wt, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, 1,
+  sweep_segment<V, true>(R, &s_tab, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, 1,
                          st[r].cur[0] + (uint32_t)jsweep, hb2, ns);
   measure_accumulate(st[r], blockIdx.x, hb2, ns, s_acc);
 }

@@ -97,6 +97,40 @@ CVF_HD U4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0
   return U4{c0, c1, c2, c3};
 }
 
+// The same block with the key schedule computed once by the caller: rk[2r], rk[2r+1] are the two
+// key words of round r. A kernel that draws several blocks with one key (every cell of a launch
+// uses the replica's seed) computes the schedule once instead of once per block.
+struct PhiloxKeys {
+  uint32_t k[20];
+};
+CVF_HD PhiloxKeys philox_keys(uint32_t k0, uint32_t k1) {
+  PhiloxKeys p;
+  for (int r = 0; r < 10; ++r) {
+    p.k[2 * r] = k0;
+    p.k[2 * r + 1] = k1;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return p;
+}
+CVF_HD U4 philox_rk(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const PhiloxKeys& rk) {
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0, lo0, hi1, lo1;
+    mulhilo32(0xD2511F53u, c0, hi0, lo0);
+    mulhilo32(0xCD9E8D57u, c2, hi1, lo1);
+    uint32_t n0 = hi1 ^ c1 ^ rk.k[2 * r];
+    uint32_t n2 = hi0 ^ c3 ^ rk.k[2 * r + 1];
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+  }
+  return U4{c0, c1, c2, c3};
+}
+
 // Lemire multiply-shift: value in [0,n) and whether the word lies in the exact (unbiased) range.
 CVF_HD bool lemire_try(uint32_t w, uint32_t n, uint32_t& out) {
   uint64_t m = (uint64_t)w * n;

@@ -148,18 +148,43 @@ def block_err(x, nb=20):
     return b.std(ddof=1) / math.sqrt(nb)
 
 
+def jackknife_reweighted(s, ro, runs, f, theta, obs, n_cells, nb=10):
+    """Jackknife covariance of reweighted means over nb blocks of every run's samples (WHAM
+    refined from f on each subsample)."""
+    idx = [np.flatnonzero(ro == j) for j in range(len(runs))]
+    vals = []
+    for k in range(nb):
+        keep = np.concatenate([ix[np.arange(len(ix)) // (len(ix) // nb) != k] for ix in idx])
+        m, _, _ = gpu_forward(s[keep], ro[keep], runs, f.copy(), theta, obs, n_cells, n_iter=200, tol=1e-9)
+        vals.append(m)
+    dev = np.asarray(vals) - np.mean(vals, 0)
+    return (nb - 1) / nb * dev.T @ dev
+
+
+def block_cov(x, nb=20):
+    """Covariance of the means of the columns of x from nb blocks."""
+    b = np.asarray(x)[: len(x) // nb * nb].reshape(nb, -1, x.shape[1]).mean(1)
+    return np.cov(b, rowvar=False, ddof=1) / nb
+
+
 def test_reweighting_reproduces_direct_simulation(engine_lib):
+    """Samples of five runs reweighted to T = 0.75 against a direct run there. E and V are
+    strongly correlated, so they are tested together: chi^2 of the difference of (E, V) under the
+    combined covariance (20-block covariance of the direct run's means plus the jackknife
+    covariance of the reweighted means over 10 blocks of every run) below the 95 % point of
+    chi^2 with 2 degrees of freedom (5.991)."""
     L, P_, N = 8, 0.45, 512
     temps = [0.70, 0.72, 0.74, 0.76, 0.78]
     s, ro = engine_samples(L, temps, P_, 40000, 4000, 10, 9100)
     runs = np.array([[1.0 / float(np.float32(t)), float(np.float32(P_))] for t in temps])
-    mean, _, f = gpu_forward(s, ro, runs, np.zeros(5), [1.0 / 0.75, float(np.float32(P_)), 0, 0, 0],
-                             ["E", "V"], float(N), n_iter=500, tol=1e-9)
+    theta = [1.0 / 0.75, float(np.float32(P_)), 0, 0, 0]
+    mean, _, f = gpu_forward(s, ro, runs, np.zeros(5), theta, ["E", "V"], float(N), n_iter=500, tol=1e-9)
+    cov = jackknife_reweighted(s, ro, runs, f, theta, ["E", "V"], float(N))
     d, _ = engine_samples(L, [0.75], P_, 40000, 4000, 10, 9200)
-    for k, col in ((0, 0), (1, 1)):
-        err = block_err(d[:, col])
-        z = (mean[k] - d[:, col].mean()) / err
-        assert abs(z) < 2.0, (k, mean[k], d[:, col].mean(), err)
+    cov = cov + block_cov(d[:, :2])
+    diff = np.asarray(mean[:2]) - d[:, :2].mean(0)
+    chi2 = float(diff @ np.linalg.solve(cov, diff))
+    assert chi2 < 5.991, (mean[:2], d[:, :2].mean(0), np.sqrt(np.diag(cov)), chi2)
     # adjoint response vs finite differences of the reweighted curve at T = 0.75 +/- 0.005
     beta = 1.0 / 0.75
     th = [beta, float(np.float32(P_)), 0, 0, 0]
