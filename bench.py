@@ -147,6 +147,24 @@ def ncu_traffic(name, tile=None):
     return d.get("dram_bytes_per_launch")
 
 
+def issue_roof(tile, cells_per_launch, launch_s, sm_mhz, n_sm):
+    """Instruction-issue roofline of the sweep launch: thread instructions per cell (from the
+    committed ncu summary of the same kernel and tile) x cells per launch / launch time, against
+    the issue peak of the SMs (4 schedulers x 32 lanes per SM per cycle) at the sampled clock."""
+    p = os.path.join(ROOT, "profiles", "sweep_l256_issue.json")
+    if not os.path.exists(p):
+        return None
+    try:
+        per_cell = json.load(open(p))["by_tile"][str(tile)]["thread_inst_per_cell"]
+    except (ValueError, OSError, KeyError):
+        return None
+    achieved = per_cell * cells_per_launch / launch_s
+    peak = n_sm * 4 * 32 * sm_mhz * 1e6
+    return {"thread_inst_per_cell": per_cell, "achieved": round(achieved / 1e12, 3),
+            "peak": round(peak / 1e12, 3), "unit": "T thread-instructions/s", "frac": round(achieved / peak, 4),
+            "sm_mhz": sm_mhz, "source": "profiles/sweep_l256_issue.json"}
+
+
 def cpu_baseline_oracle(steps_cap=3, budget_s=30.0, threads=None):
     """The CPU oracle on all host cores (or `threads`) over a bounded sample of the same workload."""
     from oracle import oracle as O
@@ -608,6 +626,8 @@ def run_engine(args):
     peak, peak_kind = peaks()
     achieved = alg_bytes_launch / launch_s / 1e9
     traffic = ncu_traffic("sweep_l256_traffic.json", tile)
+    sm_mhz = (clk or {}).get("sm_mhz") or 2070.0
+    issue = issue_roof(tile, N // 2, launch_s, sm_mhz, torch.cuda.get_device_properties(local).multi_processor_count)
     line = {
         "metric": "site-updates/ns at L=256", "value": round(value, 4), "unit": "site-updates/ns",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 5),
@@ -619,7 +639,8 @@ def run_engine(args):
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "kernel": f"k_sweep<{tile}> (one colour of the checkerboard sweep)",
                      "algorithmic_bytes_per_launch": int(alg_bytes_launch),
-                     "launch_us": round(launch_s * 1e6, 3), "peak_source": f"{peak_kind} hbm_gbs"},
+                     "launch_us": round(launch_s * 1e6, 3), "peak_source": f"{peak_kind} hbm_gbs",
+                     "issue": issue},
         "cpu_baseline": base,
         "e2e": e2e,
         "gpu_launches": 4 * args.steps,

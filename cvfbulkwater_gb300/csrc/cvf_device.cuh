@@ -20,7 +20,8 @@ struct ReplicaDesc {
   uint8_t* cubes[2];
   // Swendsen-Wang work arrays (null until the first SW step)
   int32_t* label;     // 6N parents / labels
-  uint8_t* hbmask;    // N: bits 0..2 = active x+, y+, z+ cluster bonds
+  uint32_t* cellsw;   // N: bits 0..2 = active x+, y+, z+ cluster bonds; bits 3+3a..5+3a = the
+                      // smallest arm of arm a's in-cell component (its in-cell root)
   uint32_t* flip;     // N: bits 3a..3a+2 = shift of the cluster whose root is arm site a of the cell
   int32_t* csize;     // 6N: cluster sizes by root
   int32_t* cand;      // 6N: percolation candidate id by root (-1 none)

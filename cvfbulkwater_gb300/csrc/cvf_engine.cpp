@@ -293,7 +293,7 @@ static int ensure_sw(cvf_handle* h) {
     int W = (r.L + 31) / 32;
     r.desc.max_cand = 3 * r.L * r.L;  // at most 6N / 2L clusters of size >= 2L
     if (int rc = dev_alloc(h, (void**)&r.desc.label, NS * sizeof(int32_t))) return rc;
-    if (int rc = dev_alloc(h, (void**)&r.desc.hbmask, (size_t)r.N)) return rc;
+    if (int rc = dev_alloc(h, (void**)&r.desc.cellsw, (size_t)r.N * sizeof(uint32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.flip, (size_t)r.N * sizeof(uint32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.csize, NS * sizeof(int32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.cand, NS * sizeof(int32_t))) return rc;

@@ -618,8 +618,11 @@ struct CellBlock {
 __device__ __forceinline__ uint32_t neighbour_sigmas(uint32_t xp, uint32_t xm, uint32_t yp, uint32_t ym,
                                                      uint32_t zp, uint32_t zm) {
   // arm a faces sigma_{a^1} of the neighbour along a (GW:1936-1962)
-  return ((xp >> 3) & 7u) | ((xm & 7u) << 3) | (((yp >> 9) & 7u) << 6) | (((ym >> 6) & 7u) << 9) |
-         (((zp >> 15) & 7u) << 12) | (((zm >> 12) & 7u) << 15);
+  // the three "+" neighbours give a field one place up of where it goes, the three "-" ones a
+  // field one place down: two masked selections and two shifts
+  const uint32_t up = (xp & 0x38u) | (yp & 0xe00u) | (zp & 0x38000u);
+  const uint32_t dn = (xm & 0x7u) | (ym & 0x1c0u) | (zm & 0x7000u);
+  return (up >> 3) | (dn << 3);
 }
 
 // Number of zero 3-bit fields among the six fields of x.

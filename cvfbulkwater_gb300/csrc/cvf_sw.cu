@@ -93,16 +93,34 @@ __device__ __noinline__ uint32_t sw_flip_retry(uint32_t c, uint32_t t, const Rep
   return w;
 }
 
-// U < T for link l from the high half of word `word`; th = T >> 16 (up to 65536).
-__device__ __forceinline__ bool sw_link(uint32_t word, int l, uint32_t th, unsigned long long T, uint32_t c,
-                                        uint32_t t, const ReplicaDesc& R) {
-  const uint32_t hi = (l & 1) ? (word >> 16) : (word & 0xffffu);
-  if (hi != th) return hi < th;
-  return sw_link_exact(c, t, l, hi, T, &R);
+// Exact bond mask of a cell whose fast decision met a tie (a 16-bit high half equal to T >> 16,
+// p ~ 2^-16 per link): the bond blocks drawn again and every link decided from its full 32-bit
+// uniform. eq has bit l set when link l's sigma (and eta) condition holds. Returns the 18-bit
+// bond mask.
+__device__ __noinline__ uint32_t sw_links_exact(uint32_t c, uint32_t t, uint32_t eq, const ReplicaDesc* R) {
+  uint32_t bonds = 0;
+  for (int l = 0; l < 18; ++l) {
+    if (!((eq >> l) & 1u)) continue;
+    const unsigned long long T = R->thr_sw[l < 3 ? 0 : 1];
+    const U4 q = philox(c, t, kStSwBond + (uint32_t)(l >> 3), R->replica, R->key0, R->key1);
+    const int k = (l >> 1) & 3;
+    const uint32_t word = k == 0 ? q.x : (k == 1 ? q.y : (k == 2 ? q.z : q.w));
+    const uint32_t hi = (word >> (16 * (l & 1))) & 0xffffu;
+    bool b;
+    if ((unsigned long long)hi != (T >> 16)) b = hi < (uint32_t)(T >> 16);
+    else b = sw_link_exact(c, t, l, hi, T, R);
+    bonds |= (uint32_t)b << l;
+  }
+  return bonds;
 }
 
 // GW:2383-2438: links 0..2 are the x+, y+, z+ hydrogen-bond links of the cell, links 3..17 the
-// intra-cell pairs (a<b) in row-major order.
+// intra-cell pairs (a<b) in row-major order. The sigma conditions of the 15 pairs come from three
+// whole-word comparisons (each arm against the arm 1, 2 and 3 places further round), and every
+// link is decided from its 16-bit high half; a tie sends the cell through sw_links_exact. Besides
+// the in-cell labels the kernel stores, per cell, the bond bits of its three hydrogen-bond links
+// and the in-cell root (smallest arm of its in-cell component) of every arm, for the union and
+// the finish.
 __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __restrict__ reps,
                                                        const ReplicaState* __restrict__ st,
                                                        const int* __restrict__ blk, int nrep, int jsw) {
@@ -118,40 +136,64 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
   pdl_wait();
   const uint32_t t = st[r].cur[3] + (uint32_t)jsw;
   const uint32_t w = word_at(R, x, y, z);
+  const PhiloxKeys rk = philox_keys(R.key0, R.key1);
   uint32_t rw[12];
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
-    U4 q = philox((uint32_t)c, t, kStSwBond + j, R.replica, R.key0, R.key1);
+    const U4 q = philox_rk((uint32_t)c, t, kStSwBond + j, R.replica, rk);
     rw[4 * j] = q.x;
     rw[4 * j + 1] = q.y;
     rw[4 * j + 2] = q.z;
     rw[4 * j + 3] = q.w;
   }
-  const unsigned long long thb = R.thr_sw[0], ts = R.thr_sw[1];
-  const uint32_t thb_hi = (uint32_t)(thb >> 16), ts_hi = (uint32_t)(ts >> 16);
-  uint32_t hb = 0;
+  // eq: bit l set when the sigma (and eta) condition of link l holds
+  uint32_t eq = 0;
   if (R.Jeff != 0.0) {
     const uint32_t eta = eta_of_cell(R, x, y, z);
     const int xn = x + 1 == L ? 0 : x + 1, yn = y + 1 == L ? 0 : y + 1, zn = z + 1 == L ? 0 : z + 1;
     const uint32_t wn[3] = {word_at(R, xn, y, z), word_at(R, x, yn, z), word_at(R, x, y, zn)};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const uint32_t sa = (w >> (6 * d)) & 7u, sb = (wn[d] >> (6 * d + 3)) & 7u;
-      const bool cond = R.Jeff > 0.0 ? (((eta >> (2 * d)) & 1u) && sa == sb) : sa != sb;
-      if (cond && sw_link(rw[d >> 1], d, thb_hi, thb, c, t, R)) hb |= 1u << d;
+      const bool same = ((w >> (6 * d)) & 7u) == ((wn[d] >> (6 * d + 3)) & 7u);
+      const bool cond = R.Jeff > 0.0 ? (((eta >> (2 * d)) & 1u) && same) : !same;
+      eq |= (uint32_t)cond << d;
     }
   }
-  R.hbmask[c] = (uint8_t)hb;
-  // intra-cell bonds: bit l-3 for link l = 3..17, pairs (a<b) in row-major order
-  uint32_t bm = 0;
-  int l = 3;
+  {
+    // e[k] bit 3a: sigma_a == sigma_{(a+k) mod 6}
+    const uint32_t w18 = w & 0x3ffffu;
+    uint32_t e[4];
 #pragma unroll
-  for (int a = 0; a < 5; ++a)
-#pragma unroll
-    for (int b = a + 1; b < 6; ++b, ++l) {
-      if (((w >> (3 * a)) & 7u) == ((w >> (3 * b)) & 7u) && sw_link(rw[l >> 1], l, ts_hi, ts, c, t, R))
-        bm |= 1u << (l - 3);
+    for (int k = 1; k <= 3; ++k) {
+      const uint32_t rot = ((w18 >> (3 * k)) | (w18 << (18 - 3 * k))) & 0x3ffffu;
+      const uint32_t xx = w18 ^ rot;
+      e[k] = ~(xx | (xx >> 1) | (xx >> 2)) & 0x9249u;
     }
+    int l = 3;
+#pragma unroll
+    for (int a = 0; a < 5; ++a)
+#pragma unroll
+      for (int b = a + 1; b < 6; ++b, ++l) {
+        // pairs 4 and 5 apart are the pairs (b, a) 2 and 1 apart going on round
+        const int k = b - a;
+        const uint32_t bit = k <= 3 ? (e[k] >> (3 * a)) & 1u : (e[6 - k] >> (3 * b)) & 1u;
+        eq |= bit << l;
+      }
+  }
+  // fast decisions from the high halves; a tie of a high half with T >> 16 on a link whose
+  // condition holds sends the cell through the exact path
+  const uint32_t thb = (uint32_t)(R.thr_sw[0] >> 16), ts = (uint32_t)(R.thr_sw[1] >> 16);
+  uint32_t lt = 0, tie = 0;
+#pragma unroll
+  for (int l = 0; l < 18; ++l) {
+    const uint32_t hi = (l & 1) ? (rw[l >> 1] >> 16) : (rw[l >> 1] & 0xffffu);
+    const uint32_t th = l < 3 ? thb : ts;
+    lt |= (uint32_t)(hi < th) << l;
+    tie |= (uint32_t)(hi == th) << l;
+  }
+  uint32_t bonds = eq & lt;
+  if (tie & eq) bonds = sw_links_exact(c, t, eq, &R);
+  uint32_t bm = bonds >> 3;  // intra-cell bonds: bit l-3 for link l = 3..17
   // shift digits of the clusters rooted at this cell's arm sites
   uint32_t u = rw[9];
   if (u * 46656u < 2560u) u = rw[10];
@@ -178,6 +220,7 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
     const uint32_t m7 = (~(xx | (xx >> 1) | (xx >> 2)) & 0x9249u) * 7u;
     lab = (lab & ~m7) | ((lo * 0x9249u) & m7);
   }
+  R.cellsw[c] = (bonds & 7u) | (lab << 3);
 #pragma unroll
   for (int a = 0; a < 6; ++a) R.label[a * N + c] = (int32_t)(((lab >> (3 * a)) & 7u) * N + c);
 }
@@ -214,6 +257,9 @@ __device__ __forceinline__ bool uf_unite(int32_t* p, int32_t a, int32_t b, uint3
   return false;
 }
 
+// One thread per cell with a hydrogen-bond link: the link joins the in-cell component of the
+// cell's arm 2d with the in-cell component of the neighbour's arm 2d+1, so the union starts from
+// the two in-cell roots (recorded by k_sw_local) rather than from the arm sites.
 __global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __restrict__ reps,
                                                        ReplicaState* __restrict__ st,
                                                        const int* __restrict__ blk, int nrep) {
@@ -225,7 +271,8 @@ __global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __rest
   const uint32_t c = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
   if (c >= N) return;
   pdl_wait();
-  uint32_t hb = R.hbmask[c];
+  const uint32_t sw = R.cellsw[c];
+  const uint32_t hb = sw & 7u;
   if (!hb) return;
   int xi, yi, zi;
   cell_xyz(R, c, xi, yi, zi);
@@ -234,16 +281,20 @@ __global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __rest
                           x + L * (y + L * (z + 1 == L ? 0 : z + 1))};
 #pragma unroll
   for (int d = 0; d < 3; ++d)
-    if ((hb >> d) & 1u)
-      if (!uf_unite(R.label, (int32_t)((2 * d) * N + c), (int32_t)((2 * d + 1) * N + nb[d]), R.union_iters))
-        st[r].err = 1;
+    if ((hb >> d) & 1u) {
+      const uint32_t ra = (sw >> (3 + 6 * d)) & 7u;                          // in-cell root of arm 2d
+      const uint32_t rb = (R.cellsw[nb[d]] >> (3 + 3 * (2 * d + 1))) & 7u;  // of the neighbour's arm 2d+1
+      if (!uf_unite(R.label, (int32_t)(ra * N + c), (int32_t)(rb * N + nb[d]), R.union_iters)) st[r].err = 1;
+    }
 }
 
-// Compression, cluster shift and update in one pass, one thread per cell: each of the cell's six
-// sites walks to its root (the component's minimum site id) and stores it as its label, then
-// takes the root's shift -- GW:2531-2542 gives every cluster one uniform shift in 0..5; here it
-// is digit a of the shift word that k_sw_local drew for cell c, for the root site a*N + c -- and
-// shifts its sigma. A repeated root reuses the previous arm's shift.
+// Compression, cluster shift and update in one pass, one thread per cell. An in-cell component
+// none of whose arms carries a hydrogen-bond link (the cell's own x+, y+, z+ links, or the links
+// of its x-, y-, z- neighbours into it) is a whole cluster: its root is its smallest arm site,
+// which k_sw_local already stored as the label of every arm in it. Only the arms of the other
+// components walk to their roots (the minimum site id of the cluster) and store them. Each
+// cluster's shift is digit a of the shift word that k_sw_local drew for cell c, for the root site
+// a*N + c (GW:2531-2542 gives every cluster one uniform shift in 0..5); sigma is shifted by it.
 __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __restrict__ reps,
                                                         const ReplicaState* __restrict__ st,
                                                         const int* __restrict__ blk, int nrep, int jsw) {
@@ -254,31 +305,40 @@ __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __res
   const uint32_t N = (uint32_t)L * L * L;
   const uint32_t c = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
   if (c >= N) return;
-  pdl_wait();
-  int32_t roots[6];
-#pragma unroll
-  for (int a = 0; a < 6; ++a) {
-    int32_t x = (int32_t)(a * N + c);
-    for (int it = 0; it < (1 << 30); ++it) {
-      const int32_t px = __ldcg(R.label + x);
-      if (px == x) break;
-      x = px;
-    }
-    roots[a] = x;
-  }
-#pragma unroll
-  for (int a = 0; a < 6; ++a) R.label[a * N + c] = roots[a];
   int x, y, z;
   cell_xyz(R, c, x, y, z);
+  const uint32_t cxm = (uint32_t)(x == 0 ? L - 1 : x - 1) + (uint32_t)L * ((uint32_t)y + (uint32_t)L * (uint32_t)z);
+  const uint32_t cym = (uint32_t)x + (uint32_t)L * ((uint32_t)(y == 0 ? L - 1 : y - 1) + (uint32_t)L * (uint32_t)z);
+  const uint32_t czm = (uint32_t)x + (uint32_t)L * ((uint32_t)y + (uint32_t)L * (uint32_t)(z == 0 ? L - 1 : z - 1));
+  pdl_wait();
+  const uint32_t sw = R.cellsw[c];
+  const uint32_t lab = sw >> 3;
+  // arms with a hydrogen-bond link: 0, 2, 4 from this cell's links, 1, 3, 5 from the neighbours'
+  const uint32_t ext = (sw & 1u) | ((R.cellsw[cxm] & 1u) << 1) | ((sw & 2u) << 1) | ((R.cellsw[cym] & 2u) << 2) |
+                       ((sw & 4u) << 2) | ((R.cellsw[czm] & 4u) << 3);
+  // in-cell roots of the components that some link reaches, as a 6-bit mask
+  uint32_t ext_root = 0;
+#pragma unroll
+  for (int a = 0; a < 6; ++a)
+    if ((ext >> a) & 1u) ext_root |= 1u << ((lab >> (3 * a)) & 7u);
   uint32_t* wp = R.cells[(x + y + z) & 1] + (uint32_t)(x >> 1) + (uint32_t)R.H * ((uint32_t)y + (uint32_t)L * (uint32_t)z);
   const uint32_t w = *wp;
   const uint32_t own_flip = R.flip[c];
-  uint32_t out = 0, sh = 0;
-  int32_t last = -1;
+  uint32_t out = 0;
 #pragma unroll
   for (int a = 0; a < 6; ++a) {
-    const int32_t root = roots[a];
-    if (root != last) {
+    const uint32_t m = (lab >> (3 * a)) & 7u;
+    uint32_t sh;
+    if (!((ext_root >> m) & 1u)) {
+      sh = (own_flip >> (3 * m)) & 7u;  // the in-cell root is the cluster's root; its label is stored
+    } else {
+      int32_t root = (int32_t)(m * N + c);
+      for (int it = 0; it < (1 << 30); ++it) {
+        const int32_t px = __ldcg(R.label + root);
+        if (px == root) break;
+        root = px;
+      }
+      R.label[a * N + c] = root;
       uint32_t rc = (uint32_t)root, ra = 0;
 #pragma unroll
       for (int k = 0; k < 5; ++k)
@@ -288,7 +348,6 @@ __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __res
         }
       const uint32_t fw = rc == c ? own_flip : R.flip[rc];
       sh = (fw >> (3 * ra)) & 7u;
-      last = root;
     }
     uint32_t v = ((w >> (3 * a)) & 7u) + sh;
     if (v >= 6u) v -= 6u;
