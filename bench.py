@@ -222,6 +222,7 @@ def bench_batch64(steps, warmup, local, flush, verify=4):
     cells = sum(p.L ** 3 for p in params)
     batch = Lattice(params)
     tile = batch.autotune()
+    tuned = batch.tuning()
     batch.run(warmup, 1, 0)
     batch.synchronize()
     t_batch = timed_steps(batch, steps, flush)
@@ -240,7 +241,7 @@ def bench_batch64(steps, warmup, local, flush, verify=4):
     rs_p = 64 * steps / (t_plain / 1e3)
     return {"workload": "64 replicas, L from {16,24,32,48,64} (seeded), 8x8 grid T 0.55..0.95 x P 0..0.60, "
                         "disordered starts; 1 cube + 1 volume move + 1 sweep per step",
-            "cells": cells, "steps": steps, "sweep_tile": tile,
+            "cells": cells, "steps": steps, "sweep_tile": tile, "tuning": dict(zip(("tile", "lg_rows", "launch_mode"), tuned)),
             "batched_replica_sweeps_per_s": round(rs_b, 1),
             "plain_sequential_replica_sweeps_per_s": round(rs_p, 1),
             "batched_site_updates_per_ns": round(cells * steps / (t_batch * 1e6), 4),
@@ -284,8 +285,13 @@ def bench_differentiation(local):
     from cvfbulkwater_gb300.engine import Lattice, Params
     L, N, P0, R, K = 32, 32 ** 3, 0.45, 32, 100000
     temps = np.linspace(0.60, 0.90, R)
+    # five more runs for the finite differences of independent runs: (0.75, P0) and its neighbours
+    # at T +/- 0.005 and P +/- 0.005, the same sampling
+    fd_pts = [(0.75, P0), (0.745, P0), (0.755, P0), (0.75, P0 - 0.005), (0.75, P0 + 0.005)]
     lat = Lattice([Params(L=L, T=float(t), P=P0, seed=SEED + 500 + i, start=0, replica=i, device=local,
-                          sample_capacity=K) for i, t in enumerate(temps)])
+                          sample_capacity=K) for i, t in enumerate(temps)] +
+                  [Params(L=L, T=t, P=p, seed=SEED + 600 + i, start=0, replica=R + i, device=local, sample_capacity=K)
+                   for i, (t, p) in enumerate(fd_pts)])
     lat.run(3000, 1, 0)
     lat.synchronize()
     t0 = time.perf_counter()
@@ -298,6 +304,11 @@ def bench_differentiation(local):
         e, v, nhb = sample_columns(lat, smp, r)
         cols.append(np.stack([e, v, nhb, smp["n_sigma"].astype(np.float64)], axis=1))
         run_of.append(np.full(len(smp), r, dtype=np.int32))
+    fd_runs = []
+    for i, (t, p) in enumerate(fd_pts):
+        smp = lat.samples(R + i)
+        e, v, nhb = sample_columns(lat, smp, R + i)
+        fd_runs.append({"E": e, "V": v, "H": e + float(np.float32(p)) * v})
     lat.close()
     s = np.ascontiguousarray(np.concatenate(cols))
     ro = np.ascontiguousarray(np.concatenate(run_of))
@@ -346,6 +357,7 @@ def bench_differentiation(local):
     vp, vm = forward(th(0.755), ["V"], f, 0)[0], forward(th(0.745), ["V"], f, 0)[0]
     hp, hm = forward(th(0.755), ["H"], f, 0)[0], forward(th(0.745), ["H"], f, 0)[0]
     vpp, vpm = forward(th(0.75, P + 0.005), ["V"], f, 0)[0], forward(th(0.75, P - 0.005), ["V"], f, 0)[0]
+    independent = independent_run_check(fd_runs, fd_pts, N, {"alpha_P": ap_adj, "K_T": kt_adj, "C_P": cp_adj})
     gold = {round(a, 3): (b, c) for a, b, c in np.loadtxt(os.path.join(ROOT, "tests", "golden", "isobar_P0.45_density.txt"))}
     cmp = []
     for tt in sorted(k for k in gold if 0.6 <= k <= 0.9):
@@ -367,8 +379,55 @@ def bench_differentiation(local):
                         "fluctuation": (V2 - V * V) / (t * V)},
                 "C_P": {"adjoint": cp_adj, "finite_difference": (hp - hm) / 0.01 / N,
                         "fluctuation": (H2 - H * H) / (t * t * N)}},
+            "response_vs_independent_runs": independent,
             "rho_vs_reference_isobar": {"columns": ["T", "reweighted", "reference", "(rw - ref) / ref_err"],
                                         "rows": cmp}}
+
+
+def independent_run_check(runs, pts, N, reweighted, nb=20):
+    """alpha_P, K_T and C_P from central differences of the means of independent runs at T0 +/-
+    0.005 and P0 +/- 0.005 (20-block errors; the finite differences of the reference's
+    CVF_ThermodynamicAnalysis programs), against the adjoint's fluctuation formulas on the run at
+    (T0, P0) itself (jackknife errors over the same blocks) and the adjoint of the reweighted
+    32-run ensemble at (T0, P0): z = (adjoint - difference) / combined error."""
+    def blocks(x):
+        x = np.asarray(x)[: len(x) // nb * nb]
+        return x.reshape(nb, -1)
+
+    def mean_err(x):
+        b = blocks(x).mean(1)
+        return float(b.mean()), float(b.std(ddof=1) / np.sqrt(nb))
+
+    def jack(f, *cols):
+        bl = [blocks(c) for c in cols]
+        v = np.array([f(*[np.delete(b, k, axis=0).ravel() for b in bl]) for k in range(nb)])
+        return float(np.sqrt((nb - 1) / nb * ((v - v.mean()) ** 2).sum()))
+
+    Tf = [float(np.float32(t)) for t, _ in pts]
+    Pf = [float(np.float32(p)) for _, p in pts]
+    dT, dP = Tf[2] - Tf[1], Pf[4] - Pf[3]
+    beta = 1.0 / Tf[0]
+    c = runs[0]
+    V0 = float(c["V"].mean())
+    (hm, ehm), (hp, ehp) = mean_err(runs[1]["H"]), mean_err(runs[2]["H"])
+    (vm, evm), (vp, evp) = mean_err(runs[1]["V"]), mean_err(runs[2]["V"])
+    (wm, ewm), (wp, ewp) = mean_err(runs[3]["V"]), mean_err(runs[4]["V"])
+    fd = {"C_P": ((hp - hm) / dT / N, float(np.hypot(ehp, ehm)) / dT / N),
+          "alpha_P": ((vp - vm) / dT / V0, float(np.hypot(evp, evm)) / dT / V0),
+          "K_T": (-(wp - wm) / dP / V0, float(np.hypot(ewp, ewm)) / dP / V0)}
+    fl = {"C_P": (lambda h: beta * beta * h.var() / N, (c["H"],)),
+          "alpha_P": (lambda v, h: beta * beta * float(np.mean((v - v.mean()) * (h - h.mean()))) / v.mean(),
+                      (c["V"], c["H"])),
+          "K_T": (lambda v: beta * v.var() / v.mean(), (c["V"],))}
+    out = {}
+    for k in ("alpha_P", "K_T", "C_P"):
+        f, cols = fl[k]
+        val, err = f(*cols), jack(f, *cols)
+        d, e = fd[k]
+        out[k] = {"finite_difference_of_runs": d, "fd_error": e, "adjoint_same_run": float(val),
+                  "adjoint_error": err, "z": round((val - d) / float(np.hypot(e, err)), 2),
+                  "adjoint_reweighted_32_runs": float(reweighted[k])}
+    return out
 
 
 def bench_plain_l16(steps, warmup, local, flush):
@@ -635,6 +694,7 @@ def run_engine(args):
         "data": "synthetic (ordered start, Philox seed 44648604 + rank)",
         "config": workload_config(world),
         "sweep_tile": tile,
+        "tuning": dict(zip(("tile", "lg_rows", "launch_mode"), lat.tuning())),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": traffic,
                      "kernel": f"k_sweep<{tile}> (one colour of the checkerboard sweep)",

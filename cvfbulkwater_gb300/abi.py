@@ -127,6 +127,8 @@ def lib():
         "cvf_cluster_stats_noalloc": (I, [P, I, P, P]),
         "cvf_set_wait_limits": (I, [P, C.c_longlong, C.c_longlong]),
         "cvf_packed_size": (I, [P, I, C.POINTER(LL)]),
+        "cvf_set_row_tile": (I, [P, I]),
+        "cvf_get_tuning": (I, [P, C.POINTER(I), C.POINTER(I), C.POINTER(I)]),
         "cvf_get_packed": (I, [P, I, P, LL]),
         "cvf_set_packed": (I, [P, I, P, LL]),
         "cvf_read_input_data": (I, [C.c_char_p, C.POINTER(Input)]),

@@ -44,6 +44,8 @@ struct ReplicaDesc {
   int lgL, lgH;       // log2 of L and H when they are powers of two, else -1
   int start;          // Flag_config of the replica (0 disordered, 1 from file, 2 ordered)
   int cvec;           // consecutive cubes per thread in the cube move: 4, 2 or 1 (divides H)
+  int lgty;           // sweep row order: -1 rows by y then z; else tiles of 2^lgty rows in y, the
+                      // tiles' rows by z (a block covers a patch of y and z rows); set by autotune
   uint32_t key0, key1, replica;
   float T, P, Rc;
   double vdw_shift;   // vdw_shift(Rc), computed once on the host

@@ -597,6 +597,7 @@ int cvf_batch_create(const cvf_params* params, int n, cvf_handle** out) {
     d.lgH = lg(r.H);
     d.start = r.p.start;
     d.cvec = r.H % 4 == 0 ? 4 : (r.H % 2 == 0 ? 2 : 1);
+    d.lgty = -1;
     d.key0 = (uint32_t)((unsigned long long)r.p.seed & 0xffffffffu);
     d.key1 = (uint32_t)((unsigned long long)r.p.seed >> 32);
     d.replica = r.p.replica;
@@ -1116,6 +1117,59 @@ int cvf_set_state(cvf_handle* h, int r, const cvf_state* in) {
   return 0;
 }
 
+static void set_row_tile(cvf_handle* h, int lgty) {
+  for (auto& r : h->reps) r.desc.lgty = (lgty >= 0 && (1 << lgty) < r.L && r.L % (1 << lgty) == 0) ? lgty : -1;
+}
+
+// Device copies of every replica's lattice, cube states and scalar state, restored after timing.
+struct StateBackup {
+  std::vector<void*> bufs;
+  void* st = nullptr;
+  ~StateBackup() {
+    for (void* p : bufs) cudaFree(p);
+    if (st) cudaFree(st);
+  }
+};
+
+static int backup_state(cvf_handle* h, StateBackup& b, bool cubes_and_scalars) {
+  for (auto& r : h->reps) {
+    const size_t half = (size_t)(r.N / 2) * sizeof(uint32_t), nc = (size_t)r.H * r.H * r.H;
+    const size_t bytes = 2 * half + (cubes_and_scalars ? 2 * nc : 0);
+    void* p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return fail(CVF_ENOMEM, "autotune: cannot allocate the state backup");
+    b.bufs.push_back(p);
+    CK(cudaMemcpyAsync(p, r.desc.cells[0], half, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync((char*)p + half, r.desc.cells[1], half, cudaMemcpyDeviceToDevice, h->stream));
+    if (cubes_and_scalars) {
+      CK(cudaMemcpyAsync((char*)p + 2 * half, r.desc.cubes[0], nc, cudaMemcpyDeviceToDevice, h->stream));
+      CK(cudaMemcpyAsync((char*)p + 2 * half + nc, r.desc.cubes[1], nc, cudaMemcpyDeviceToDevice, h->stream));
+    }
+  }
+  if (cubes_and_scalars) {
+    const size_t sb = h->reps.size() * sizeof(ReplicaState);
+    if (cudaMalloc(&b.st, sb) != cudaSuccess) return fail(CVF_ENOMEM, "autotune: cannot allocate the state backup");
+    CK(cudaMemcpyAsync(b.st, h->b.st, sb, cudaMemcpyDeviceToDevice, h->stream));
+  }
+  return 0;
+}
+
+static int restore_state(cvf_handle* h, const StateBackup& b) {
+  for (size_t i = 0; i < h->reps.size(); ++i) {
+    auto& r = h->reps[i];
+    const size_t half = (size_t)(r.N / 2) * sizeof(uint32_t), nc = (size_t)r.H * r.H * r.H;
+    char* p = (char*)b.bufs[i];
+    CK(cudaMemcpyAsync(r.desc.cells[0], p, half, cudaMemcpyDeviceToDevice, h->stream));
+    CK(cudaMemcpyAsync(r.desc.cells[1], p + half, half, cudaMemcpyDeviceToDevice, h->stream));
+    if (b.st) {
+      CK(cudaMemcpyAsync(r.desc.cubes[0], p + 2 * half, nc, cudaMemcpyDeviceToDevice, h->stream));
+      CK(cudaMemcpyAsync(r.desc.cubes[1], p + 2 * half + nc, nc, cudaMemcpyDeviceToDevice, h->stream));
+    }
+  }
+  if (b.st) CK(cudaMemcpyAsync(h->b.st, b.st, h->reps.size() * sizeof(ReplicaState), cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
 int cvf_autotune(cvf_handle* h, int* vec_out) {
   if (!h) return fail(CVF_EINVAL, "null handle");
   h->count_valid = false;
@@ -1125,75 +1179,122 @@ int cvf_autotune(cvf_handle* h, int* vec_out) {
   }
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
-  std::vector<int> cands;
+  std::vector<int> vecs;
   for (int v : {8, 4, 2, 1}) {
     bool ok = true;
     for (auto& r : h->reps) ok = ok && (r.H % v == 0);
-    if (ok) cands.push_back(v);
+    if (ok) vecs.push_back(v);
+  }
+  // row tiles: plain order (-1) and patches of 8, 4 or 2 rows in y where they differ from it
+  std::vector<int> tys{-1};
+  for (int lg : {3, 2, 1}) {
+    bool ok = true;
+    for (auto& r : h->reps) ok = ok && (1 << lg) < r.L && r.L % (1 << lg) == 0;
+    if (ok) tys.push_back(lg);
   }
   // save every lattice; the timing sweeps are undone afterwards
-  std::vector<void*> saved;
-  for (auto& r : h->reps) {
-    void* p = nullptr;
-    size_t bytes = (size_t)r.N * sizeof(uint32_t);
-    if (cudaMalloc(&p, bytes) != cudaSuccess) {
-      for (void* q : saved) cudaFree(q);
-      return fail(CVF_ENOMEM, "autotune: cannot allocate the lattice backup");
-    }
-    cudaMemcpyAsync(p, r.desc.cells[0], bytes / 2, cudaMemcpyDeviceToDevice, h->stream);
-    cudaMemcpyAsync((char*)p + bytes / 2, r.desc.cells[1], bytes / 2, cudaMemcpyDeviceToDevice, h->stream);
-    saved.push_back(p);
-  }
-  // block tables of every candidate (block counts depend on the tile)
+  StateBackup saved;
+  if (int rc = backup_state(h, saved, false)) return rc;
+  // block tables of every tile (block counts depend on the tile)
   std::vector<BatchDev> tabs;
-  for (int v : cands) {
-    if (int rc = build_tables(h, v)) {
-      for (void* q : saved) cudaFree(q);
-      return rc;
-    }
+  for (int v : vecs) {
+    if (int rc = build_tables(h, v)) return rc;
     tabs.push_back(h->b);
   }
+  struct Cand {
+    size_t tab;
+    int lgty;
+    float ms;
+  };
+  std::vector<Cand> cands;
+  for (size_t i = 0; i < vecs.size(); ++i)
+    for (int lg : tys) cands.push_back({i, lg, 1e30f});
   // three interleaved rounds, the best time of each candidate: tiles within a few per cent of
   // each other are not told apart by one timing taken after another
   cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  std::vector<float> cand_ms(cands.size(), 1e30f);
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
   for (int round = 0; round < 3; ++round) {
-    for (size_t c = 0; c < cands.size(); ++c) {
-      launch_sweep(tabs[c], 0, 0, h->stream);  // warm-up
-      launch_sweep(tabs[c], 1, 0, h->stream);
+    for (auto& c : cands) {
+      set_row_tile(h, c.lgty);
+      if (int rc = upload_descs(h)) return rc;
+      const BatchDev& tb = tabs[c.tab];
+      launch_sweep(tb, 0, 0, h->stream);  // warm-up
+      launch_sweep(tb, 1, 0, h->stream);
       cudaEventRecord(e0, h->stream);
       for (int i = 0; i < 5; ++i) {
-        launch_sweep(tabs[c], 0, i, h->stream);
-        launch_sweep(tabs[c], 1, i, h->stream);
+        launch_sweep(tb, 0, i, h->stream);
+        launch_sweep(tb, 1, i, h->stream);
       }
       cudaEventRecord(e1, h->stream);
       cudaEventSynchronize(e1);
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e0, e1);
-      cand_ms[c] = std::min(cand_ms[c], ms);
+      c.ms = std::min(c.ms, ms);
     }
   }
   size_t bi = 0;
   for (size_t c = 1; c < cands.size(); ++c)
-    if (cand_ms[c] < cand_ms[bi]) bi = c;
-  const int best = cands.empty() ? h->b.vec : cands[bi];
-  for (size_t i = 0; i < h->reps.size(); ++i) {
-    auto& r = h->reps[i];
-    size_t bytes = (size_t)r.N * sizeof(uint32_t);
-    cudaMemcpyAsync(r.desc.cells[0], saved[i], bytes / 2, cudaMemcpyDeviceToDevice, h->stream);
-    cudaMemcpyAsync(r.desc.cells[1], (char*)saved[i] + bytes / 2, bytes / 2, cudaMemcpyDeviceToDevice, h->stream);
-  }
-  cudaError_t e = cudaStreamSynchronize(h->stream);
-  for (void* q : saved) cudaFree(q);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  if (e != cudaSuccess) return fail(CVF_ECUDA, std::string("autotune: ") + cudaGetErrorString(e));
+    if (cands[c].ms < cands[bi].ms) bi = c;
+  set_row_tile(h, cands[bi].lgty);
+  if (int rc = upload_descs(h)) return rc;
+  if (int rc = restore_state(h, saved)) return rc;
   // the sweep blocks depend on the tile: keep the chosen tables and drop captured graphs
   drop_graphs(h);
-  if (!tabs.empty()) h->b = tabs[bi];
-  if (vec_out) *vec_out = best;
+  h->b = tabs[cands[bi].tab];
+  // a batch of replicas also chooses its launch mode: 16 Metropolis steps of each mode from the
+  // same saved state (lattice, cube states, r_cell, volume, counters), the faster kept
+  if (h->reps.size() > 1 && !h->corr_on) {
+    StateBackup full;
+    if (int rc = backup_state(h, full, true)) return rc;
+    float best_ms = 1e30f;
+    int best_mode = h->launch_mode;
+    for (int mode : {0, 1}) {
+      drop_graphs(h);
+      h->launch_mode = mode;
+      if (int rc = cvf_run_steps(h, 16, 1, 0)) return rc;  // captures the graph, warms up
+      if (h->launch_mode != mode) continue;                  // the cooperative capture fell back
+      float ms = 1e30f;
+      for (int round = 0; round < 2; ++round) {
+        cudaEventRecord(e0, h->stream);
+        if (int rc = cvf_run_steps(h, 16, 1, 0)) return rc;
+        cudaEventRecord(e1, h->stream);
+        cudaEventSynchronize(e1);
+        float m = 0.f;
+        cudaEventElapsedTime(&m, e0, e1);
+        ms = std::min(ms, m);
+      }
+      if (int rc = check_err(h)) return rc;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_mode = mode;
+      }
+    }
+    drop_graphs(h);
+    h->launch_mode = best_mode;
+    h->count_valid = false;
+    if (int rc = restore_state(h, full)) return rc;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (vec_out) *vec_out = vecs.empty() ? h->b.vec : vecs[cands[bi].tab];
+  return 0;
+}
+
+int cvf_set_row_tile(cvf_handle* h, int lgty) {
+  if (!h || lgty < -1 || lgty > 8) return fail(CVF_EINVAL, "row tile must be -1 (plain) or log2 of 2..256 rows");
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  set_row_tile(h, lgty);
+  drop_graphs(h);
+  return upload_descs(h);
+}
+
+int cvf_get_tuning(const cvf_handle* h, int* tile, int* lgty, int* launch_mode) {
+  if (!h) return fail(CVF_EINVAL, "null handle");
+  if (tile) *tile = h->b.vec;
+  if (lgty) *lgty = h->reps.empty() ? -1 : h->reps[0].desc.lgty;
+  if (launch_mode) *launch_mode = h->launch_mode;
   return 0;
 }
 

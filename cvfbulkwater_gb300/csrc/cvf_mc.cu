@@ -544,14 +544,23 @@ __global__ void __launch_bounds__(kThreads, 4) k_cube_volume(const ReplicaDesc* 
 }
 
 // ------------------------------------------------------------------ checkerboard sweep
-// Thread -> (row segment, y, z) of a replica's colour array: q = hc + (H/V) * (y + L*z).
+// Thread -> (row segment, y, z) of a replica's colour array: q = hc + (H/V) * row. Rows run by y
+// then z (row = y + L*z), or with R.lgty >= 0 in tiles of TY = 2^lgty rows in y: row = yi + TY*(z
+// + L*yt), y = TY*yt + yi, so the consecutive threads of a block cover TY rows in y and several
+// planes in z. The order only places work on threads; every cell's update is the same.
 template <int V>
 __device__ __forceinline__ bool segment_of(const ReplicaDesc& R, uint32_t q, int& hc, int& y, int& z) {
   const uint32_t L = R.L, cpr = R.H / V;
   if (q >= cpr * L * L) return false;
   uint32_t row, hh, zz, yy;
   divmod32(q, cpr, R.lgH >= 0 ? R.lgH - Log2V<V>::v : -1, row, hh);
-  divmod32(row, L, R.lgL, zz, yy);
+  if (R.lgty < 0) {
+    divmod32(row, L, R.lgL, zz, yy);
+  } else {
+    uint32_t yt;
+    divmod32(row >> R.lgty, L, R.lgL, yt, zz);
+    yy = (yt << R.lgty) + (row & ((1u << R.lgty) - 1u));
+  }
   hc = (int)hh;
   y = (int)yy;
   z = (int)zz;

@@ -126,6 +126,15 @@ class Lattice:
         check(lib().cvf_autotune(self._h, C.byref(v)))
         return v.value
 
+    def tuning(self):
+        """(tile, log2 of the row patch or -1, launch mode) in effect."""
+        t, g, m = C.c_int(), C.c_int(), C.c_int()
+        check(lib().cvf_get_tuning(self._h, C.byref(t), C.byref(g), C.byref(m)))
+        return t.value, g.value, m.value
+
+    def set_row_tile(self, lg_rows: int):
+        check(lib().cvf_set_row_tile(self._h, int(lg_rows)))
+
     @property
     def replica_groups(self) -> int:
         """Groups of consecutive replicas captured on parallel graph branches (count in effect)."""

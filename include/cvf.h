@@ -308,11 +308,20 @@ int cvf_kt_derivative(const double* T, const double* P, const double* rho, const
                       double* EKT);
 
 /* Autotuner: times the checkerboard sweep kernel on this handle's replicas for every supported
- * cells-per-thread tile (1, 2, 4 or 8 consecutive colour cells: 32-, 64-, 128- or 2x128-bit accesses) and
- * keeps the fastest. The lattices are saved before and restored after, so the Markov chains are
- * unchanged (the tile only changes the thread mapping, never the result). vec_out may be NULL.
- * No reference counterpart. */
+ * cells-per-thread tile (1, 2, 4 or 8 consecutive colour cells: 32-, 64-, 128- or 2x128-bit
+ * accesses) and every row order (rows by y then z, or patches of 8, 4 or 2 rows in y across
+ * several z planes per block) and keeps the fastest pair; a batch of several replicas then times
+ * 16 Metropolis steps in each launch mode (cvf_set_launch_mode) and keeps the faster. The lattices
+ * (and for the mode choice the cube states, r_cell, volume and counters) are saved before and
+ * restored after, so the Markov chains are unchanged (the tile and row order only change the
+ * thread mapping, never the result). vec_out may be NULL; cvf_get_tuning reports all three
+ * choices. No reference counterpart. */
 int cvf_autotune(cvf_handle* h, int* vec_out);
+/* Row order of the sweep set by hand: -1 rows by y then z, k >= 1 patches of 2^k rows in y (used
+ * where 2^k divides L and is below it). cvf_get_tuning: the tile, the row order and the launch
+ * mode in effect (any pointer may be NULL). No reference counterpart. */
+int cvf_set_row_tile(cvf_handle* h, int lg_rows);
+int cvf_get_tuning(const cvf_handle* h, int* tile, int* lg_rows, int* launch_mode);
 /* Sets the sweep tile by hand (1, 2, 4 or 8 cells per thread; reduced to the largest that divides
  * every replica's L/2), as the autotuner would. The environment variable CVF_SWEEP_VEC gives the
  * tile a new handle starts with (default 4). Returns the tile in effect through vec_out (may be
