@@ -23,6 +23,7 @@ struct ReplicaDesc {
   uint32_t* cellsw;   // N: bits 0..2 = active x+, y+, z+ cluster bonds; bits 3+3a..5+3a = the
                       // smallest arm of arm a's in-cell component (its in-cell root)
   uint32_t* flip;     // N: bits 3a..3a+2 = shift of the cluster whose root is arm site a of the cell
+  uint32_t* swlist;   // N: cells with a hydrogen-bond link in the current SW step (ReplicaState.swq of them)
   int32_t* csize;     // 6N: cluster sizes by root
   int32_t* cand;      // 6N: percolation candidate id by root (-1 none)
   uint32_t* cover;    // max_cand * 3 * W: coordinate coverage bitmaps
@@ -86,6 +87,7 @@ struct ReplicaState {
   unsigned long long ncl, sum2, sum2w, nperc;
   int ncand;
   int err;  // nonzero: a bounded loop gave up (1 SW union, 2 candidate overflow, 3 grid barrier)
+  uint32_t swq;  // entries of the replica's SW worklist (k_sw_local appends, k_sw_finish clears)
   uint32_t n_samples, n_cstats;
   uint32_t cap_samples, cap_cstats;
   SampleRec* samples;   // device sample stream

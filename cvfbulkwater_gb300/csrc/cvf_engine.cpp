@@ -295,6 +295,7 @@ static int ensure_sw(cvf_handle* h) {
     if (int rc = dev_alloc(h, (void**)&r.desc.label, NS * sizeof(int32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.cellsw, (size_t)r.N * sizeof(uint32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.flip, (size_t)r.N * sizeof(uint32_t))) return rc;
+    if (int rc = dev_alloc(h, (void**)&r.desc.swlist, (size_t)r.N * sizeof(uint32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.csize, NS * sizeof(int32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.cand, NS * sizeof(int32_t))) return rc;
     if (int rc = dev_alloc(h, (void**)&r.desc.cover, (size_t)r.desc.max_cand * 3 * W * sizeof(uint32_t))) return rc;

@@ -122,7 +122,7 @@ __device__ __noinline__ uint32_t sw_links_exact(uint32_t c, uint32_t t, uint32_t
 // and the in-cell root (smallest arm of its in-cell component) of every arm, for the union and
 // the finish.
 __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __restrict__ reps,
-                                                       const ReplicaState* __restrict__ st,
+                                                       ReplicaState* __restrict__ st,
                                                        const int* __restrict__ blk, int nrep, int jsw) {
   pdl_trigger();
   const int r = find_replica_sw(blk, nrep, blockIdx.x);
@@ -221,6 +221,16 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
     lab = (lab & ~m7) | ((lo * 0x9249u) & m7);
   }
   R.cellsw[c] = (bonds & 7u) | (lab << 3);
+  {
+    // cells with a hydrogen-bond link go to the replica's worklist (one atomic per warp)
+    const unsigned act = __activemask();
+    const unsigned linked = __ballot_sync(act, (bonds & 7u) != 0u);
+    const int lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (linked && lane == __ffs(linked) - 1) base = atomicAdd(&st[r].swq, (uint32_t)__popc(linked));
+    base = __shfl_sync(act, base, __ffs(linked ? linked : 1u) - 1);
+    if ((linked >> lane) & 1u) R.swlist[base + __popc(linked & ((1u << lane) - 1u))] = c;
+  }
 #pragma unroll
   for (int a = 0; a < 6; ++a) R.label[a * N + c] = (int32_t)(((lab >> (3 * a)) & 7u) * N + c);
 }
@@ -257,9 +267,10 @@ __device__ __forceinline__ bool uf_unite(int32_t* p, int32_t a, int32_t b, uint3
   return false;
 }
 
-// One thread per cell with a hydrogen-bond link: the link joins the in-cell component of the
-// cell's arm 2d with the in-cell component of the neighbour's arm 2d+1, so the union starts from
-// the two in-cell roots (recorded by k_sw_local) rather than from the arm sites.
+// The worklist of the cells with a hydrogen-bond link, spread over the replica's threads (one
+// thread per four cells of the lattice, each taking every nth entry): a link joins the in-cell
+// component of the cell's arm 2d with the in-cell component of the neighbour's arm 2d+1, so the
+// union starts from the two in-cell roots (recorded by k_sw_local) rather than from the arm sites.
 __global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __restrict__ reps,
                                                        ReplicaState* __restrict__ st,
                                                        const int* __restrict__ blk, int nrep) {
@@ -268,24 +279,27 @@ __global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __rest
   const ReplicaDesc& R = reps[r];
   const uint32_t L = R.L;
   const uint32_t N = L * L * L;
-  const uint32_t c = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
-  if (c >= N) return;
+  const uint32_t nth = (uint32_t)(blk[r + 1] - blk[r]) * blockDim.x;
+  const uint32_t t0 = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
   pdl_wait();
-  const uint32_t sw = R.cellsw[c];
-  const uint32_t hb = sw & 7u;
-  if (!hb) return;
-  int xi, yi, zi;
-  cell_xyz(R, c, xi, yi, zi);
-  const uint32_t x = xi, y = yi, z = zi;
-  const uint32_t nb[3] = {(x + 1 == L ? 0 : x + 1) + L * (y + L * z), x + L * ((y + 1 == L ? 0 : y + 1) + L * z),
-                          x + L * (y + L * (z + 1 == L ? 0 : z + 1))};
+  const uint32_t n = st[r].swq;
+  for (uint32_t i = t0; i < n; i += nth) {
+    const uint32_t c = R.swlist[i];
+    const uint32_t sw = R.cellsw[c];
+    const uint32_t hb = sw & 7u;
+    int xi, yi, zi;
+    cell_xyz(R, c, xi, yi, zi);
+    const uint32_t x = xi, y = yi, z = zi;
+    const uint32_t nb[3] = {(x + 1 == L ? 0 : x + 1) + L * (y + L * z), x + L * ((y + 1 == L ? 0 : y + 1) + L * z),
+                            x + L * (y + L * (z + 1 == L ? 0 : z + 1))};
 #pragma unroll
-  for (int d = 0; d < 3; ++d)
-    if ((hb >> d) & 1u) {
-      const uint32_t ra = (sw >> (3 + 6 * d)) & 7u;                          // in-cell root of arm 2d
-      const uint32_t rb = (R.cellsw[nb[d]] >> (3 + 3 * (2 * d + 1))) & 7u;  // of the neighbour's arm 2d+1
-      if (!uf_unite(R.label, (int32_t)(ra * N + c), (int32_t)(rb * N + nb[d]), R.union_iters)) st[r].err = 1;
-    }
+    for (int d = 0; d < 3; ++d)
+      if ((hb >> d) & 1u) {
+        const uint32_t ra = (sw >> (3 + 6 * d)) & 7u;                          // in-cell root of arm 2d
+        const uint32_t rb = (R.cellsw[nb[d]] >> (3 + 3 * (2 * d + 1))) & 7u;  // of the neighbour's arm 2d+1
+        if (!uf_unite(R.label, (int32_t)(ra * N + c), (int32_t)(rb * N + nb[d]), R.union_iters)) st[r].err = 1;
+      }
+  }
 }
 
 // Compression, cluster shift and update in one pass, one thread per cell. An in-cell component
@@ -296,7 +310,7 @@ __global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __rest
 // cluster's shift is digit a of the shift word that k_sw_local drew for cell c, for the root site
 // a*N + c (GW:2531-2542 gives every cluster one uniform shift in 0..5); sigma is shifted by it.
 __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __restrict__ reps,
-                                                        const ReplicaState* __restrict__ st,
+                                                        ReplicaState* __restrict__ st,
                                                         const int* __restrict__ blk, int nrep, int jsw) {
   pdl_trigger();
   const int r = find_replica_sw(blk, nrep, blockIdx.x);
@@ -311,6 +325,7 @@ __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __res
   const uint32_t cym = (uint32_t)x + (uint32_t)L * ((uint32_t)(y == 0 ? L - 1 : y - 1) + (uint32_t)L * (uint32_t)z);
   const uint32_t czm = (uint32_t)x + (uint32_t)L * ((uint32_t)y + (uint32_t)L * (uint32_t)(z == 0 ? L - 1 : z - 1));
   pdl_wait();
+  if (c == 0) st[r].swq = 0;  // the union has used the worklist; the next SW step refills it
   const uint32_t sw = R.cellsw[c];
   const uint32_t lab = sw >> 3;
   // arms with a hydrogen-bond link: 0, 2, 4 from this cell's links, 1, 3, 5 from the neighbours'
@@ -325,6 +340,18 @@ __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __res
   const uint32_t w = *wp;
   const uint32_t own_flip = R.flip[c];
   uint32_t out = 0;
+  if (ext_root == 0) {
+    // no link reaches the cell: every cluster is an in-cell component, rooted here
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+      const uint32_t m = (lab >> (3 * a)) & 7u;
+      uint32_t v = ((w >> (3 * a)) & 7u) + ((own_flip >> (3 * m)) & 7u);
+      v = v >= 6u ? v - 6u : v;
+      out |= v << (3 * a);
+    }
+    *wp = out;
+    return;
+  }
 #pragma unroll
   for (int a = 0; a < 6; ++a) {
     const uint32_t m = (lab >> (3 * a)) & 7u;
@@ -537,7 +564,7 @@ __global__ void k_cs_begin(ReplicaState* __restrict__ st, int nrep) {
 void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s) {
   const dim3 g((unsigned)b.nblk_cell);
   launch_pdl(k_sw_local, g, s, b.pdl, b.reps, b.st, b.blk_cell, b.nrep, jsw);
-  launch_pdl(k_sw_union, g, s, b.pdl, b.reps, b.st, b.blk_cell, b.nrep);
+  launch_pdl(k_sw_union, dim3((unsigned)b.nblk_cell4), s, b.pdl, b.reps, b.st, b.blk_cell4, b.nrep);
   launch_pdl(k_sw_finish, g, s, b.pdl, b.reps, b.st, b.blk_cell, b.nrep, jsw);
 }
 
