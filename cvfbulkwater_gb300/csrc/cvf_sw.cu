@@ -123,7 +123,8 @@ __device__ __noinline__ uint32_t sw_links_exact(uint32_t c, uint32_t t, uint32_t
 // the finish.
 __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __restrict__ reps,
                                                        ReplicaState* __restrict__ st,
-                                                       const int* __restrict__ blk, int nrep, int jsw) {
+                                                       const int* __restrict__ blk, int nrep, int jsw,
+                                                       int worklist) {
   pdl_trigger();
   const int r = find_replica_sw(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
@@ -221,7 +222,7 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
     lab = (lab & ~m7) | ((lo * 0x9249u) & m7);
   }
   R.cellsw[c] = (bonds & 7u) | (lab << 3);
-  {
+  if (worklist) {
     // cells with a hydrogen-bond link go to the replica's worklist (one atomic per warp)
     const unsigned act = __activemask();
     const unsigned linked = __ballot_sync(act, (bonds & 7u) != 0u);
@@ -268,7 +269,7 @@ __device__ __forceinline__ bool uf_unite(int32_t* p, int32_t a, int32_t b, uint3
 }
 
 // The worklist of the cells with a hydrogen-bond link, spread over the replica's threads (one
-// thread per four cells of the lattice, each taking every nth entry): a link joins the in-cell
+// thread per four cells of the lattice): a link joins the in-cell
 // component of the cell's arm 2d with the in-cell component of the neighbour's arm 2d+1, so the
 // union starts from the two in-cell roots (recorded by k_sw_local) rather than from the arm sites.
 __global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __restrict__ reps,
@@ -300,6 +301,36 @@ __global__ void __launch_bounds__(kThreads) k_sw_union(const ReplicaDesc* __rest
         if (!uf_unite(R.label, (int32_t)(ra * N + c), (int32_t)(rb * N + nb[d]), R.union_iters)) st[r].err = 1;
       }
   }
+}
+
+// The same unions with one thread per cell (cells without a hydrogen-bond link return at once),
+// for lattices small enough that the worklist's few threads would leave SMs idle.
+__global__ void __launch_bounds__(kThreads) k_sw_union_cells(const ReplicaDesc* __restrict__ reps,
+                                                             ReplicaState* __restrict__ st,
+                                                             const int* __restrict__ blk, int nrep) {
+  pdl_trigger();
+  const int r = find_replica_sw(blk, nrep, blockIdx.x);
+  const ReplicaDesc& R = reps[r];
+  const uint32_t L = R.L;
+  const uint32_t N = L * L * L;
+  const uint32_t c = (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  pdl_wait();
+  const uint32_t sw = R.cellsw[c];
+  const uint32_t hb = sw & 7u;
+  if (!hb) return;
+  int xi, yi, zi;
+  cell_xyz(R, c, xi, yi, zi);
+  const uint32_t x = xi, y = yi, z = zi;
+  const uint32_t nb[3] = {(x + 1 == L ? 0 : x + 1) + L * (y + L * z), x + L * ((y + 1 == L ? 0 : y + 1) + L * z),
+                          x + L * (y + L * (z + 1 == L ? 0 : z + 1))};
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    if ((hb >> d) & 1u) {
+      const uint32_t ra = (sw >> (3 + 6 * d)) & 7u;
+      const uint32_t rb = (R.cellsw[nb[d]] >> (3 + 3 * (2 * d + 1))) & 7u;
+      if (!uf_unite(R.label, (int32_t)(ra * N + c), (int32_t)(rb * N + nb[d]), R.union_iters)) st[r].err = 1;
+    }
 }
 
 // Compression, cluster shift and update in one pass, one thread per cell. An in-cell component
@@ -561,10 +592,15 @@ __global__ void k_cs_begin(ReplicaState* __restrict__ st, int nrep) {
 }
 
 // ---------------------------------------------------------------- launchers
+// Lattices of 2^20 cells or more (L >= 102) unite over the worklist; smaller ones with one thread
+// per cell, whose bonded threads spread over every SM (L=64 step 38 us with the worklist against
+// 34 us per cell; L=128 125-127 us against 129-133 us).
 void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s) {
   const dim3 g((unsigned)b.nblk_cell);
-  launch_pdl(k_sw_local, g, s, b.pdl, b.reps, b.st, b.blk_cell, b.nrep, jsw);
-  launch_pdl(k_sw_union, dim3((unsigned)b.nblk_cell4), s, b.pdl, b.reps, b.st, b.blk_cell4, b.nrep);
+  const int wl = (long long)b.max_L * b.max_L * b.max_L >= (1ll << 20);
+  launch_pdl(k_sw_local, g, s, b.pdl, b.reps, b.st, b.blk_cell, b.nrep, jsw, wl);
+  if (wl) launch_pdl(k_sw_union, dim3((unsigned)b.nblk_cell4), s, b.pdl, b.reps, b.st, b.blk_cell4, b.nrep);
+  else launch_pdl(k_sw_union_cells, g, s, b.pdl, b.reps, b.st, b.blk_cell, b.nrep);
   launch_pdl(k_sw_finish, g, s, b.pdl, b.reps, b.st, b.blk_cell, b.nrep, jsw);
 }
 
