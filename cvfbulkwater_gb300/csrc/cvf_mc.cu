@@ -671,7 +671,7 @@ __device__ __noinline__ uint32_t sweep_proposal_retry(uint32_t c0, uint32_t t, u
 // low halves from the refinement block). Taken only when a 16-bit comparison tied.
 // Returns the new word in the low 32 bits and the packed count changes of the accepted arms,
 // 65536 dN_hb + dN_sigma, in the high 32 bits.
-__device__ __noinline__ unsigned long long sweep_cell_exact(uint32_t w, uint32_t nbs, uint32_t eta, uint32_t u,
+__device__ __noinline__ unsigned long long sweep_cell_exact(uint32_t w, uint32_t nbe, uint32_t u,
                                                             uint32_t a1, uint32_t a2, uint32_t a3, uint32_t c0,
                                                             uint32_t t, const ReplicaDesc* R) {
   const U4 rf = philox(c0, t, kStSweepRefine, R->replica, R->key0, R->key1);
@@ -684,8 +684,8 @@ __device__ __noinline__ unsigned long long sweep_cell_exact(uint32_t w, uint32_t
     f = (uint32_t)m;
     const uint32_t o = (w >> (3 * a)) & 7u;
     if (n == o) continue;
-    const uint32_t nb = (nbs >> (3 * a)) & 7u;
-    const int dhb = ((eta >> a) & 1u) ? ((int)(n == nb) - (int)(o == nb)) : 0;
+    const uint32_t nb = (nbe >> (3 * a)) & 7u;  // 7 where eta_a = 0: never equal to a sigma
+    const int dhb = (int)(n == nb) - (int)(o == nb);
     const int dns = (int)((h >> (4 * n)) & 15u) - (int)((h >> (4 * o)) & 15u) + 1;
     const unsigned long long T = R->thr_sweep[(dhb + 1) * 11 + dns + 5];
     const uint32_t hw = a < 2 ? a1 : (a < 4 ? a2 : a3);
@@ -812,12 +812,20 @@ __device__ __forceinline__ void fill_block_sweep_tables(const ReplicaDesc& R, Sw
 // decides every arm from the full 32-bit uniforms. A proposal equal to the old
 // value lands on entry 17 (dN = 0), which always accepts and changes nothing.
 // kCount: dacc also receives the packed count changes (pk) of the accepted arms that change a value.
-template <bool kCount>
-__device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32_t nbe, uint32_t eta, const U4& rr,
+template <bool kCount, bool kFold>
+__device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbe, const U4& rr,
                                                 uint32_t c0, uint32_t t, const ReplicaDesc& R, const SweepTables* wt,
                                                 int32_t& dacc) {
+  // a proposal word in the rejected range of the exact draw (p = 6e-7): with kFold it sends the
+  // cell through the exact path, which draws the retry word, and the fast path's decisions are
+  // discarded (one rare-path test per cell instead of two); otherwise the retry word is drawn
+  // first (the counting, measuring and persistent kernels keep within their registers so)
   uint32_t u = rr.x;
-  if (u * 46656u < 2560u) u = sweep_proposal_retry(c0, t, R.replica, R.key0, R.key1);
+  bool reject = u * 46656u < 2560u;
+  if (!kFold && reject) {
+    u = sweep_proposal_retry(c0, t, R.replica, R.key0, R.key1);
+    reject = false;
+  }
   const uint32_t w0 = w;
   uint32_t hx = 0, hy = 0;
 #pragma unroll
@@ -860,8 +868,9 @@ __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbs, uint32
           : "r"(d), "r"(dw), "r"(cn.x), "r"(co.x), "r"(cn.y), "r"(co.y));
     }
   }
-  if (tprod == 0u) {
-    const unsigned long long x = sweep_cell_exact(w0, nbs, eta, u, rr.y, rr.z, rr.w, c0, t, &R);
+  if (tprod == 0u || reject) {
+    const uint32_t ue = reject ? sweep_proposal_retry(c0, t, R.replica, R.key0, R.key1) : u;
+    const unsigned long long x = sweep_cell_exact(w0, nbe, ue, rr.y, rr.z, rr.w, c0, t, &R);
     w = (uint32_t)x;
     cacc = (int32_t)(uint32_t)(x >> 32);
   }
@@ -884,12 +893,14 @@ struct SweepMinBlocks {
 // colour-1 cells count all bonds (delta of the facing sigmas times the bond's eta, twice), and
 // each colour-1 cell adds the sigma pairs of itself and of the colour-0 cell with the same word
 // index (the x-neighbour the segment loads anyway).
-template <int V, bool kMeasure, bool kCount = false>
+template <int V, bool kMeasure, bool kCount = false, bool kFold = false>
 __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepTables* wt, uint32_t q, int colour,
                                               uint32_t t, uint32_t& hb2, uint32_t& ns, int32_t* dacc = nullptr) {
   int hc, y, z;
   if (!segment_of<V>(R, q, hc, y, z)) return;
-  uint32_t out[V], nbs[V], nbe[V], eta[V];
+  // nbe: the facing neighbour sigmas with 7 in the field of every arm whose eta is 0 -- all that
+  // the decisions and the measurement need of the neighbours and of eta
+  uint32_t out[V], nbe[V];
   uint32_t* own_ptr;
   int x0;
   {
@@ -897,9 +908,8 @@ __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepT
     cb.load(R, colour, hc, y, z, wt->et.eta);
 #pragma unroll
     for (int k = 0; k < V; ++k) {
-      nbs[k] = neighbour_sigmas(cb.xp[k], cb.xm[k], cb.yp[k], cb.ym[k], cb.zp[k], cb.zm[k]);
-      eta[k] = cb.eta[k];
-      nbe[k] = nbs[k] | wt->et.nbmask[~cb.eta[k] & 63u];
+      nbe[k] = neighbour_sigmas(cb.xp[k], cb.xm[k], cb.yp[k], cb.ym[k], cb.zp[k], cb.zm[k]) |
+               wt->et.nbmask[~cb.eta[k] & 63u];
       out[k] = cb.own[k];
       if (kMeasure) ns += sigma_pairs(cb.s == 0 ? cb.xp[k] : cb.xm[k]);
     }
@@ -914,14 +924,14 @@ __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepT
     const uint32_t c0 = cbase + 2u * k;
     const U4 rr = philox_rk(c0, t, kStSweep, R.replica, rk);
     int32_t dummy = 0;
-    out[k] = update_cell<kCount>(out[k], nbs[k], nbe[k], eta[k], rr, c0, t, R, wt, kCount ? *dacc : dummy);
+    out[k] = update_cell<kCount, kFold>(out[k], nbe[k], rr, c0, t, R, wt, kCount ? *dacc : dummy);
   }
   VecLoad<V>::st(own_ptr, out);
   if (kMeasure) {
 #pragma unroll
     for (int k = 0; k < V; ++k) {
-      const uint32_t x = out[k] ^ nbs[k];
-      const uint32_t eqm = ~(x | (x >> 1) | (x >> 2)) & wt->et.nbmask[eta[k] & 63u] & 0x9249u;
+      const uint32_t x = out[k] ^ nbe[k];  // a field of 7 (eta = 0) never matches
+      const uint32_t eqm = ~(x | (x >> 1) | (x >> 2)) & 0x9249u;
       hb2 += 2u * (uint32_t)__popc(eqm);
       ns += sigma_pairs(out[k]);
     }
@@ -941,7 +951,7 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const 
   pdl_wait();
   uint32_t hb2 = 0, ns = 0;
   int32_t dacc = 0;
-  sweep_segment<V, false, kCount>(R, &s_tab, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
+  sweep_segment<V, false, kCount, !kCount>(R, &s_tab, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
                                   st[r].cur[0] + (uint32_t)jsweep, hb2, ns, &dacc);
   if (kCount) {
     const int ds = (int)(int16_t)(dacc & 0xffff);  // |dN_sigma| per thread <= 8 cells x 30
@@ -1000,7 +1010,7 @@ __global__ void __launch_bounds__(kThreads) k_chunk_cluster(const ReplicaDesc* _
       for (int colour = 0; colour < 2; ++colour) {
         if (live)
           for (uint32_t q = rank * kThreads + threadIdx.x; q < nseg; q += kClusterCtas * kThreads)
-            sweep_segment<V, false>(R, wt, q, colour, t, hb2, ns);
+            sweep_segment<V, false, false, true>(R, wt, q, colour, t, hb2, ns);
         cluster_barrier();
       }
     }
