@@ -168,10 +168,16 @@ void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do
 // moves (do_volume): the two moves are independent, so the volume move hides under the cubes.
 // count: the counting variants also add the changes of N_hb and N_sigma they make to the
 // replicas' running counts (dlt_slot).
-void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, bool count = false);
+// soff >= 0: the step is step soff of a chunk whose kernels take their counters as offsets from
+// ctr (no k_step_begin; launch_chunk_end after the chunk); soff < 0: the counters of cur.
+void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, bool count = false,
+                        int soff = -1);
+void launch_chunk_end(const BatchDev& b, int steps, int nmet, int ncl, int do_volume, cudaStream_t s);
 void launch_volume_chain(const BatchDev& b, int steps, cudaStream_t s);
 cudaError_t launch_chunk_cluster(const BatchDev& b, int steps, int nmet, cudaStream_t s);
-void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, bool count = false);
+// jsweep: the sweep's offset from cur[0], or with from_ctr from ctr[0] (step i, sweep j of a chunk:
+// i * nmet + j).
+void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, bool count = false, int from_ctr = 0);
 // The running counts into every replica's last record (with its r_cell and volume; appended to
 // the sample stream when record is set), and the re-basing after a full measurement (base =
 // last record, changes zeroed).
@@ -187,7 +193,7 @@ void launch_measure_end(const BatchDev& b, int record, cudaStream_t s);
 // every replica, with a recorded measurement after every step s with s % interval == 0 when
 // interval > 0. Same lattice, counters and samples as the per-phase kernels.
 cudaError_t launch_run(const BatchDev& b, int nsteps, int nmet, int interval, cudaStream_t s);
-void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s);
+void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s, int from_ctr = 0);
 // Flag_chessboard = 0: bond counts from the lattice and eta6 (GW:841-862; one replica, or all for
 // only_replica < 0), one Metropolis sweep
 // (12 launches: colour 0 arms 0..5, colour 1 arms 0..5) and the measurement with the greedy

@@ -319,6 +319,18 @@ static void enqueue_step(cvf_handle* h, int nmet, int ncl, bool count = false, b
   for (int j = 0; j < ncl; ++j) launch_sw_step(h->b, j, h->stream);
 }
 
+// Step i of a chunk without records: the kernels take their counters as offsets from ctr (cube
+// ctr[1] + i, volume ctr[2] + i, sweep j ctr[0] + i*nmet + j, SW step j ctr[3] + i*ncl + j), and
+// one launch_chunk_end after the chunk advances the counters, instead of one k_step_begin per step.
+static void enqueue_step_at(const BatchDev& b, cudaStream_t s, int nmet, int ncl, bool count, bool volume, int i) {
+  launch_cube_volume(b, 1, volume ? 1 : 0, s, count, i);
+  for (int j = 0; j < nmet; ++j) {
+    launch_sweep(b, 0, i * nmet + j, s, count, 1);
+    launch_sweep(b, 1, i * nmet + j, s, count, 1);
+  }
+  for (int j = 0; j < ncl; ++j) launch_sw_step(b, i * ncl + j, s, 1);
+}
+
 // A Metropolis-only step followed by a recorded measurement: the measurement rides on the last
 // colour-1 sweep (slots zeroed by the step's begin kernel), then the slots are summed.
 static void enqueue_recorded_metropolis_step(cvf_handle* h, int nmet) {
@@ -403,8 +415,17 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     CK(cudaEventRecord(h->fork, h->stream));
     for (auto& gr : h->groups) CK(cudaStreamWaitEvent(gr.s, h->fork, 0));
-    for (auto& gr : h->groups)
-      for (int i = 0; i < steps; ++i) enqueue_metropolis_on(gr.b, gr.s, nmet, i == 0 && record, h->corr_on);
+    for (auto& gr : h->groups) {
+      if (record) {
+        for (int i = 0; i < steps; ++i) enqueue_metropolis_on(gr.b, gr.s, nmet, i == 0, h->corr_on);
+      } else {
+        for (int i = 0; i < steps; ++i) {
+          enqueue_step_at(gr.b, gr.s, nmet, 0, false, true, i);
+          if (h->corr_on) launch_corr_step(gr.b, gr.s);
+        }
+        launch_chunk_end(gr.b, steps, nmet, 0, 1, gr.s);
+      }
+    }
     for (auto& gr : h->groups) {
       CK(cudaEventRecord(gr.done, gr.s));
       CK(cudaStreamWaitEvent(h->stream, gr.done, 0));
@@ -459,7 +480,14 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     clustered = launch_chunk_cluster(h->b, steps, nmet, h->stream) == cudaSuccess;
     if (!clustered) cudaGetLastError();
   }
-  for (int i = 0; i < steps && !h->nhb_mode && !clustered; ++i) {
+  // chunks without records take their counters as offsets (one end kernel per chunk)
+  const bool offsets = !record && !h->nhb_mode && !clustered && steps > 0;
+  for (int i = 0; i < steps && offsets; ++i) {
+    enqueue_step_at(h->b, h->stream, nmet, ncl, count, !side, i);
+    if (h->corr_on) launch_corr_step(h->b, h->stream);
+  }
+  if (offsets) launch_chunk_end(h->b, steps, nmet, ncl, side ? 0 : 1, h->stream);
+  for (int i = 0; i < steps && !h->nhb_mode && !clustered && !offsets; ++i) {
     if (side) {
       enqueue_step(h, nmet, ncl, count, false);
     } else if (count) {

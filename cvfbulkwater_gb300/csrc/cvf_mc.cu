@@ -198,6 +198,29 @@ __global__ void k_step_begin(ReplicaState* __restrict__ st, int nrep, int nmet, 
   S.ctr[3] += (uint32_t)ncl;
 }
 
+// The counters after a chunk of `steps` steps whose kernels took them as offsets from ctr (step
+// i: cube ctr[1] + i, volume ctr[2] + i, sweep j ctr[0] + i*nmet + j, SW step j ctr[3] + i*ncl +
+// j): ctr advanced and cur left as the last step's k_step_begin would leave them. One launch per
+// chunk instead of one k_step_begin per step.
+__global__ void k_chunk_end(ReplicaState* __restrict__ st, int nrep, int steps, int nmet, int ncl, int do_volume) {
+  pdl_trigger();
+  pdl_wait();
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrep) return;
+  ReplicaState& S = st[r];
+  const uint32_t last = (uint32_t)(steps - 1);
+  S.cur[0] = S.ctr[0] + last * (uint32_t)nmet;
+  S.ctr[0] += (uint32_t)(steps * nmet);
+  S.cur[1] = S.ctr[1] + last;
+  S.ctr[1] += (uint32_t)steps;
+  if (do_volume) {  // otherwise the side branch moves the volume counter
+    S.cur[2] = S.ctr[2] + last;
+    S.ctr[2] += (uint32_t)steps;
+  }
+  S.cur[3] = S.ctr[3] + last * (uint32_t)ncl;
+  S.ctr[3] += (uint32_t)(steps * ncl);
+}
+
 // ------------------------------------------------------------------ volume move (one warp)
 // NPT volume move of GW:1740-1781 in FP64, every operation rounded separately. The shell terms
 // of E_vdW(r') are computed by the 32 lanes and summed by lane 0 in shell order, which is the
@@ -522,12 +545,14 @@ __device__ __forceinline__ void count_accumulate(ReplicaState& S, int vb, int dn
 template <bool kCount>
 __global__ void __launch_bounds__(kThreads, 4) k_cube_volume(const ReplicaDesc* __restrict__ reps,
                                                           ReplicaState* __restrict__ st,
-                                                          const int* __restrict__ blk, int nrep, int nvol) {
+                                                          const int* __restrict__ blk, int nrep, int nvol,
+                                                          int soff) {
   pdl_trigger();
   if ((int)blockIdx.x < nvol) {
     pdl_wait();
     const int r = blockIdx.x;
-    if (threadIdx.x < 32 && r < nrep) volume_move_warp(reps[r], st[r], st[r].cur[2]);
+    if (threadIdx.x < 32 && r < nrep)
+      volume_move_warp(reps[r], st[r], soff < 0 ? st[r].cur[2] : st[r].ctr[2] + (uint32_t)soff);
     return;
   }
   __shared__ CubeTables s_ct[kThreads / 32];
@@ -539,7 +564,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_cube_volume(const ReplicaDesc* 
   __syncwarp();
   pdl_wait();
   int cdh = 0;
-  cube_move(R, ct, blk, r, vb, st[r].cur[1], cdh);
+  cube_move(R, ct, blk, r, vb, soff < 0 ? st[r].cur[1] : st[r].ctr[1] + (uint32_t)soff, cdh);
   if (kCount) count_accumulate(st[r], vb, cdh, 0);
 }
 
@@ -941,7 +966,8 @@ __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepT
 template <int V, bool kCount>
 __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const ReplicaDesc* __restrict__ reps,
                                                     ReplicaState* __restrict__ st,
-                                                    const int* __restrict__ blk, int nrep, int colour, int jsweep) {
+                                                    const int* __restrict__ blk, int nrep, int colour, int jsweep,
+                                                    int from_ctr) {
   pdl_trigger();
   __shared__ SweepTables s_tab;
   const int r = find_replica(blk, nrep, blockIdx.x);
@@ -952,7 +978,7 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const 
   uint32_t hb2 = 0, ns = 0;
   int32_t dacc = 0;
   sweep_segment<V, false, kCount, !kCount>(R, &s_tab, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
-                                  st[r].cur[0] + (uint32_t)jsweep, hb2, ns, &dacc);
+                                  (from_ctr ? st[r].ctr[0] : st[r].cur[0]) + (uint32_t)jsweep, hb2, ns, &dacc);
   if (kCount) {
     const int ds = (int)(int16_t)(dacc & 0xffff);  // |dN_sigma| per thread <= 8 cells x 30
     count_accumulate(st[r], blockIdx.x, (dacc - ds) / 65536, ds);
@@ -1313,35 +1339,41 @@ void launch_measure_end(const BatchDev& b, int record, cudaStream_t s) {
   k_measure_end<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, record);
 }
 
-void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, bool count) {
+void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, bool count, int soff) {
   const int cube_blocks = do_cubes ? b.nblk_cubev : 0;
   const int vol_blocks = do_volume ? b.nrep : 0;
   if (cube_blocks + vol_blocks == 0) return;
   const dim3 grid((unsigned)(cube_blocks + vol_blocks));
-  if (count) launch_pdl(k_cube_volume<true>, grid, s, b.pdl, b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks);
-  else launch_pdl(k_cube_volume<false>, grid, s, b.pdl, b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks);
+  if (count) launch_pdl(k_cube_volume<true>, grid, s, b.pdl, b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks, soff);
+  else launch_pdl(k_cube_volume<false>, grid, s, b.pdl, b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks, soff);
+}
+
+void launch_chunk_end(const BatchDev& b, int steps, int nmet, int ncl, int do_volume, cudaStream_t s) {
+  launch_pdl(k_chunk_end, dim3((unsigned)((b.nrep + kThreads - 1) / kThreads)), s, b.pdl, b.st, b.nrep, steps, nmet,
+             ncl, do_volume);
 }
 
 // The counting sweep runs at most 4 cells per thread (its 8-cell tile spills registers under
 // the 3-blocks-per-SM bound and ran 2 us per step slower at L=256).
-void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, bool count) {
+void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, bool count, int from_ctr) {
   if (count) {
     const int n = b.nblk_sweep_count;
     const int* blk = b.blk_sweep_count;
     const dim3 g((unsigned)n);
     switch (b.vec_count) {
-      case 4: launch_pdl(k_sweep<4, true>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep); break;
-      case 2: launch_pdl(k_sweep<2, true>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep); break;
-      default: launch_pdl(k_sweep<1, true>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep); break;
+      case 4: launch_pdl(k_sweep<4, true>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
+      case 2: launch_pdl(k_sweep<2, true>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
+      default: launch_pdl(k_sweep<1, true>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
     }
     return;
   }
   const dim3 g((unsigned)b.nblk_sweep);
+  const int* blk = b.blk_sweep;
   switch (b.vec) {
-    case 8: launch_pdl(k_sweep<8, false>, g, s, b.pdl, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    case 4: launch_pdl(k_sweep<4, false>, g, s, b.pdl, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    case 2: launch_pdl(k_sweep<2, false>, g, s, b.pdl, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
-    default: launch_pdl(k_sweep<1, false>, g, s, b.pdl, b.reps, b.st, b.blk_sweep, b.nrep, colour, jsweep); break;
+    case 8: launch_pdl(k_sweep<8, false>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
+    case 4: launch_pdl(k_sweep<4, false>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
+    case 2: launch_pdl(k_sweep<2, false>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
+    default: launch_pdl(k_sweep<1, false>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
   }
 }
 

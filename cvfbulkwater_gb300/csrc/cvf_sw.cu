@@ -124,7 +124,7 @@ __device__ __noinline__ uint32_t sw_links_exact(uint32_t c, uint32_t t, uint32_t
 __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __restrict__ reps,
                                                        ReplicaState* __restrict__ st,
                                                        const int* __restrict__ blk, int nrep, int jsw,
-                                                       int worklist) {
+                                                       int worklist, int from_ctr) {
   pdl_trigger();
   const int r = find_replica_sw(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
   int x, y, z;
   cell_xyz(R, c, x, y, z);
   pdl_wait();
-  const uint32_t t = st[r].cur[3] + (uint32_t)jsw;
+  const uint32_t t = (from_ctr ? st[r].ctr[3] : st[r].cur[3]) + (uint32_t)jsw;
   const uint32_t w = word_at(R, x, y, z);
   const PhiloxKeys rk = philox_keys(R.key0, R.key1);
   uint32_t rw[12];
@@ -595,10 +595,10 @@ __global__ void k_cs_begin(ReplicaState* __restrict__ st, int nrep) {
 // Lattices of 2^20 cells or more (L >= 102) unite over the worklist; smaller ones with one thread
 // per cell, whose bonded threads spread over every SM (L=64 step 38 us with the worklist against
 // 34 us per cell; L=128 125-127 us against 129-133 us).
-void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s) {
+void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s, int from_ctr) {
   const dim3 g((unsigned)b.nblk_cell);
   const int wl = (long long)b.max_L * b.max_L * b.max_L >= (1ll << 20);
-  launch_pdl(k_sw_local, g, s, b.pdl, b.reps, b.st, b.blk_cell, b.nrep, jsw, wl);
+  launch_pdl(k_sw_local, g, s, b.pdl, b.reps, b.st, b.blk_cell, b.nrep, jsw, wl, from_ctr);
   if (wl) launch_pdl(k_sw_union, dim3((unsigned)b.nblk_cell4), s, b.pdl, b.reps, b.st, b.blk_cell4, b.nrep);
   else launch_pdl(k_sw_union_cells, g, s, b.pdl, b.reps, b.st, b.blk_cell, b.nrep);
   launch_pdl(k_sw_finish, g, s, b.pdl, b.reps, b.st, b.blk_cell, b.nrep, jsw);
