@@ -336,8 +336,9 @@ __global__ void __launch_bounds__(kThreads) k_sw_union_cells(const ReplicaDesc* 
 // Compression, cluster shift and update in one pass, one thread per cell. An in-cell component
 // none of whose arms carries a hydrogen-bond link (the cell's own x+, y+, z+ links, or the links
 // of its x-, y-, z- neighbours into it) is a whole cluster: its root is its smallest arm site,
-// which k_sw_local already stored as the label of every arm in it. Only the arms of the other
-// components walk to their roots (the minimum site id of the cluster) and store them. Each
+// which k_sw_local already stored as the label of every arm in it. Each of the other components
+// walks once, from its in-cell root to the cluster's root (the minimum site id of the cluster),
+// which becomes the label of each of its arms. Each
 // cluster's shift is digit a of the shift word that k_sw_local drew for cell c, for the root site
 // a*N + c (GW:2531-2542 gives every cluster one uniform shift in 0..5); sigma is shifted by it.
 __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __restrict__ reps,
@@ -383,31 +384,36 @@ __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __res
     *wp = out;
     return;
   }
+  // one walk per in-cell component that a link reaches: its root (stored as the label of each of
+  // its arms) and the root's shift digit, which replaces field m of the cell's shift word
+  uint32_t shw = own_flip;
+  uint32_t todo = ext_root;
+  while (todo) {
+    const uint32_t m = (uint32_t)__ffs(todo) - 1u;
+    todo &= todo - 1u;
+    int32_t root = (int32_t)(m * N + c);
+    for (int it = 0; it < (1 << 30); ++it) {
+      const int32_t px = __ldcg(R.label + root);
+      if (px == root) break;
+      root = px;
+    }
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+      if (((lab >> (3 * a)) & 7u) == m) R.label[a * N + c] = root;
+    uint32_t rc = (uint32_t)root, ra = 0;
+#pragma unroll
+    for (int k = 0; k < 5; ++k)
+      if (rc >= N) {
+        rc -= N;
+        ++ra;
+      }
+    const uint32_t fw = rc == c ? own_flip : R.flip[rc];
+    shw = (shw & ~(7u << (3 * m))) | (((fw >> (3 * ra)) & 7u) << (3 * m));
+  }
 #pragma unroll
   for (int a = 0; a < 6; ++a) {
     const uint32_t m = (lab >> (3 * a)) & 7u;
-    uint32_t sh;
-    if (!((ext_root >> m) & 1u)) {
-      sh = (own_flip >> (3 * m)) & 7u;  // the in-cell root is the cluster's root; its label is stored
-    } else {
-      int32_t root = (int32_t)(m * N + c);
-      for (int it = 0; it < (1 << 30); ++it) {
-        const int32_t px = __ldcg(R.label + root);
-        if (px == root) break;
-        root = px;
-      }
-      R.label[a * N + c] = root;
-      uint32_t rc = (uint32_t)root, ra = 0;
-#pragma unroll
-      for (int k = 0; k < 5; ++k)
-        if (rc >= N) {
-          rc -= N;
-          ++ra;
-        }
-      const uint32_t fw = rc == c ? own_flip : R.flip[rc];
-      sh = (fw >> (3 * ra)) & 7u;
-    }
-    uint32_t v = ((w >> (3 * a)) & 7u) + sh;
+    uint32_t v = ((w >> (3 * a)) & 7u) + ((shw >> (3 * m)) & 7u);
     if (v >= 6u) v -= 6u;
     out |= v << (3 * a);
   }
