@@ -15,11 +15,34 @@ namespace cvf {
 // memory is per translation unit without relocatable device code.
 static __constant__ uint8_t c_eta_table[72];
 
+// In-cell components of every intra-cell bond mask: entry m (bit e set when the e-th pair (a, b),
+// a < b in row-major order, is bonded) holds in 3-bit field a the smallest arm of arm a's
+// component.
+static __device__ uint32_t g_incell_lab[1 << 15];
+
+static uint32_t incell_components(uint32_t m) {
+  int root[6] = {0, 1, 2, 3, 4, 5};
+  int e = 0;
+  for (int a = 0; a < 5; ++a)
+    for (int b = a + 1; b < 6; ++b, ++e) {
+      if (!((m >> e) & 1u)) continue;
+      const int ra = root[a], rb = root[b], lo = ra < rb ? ra : rb, hi = ra < rb ? rb : ra;
+      for (int k = 0; k < 6; ++k)
+        if (root[k] == hi) root[k] = lo;
+    }
+  uint32_t lab = 0;
+  for (int k = 0; k < 6; ++k) lab |= (uint32_t)root[k] << (3 * k);
+  return lab;
+}
+
 void init_sw_device_tables() {
   uint8_t eta[72];
   for (int s = 0; s < 9; ++s)
     for (int p = 0; p < 8; ++p) eta[s * 8 + p] = (uint8_t)cube_eta_bits(s, p);
   cudaMemcpyToSymbol(c_eta_table, eta, sizeof(eta));
+  static uint32_t lab[1 << 15];
+  for (uint32_t m = 0; m < (1u << 15); ++m) lab[m] = incell_components(m);
+  cudaMemcpyToSymbol(g_incell_lab, lab, sizeof(lab));
 }
 
 __device__ __forceinline__ int find_replica_sw(const int* __restrict__ blk, int nrep, int b) {
@@ -194,7 +217,7 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
   }
   uint32_t bonds = eq & lt;
   if (tie & eq) bonds = sw_links_exact(c, t, eq, &R);
-  uint32_t bm = bonds >> 3;  // intra-cell bonds: bit l-3 for link l = 3..17
+  const uint32_t bm = bonds >> 3;  // intra-cell bonds: bit l-3 for link l = 3..17
   // shift digits of the clusters rooted at this cell's arm sites
   uint32_t u = rw[9];
   if (u * 46656u < 2560u) u = rw[10];
@@ -207,20 +230,8 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
     u = (uint32_t)m;
   }
   R.flip[c] = fw;
-  // in-cell components: lab holds 3 bits per arm, the smallest arm of its component; merging
-  // two components rewrites every field equal to the larger minimum with the smaller one
-  const unsigned long long kPairA = 0x11b491248000ull, kPairB = 0x16cb1d8d58d1ull;  // e -> (a, b), 3 bits each
-  uint32_t lab = 0x2c688u;  // fields 0,1,2,3,4,5
-  while (bm) {
-    const int e = __ffs(bm) - 1;
-    bm &= bm - 1u;
-    const uint32_t a = (uint32_t)(kPairA >> (3 * e)) & 7u, b = (uint32_t)(kPairB >> (3 * e)) & 7u;
-    const uint32_t la = (lab >> (3 * a)) & 7u, lb = (lab >> (3 * b)) & 7u;
-    const uint32_t lo = la < lb ? la : lb, hi = la < lb ? lb : la;
-    const uint32_t xx = lab ^ (hi * 0x9249u);
-    const uint32_t m7 = (~(xx | (xx >> 1) | (xx >> 2)) & 0x9249u) * 7u;
-    lab = (lab & ~m7) | ((lo * 0x9249u) & m7);
-  }
+  // in-cell components: lab holds 3 bits per arm, the smallest arm of its component
+  const uint32_t lab = __ldg(g_incell_lab + bm);
   R.cellsw[c] = (bonds & 7u) | (lab << 3);
   if (worklist) {
     // cells with a hydrogen-bond link go to the replica's worklist (one atomic per warp)
