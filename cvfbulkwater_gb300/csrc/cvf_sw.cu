@@ -204,19 +204,32 @@ __global__ void __launch_bounds__(kThreads) k_sw_local(const ReplicaDesc* __rest
         eq |= bit << l;
       }
   }
-  // fast decisions from the high halves; a tie of a high half with T >> 16 on a link whose
-  // condition holds sends the cell through the exact path
+  // fast decisions from the 16-bit high halves: link l (half l & 1 of word l >> 1) bonds when its
+  // condition holds and its half is below th = T >> 16 (T in [0, 2^32], so th in [0, 65536]);
+  // the odd half compares the whole word with th * 65536 - 1, and a link class with th = 0 (never
+  // bonds) leaves eq. Any half equal to th (65536 counted as 0xffff) sends the cell through the
+  // exact path, which decides the links whose condition holds from their 32-bit uniforms: a
+  // zero-halfword test of the word xor the two thresholds per word.
   const uint32_t thb = (uint32_t)(R.thr_sw[0] >> 16), ts = (uint32_t)(R.thr_sw[1] >> 16);
-  uint32_t lt = 0, tie = 0;
+  const uint32_t ub = thb >= 65536u ? 0xffffffffu : (thb << 16) - 1u;
+  const uint32_t us = ts >= 65536u ? 0xffffffffu : (ts << 16) - 1u;
+  const uint32_t cb = thb < 0xffffu ? thb : 0xffffu, cs = ts < 0xffffu ? ts : 0xffffu;
+  if (thb == 0u) eq &= ~7u;
+  if (ts == 0u) eq &= 7u;
+  uint32_t lt = 0, tz = 0;
 #pragma unroll
-  for (int l = 0; l < 18; ++l) {
-    const uint32_t hi = (l & 1) ? (rw[l >> 1] >> 16) : (rw[l >> 1] & 0xffffu);
-    const uint32_t th = l < 3 ? thb : ts;
-    lt |= (uint32_t)(hi < th) << l;
-    tie |= (uint32_t)(hi == th) << l;
+  for (int k = 0; k < 9; ++k) {
+    const uint32_t w = rw[k];
+    const uint32_t th0 = 2 * k < 3 ? thb : ts, u1 = 2 * k + 1 < 3 ? ub : us;
+    asm("{\n\t.reg .pred p;\n\tsetp.lt.u32 p, %1, %2;\n\t@p or.b32 %0, %0, %4;"
+        "\n\tsetp.le.u32 p, %3, %5;\n\t@p or.b32 %0, %0, %6;\n\t}"
+        : "+r"(lt)
+        : "r"(w & 0xffffu), "r"(th0), "r"(w), "r"(1u << (2 * k)), "r"(u1), "r"(1u << (2 * k + 1)));
+    const uint32_t x = w ^ (((2 * k + 1 < 3 ? cb : cs) << 16) | (2 * k < 3 ? cb : cs));
+    tz |= (x - 0x00010001u) & ~x;
   }
   uint32_t bonds = eq & lt;
-  if (tie & eq) bonds = sw_links_exact(c, t, eq, &R);
+  if (tz & 0x80008000u) bonds = sw_links_exact(c, t, eq, &R);
   const uint32_t bm = bonds >> 3;  // intra-cell bonds: bit l-3 for link l = 3..17
   // shift digits of the clusters rooted at this cell's arm sites
   uint32_t u = rw[9];
