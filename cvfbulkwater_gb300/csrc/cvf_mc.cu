@@ -528,14 +528,28 @@ __device__ __forceinline__ void cube_move(const ReplicaDesc& R, const CubeTables
   else cube_move_v<1>(R, ct, blk, r, vb, t, cdh);
 }
 
-// Warp sums of the threads' count changes (dn in N_hb units, ds in N_sigma units) added to one
-// of the replica's 32 running-count slots (no block barrier). Every lane of the warp calls it.
-__device__ __forceinline__ void count_accumulate(ReplicaState& S, int vb, int dn, int ds) {
+// Block sums of the threads' count changes (dn in N_hb units, ds in N_sigma units) added to one
+// of the replica's 32 running-count slots: one pair of atomics per block (per warp they queued
+// on the few cache lines of the slots). Every thread of the block calls it.
+__device__ __forceinline__ void count_accumulate_block(ReplicaState& S, int vb, int dn, int ds) {
+  __shared__ int s_cnt[2][kThreads / 32];
   const int wn = __reduce_add_sync(0xffffffffu, dn), wsum = __reduce_add_sync(0xffffffffu, ds);
-  if ((threadIdx.x & 31) == 0 && (wn | wsum)) {
-    const int slot = (vb * (kThreads / 32) + (int)(threadIdx.x >> 5)) & 31;
-    atomicAdd(&S.dlt_slot[0][slot], (unsigned long long)(long long)wn);
-    atomicAdd(&S.dlt_slot[1][slot], (unsigned long long)(long long)wsum);
+  const int warp = (int)(threadIdx.x >> 5);
+  if ((threadIdx.x & 31) == 0) {
+    s_cnt[0][warp] = wn;
+    s_cnt[1][warp] = wsum;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int nw = (int)(blockDim.x >> 5);
+    const int a = threadIdx.x < (unsigned)nw ? s_cnt[0][threadIdx.x] : 0;
+    const int b = threadIdx.x < (unsigned)nw ? s_cnt[1][threadIdx.x] : 0;
+    const int bn = __reduce_add_sync(0xffffffffu, a), bs = __reduce_add_sync(0xffffffffu, b);
+    if (threadIdx.x == 0 && (bn | bs)) {
+      const int slot = vb & 31;
+      atomicAdd(&S.dlt_slot[0][slot], (unsigned long long)(long long)bn);
+      atomicAdd(&S.dlt_slot[1][slot], (unsigned long long)(long long)bs);
+    }
   }
 }
 
@@ -565,7 +579,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_cube_volume(const ReplicaDesc* 
   pdl_wait();
   int cdh = 0;
   cube_move(R, ct, blk, r, vb, soff < 0 ? st[r].cur[1] : st[r].ctr[1] + (uint32_t)soff, cdh);
-  if (kCount) count_accumulate(st[r], vb, cdh, 0);
+  if (kCount) count_accumulate_block(st[r], vb, cdh, 0);
 }
 
 // ------------------------------------------------------------------ checkerboard sweep
@@ -749,23 +763,12 @@ struct EtaTables {
 //   nbw[v]  44 at byte v (v = 0..5), zero for v = 6, 7 (7 marks an arm with eta = 0)
 //   tv[i]   2*(T_i >> 16) + ((T_i & 0xffff) != 0) - 1 for the threshold T_i of entry
 //           i = 11*dN_hb + (h_new - h_old) + 17
-//   pk[i]   65536 dN_hb + dN_sigma of entry i (dN_sigma = h_new - h_old + 1): the change of the
-//           counts an accepted arm makes, for the running counts of cvf_observables
 struct SweepTables {
   uint2 cnt[8];
   uint2 nbw[8];
   uint32_t tv[33];
-  int32_t pk[33];
   EtaTables et;
 };
-
-// 65536 dN_hb + dN_sigma for table entry i = 11 dN_hb + (h_new - h_old) + 17 (h_new - h_old in
-// [-6, 4], so the split is unique).
-__device__ __forceinline__ int32_t entry_delta(int i) {
-  const int v = i - 17;
-  const int dn = v + 6 >= 11 ? 1 : (v + 6 < 0 ? -1 : 0);
-  return dn * 65536 + (v - 11 * dn + 1);
-}
 
 __device__ __forceinline__ uint2 count_bytes(uint32_t v, uint32_t b) {
   return v < 4 ? make_uint2(b << (8 * v), 0u) : (v < 6 ? make_uint2(0u, b << (8 * (v - 4))) : make_uint2(0u, 0u));
@@ -787,11 +790,7 @@ __device__ __forceinline__ const EtaTables* warp_eta_tables(const ReplicaDesc& R
 __device__ __forceinline__ void fill_sweep_tables(const ReplicaDesc& R, SweepTables* wt, uint32_t lane) {
   fill_eta_tables(R, &wt->et, lane);
   wt->tv[lane] = R.tv[lane];
-  wt->pk[lane] = entry_delta((int)lane);
-  if (lane == 0) {
-    wt->tv[32] = R.tv[32];
-    wt->pk[32] = entry_delta(32);
-  }
+  if (lane == 0) wt->tv[32] = R.tv[32];
   if (lane < 8) {
     wt->cnt[lane] = count_bytes(lane, 4u);
     wt->nbw[lane] = count_bytes(lane, 44u);
@@ -813,10 +812,7 @@ __device__ __forceinline__ void fill_block_sweep_tables(const ReplicaDesc& R, Sw
   const int i = threadIdx.x;
   if (i < 64) t->et.nbmask[i] = R.nbmask[i];
   if (i < 18) reinterpret_cast<uint32_t*>(t->et.eta)[i] = reinterpret_cast<const uint32_t*>(R.eta_tab)[i];
-  if (i < 33) {
-    t->tv[i] = R.tv[i];
-    t->pk[i] = entry_delta(i);
-  }
+  if (i < 33) t->tv[i] = R.tv[i];
   if (i < 8) {
     t->cnt[i] = count_bytes((uint32_t)i, 4u);
     t->nbw[i] = count_bytes((uint32_t)i, 44u);
@@ -836,7 +832,7 @@ __device__ __forceinline__ void fill_block_sweep_tables(const ReplicaDesc& R, Sw
 // that wraps to zero without a tie only sends the cell through the exact path as well, which
 // decides every arm from the full 32-bit uniforms. A proposal equal to the old
 // value lands on entry 17 (dN = 0), which always accepts and changes nothing.
-// kCount: dacc also receives the packed count changes (pk) of the accepted arms that change a value.
+// kCount: dacc also receives the cell's count changes, packed as 65536 dN_hb + dN_sigma.
 template <bool kCount, bool kFold>
 __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbe, const U4& rr,
                                                 uint32_t c0, uint32_t t, const ReplicaDesc& R, const SweepTables* wt,
@@ -844,7 +840,7 @@ __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbe, const 
   // a proposal word in the rejected range of the exact draw (p = 6e-7): with kFold it sends the
   // cell through the exact path, which draws the retry word, and the fast path's decisions are
   // discarded (one rare-path test per cell instead of two); otherwise the retry word is drawn
-  // first (the counting, measuring and persistent kernels keep within their registers so)
+  // first (the measuring and persistent kernels keep within their registers so)
   uint32_t u = rr.x;
   bool reject = u * 46656u < 2560u;
   if (!kFold && reject) {
@@ -859,10 +855,9 @@ __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbe, const 
     hx += c.x;
     hy += c.y;
   }
+  const int s0 = kCount ? (int)__dp4a(hx, hx, __dp4a(hy, hy, 0u)) : 0;
   const char* tvb = reinterpret_cast<const char*>(wt->tv) + 68;
-  const char* pkb = reinterpret_cast<const char*>(wt->pk) + 68;
   uint32_t f = u, tprod = 1u;
-  int32_t cacc = 0;
 #pragma unroll
   for (int a = 0; a < 6; ++a) {
     const unsigned long long m = (unsigned long long)f * 6ull + (0x7770ull << 32);
@@ -879,27 +874,25 @@ __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbe, const 
     tprod *= (uint32_t)d;
     const uint2 cn = wt->cnt[sn - 0x7770u], co = wt->cnt[o];
     const uint32_t dw = (sn - 0x7770u - o) << (3 * a);
-    if (kCount) {
-      const int32_t pk = dw ? *reinterpret_cast<const int32_t*>(pkb + off) : 0;
-      asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %4, 1;\n\t@p add.u32 %0, %0, %5;\n\t@p add.u32 %1, %1, %6;"
-          "\n\t@p sub.u32 %1, %1, %7;\n\t@p add.u32 %2, %2, %8;\n\t@p sub.u32 %2, %2, %9;"
-          "\n\t@p add.u32 %3, %3, %10;\n\t}"
-          : "+r"(w), "+r"(hx), "+r"(hy), "+r"(cacc)
-          : "r"(d), "r"(dw), "r"(cn.x), "r"(co.x), "r"(cn.y), "r"(co.y), "r"(pk));
-    } else {
-      asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %3, 1;\n\t@p add.u32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;"
-          "\n\t@p sub.u32 %1, %1, %6;\n\t@p add.u32 %2, %2, %7;\n\t@p sub.u32 %2, %2, %8;\n\t}"
-          : "+r"(w), "+r"(hx), "+r"(hy)
-          : "r"(d), "r"(dw), "r"(cn.x), "r"(co.x), "r"(cn.y), "r"(co.y));
-    }
+    asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %3, 1;\n\t@p add.u32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;"
+        "\n\t@p sub.u32 %1, %1, %6;\n\t@p add.u32 %2, %2, %7;\n\t@p sub.u32 %2, %2, %8;\n\t}"
+        : "+r"(w), "+r"(hx), "+r"(hy)
+        : "r"(d), "r"(dw), "r"(cn.x), "r"(co.x), "r"(cn.y), "r"(co.y));
   }
   if (tprod == 0u || reject) {
     const uint32_t ue = reject ? sweep_proposal_retry(c0, t, R.replica, R.key0, R.key1) : u;
     const unsigned long long x = sweep_cell_exact(w0, nbe, ue, rr.y, rr.z, rr.w, c0, t, &R);
     w = (uint32_t)x;
-    cacc = (int32_t)(uint32_t)(x >> 32);
+    if (kCount) dacc += (int32_t)(uint32_t)(x >> 32);
+  } else if (kCount) {
+    // the cell's count changes: N_hb from its arms equal to the facing neighbour value before
+    // and after (a field of 7 in nbe never matches), N_sigma from the sum of the squared
+    // histogram bytes b = 4h: the equal pairs of a cell are (sum h^2 - 6) / 2 = (sum b^2 / 16 - 6) / 2
+    const uint32_t x0 = w0 ^ nbe, x1 = w ^ nbe;
+    const int dhb = __popc(~(x1 | (x1 >> 1) | (x1 >> 2)) & 0x9249u) - __popc(~(x0 | (x0 >> 1) | (x0 >> 2)) & 0x9249u);
+    const int s1 = (int)__dp4a(hx, hx, __dp4a(hy, hy, 0u));
+    dacc += dhb * 65536 + (s1 - s0) / 32;
   }
-  if (kCount) dacc += cacc;
   return w;
 }
 
@@ -977,11 +970,11 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const 
   pdl_wait();
   uint32_t hb2 = 0, ns = 0;
   int32_t dacc = 0;
-  sweep_segment<V, false, kCount, !kCount>(R, &s_tab, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
+  sweep_segment<V, false, kCount, true>(R, &s_tab, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
                                   (from_ctr ? st[r].ctr[0] : st[r].cur[0]) + (uint32_t)jsweep, hb2, ns, &dacc);
   if (kCount) {
     const int ds = (int)(int16_t)(dacc & 0xffff);  // |dN_sigma| per thread <= 8 cells x 30
-    count_accumulate(st[r], blockIdx.x, (dacc - ds) / 65536, ds);
+    count_accumulate_block(st[r], blockIdx.x, (dacc - ds) / 65536, ds);
   }
 }
 
@@ -1354,7 +1347,7 @@ void launch_chunk_end(const BatchDev& b, int steps, int nmet, int ncl, int do_vo
 }
 
 // The counting sweep runs at most 4 cells per thread (its 8-cell tile spills registers under
-// the 3-blocks-per-SM bound and ran 2 us per step slower at L=256).
+// the 3-blocks-per-SM bound and ran 3-6 us per step slower at L=256).
 void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, bool count, int from_ctr) {
   if (count) {
     const int n = b.nblk_sweep_count;
