@@ -377,12 +377,16 @@ static void enqueue_cstats(cvf_handle* h, int record) {
   launch_cluster_stats_impl(h->b, h->blocktop, record, h->stream);
 }
 
-// Graph of `steps` MC steps; when record is set, the first step is followed by a recorded
-// measurement (and cluster statistics when ncl > 0).
-// count: plain steps with the counting kernels (ungrouped per-phase capture; record must be 0).
+// Graph of `steps` MC steps; when record is set, step i is followed by a recorded measurement (and
+// cluster statistics when ncl > 0) for every i with i % rec_every == 0 (rec_every = 0: the first
+// step only), so one graph can hold several intervals of a sampled run.
+// count: plain steps with the counting kernels (ungrouped per-phase capture; with record, the
+// records are read from the running counts).
 static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cudaGraphExec_t* out,
-                     bool count = false) {
-  auto key = std::make_tuple(steps, nmet, ncl, record | (count ? 2 : 0));
+                     bool count = false, int rec_every = 0) {
+  if (!record) rec_every = 0;
+  const auto rec_at = [&](int i) { return record && (rec_every > 0 ? i % rec_every == 0 : i == 0); };
+  auto key = std::make_tuple(steps, nmet, ncl, record | (count ? 2 : 0) | (rec_every << 2));
   auto it = h->graphs.find(key);
   if (it != h->graphs.end()) {
     *out = it->second;
@@ -393,7 +397,7 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     // one persistent launch; a driver that cannot capture a cooperative launch leaves the
     // handle on the per-phase kernels
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t el = launch_run(h->b, steps, nmet, record ? steps : 0, h->stream);
+    cudaError_t el = launch_run(h->b, steps, nmet, record ? (rec_every > 0 ? rec_every : steps) : 0, h->stream);
     cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
     cudaGraphExec_t ex = nullptr;
     if (el == cudaSuccess && ec == cudaSuccess) {
@@ -417,7 +421,7 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     for (auto& gr : h->groups) CK(cudaStreamWaitEvent(gr.s, h->fork, 0));
     for (auto& gr : h->groups) {
       if (record) {
-        for (int i = 0; i < steps; ++i) enqueue_metropolis_on(gr.b, gr.s, nmet, i == 0, h->corr_on);
+        for (int i = 0; i < steps; ++i) enqueue_metropolis_on(gr.b, gr.s, nmet, rec_at(i), h->corr_on);
       } else {
         for (int i = 0; i < steps; ++i) {
           enqueue_step_at(gr.b, gr.s, nmet, 0, false, true, i);
@@ -448,7 +452,7 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     launch_cube_volume(h->b, 0, 1, h->stream);
     for (int j = 0; j < nmet; ++j) launch_nhb_sweep(h->b, j, h->stream);
     for (int j = 0; j < ncl; ++j) launch_sw_step(h->b, j, h->stream);
-    if (i == 0 && record) {
+    if (rec_at(i)) {
       launch_nhb_measure(h->b, 1, h->stream);
       if (ncl > 0) enqueue_cstats(h, 1);
     }
@@ -493,12 +497,12 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     } else if (count) {
       // the record of a counting step is the running counts
       enqueue_step(h, nmet, ncl, true);
-      if (i == 0 && record) launch_count_read(h->b, h->stream, 1);
-    } else if (i == 0 && record && ncl == 0 && nmet > 0) {
+      if (rec_at(i)) launch_count_read(h->b, h->stream, 1);
+    } else if (rec_at(i) && ncl == 0 && nmet > 0) {
       enqueue_recorded_metropolis_step(h, nmet);
     } else {
       enqueue_step(h, nmet, ncl, count);
-      if (i == 0 && record) {
+      if (rec_at(i)) {
         launch_measure(h->b, 1, h->stream);
         if (ncl > 0) enqueue_cstats(h, 1);
       }
@@ -926,14 +930,21 @@ static int run_impl(cvf_handle* h, int n_steps, int nmet, int ncl, int interval)
       launch_count_rebase(h->b, h->stream);
     }
     h->count_valid = count;
-    int full = n_steps / interval, rem = n_steps % interval;
+    // graphs of m intervals (about 32 steps) while enough steps remain, then single intervals,
+    // then the remainder: each graph launch costs a few microseconds on the device
+    const int m = interval >= chunk_plain ? 1 : chunk_plain / interval;
+    int left = n_steps;
     cudaGraphExec_t g;
-    if (full) {
-      if (int rc = get_graph(h, interval, nmet, ncl, 1, &g, count)) return rc;
-      for (int i = 0; i < full; ++i) CK(cudaGraphLaunch(g, h->stream));
+    if (m > 1 && left >= m * interval) {
+      if (int rc = get_graph(h, m * interval, nmet, ncl, 1, &g, count, interval)) return rc;
+      for (; left >= m * interval; left -= m * interval) CK(cudaGraphLaunch(g, h->stream));
     }
-    if (rem) {
-      if (int rc = get_graph(h, rem, nmet, ncl, 1, &g, count)) return rc;
+    if (left >= interval) {
+      if (int rc = get_graph(h, interval, nmet, ncl, 1, &g, count)) return rc;
+      for (; left >= interval; left -= interval) CK(cudaGraphLaunch(g, h->stream));
+    }
+    if (left) {
+      if (int rc = get_graph(h, left, nmet, ncl, 1, &g, count)) return rc;
       CK(cudaGraphLaunch(g, h->stream));
     }
   }
