@@ -150,6 +150,9 @@ def lib():
         "cvf_h2d_set_constants": (I, [P, P]),
         "cvf_h2d_destroy": (I, [P]),
         "cvf_set_correlation": (I, [P, I]),
+        "cvf_set_cluster_algorithm": (I, [P, I]),
+        "cvf_wolff_stats": (I, [P, I, P]),
+        "cvf_set_wolff_counter": (I, [P, I, C.c_ulonglong]),
         "cvf_get_correlation": (I, [P, I, P, P, I, C.POINTER(I)]),
         "cvf_run_statistics": (I, [P, C.POINTER(RunStats), I]),
         "cvf_isobar_point_from_stats": (I, [C.POINTER(RunStats), C.POINTER(IsobarPoint)]),

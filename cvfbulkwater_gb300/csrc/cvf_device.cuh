@@ -98,6 +98,10 @@ struct ReplicaState {
   // changes the counting kernels added since (two's complement in slot block % 32)
   long long base_hb2, base_ns;
   unsigned long long dlt_slot[2][32];
+  // Wolff cluster steps: the poke counter (the random streams of poke P) and the last step's
+  // pokes, summed cluster sizes and largest cluster
+  unsigned long long wpoke;
+  long long w_pokes, w_sum, w_max;
 };
 
 // Multi-tau correlator of one replica (GW:165-181, GW:2983-3128): kCorrLevels levels of kCorrP
@@ -127,6 +131,26 @@ struct GridSync {
   unsigned int ticket; // block tickets handed out in the current launch
 };
 
+// Scratch of the Wolff step kernel (one replica at a time; sized for the largest replica) and
+// its loop state. A batch is one poke per warp of the cooperative grid.
+struct WolffLoop {
+  unsigned long long p0;  // first poke of the current batch
+  long long done, pokes, maxs;  // sites flipped, pokes and largest cluster of the step so far
+  int commit;             // pokes of the batch committed (the prefix before the first conflict)
+  int big;                // the batch's first poke outgrew its warp: the whole grid grows it
+  unsigned int tail, level0, level1;  // global queue of the grid-wide growth
+};
+struct WolffDev {
+  int* chg;            // [N] per cell: smallest poke of the batch whose cluster changes it (INT_MAX)
+  uint32_t* q;         // [6N] sites of a cluster grown by the whole grid
+  uint32_t* mark;      // [6N/32] bitmask of those sites
+  int* size;           // [B] cluster size per poke of the batch
+  int* flag;           // [B] 1: examines a cell an earlier poke changes, 2: outgrew its warp
+  WolffLoop* loop;
+  int B;               // pokes per batch (warps of the grid)
+  int grid;            // blocks of the cooperative launch
+};
+
 // ------------------------------------------------------------- launch entry points
 struct BatchDev {
   ReplicaDesc* reps;    // device array [nrep]
@@ -149,6 +173,8 @@ struct BatchDev {
   GridSync* gsync;      // device barrier state of the persistent step kernel
   unsigned int barrier_polls;  // polls of one grid-barrier wait before it gives up (error code 3)
   CorrState* corr;      // device array [nrep] of correlators (null until enabled)
+  int wolff;            // cluster steps are Wolff steps (GW:2199-2357) instead of Swendsen-Wang
+  WolffDev wdev;        // its scratch (allocated when enabled)
 };
 
 constexpr int kThreads = 256;
@@ -194,6 +220,11 @@ void launch_measure_end(const BatchDev& b, int record, cudaStream_t s);
 // interval > 0. Same lattice, counters and samples as the per-phase kernels.
 cudaError_t launch_run(const BatchDev& b, int nsteps, int nmet, int interval, cudaStream_t s);
 void launch_sw_step(const BatchDev& b, int jsw, cudaStream_t s, int from_ctr = 0);
+// One Wolff cluster step of every replica (one cooperative launch per replica): pokes until the
+// flipped clusters add up to 6N sites.
+cudaError_t launch_wolff_step(const BatchDev& b, cudaStream_t s);
+// Blocks per SM of the Wolff kernel (the cooperative grid is this times the SM count).
+int wolff_blocks_per_sm();
 // Flag_chessboard = 0: bond counts from the lattice and eta6 (GW:841-862; one replica, or all for
 // only_replica < 0), one Metropolis sweep
 // (12 launches: colour 0 arms 0..5, colour 1 arms 0..5) and the measurement with the greedy
@@ -250,6 +281,43 @@ static inline void launch_pdl(void (*kernel)(P...), dim3 grid, cudaStream_t s, i
   cfg.attrs = at;
   cfg.numAttrs = pdl ? 1 : 0;
   cudaLaunchKernelEx(&cfg, kernel, ((P)args)...);
+}
+
+// Grid-wide barrier of a cooperative (co-resident) launch: the last block to arrive bumps the
+// generation word the others poll. A wait gives up after max_polls looks (with a short sleep
+// between them, so the default bound is about a second), sets gs->err and the replica's error
+// code 3, and every block then leaves; returns false once any block has given up.
+static __device__ __noinline__ bool grid_barrier(GridSync* gs, ReplicaState* st0, unsigned int max_polls) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* gen = &gs->gen;
+    volatile int* err = &gs->err;
+    const unsigned int g = *gen;
+    __threadfence();
+    int ok = 1;
+    if (atomicAdd(&gs->count, 1u) == gridDim.x - 1) {
+      atomicExch(&gs->count, 0u);
+      __threadfence();
+      atomicAdd(&gs->gen, 1u);
+    } else {
+      // the bound is checked before each look at the generation word, so a bound of 0 makes
+      // every block that has to wait give up
+      for (unsigned int polls = 0;; ++polls) {
+        if (*err != 0 || polls >= max_polls) {
+          ok = 0;
+          break;
+        }
+        if (*gen != g) break;
+        __nanosleep(64);
+      }
+      if (!ok && atomicExch(&gs->err, 1) == 0) atomicExch(&st0->err, 3);
+    }
+    __threadfence();
+    s_ok = ok && *err == 0;
+  }
+  __syncthreads();
+  return s_ok != 0;
 }
 #endif
 

@@ -286,6 +286,34 @@ static int build_groups(cvf_handle* h) {
   return 0;
 }
 
+// Scratch of the Wolff step (sized for the largest replica; one replica's step runs at a time).
+static int ensure_wolff(cvf_handle* h) {
+  if (h->b.wdev.loop) return 0;
+  long long nmax = 0;
+  for (auto& r : h->reps) nmax = std::max(nmax, r.N);
+  int nsm = 0;
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device));
+  // at most 2 blocks per SM, one slot fewer than fit, so that a kernel on a side branch (the
+  // volume chain) never keeps the cooperative grid from being resident
+  const int fit = wolff_blocks_per_sm();
+  if (fit < 1) return fail(CVF_ECUDA, "the Wolff kernel does not fit on an SM");
+  const int per = std::max(1, std::min(fit - 1, 2));
+  WolffDev& w = h->b.wdev;
+  w.grid = nsm * per;
+  w.B = w.grid * 8;  // one poke per warp of 256-thread blocks
+  if (int rc = dev_alloc(h, (void**)&w.chg, (size_t)nmax * sizeof(int))) return rc;
+  if (int rc = dev_alloc(h, (void**)&w.q, (size_t)(6 * nmax) * sizeof(uint32_t))) return rc;
+  if (int rc = dev_alloc(h, (void**)&w.mark, (size_t)((6 * nmax + 31) / 32) * sizeof(uint32_t))) return rc;
+  if (int rc = dev_alloc(h, (void**)&w.size, (size_t)w.B * sizeof(int))) return rc;
+  if (int rc = dev_alloc(h, (void**)&w.flag, (size_t)w.B * sizeof(int))) return rc;
+  if (int rc = dev_alloc(h, (void**)&w.loop, sizeof(WolffLoop))) return rc;
+  CK(cudaMemset(w.chg, 0x7f, (size_t)nmax * sizeof(int)));  // no poke changes any cell
+  CK(cudaMemset(w.mark, 0, (size_t)((6 * nmax + 31) / 32) * sizeof(uint32_t)));
+  CK(cudaMemset(w.loop, 0, sizeof(WolffLoop)));
+  drop_graphs(h);
+  return 0;
+}
+
 static int ensure_sw(cvf_handle* h) {
   if (h->sw_alloc) return 0;
   for (auto& r : h->reps) {
@@ -307,6 +335,13 @@ static int ensure_sw(cvf_handle* h) {
   return upload_descs(h);
 }
 
+// Cluster step j (of the step's ncl): a Wolff step when the handle's cluster steps are Wolff
+// steps, else a Swendsen-Wang step.
+static void launch_cluster_step(const BatchDev& b, int jsw, cudaStream_t s, int from_ctr = 0) {
+  if (b.wolff) launch_wolff_step(b, s);
+  else launch_sw_step(b, jsw, s, from_ctr);
+}
+
 // volume: the step's volume move in the cube kernel (false when a side branch runs the chunk's
 // volume moves).
 static void enqueue_step(cvf_handle* h, int nmet, int ncl, bool count = false, bool volume = true) {
@@ -316,7 +351,7 @@ static void enqueue_step(cvf_handle* h, int nmet, int ncl, bool count = false, b
     launch_sweep(h->b, 0, j, h->stream, count);
     launch_sweep(h->b, 1, j, h->stream, count);
   }
-  for (int j = 0; j < ncl; ++j) launch_sw_step(h->b, j, h->stream);
+  for (int j = 0; j < ncl; ++j) launch_cluster_step(h->b, j, h->stream);
 }
 
 // Step i of a chunk without records: the kernels take their counters as offsets from ctr (cube
@@ -328,7 +363,7 @@ static void enqueue_step_at(const BatchDev& b, cudaStream_t s, int nmet, int ncl
     launch_sweep(b, 0, i * nmet + j, s, count, 1);
     launch_sweep(b, 1, i * nmet + j, s, count, 1);
   }
-  for (int j = 0; j < ncl; ++j) launch_sw_step(b, i * ncl + j, s, 1);
+  for (int j = 0; j < ncl; ++j) launch_cluster_step(b, i * ncl + j, s, 1);
 }
 
 // A Metropolis-only step followed by a recorded measurement: the measurement rides on the last
@@ -451,10 +486,10 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     launch_step_begin(h->b, nmet, ncl, 0, 1, h->stream);
     launch_cube_volume(h->b, 0, 1, h->stream);
     for (int j = 0; j < nmet; ++j) launch_nhb_sweep(h->b, j, h->stream);
-    for (int j = 0; j < ncl; ++j) launch_sw_step(h->b, j, h->stream);
+    for (int j = 0; j < ncl; ++j) launch_cluster_step(h->b, j, h->stream);
     if (rec_at(i)) {
       launch_nhb_measure(h->b, 1, h->stream);
-      if (ncl > 0) enqueue_cstats(h, 1);
+      if (ncl > 0 && !h->b.wolff) enqueue_cstats(h, 1);
     }
     if (h->corr_on) launch_corr_step(h->b, h->stream);
   }
@@ -504,7 +539,7 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
       enqueue_step(h, nmet, ncl, count);
       if (rec_at(i)) {
         launch_measure(h->b, 1, h->stream);
-        if (ncl > 0) enqueue_cstats(h, 1);
+        if (ncl > 0 && !h->b.wolff) enqueue_cstats(h, 1);
       }
     }
     if (h->corr_on) launch_corr_step(h->b, h->stream);  // after the step's measurement, as GW:1245
@@ -903,7 +938,7 @@ static int run_impl(cvf_handle* h, int n_steps, int nmet, int ncl, int interval)
   h->obs_since_run = false;
   CK(cudaSetDevice(h->device));
   if (ncl > 0) {
-    if (int rc = ensure_sw(h)) return rc;
+    if (int rc = h->b.wolff ? ensure_wolff(h) : ensure_sw(h)) return rc;
   }
   if (n_steps == 0) return 0;
   const int chunk_plain = 32;
@@ -948,7 +983,7 @@ static int run_impl(cvf_handle* h, int n_steps, int nmet, int ncl, int interval)
       CK(cudaGraphLaunch(g, h->stream));
     }
   }
-  if (ncl > 0) h->sw_done = true;
+  if (ncl > 0 && !h->b.wolff) h->sw_done = true;
   CK(cudaGetLastError());
   return 0;
 }
@@ -1040,6 +1075,41 @@ static void from_rec(const CStatsRec& x, cvf_cstats* c) {
   c->sum_size2 = x.sum_size2;
   c->sum_size2_wrap32 = x.sum_size2_wrap32;
   fill_cstats(c);
+}
+
+int cvf_set_cluster_algorithm(cvf_handle* h, int algorithm) {
+  if (!h) return fail(CVF_EINVAL, "null handle");
+  if (algorithm != CVF_CLUSTER_SW && algorithm != CVF_CLUSTER_WOLFF) return fail(CVF_EINVAL, "unknown cluster algorithm");
+  CK(cudaSetDevice(h->device));
+  const int w = algorithm == CVF_CLUSTER_WOLFF ? 1 : 0;
+  if (w == h->b.wolff) return 0;
+  if (w)
+    if (int rc = ensure_wolff(h)) return rc;
+  h->b.wolff = w;
+  drop_graphs(h);
+  return 0;
+}
+
+int cvf_wolff_stats(cvf_handle* h, int r, long long* out4) {
+  if (int rc = check_rep(h, r)) return rc;
+  if (!out4) return fail(CVF_EINVAL, "null out");
+  CK(cudaSetDevice(h->device));
+  if (int rc = check_err(h)) return rc;
+  ReplicaState s;
+  if (int rc = read_state(h, r, &s)) return rc;
+  out4[0] = s.w_pokes;
+  out4[1] = s.w_sum;
+  out4[2] = s.w_max;
+  out4[3] = (long long)s.wpoke;
+  return 0;
+}
+
+int cvf_set_wolff_counter(cvf_handle* h, int r, unsigned long long pokes) {
+  if (int rc = check_rep(h, r)) return rc;
+  CK(cudaSetDevice(h->device));
+  if (int rc = check_err(h)) return rc;
+  CK(cudaMemcpy((char*)(h->b.st + r) + offsetof(ReplicaState, wpoke), &pokes, sizeof(pokes), cudaMemcpyHostToDevice));
+  return 0;
 }
 
 int cvf_cluster_stats(cvf_handle* h, int r, cvf_cstats* out) {

@@ -1114,43 +1114,9 @@ __global__ void k_measure_end(ReplicaState* __restrict__ st, int nrep, int recor
 }
 
 // ------------------------------------------------------------------ persistent step kernel
-// Grid barrier of the persistent kernel; every block of the cooperative launch is resident. A
-// waiting block polls the generation word at most max_polls times (kBarrierPolls by default,
-// with a short sleep between polls, about a second in all); when the bound is reached it sets
-// gs->err and error code 3 of replica 0, and every block leaves the kernel at its next barrier.
-__device__ __noinline__ bool grid_barrier(GridSync* gs, ReplicaState* st0, unsigned int max_polls) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile unsigned int* gen = &gs->gen;
-    volatile int* err = &gs->err;
-    const unsigned int g = *gen;
-    __threadfence();
-    int ok = 1;
-    if (atomicAdd(&gs->count, 1u) == gridDim.x - 1) {
-      atomicExch(&gs->count, 0u);
-      __threadfence();
-      atomicAdd(&gs->gen, 1u);
-    } else {
-      // the bound is checked before each look at the generation word, so a bound of 0 makes
-      // every block that has to wait give up
-      for (unsigned int polls = 0;; ++polls) {
-        if (*err != 0 || polls >= max_polls) {
-          ok = 0;
-          break;
-        }
-        if (*gen != g) break;
-        __nanosleep(64);
-      }
-      if (!ok && atomicExch(&gs->err, 1) == 0) atomicExch(&st0->err, 3);
-    }
-    __threadfence();
-    s_ok = ok && *err == 0;
-  }
-  __syncthreads();
-  return s_ok != 0;
-}
-
+// The persistent kernel separates its phases with grid_barrier (every block of the cooperative
+// launch is resident; a wait gives up after b.barrier_polls looks, error code 3 of replica 0).
+//
 // Per-warp tables of the persistent kernel: the sweep and cube tables of one replica, reloaded
 // when the warp moves to a block of another replica.
 struct StepTables {

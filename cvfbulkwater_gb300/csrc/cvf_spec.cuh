@@ -59,6 +59,9 @@ enum : uint32_t {
   kStCubeRefine = 0x09u,   // per 4 cubes per cube move, drawn only on a high-half tie
   kStSwBond = 0x10u,       // + 0..2: 12 words per cell per SW step: 18 link high halves, shift digits
   kStSwBondRefine = 0x18u, // + 0..2: the links' low halves, drawn only on a high-half tie
+  kStWolffPoke = 0x0Au,    // per Wolff poke P at counter (lo P, hi P): w0..w2 seed site, w3 shift
+  kStWolffShift = 0x0Bu,   // retry kind of the Wolff shift draw
+  kStWolffBond = 0x20u,    // + l/4: link l of an owner cell in poke P, counter (cell, lo P, tag | hi P << 8)
 };
 CVF_HD uint32_t retry_tag(uint32_t kind, uint32_t k) { return 0x1000u | (kind << 8) | k; }
 

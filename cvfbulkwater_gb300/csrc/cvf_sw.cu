@@ -444,6 +444,340 @@ __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __res
   *wp = out;
 }
 
+// ---------------------------------------------------------------- Wolff cluster step
+// GW:2199-2357 (cluster_step, cluster_poke, add_to_cluster, update_cluster): pokes until the
+// flipped clusters add up to 6N sites. Poke P takes a seed site in [0, 6N) and a shift in 1..5,
+// grows the seed's cluster over the bonds of the Swendsen-Wang step and shifts every site of it.
+// Here every bond has its own uniform per poke, so the cluster is the seed's connected component
+// of the poke's bond graph, whatever order it is searched in, and pokes can be grown in parallel:
+// a batch grows one poke per warp of a cooperative grid from the same lattice, marks per cell the
+// first poke of the batch that changes it, and commits the pokes before the first one that
+// examined (read) a cell an earlier poke of the batch changes -- exactly the lattice that pokes
+// applied one after another give. A poke whose cluster outgrows its warp (kWolffQ sites) is grown
+// by the whole grid when it heads a batch.
+//   poke P: block kStWolffPoke at (lo P, hi P): words 0-2 an exact draw of the seed site, word 3
+//           an exact draw in [0, 5) (then the retry streams), shift = 1 + it
+//   bond:   link l of owner cell c (the Swendsen-Wang numbering: 0-2 the x+, y+, z+ hydrogen-bond
+//           links of c, 3-17 the intra-cell pairs) in poke P: U < T with U word l & 3 of block
+//           kStWolffBond + l/4 at (c, lo P, tag | hi P << 8)
+constexpr int kWolffQ = 128;   // cluster sites one warp grows
+constexpr int kWolffH = 256;   // slots of its hash set of cluster sites (a power of two > 2 kWolffQ)
+constexpr int kWolffThreads = 256;
+constexpr int kChgNone = 0x7f7f7f7f;  // chg of a cell no poke of the batch changes
+
+struct WolffWarp {
+  uint32_t q[kWolffQ];
+  uint32_t hs[kWolffH];
+};
+
+__device__ __forceinline__ uint32_t* word_ptr(const ReplicaDesc& R, uint32_t c) {
+  int x, y, z;
+  cell_xyz(R, c, x, y, z);
+  return R.cells[(x + y + z) & 1] + (uint32_t)(x >> 1) + (uint32_t)R.H * ((uint32_t)y + (uint32_t)R.L * (uint32_t)z);
+}
+
+// Neighbour of cell c along arm a (0 x+, 1 x-, 2 y+, 3 y-, 4 z+, 5 z-).
+__device__ __forceinline__ uint32_t nb_cell(const ReplicaDesc& R, uint32_t c, int a) {
+  int x, y, z;
+  cell_xyz(R, c, x, y, z);
+  const int L = R.L;
+  switch (a) {
+    case 0: x = x + 1 == L ? 0 : x + 1; break;
+    case 1: x = x == 0 ? L - 1 : x - 1; break;
+    case 2: y = y + 1 == L ? 0 : y + 1; break;
+    case 3: y = y == 0 ? L - 1 : y - 1; break;
+    case 4: z = z + 1 == L ? 0 : z + 1; break;
+    default: z = z == 0 ? L - 1 : z - 1; break;
+  }
+  return (uint32_t)x + (uint32_t)L * ((uint32_t)y + (uint32_t)L * (uint32_t)z);
+}
+
+__device__ __forceinline__ bool wolff_link(const ReplicaDesc& R, uint32_t owner, int l, unsigned long long P) {
+  const U4 r = philox(owner, (uint32_t)P, (kStWolffBond + (uint32_t)(l >> 2)) | ((uint32_t)(P >> 32) << 8), R.replica,
+                      R.key0, R.key1);
+  const uint32_t u = (l & 3) == 0 ? r.x : ((l & 3) == 1 ? r.y : ((l & 3) == 2 ? r.z : r.w));
+  return (unsigned long long)u < R.thr_sw[l < 3 ? 0 : 1];
+}
+
+// Seed site and shift of poke P.
+__device__ __forceinline__ void wolff_poke(const ReplicaDesc& R, unsigned long long P, uint32_t NS, uint32_t& seed,
+                                           uint32_t& shift) {
+  const uint32_t lo = (uint32_t)P, hi = (uint32_t)(P >> 32);
+  const U4 r = philox(lo, hi, kStWolffPoke, R.replica, R.key0, R.key1);
+  if (!lemire_try(r.x, NS, seed) && !lemire_try(r.y, NS, seed) && !lemire_try(r.z, NS, seed))
+    seed = lemire_retry(NS, lo, hi, kStWolffPoke, R.replica, R.key0, R.key1);
+  uint32_t d;
+  if (!lemire_try(r.w, 5u, d)) d = lemire_retry(5u, lo, hi, kStWolffShift, R.replica, R.key0, R.key1);
+  shift = 1u + d;
+}
+
+// The sites bonded to site (a, c) in poke P: up to five intra-cell arms and the facing arm of the
+// neighbour; out[k] = site or 0xffffffff. Cell words are read through L2 (other blocks change
+// them between batches). Returns the hydrogen-bond partner's cell (examined either way).
+__device__ __forceinline__ uint32_t wolff_bonds(const ReplicaDesc& R, uint32_t site, unsigned long long P, uint32_t N,
+                                                uint32_t out[6]) {
+  const uint32_t a = site / N, c = site - a * N;
+  const uint32_t w = __ldcg(word_ptr(R, c));
+  const uint32_t sa = (w >> (3 * a)) & 7u;
+#pragma unroll
+  for (int b = 0; b < 6; ++b) {
+    out[b] = 0xffffffffu;
+    if ((uint32_t)b == a || ((w >> (3 * b)) & 7u) != sa) continue;
+    const int lo = (uint32_t)b < a ? b : (int)a, hi = (uint32_t)b < a ? (int)a : b;
+    const int l = 3 + (lo == 0 ? 0 : lo == 1 ? 5 : lo == 2 ? 9 : lo == 3 ? 12 : 14) + (hi - lo - 1);
+    if (wolff_link(R, c, l, P)) out[b] = (uint32_t)b * N + c;
+  }
+  const int d = (int)a >> 1;
+  const uint32_t nbc = nb_cell(R, c, (int)a);
+  const uint32_t owner = (a & 1u) ? nbc : c;
+  const uint32_t pa = a ^ 1u;  // the facing arm
+  out[a] = 0xffffffffu;
+  if (R.Jeff != 0.0) {
+    const uint32_t sb = (__ldcg(word_ptr(R, nbc)) >> (3 * pa)) & 7u;
+    int x, y, z;
+    cell_xyz(R, c, x, y, z);
+    const bool cond = R.Jeff > 0.0 ? (((eta_of_cell(R, x, y, z) >> a) & 1u) && sb == sa) : sb != sa;
+    if (cond && wolff_link(R, owner, d, P)) out[a] = pa * N + nbc;
+  }
+  return nbc;
+}
+
+// Inserts site into the warp's hash set; true when it was not there.
+__device__ __forceinline__ bool hs_insert(uint32_t* hs, uint32_t site) {
+  uint32_t h = (site * 2654435761u) >> 24;  // top 8 bits: kWolffH = 256 slots
+  for (int k = 0; k < kWolffH; ++k) {
+    const uint32_t old = atomicCAS(hs + h, 0xffffffffu, site);
+    if (old == 0xffffffffu) return true;
+    if (old == site) return false;
+    h = (h + 1u) & (kWolffH - 1);
+  }
+  return false;
+}
+
+// Shifts site by sh (mod 6) in place: an atomic add of the field's change, so that sites of one
+// cell word updated by different threads compose.
+__device__ __forceinline__ void wolff_shift(const ReplicaDesc& R, uint32_t site, uint32_t N, uint32_t sh) {
+  const uint32_t a = site / N, c = site - a * N;
+  uint32_t* p = word_ptr(R, c);
+  const uint32_t v = (__ldcg(p) >> (3 * a)) & 7u;
+  uint32_t nv = v + sh;
+  if (nv >= 6u) nv -= 6u;
+  atomicAdd(p, (nv - v) << (3 * a));
+}
+
+__global__ void __launch_bounds__(kWolffThreads) k_wolff(const ReplicaDesc* __restrict__ reps,
+                                                         ReplicaState* __restrict__ st, int r, WolffDev W,
+                                                         GridSync* gs, unsigned int polls) {
+  __shared__ WolffWarp s_w[kWolffThreads / 32];
+  __shared__ int s_commit, s_big;
+  __shared__ long long s_sum, s_max;
+  const ReplicaDesc& R = reps[r];
+  ReplicaState& S = st[r];
+  const uint32_t N = (uint32_t)R.L * R.L * R.L, NS = 6u * N;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int gw = blockIdx.x * (kWolffThreads / 32) + wib;  // the warp's poke within a batch
+  const unsigned int nthr = gridDim.x * blockDim.x, tid = blockIdx.x * blockDim.x + threadIdx.x;
+  WolffWarp& ww = s_w[wib];
+  volatile WolffLoop* lp = W.loop;
+  if (tid == 0) {
+    lp->p0 = S.wpoke;
+    lp->done = lp->pokes = lp->maxs = 0;
+    lp->big = 0;
+  }
+  if (!grid_barrier(gs, st, polls)) return;
+  for (int batch = 0;; ++batch) {
+    // the loop state as the previous batch left it (block 0 changes it only after every block
+    // has passed the batch's second barrier)
+    const long long done0 = lp->done;
+    if (done0 >= (long long)NS) break;
+    const unsigned long long p0 = lp->p0;
+    if (!lp->big) {
+      // grow: one poke per warp
+      for (int i = lane; i < kWolffH; i += 32) ww.hs[i] = 0xffffffffu;
+      __syncwarp();
+      uint32_t seed = 0, shift = 0;
+      const unsigned long long P = p0 + (unsigned long long)gw;
+      if (lane == 0) {
+        wolff_poke(R, P, NS, seed, shift);
+        hs_insert(ww.hs, seed);
+        ww.q[0] = seed;
+      }
+      shift = __shfl_sync(0xffffffffu, shift, 0);
+      __syncwarp();
+      int n = 1, head = 0;
+      bool over = false;
+      while (head < n && !over) {
+        const int end = n;
+        for (int base = head; base < end && !over; base += 32) {
+          const int i = base + lane;
+          uint32_t nb[6];
+          if (i < end) {
+            wolff_bonds(R, ww.q[i], P, N, nb);
+          } else {
+#pragma unroll
+            for (int k = 0; k < 6; ++k) nb[k] = 0xffffffffu;
+          }
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            const bool fresh = nb[k] != 0xffffffffu && hs_insert(ww.hs, nb[k]);
+            const unsigned m = __ballot_sync(0xffffffffu, fresh);
+            const int pos = n + __popc(m & ((1u << lane) - 1u));
+            if (fresh && pos < kWolffQ) ww.q[pos] = nb[k];
+            n += __popc(m);
+            if (n > kWolffQ) over = true;
+          }
+          __syncwarp();
+        }
+        head = end;
+      }
+      const int size = over ? kWolffQ : n;
+      // mark the cells this poke changes, then (after the barrier) look for an earlier poke of the
+      // batch that changes a cell this one examined
+      for (int i = lane; i < size; i += 32) atomicMin(W.chg + (ww.q[i] % N), gw);
+      if (!grid_barrier(gs, st, polls)) return;
+      bool conflict = false;
+      for (int i = lane; i < size && !over; i += 32) {
+        const uint32_t site = ww.q[i], a = site / N, c = site - a * N;
+        if (__ldcg(W.chg + c) < gw || __ldcg(W.chg + nb_cell(R, c, (int)a)) < gw) conflict = true;
+      }
+      conflict = __any_sync(0xffffffffu, conflict);
+      if (lane == 0) {
+        W.size[gw] = n;
+        W.flag[gw] = (over ? 2 : 0) | (conflict ? 1 : 0);
+      }
+      if (!grid_barrier(gs, st, polls)) return;
+      // commit: the pokes before the first flagged one, up to the one that completes 6N sites
+      if (wib == 0) {
+        const long long rem = (long long)NS - done0;
+        long long cum = 0, mx = 0;
+        int commit = W.B;
+        for (int base = 0; base < W.B; base += 32) {
+          const int w = base + lane;
+          const int f = w < W.B ? __ldcg(W.flag + w) : 0;
+          const long long sz = w < W.B ? __ldcg(W.size + w) : 0;
+          long long incl = sz;  // inclusive prefix sum of the sizes in this chunk
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const long long t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+          }
+          const unsigned fm = __ballot_sync(0xffffffffu, w < W.B && f != 0);
+          const unsigned dm = __ballot_sync(0xffffffffu, w < W.B && f == 0 && cum + incl >= rem);
+          const int first_f = fm ? __ffs(fm) - 1 : 32, first_d = dm ? __ffs(dm) - 1 : 32;
+          const int stop = first_d < first_f ? first_d + 1 : first_f;  // pokes of this chunk taken
+          const long long take = stop > 0 ? __shfl_sync(0xffffffffu, incl, stop - 1) : 0;
+          long long m = lane < stop ? sz : 0;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            const long long t = __shfl_xor_sync(0xffffffffu, m, o);
+            m = t > m ? t : m;
+          }
+          cum += take;
+          mx = m > mx ? m : mx;
+          if (stop < 32 || base + 32 >= W.B) {
+            commit = base + (stop < 32 ? stop : 32);
+            if (commit > W.B) commit = W.B;
+            break;
+          }
+        }
+        if (lane == 0) {
+          s_commit = commit;
+          s_sum = cum;
+          s_max = mx;
+          s_big = commit == 0;  // the first poke outgrew its warp
+        }
+      }
+      __syncthreads();
+      const int commit = s_commit;
+      if (gw < commit)
+        for (int i = lane; i < n; i += 32) wolff_shift(R, ww.q[i], N, shift);
+      for (int i = lane; i < size; i += 32) W.chg[ww.q[i] % N] = kChgNone;
+      if (tid == 0) {
+        lp->p0 = p0 + (unsigned long long)commit;
+        lp->done = done0 + s_sum;
+        lp->pokes = lp->pokes + commit;
+        if (s_max > lp->maxs) lp->maxs = s_max;
+        lp->big = s_big;
+      }
+      if (!grid_barrier(gs, st, polls)) return;
+    } else {
+      // the batch's first poke outgrew its warp: the whole grid grows it, a level at a time
+      uint32_t seed = 0, shift = 0;
+      wolff_poke(R, p0, NS, seed, shift);
+      if (tid == 0) {
+        W.q[0] = seed;
+        atomicOr(W.mark + (seed >> 5), 1u << (seed & 31));
+        lp->tail = 1;
+        lp->level1 = 1;
+      }
+      if (!grid_barrier(gs, st, polls)) return;
+      unsigned int l0 = 0, l1 = lp->level1;
+      while (l0 < l1) {
+        for (unsigned int i = l0 + tid; i < l1; i += nthr) {
+          uint32_t nb[6];
+          wolff_bonds(R, __ldcg(W.q + i), p0, N, nb);
+#pragma unroll
+          for (int k = 0; k < 6; ++k) {
+            if (nb[k] == 0xffffffffu) continue;
+            const uint32_t bit = 1u << (nb[k] & 31);
+            if (atomicOr(W.mark + (nb[k] >> 5), bit) & bit) continue;
+            W.q[atomicAdd((unsigned int*)&lp->tail, 1u)] = nb[k];
+          }
+        }
+        if (!grid_barrier(gs, st, polls)) return;
+        if (tid == 0) lp->level1 = lp->tail;
+        if (!grid_barrier(gs, st, polls)) return;
+        l0 = l1;
+        l1 = lp->level1;
+      }
+      for (unsigned int i = tid; i < l1; i += nthr) {
+        const uint32_t site = __ldcg(W.q + i);
+        wolff_shift(R, site, N, shift);
+        W.mark[site >> 5] = 0u;
+      }
+      if (!grid_barrier(gs, st, polls)) return;
+      if (tid == 0) {
+        lp->p0 = p0 + 1ull;
+        lp->done = done0 + (long long)l1;
+        lp->pokes = lp->pokes + 1;
+        if ((long long)l1 > lp->maxs) lp->maxs = (long long)l1;
+        lp->big = 0;
+      }
+      if (!grid_barrier(gs, st, polls)) return;
+    }
+  }
+  if (tid == 0) {
+    S.wpoke = lp->p0;
+    S.w_pokes = lp->pokes;
+    S.w_sum = lp->done;
+    S.w_max = lp->maxs;
+  }
+}
+
+int wolff_blocks_per_sm() {
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_wolff, kWolffThreads, 0) != cudaSuccess) return 0;
+  return per;
+}
+
+cudaError_t launch_wolff_step(const BatchDev& b, cudaStream_t s) {
+  for (int r = 0; r < b.nrep; ++r) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)b.wdev.grid);
+    cfg.blockDim = dim3(kWolffThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, k_wolff, (const ReplicaDesc*)b.reps, b.st, r, b.wdev, b.gsync,
+                                       b.barrier_polls);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 // ---------------------------------------------------------------- cluster statistics
 __global__ void __launch_bounds__(kThreads) k_cs_count(const ReplicaDesc* __restrict__ reps,
                                                        const int* __restrict__ blk, int nrep) {

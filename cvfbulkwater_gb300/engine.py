@@ -146,6 +146,21 @@ class Lattice:
     def replica_groups(self, groups: int):
         check(lib().cvf_set_replica_groups(self._h, int(groups)))
 
+    def set_cluster_algorithm(self, wolff: bool):
+        """Cluster steps of run() are Wolff steps (pokes until their clusters cover 6N sites)
+        instead of Swendsen-Wang steps."""
+        check(lib().cvf_set_cluster_algorithm(self._h, 1 if wolff else 0))
+
+    def wolff_stats(self, r: int = 0):
+        """The last Wolff step of replica r: (pokes, summed cluster sizes, largest cluster,
+        poke counter)."""
+        a = np.zeros(4, dtype=np.int64)
+        check(lib().cvf_wolff_stats(self._h, r, _ptr(a)))
+        return tuple(int(v) for v in a)
+
+    def set_wolff_counter(self, r: int, pokes: int):
+        check(lib().cvf_set_wolff_counter(self._h, r, int(pokes)))
+
     def set_correlation(self, enable: bool):
         """Start (and reset) or stop the per-step multi-tau autocorrelation of every replica."""
         check(lib().cvf_set_correlation(self._h, 1 if enable else 0))

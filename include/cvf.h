@@ -246,6 +246,24 @@ int cvf_h2d_destroy(cvf_h2d* H);
 int cvf_set_correlation(cvf_handle* h, int enable);
 int cvf_get_correlation(cvf_handle* h, int r, double* t, double* f, int cap, int* n_out);
 
+/* Cluster algorithm of the n_cluster steps of cvf_run_steps / cvf_run_sampled (replaces the
+ * compile-time choice GW:195-213 #define WOLFF vs GW:214 #define SWENDSEN_WANG):
+ *   CVF_CLUSTER_SW (default): one Swendsen-Wang step (GW:2365-2542);
+ *   CVF_CLUSTER_WOLFF: one Wolff step, cluster_step() GW:2199-2357: pokes (a random seed site
+ *   and a shift in 1..5) until the flipped clusters add up to 6N sites, over the Swendsen-Wang
+ *   bonds. Wolff steps leave no labels: cvf_cluster_stats then reports the all-singleton
+ *   statistics of a handle without Swendsen-Wang steps, and cvf_wolff_stats the step's own
+ *   figures. */
+#define CVF_CLUSTER_SW 0
+#define CVF_CLUSTER_WOLFF 1
+int cvf_set_cluster_algorithm(cvf_handle* h, int algorithm);
+/* The last Wolff step of replica r (GW:2205-2222 num_clusters, cumm_cluster_size,
+ * tmp_max_cluster_size): out4 = {pokes, summed cluster sizes, largest cluster, poke counter}.
+ * The poke counter numbers the Wolff random streams; cvf_set_wolff_counter restores it when a
+ * run resumes from a checkpoint. */
+int cvf_wolff_stats(cvf_handle* h, int r, long long* out4);
+int cvf_set_wolff_counter(cvf_handle* h, int r, unsigned long long pokes);
+
 /* ---------------------------------------------------------------- isobar analysis
  * The reference's thermodynamic analysis (CVF_ThermodynamicAnalysis/) on the engine's results.
  *

@@ -49,6 +49,9 @@
 #define ST_CUBE_REFINE 0x09u
 #define ST_SW_BOND 0x10u        /* + 0..2 */
 #define ST_SW_BOND_REFINE 0x18u /* + 0..2 */
+#define ST_WOLFF_POKE 0x0Au     /* counter (lo P, hi P, tag): seed site and shift of poke P */
+#define ST_WOLFF_SHIFT 0x0Bu    /* retry kind of the shift draw */
+#define ST_WOLFF_BOND 0x20u     /* + l/4, counter (owner cell, lo P, tag | hi P << 8) */
 #define ST_RETRY(kind, k) (0x1000u | ((uint32_t)(kind) << 8) | (uint32_t)(k))
 
 /* ------------------------------------------------------------------ Philox */
@@ -89,6 +92,9 @@ struct oracle {
     uint64_t thr_sweep[33], thr_cube[9], thr_sw[2];
     int nthreads;
     int chess;    /* Flag_chessboard: 1 cube moves, 0 the nhb<=4 mode */
+    int wolff;    /* cluster steps are Wolff steps (GW:2199-2357) instead of Swendsen-Wang */
+    uint64_t wpoke;                 /* Wolff pokes so far (the poke counter P) */
+    int64_t w_pokes, w_sum, w_max;  /* the last Wolff step: pokes, summed and largest size */
     uint8_t* nhb; /* Flag_chessboard = 0: dev_nhb of GW:1974-2007, one byte per cell */
 };
 
@@ -816,18 +822,118 @@ void oracle_sw_step(oracle_t* o)
     o->ctr[3]++;
 }
 
+/* ------------------------------------------------------------ Wolff */
+/* Bond of link l of owner cell c in Wolff poke P: U < T with the 32-bit uniform U = word l & 3 of
+ * the block ST_WOLFF_BOND + l/4 at counter (c, lo P, tag | hi P << 8). */
+static int wolff_link(const oracle_t* o, int64_t c, int l, uint64_t P)
+{
+    uint32_t r[4];
+    rng(o, (uint32_t)c, (uint32_t)P, (ST_WOLFF_BOND + (uint32_t)(l >> 2)) | ((uint32_t)(P >> 32) << 8), r);
+    return (uint64_t)r[l & 3] < o->thr_sw[l < 3 ? 0 : 1];
+}
+
+/* Link index of the intra-cell pair (a, b), a < b, in row-major order after the three
+ * hydrogen-bond links (the numbering of the Swendsen-Wang links). */
+static int pair_link(int a, int b)
+{
+    static const int base[5] = {0, 5, 9, 12, 14};
+    return 3 + base[a] + (b - a - 1);
+}
+
+/* GW:2199-2357, cluster_step: pokes until the clusters flipped add up to 6N sites. Poke P takes
+ * a seed site in [0, 6N) and a shift in 1..5 (block ST_WOLFF_POKE at (lo P, hi P): words 0-2 and
+ * 3, exact draws), grows the seed's cluster over the bonds of the Swendsen-Wang step (the
+ * hydrogen-bond link of arm 2d of a cell with arm 2d+1 of its +d neighbour: eta and equal sigma
+ * for Jeff > 0, different sigma for Jeff < 0; the 15 intra-cell pairs: equal sigma), each bond
+ * decided once per poke from its own uniform, and shifts every site of it by the shift (mod 6).
+ * The cluster is the seed's connected component in the bond graph of the poke, so it does not
+ * depend on the order of the search (the reference's recursion order picks which random number
+ * tests which bond). */
+void oracle_wolff_step(oracle_t* o)
+{
+    int L = o->L;
+    int64_t N = o->N, NS = ARMS * N;
+    int64_t* stack = (int64_t*)malloc((size_t)(NS > 0 ? NS : 1) * sizeof(int64_t));
+    uint8_t* mark = (uint8_t*)calloc((size_t)(NS > 0 ? NS : 1), 1);
+    int64_t done = 0, pokes = 0, maxs = 0;
+    while (done < NS) {
+        uint64_t P = o->wpoke++;
+        uint32_t r[4];
+        rng(o, (uint32_t)P, (uint32_t)(P >> 32), ST_WOLFF_POKE, r);
+        int64_t seed = draw_below(o, (uint32_t)NS, r, 3, (uint32_t)P, (uint32_t)(P >> 32), ST_WOLFF_POKE);
+        uint32_t shift = 1u + draw_below(o, 5u, &r[3], 1, (uint32_t)P, (uint32_t)(P >> 32), ST_WOLFF_SHIFT);
+        int64_t n = 0, head = 0;
+        stack[n++] = seed;
+        mark[seed] = 1;
+        while (head < n) {
+            int64_t site = stack[head++];
+            int a = (int)(site / N);
+            int64_t c = site % N;
+            uint8_t sa = o->s[site];
+            for (int b = 0; b < ARMS; ++b) {
+                if (b == a) continue;
+                int64_t sb = (int64_t)b * N + c;
+                if (mark[sb] || o->s[sb] != sa) continue;
+                if (!wolff_link(o, c, pair_link(a < b ? a : b, a < b ? b : a), P)) continue;
+                mark[sb] = 1;
+                stack[n++] = sb;
+            }
+            int d = a >> 1;
+            int64_t owner = (a & 1) ? neighbour(L, c, a) : c;
+            int64_t other = (a & 1) ? (int64_t)(2 * d) * N + owner : (int64_t)(2 * d + 1) * N + neighbour(L, c, a);
+            if (mark[other]) continue;
+            int cond = 0;
+            if (o->Jeff > 0) cond = o->eta[(int64_t)(2 * d) * N + owner] && o->s[other] == sa;
+            else if (o->Jeff < 0) cond = o->s[other] != sa;
+            if (cond && wolff_link(o, owner, d, P)) {
+                mark[other] = 1;
+                stack[n++] = other;
+            }
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            o->s[stack[i]] = (uint8_t)((o->s[stack[i]] + shift) % Q);
+            mark[stack[i]] = 0;
+        }
+        done += n;
+        ++pokes;
+        if (n > maxs) maxs = n;
+    }
+    o->w_pokes = pokes;
+    o->w_sum = done;
+    o->w_max = maxs;
+    free(stack);
+    free(mark);
+    o->ctr[3]++;
+}
+
+void oracle_set_wolff(oracle_t* o, int on) { o->wolff = on != 0; }
+
+void oracle_wolff_stats(const oracle_t* o, int64_t out[4])
+{
+    out[0] = o->w_pokes;
+    out[1] = o->w_sum;
+    out[2] = o->w_max;
+    out[3] = (int64_t)o->wpoke;
+}
+
+static void cluster_step(oracle_t* o)
+{
+    if (o->wolff) oracle_wolff_step(o);
+    else oracle_sw_step(o);
+}
+
 void oracle_step(oracle_t* o, int nmet, int ncl)
 {
     if (!o->chess) { /* GW:1348-1384: no cube move; SW leaves the bond counts stale (GW:2531-2542) */
         oracle_volume_move(o);
         for (int j = 0; j < nmet; ++j) oracle_sweep(o);
-        for (int j = 0; j < ncl; ++j) oracle_sw_step(o);
+        for (int j = 0; j < ncl; ++j) cluster_step(o);
         return;
     }
     oracle_cube_move(o);
     oracle_volume_move(o);
     for (int j = 0; j < nmet; ++j) oracle_sweep(o);
-    for (int j = 0; j < ncl; ++j) oracle_sw_step(o);
+    for (int j = 0; j < ncl; ++j) cluster_step(o);
 }
 
 /* ------------------------------------------------------------ observables */

@@ -69,6 +69,12 @@ void oracle_cube_move(oracle_t* o);
 void oracle_volume_move(oracle_t* o);
 void oracle_sweep(oracle_t* o);
 void oracle_sw_step(oracle_t* o);
+/* One Wolff cluster step (GW:2199-2357): pokes until their clusters add up to 6N sites. */
+void oracle_wolff_step(oracle_t* o);
+/* Cluster steps of oracle_step are Wolff steps when on (default: Swendsen-Wang). */
+void oracle_set_wolff(oracle_t* o, int on);
+/* The last Wolff step: pokes, summed cluster sizes, largest cluster; then the poke counter. */
+void oracle_wolff_stats(const oracle_t* o, int64_t out[4]);
 /* One MC step in the reference's order (GW:1346-1733): cube move, volume move,
  * n_metropolis sweeps, n_cluster Swendsen-Wang steps. */
 void oracle_step(oracle_t* o, int n_metropolis, int n_cluster);

@@ -45,9 +45,11 @@ def lib():
         L.oracle_set_config.argtypes = [P, P, C.c_int64]
         L.oracle_get_config.argtypes = [P, P, C.c_int64]
         L.oracle_get_cubes.argtypes = [P, P, P]
-        for f in ("oracle_cube_move", "oracle_volume_move", "oracle_sweep", "oracle_sw_step"):
+        for f in ("oracle_cube_move", "oracle_volume_move", "oracle_sweep", "oracle_sw_step", "oracle_wolff_step"):
             getattr(L, f).argtypes = [P]
         L.oracle_step.argtypes = [P, C.c_int, C.c_int]
+        L.oracle_set_wolff.argtypes = [P, C.c_int]
+        L.oracle_wolff_stats.argtypes = [P, P]
         L.oracle_measure.argtypes = [P, C.POINTER(Obs)]
         L.oracle_cluster_stats.argtypes = [P, C.POINTER(CStats)]
         L.oracle_get_labels.argtypes = [P, P]
@@ -148,6 +150,19 @@ class Oracle:
 
     def step(self, n_metropolis=1, n_cluster=0):
         lib().oracle_step(self._h, n_metropolis, n_cluster)
+
+    def wolff_step(self):
+        lib().oracle_wolff_step(self._h)
+
+    def set_wolff(self, on: bool):
+        """Cluster steps of step() are Wolff steps (GW:2199-2357) instead of Swendsen-Wang."""
+        lib().oracle_set_wolff(self._h, 1 if on else 0)
+
+    def wolff_stats(self):
+        """The last Wolff step: (pokes, summed cluster sizes, largest cluster, poke counter)."""
+        a = np.zeros(4, dtype=np.int64)
+        lib().oracle_wolff_stats(self._h, _ptr(a))
+        return tuple(int(v) for v in a)
 
     def measure(self) -> Obs:
         o = Obs()
