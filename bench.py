@@ -492,6 +492,42 @@ def bench_sw(steps, warmup, local, flush):
     return out
 
 
+def bench_wolff(local):
+    """Wolff cluster steps (GW:2199-2357, compiled out of the reference's default build): L=64 and
+    L=128, T=0.60, P=0.45, disordered start, Cluster_Steps=1, Metropolis_Steps=0, against the
+    oracle's sequential pokes on one host core (one step at L=64)."""
+    import torch
+    from cvfbulkwater_gb300.engine import Lattice, Params
+    from oracle import oracle as O
+    out = []
+    for L, steps in ((64, 3), (128, 2)):
+        lat = Lattice(Params(L=L, T=0.60, P=0.45, seed=SEED, start=0, device=local))
+        lat.set_cluster_algorithm(True)
+        lat.run(1, 0, 1)
+        lat.synchronize()
+        s = torch.cuda.ExternalStream(lat.stream_ptr(), device=f"cuda:{local}")
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        lat.run(steps, 0, 1)
+        e1.record(s)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        pokes, total, largest, _ = lat.wolff_stats()
+        row = {"L": L, "T": 0.60, "ms_per_step": round(ms, 2), "pokes_per_step": pokes, "largest_cluster": largest,
+               "pokes_per_us": round(pokes / (ms * 1e3), 2)}
+        lat.close()
+        if L == 64:
+            o = O.Oracle(L, 0.60, 0.45, SEED, 6.0, 0, 0)
+            o.set_wolff(True)
+            o.step(0, 1)
+            t0 = time.perf_counter()
+            o.step(0, 1)
+            row["cpu_baseline"] = {"ms_per_step": round((time.perf_counter() - t0) * 1e3, 1), "cores": 1,
+                                   "kind": "port", "sample": "one Wolff step of the same L=64 lattice"}
+        out.append(row)
+    return out
+
+
 def workload_config(n_gpus):
     """The `config` object both arms print: the same workload, so the lines compare one to one."""
     return {"workload": "L=256 ordered start, T=0.70, P=0.45, Metropolis only; 1 cube move + "
@@ -677,6 +713,7 @@ def run_engine(args):
     if rank == 0 and world == 1 and not args.no_extras:
         extras["batched"] = bench_batch64(max(10, min(args.steps, 50)), args.warmup, local, flush)
         extras["swendsen_wang"] = bench_sw(max(10, min(args.steps, 30)), args.warmup, local, flush)
+        extras["wolff"] = bench_wolff(local)
         extras["plain_l16"] = bench_plain_l16(max(10, min(args.steps, 50)), args.warmup, local, flush)
         extras["differentiation"] = bench_differentiation(local)
         if not args.no_cpu_baseline:

@@ -5,7 +5,8 @@
 Creates one lattice (ordered start, T=0.70, P=0.45), runs --warmup full Monte Carlo steps
 and then --launches profiled repetitions of the chosen kind: a single kernel kind through
 cvf_profile_launch (sweep = 2 launches per repetition), or whole steps (kind "step": cube +
-volume + sweep; kind "step_sw": cube + volume + one Swendsen-Wang step; --correlation adds
+volume + sweep; kind "step_sw": cube + volume + one Swendsen-Wang step; kind "step_wolff": cube +
+volume + one Wolff step; --correlation adds
 the multi-tau correlator's histogram and update to every step).
 Prints the mean time per repetition measured with CUDA events on the engine's stream. Kind
 "c2c" times the configuration transfers against plain copies over the host link, kind
@@ -18,7 +19,8 @@ import ctypes as C
 
 KINDS = {"sweep": 0, "cube": 1, "volume": 2, "measure": 3}
 ANALYSIS = ("h2d_scan", "c2c")
-STEPS = {"step": (1, 0), "step_sw": (0, 1)}  # full MC steps: (Metropolis sweeps, SW steps)
+# full MC steps: (Metropolis sweeps, cluster steps); step_wolff's cluster steps are Wolff steps
+STEPS = {"step": (1, 0), "step_sw": (0, 1), "step_wolff": (0, 1)}
 
 
 def main():
@@ -52,6 +54,8 @@ def main():
         lat.launch_mode = a.mode
     if a.correlation:
         lat.set_correlation(True)
+    if a.kind == "step_wolff":
+        lat.set_cluster_algorithm(True)
     nmet, ncl = STEPS.get(a.kind, (1, 0))
     lat.run(a.warmup, nmet, ncl)
     lat.synchronize()
