@@ -573,7 +573,18 @@ static int check_err(cvf_handle* h) {
     int err = 0;
     CK(cudaMemcpy(&err, (char*)(h->b.st + r) + offsetof(ReplicaState, err), sizeof(int), cudaMemcpyDeviceToHost));
     if (err) {
-      if (err == 3) cudaMemset(h->b.gsync, 0, sizeof(GridSync));  // the barrier state is stale
+      if (err == 3) {
+        // the barrier state is stale, and so is the scratch of a Wolff step that stopped midway
+        cudaMemset(h->b.gsync, 0, sizeof(GridSync));
+        WolffDev& w = h->b.wdev;
+        if (w.loop) {
+          long long nmax = 0;
+          for (auto& rr : h->reps) nmax = std::max(nmax, rr.N);
+          cudaMemset(w.chg, 0x7f, (size_t)nmax * sizeof(int));
+          cudaMemset(w.mark, 0, (size_t)((6 * nmax + 31) / 32) * sizeof(uint32_t));
+          cudaMemset(w.loop, 0, sizeof(WolffLoop));
+        }
+      }
       return fail(CVF_ELIMIT, "device loop limit reached (code " + std::to_string(err) + ") in replica " + std::to_string(r));
     }
   }

@@ -61,6 +61,27 @@ def test_grid_barrier_bound_reports_elimit(engine_lib, oracle_mod):
     _fresh_matches_oracle(oracle_mod, 1, 0, launch_mode=1)
 
 
+def test_wolff_grid_barrier_bound_reports_elimit(engine_lib, oracle_mod):
+    """The Wolff step's cooperative grid waits at the same bounded barrier (three per batch)."""
+    lat = Lattice(Params(L=16, T=0.7, P=0.45, seed=404, start=0))
+    lat.set_cluster_algorithm(True)
+    assert engine_lib.cvf_set_wait_limits(lat._h, 0, -1) == 0
+    lat.run(1, 0, 1)
+    assert _sync_rc(lat) == CVF_ELIMIT
+    assert b"code 3" in engine_lib.cvf_last_error_string()
+    lat.close()
+    eng = Lattice(Params(L=16, T=0.7, P=0.45, seed=404, start=0))
+    eng.set_cluster_algorithm(True)
+    ora = oracle_mod.Oracle(16, 0.7, 0.45, 404, 6.0, 0, 0)
+    ora.set_wolff(True)
+    eng.run(2, 1, 1)
+    for _ in range(2):
+        ora.step(1, 1)
+    assert np.array_equal(eng.get_config(), ora.get_config())
+    assert eng.wolff_stats() == ora.wolff_stats()
+    eng.close()
+
+
 def test_default_bounds_restored(engine_lib, oracle_mod):
     """Negative values restore the defaults: the same handle then runs as an untouched one."""
     eng = Lattice(Params(L=16, T=0.7, P=0.45, seed=404, start=0))
