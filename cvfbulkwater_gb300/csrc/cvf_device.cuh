@@ -141,7 +141,7 @@ struct WolffLoop {
   unsigned int tail, level0, level1;  // global queue of the grid-wide growth
 };
 struct WolffDev {
-  int* chg;            // [N] per cell: smallest poke of the batch whose cluster changes it (INT_MAX)
+  int* chg;            // [6N] per site: smallest poke of the batch whose cluster changes it
   uint32_t* q;         // [6N] sites of a cluster grown by the whole grid
   uint32_t* mark;      // [6N/32] bitmask of those sites
   int* size;           // [B] cluster size per poke of the batch

@@ -301,13 +301,13 @@ static int ensure_wolff(cvf_handle* h) {
   WolffDev& w = h->b.wdev;
   w.grid = nsm * per;
   w.B = w.grid * 8;  // one poke per warp of 256-thread blocks
-  if (int rc = dev_alloc(h, (void**)&w.chg, (size_t)nmax * sizeof(int))) return rc;
+  if (int rc = dev_alloc(h, (void**)&w.chg, (size_t)(6 * nmax) * sizeof(int))) return rc;
   if (int rc = dev_alloc(h, (void**)&w.q, (size_t)(6 * nmax) * sizeof(uint32_t))) return rc;
   if (int rc = dev_alloc(h, (void**)&w.mark, (size_t)((6 * nmax + 31) / 32) * sizeof(uint32_t))) return rc;
   if (int rc = dev_alloc(h, (void**)&w.size, (size_t)w.B * sizeof(int))) return rc;
   if (int rc = dev_alloc(h, (void**)&w.flag, (size_t)w.B * sizeof(int))) return rc;
   if (int rc = dev_alloc(h, (void**)&w.loop, sizeof(WolffLoop))) return rc;
-  CK(cudaMemset(w.chg, 0x7f, (size_t)nmax * sizeof(int)));  // no poke changes any cell
+  CK(cudaMemset(w.chg, 0x7f, (size_t)(6 * nmax) * sizeof(int)));  // no poke changes any site
   CK(cudaMemset(w.mark, 0, (size_t)((6 * nmax + 31) / 32) * sizeof(uint32_t)));
   CK(cudaMemset(w.loop, 0, sizeof(WolffLoop)));
   drop_graphs(h);
@@ -580,7 +580,7 @@ static int check_err(cvf_handle* h) {
         if (w.loop) {
           long long nmax = 0;
           for (auto& rr : h->reps) nmax = std::max(nmax, rr.N);
-          cudaMemset(w.chg, 0x7f, (size_t)nmax * sizeof(int));
+          cudaMemset(w.chg, 0x7f, (size_t)(6 * nmax) * sizeof(int));
           cudaMemset(w.mark, 0, (size_t)((6 * nmax + 31) / 32) * sizeof(uint32_t));
           cudaMemset(w.loop, 0, sizeof(WolffLoop));
         }

@@ -450,9 +450,9 @@ __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __res
 // grows the seed's cluster over the bonds of the Swendsen-Wang step and shifts every site of it.
 // Here every bond has its own uniform per poke, so the cluster is the seed's connected component
 // of the poke's bond graph, whatever order it is searched in, and pokes can be grown in parallel:
-// a batch grows one poke per warp of a cooperative grid from the same lattice, marks per cell the
+// a batch grows one poke per warp of a cooperative grid from the same lattice, marks per site the
 // first poke of the batch that changes it, and commits the pokes before the first one that
-// examined (read) a cell an earlier poke of the batch changes -- exactly the lattice that pokes
+// examined (read) a site an earlier poke of the batch changes -- exactly the lattice that pokes
 // applied one after another give. A poke whose cluster outgrows its warp (kWolffQ sites) is grown
 // by the whole grid when it heads a batch.
 //   poke P: block kStWolffPoke at (lo P, hi P): words 0-2 an exact draw of the seed site, word 3
@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __res
 constexpr int kWolffQ = 128;   // cluster sites one warp grows
 constexpr int kWolffH = 256;   // slots of its hash set of cluster sites (a power of two > 2 kWolffQ)
 constexpr int kWolffThreads = 256;
-constexpr int kChgNone = 0x7f7f7f7f;  // chg of a cell no poke of the batch changes
+constexpr int kChgNone = 0x7f7f7f7f;  // chg of a site no poke of the batch changes
 
 struct WolffWarp {
   uint32_t q[kWolffQ];
@@ -631,14 +631,18 @@ __global__ void __launch_bounds__(kWolffThreads) k_wolff(const ReplicaDesc* __re
         head = end;
       }
       const int size = over ? kWolffQ : n;
-      // mark the cells this poke changes, then (after the barrier) look for an earlier poke of the
-      // batch that changes a cell this one examined
-      for (int i = lane; i < size; i += 32) atomicMin(W.chg + (ww.q[i] % N), gw);
+      // mark the sites this poke changes, then (after the barrier) look for an earlier poke of the
+      // batch that changes a site this one examined: the six arms of each cluster site's cell and
+      // the facing arm of its hydrogen-bond partner
+      for (int i = lane; i < size; i += 32) atomicMin(W.chg + ww.q[i], gw);
       if (!grid_barrier(gs, st, polls)) return;
       bool conflict = false;
       for (int i = lane; i < size && !over; i += 32) {
         const uint32_t site = ww.q[i], a = site / N, c = site - a * N;
-        if (__ldcg(W.chg + c) < gw || __ldcg(W.chg + nb_cell(R, c, (int)a)) < gw) conflict = true;
+#pragma unroll
+        for (uint32_t b = 0; b < 6; ++b)
+          if (__ldcg(W.chg + b * N + c) < gw) conflict = true;
+        if (__ldcg(W.chg + (a ^ 1u) * N + nb_cell(R, c, (int)a)) < gw) conflict = true;
       }
       conflict = __any_sync(0xffffffffu, conflict);
       if (lane == 0) {
@@ -691,7 +695,7 @@ __global__ void __launch_bounds__(kWolffThreads) k_wolff(const ReplicaDesc* __re
       const int commit = s_commit;
       if (gw < commit)
         for (int i = lane; i < n; i += 32) wolff_shift(R, ww.q[i], N, shift);
-      for (int i = lane; i < size; i += 32) W.chg[ww.q[i] % N] = kChgNone;
+      for (int i = lane; i < size; i += 32) W.chg[ww.q[i]] = kChgNone;
       if (tid == 0) {
         lp->p0 = p0 + (unsigned long long)commit;
         lp->done = done0 + s_sum;
