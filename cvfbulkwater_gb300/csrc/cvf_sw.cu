@@ -569,8 +569,9 @@ __global__ void __launch_bounds__(kWolffThreads) k_wolff(const ReplicaDesc* __re
                                                          ReplicaState* __restrict__ st, int r, WolffDev W,
                                                          GridSync* gs, unsigned int polls) {
   __shared__ WolffWarp s_w[kWolffThreads / 32];
-  __shared__ int s_commit, s_big;
-  __shared__ long long s_sum, s_max;
+  __shared__ int s_commit, s_big, s_first;
+  __shared__ long long s_sum, s_max, s_take;
+  __shared__ long long s_wsum[kWolffThreads / 32], s_wmax[kWolffThreads / 32];
   const ReplicaDesc& R = reps[r];
   ReplicaState& S = st[r];
   const uint32_t N = (uint32_t)R.L * R.L * R.L, NS = 6u * N;
@@ -650,41 +651,63 @@ __global__ void __launch_bounds__(kWolffThreads) k_wolff(const ReplicaDesc* __re
         W.flag[gw] = (over ? 2 : 0) | (conflict ? 1 : 0);
       }
       if (!grid_barrier(gs, st, polls)) return;
-      // commit: the pokes before the first flagged one, up to the one that completes 6N sites
-      if (wib == 0) {
+      // commit: the pokes before the first flagged one, up to the one that completes 6N sites;
+      // every block computes the same answer, a round of kWolffThreads pokes at a time (the
+      // loads of a round in parallel, a block scan of the sizes)
+      {
         const long long rem = (long long)NS - done0;
         long long cum = 0, mx = 0;
         int commit = W.B;
-        for (int base = 0; base < W.B; base += 32) {
-          const int w = base + lane;
-          const int f = w < W.B ? __ldcg(W.flag + w) : 0;
-          const long long sz = w < W.B ? __ldcg(W.size + w) : 0;
-          long long incl = sz;  // inclusive prefix sum of the sizes in this chunk
+        for (int base = 0; base < W.B; base += kWolffThreads) {
+          const int w = base + (int)threadIdx.x;
+          const bool in = w < W.B;
+          const int f = in ? __ldcg(W.flag + w) : 0;
+          const long long sz = in ? __ldcg(W.size + w) : 0;
+          long long incl = sz;
 #pragma unroll
           for (int o = 1; o < 32; o <<= 1) {
             const long long t = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= o) incl += t;
           }
-          const unsigned fm = __ballot_sync(0xffffffffu, w < W.B && f != 0);
-          const unsigned dm = __ballot_sync(0xffffffffu, w < W.B && f == 0 && cum + incl >= rem);
-          const int first_f = fm ? __ffs(fm) - 1 : 32, first_d = dm ? __ffs(dm) - 1 : 32;
-          const int stop = first_d < first_f ? first_d + 1 : first_f;  // pokes of this chunk taken
-          const long long take = stop > 0 ? __shfl_sync(0xffffffffu, incl, stop - 1) : 0;
-          long long m = lane < stop ? sz : 0;
+          if (lane == 31) s_wsum[wib] = incl;
+          if (threadIdx.x == 0) s_first = 0x7fffffff;
+          __syncthreads();
+          long long off = 0, tot = 0;
+#pragma unroll
+          for (int k = 0; k < kWolffThreads / 32; ++k) {
+            off += k < wib ? s_wsum[k] : 0;
+            tot += s_wsum[k];
+          }
+          incl += off;  // inclusive prefix of the round's sizes
+          // 2w: stop before poke w (flagged); 2w + 1: stop after it (it completes 6N sites)
+          if (in && f != 0) atomicMin(&s_first, 2 * w);
+          if (in && f == 0 && cum + incl >= rem) atomicMin(&s_first, 2 * w + 1);
+          __syncthreads();
+          const int fs = s_first;
+          const int stop = fs == 0x7fffffff ? base + kWolffThreads : (fs >> 1) + (fs & 1);  // pokes taken so far
+          const bool taken = in && w < stop;
+          if (taken && w == stop - 1) s_take = incl;
+          long long m = taken ? sz : 0;
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) {
             const long long t = __shfl_xor_sync(0xffffffffu, m, o);
             m = t > m ? t : m;
           }
-          cum += take;
-          mx = m > mx ? m : mx;
-          if (stop < 32 || base + 32 >= W.B) {
-            commit = base + (stop < 32 ? stop : 32);
-            if (commit > W.B) commit = W.B;
+          if (lane == 0) s_wmax[wib] = m;
+          __syncthreads();
+          long long rm = 0;
+#pragma unroll
+          for (int k = 0; k < kWolffThreads / 32; ++k) rm = s_wmax[k] > rm ? s_wmax[k] : rm;
+          mx = rm > mx ? rm : mx;
+          if (fs != 0x7fffffff || base + kWolffThreads >= W.B) {
+            commit = stop < W.B ? stop : W.B;
+            cum += stop > base ? (fs != 0x7fffffff ? s_take : tot) : 0;
             break;
           }
+          cum += tot;
+          __syncthreads();  // s_wsum and s_wmax are rewritten by the next round
         }
-        if (lane == 0) {
+        if (threadIdx.x == 0) {
           s_commit = commit;
           s_sum = cum;
           s_max = mx;
