@@ -108,3 +108,46 @@ def test_wolff_batch_and_counter_restore(engine_lib, oracle_mod):
     assert np.array_equal(e2.get_config(), o.get_config())
     assert e2.wolff_stats()[:3] == o.wolff_stats()[:3]
     e2.close()
+
+
+def test_wolff_switching_sampled_and_tiny(engine_lib, oracle_mod):
+    """Swendsen-Wang and Wolff steps alternate on one handle as the oracle alternates them; a
+    sampled run records after Wolff steps; an L=4 lattice (48 sites, far fewer than a batch's
+    pokes) steps like the oracle."""
+    eng, ora = _pair(oracle_mod, 12, 0.7, 0.45, 55, 0)
+    eng.set_cluster_algorithm(False)
+    ora.set_wolff(False)
+    eng.run(1, 1, 1)
+    ora.step(1, 1)
+    eng.set_cluster_algorithm(True)
+    ora.set_wolff(True)
+    eng.run(2, 1, 1)
+    ora.step(1, 1)
+    ora.step(1, 1)
+    eng.set_cluster_algorithm(False)
+    ora.set_wolff(False)
+    eng.run(1, 0, 1)
+    ora.step(0, 1)
+    assert np.array_equal(eng.get_config(), ora.get_config())
+    assert np.array_equal(eng.labels(), ora.labels())
+    eng.set_cluster_algorithm(True)
+    ora.set_wolff(True)
+    eng.run_sampled(4, 1, 1, 2)
+    rec = []
+    for k in range(4):
+        ora.step(1, 1)
+        if k % 2 == 0:
+            rec.append(ora.measure())
+    smp = eng.samples()
+    assert len(smp) == 2
+    for got, want in zip(smp, rec):
+        assert (got["n_hb2"], got["n_sigma"], got["r_cell"]) == (want.n_hb2, want.n_sigma, want.r_cell)
+    assert np.array_equal(eng.get_config(), ora.get_config())
+    assert eng.wolff_stats() == ora.wolff_stats()
+    eng.close()
+    eng, ora = _pair(oracle_mod, 4, 0.7, 0.45, 56, 0)
+    for step in range(3):
+        eng.run(1, 1, 1)
+        ora.step(1, 1)
+        _compare(eng, ora, step)
+    eng.close()
