@@ -132,7 +132,9 @@ struct GridSync {
 };
 
 // Scratch of the Wolff step kernel (one replica at a time; sized for the largest replica) and
-// its loop state. A batch is one poke per warp of the cooperative grid.
+// its loop state. A batch is one poke per warp of the cooperative grid of kWolffThreads-thread
+// blocks.
+constexpr int kWolffThreads = 512;
 struct WolffLoop {
   unsigned long long p0;  // first poke of the current batch
   long long done, pokes, maxs;  // sites flipped, pokes and largest cluster of the step so far

@@ -293,14 +293,14 @@ static int ensure_wolff(cvf_handle* h) {
   for (auto& r : h->reps) nmax = std::max(nmax, r.N);
   int nsm = 0;
   CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device));
-  // at most 2 blocks per SM, one slot fewer than fit, so that a kernel on a side branch (the
-  // volume chain) never keeps the cooperative grid from being resident
+  // one block per SM (two fit), so that a kernel on a side branch (the volume chain) never keeps
+  // the cooperative grid from being resident; 16 warps per block, one poke each (152 blocks of
+  // 512 threads: L=64 step 59 -> 57 ms, L=128 204 -> 189 ms against 304 blocks of 256)
   const int fit = wolff_blocks_per_sm();
   if (fit < 1) return fail(CVF_ECUDA, "the Wolff kernel does not fit on an SM");
-  const int per = std::max(1, std::min(fit - 1, 2));
   WolffDev& w = h->b.wdev;
-  w.grid = nsm * per;
-  w.B = w.grid * 8;  // one poke per warp of 256-thread blocks
+  w.grid = nsm;
+  w.B = w.grid * (kWolffThreads / 32);
   if (int rc = dev_alloc(h, (void**)&w.chg, (size_t)(6 * nmax) * sizeof(int))) return rc;
   if (int rc = dev_alloc(h, (void**)&w.q, (size_t)(6 * nmax) * sizeof(uint32_t))) return rc;
   if (int rc = dev_alloc(h, (void**)&w.mark, (size_t)((6 * nmax + 31) / 32) * sizeof(uint32_t))) return rc;

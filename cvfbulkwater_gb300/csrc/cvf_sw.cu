@@ -462,7 +462,6 @@ __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __res
 //           kStWolffBond + l/4 at (c, lo P, tag | hi P << 8)
 constexpr int kWolffQ = 128;   // cluster sites one warp grows
 constexpr int kWolffH = 256;   // slots of its hash set of cluster sites (a power of two > 2 kWolffQ)
-constexpr int kWolffThreads = 256;
 constexpr int kChgNone = 0x7f7f7f7f;  // chg of a site no poke of the batch changes
 
 struct WolffWarp {
