@@ -1,7 +1,8 @@
-// Swendsen-Wang cluster step and cluster statistics of the GB300 CVF engine.
+// Cluster steps (Swendsen-Wang and Wolff) and cluster statistics of the GB300 CVF engine.
 //
 // Reference: SOURCE/gpu_water3D.cu ("GW") GW:2365-2542 (bond activation, min-label scans until
-// nothing changes, cluster shift) and GW:2677-2780 (cluster statistics on the host).
+// nothing changes, cluster shift), GW:2199-2357 (the CPU Wolff step of the WOLFF build) and
+// GW:2677-2780 (cluster statistics on the host).
 // Here the labelling is a lock-free union-find over the 6N arm sites (site = arm*N + cell):
 // parents only ever point to smaller site ids, roots are hooked under smaller roots with
 // atomicMin, so each component's root is its minimum site id -- the same canonical label the
@@ -461,7 +462,9 @@ __global__ void __launch_bounds__(kThreads) k_sw_finish(const ReplicaDesc* __res
 //           links of c, 3-17 the intra-cell pairs) in poke P: U < T with U word l & 3 of block
 //           kStWolffBond + l/4 at (c, lo P, tag | hi P << 8)
 constexpr int kWolffQ = 128;   // cluster sites one warp grows
-constexpr int kWolffH = 256;   // slots of its hash set of cluster sites (a power of two > 2 kWolffQ)
+constexpr int kWolffH = 256;   // slots of its hash set of cluster sites (2 kWolffQ; hs_insert
+                               // takes the top 8 bits of a multiplicative hash)
+static_assert(kWolffH == 256 && kWolffH >= 2 * kWolffQ, "hs_insert hashes to 8 bits");
 constexpr int kChgNone = 0x7f7f7f7f;  // chg of a site no poke of the batch changes
 
 struct WolffWarp {
