@@ -1313,7 +1313,7 @@ void launch_chunk_end(const BatchDev& b, int steps, int nmet, int ncl, int do_vo
 }
 
 // The counting sweep runs at most 4 cells per thread (its 8-cell tile spills registers under
-// the 3-blocks-per-SM bound and ran 3-6 us per step slower at L=256).
+// the 3-blocks-per-SM bound and ran 6-13 us per recorded step slower at L=256).
 void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, bool count, int from_ctr) {
   if (count) {
     const int n = b.nblk_sweep_count;
