@@ -757,15 +757,20 @@ struct EtaTables {
   uint8_t eta[72];
 };
 // Histograms are eight bytes {hi:lo} holding 4x the count of each sigma value 0..5 (bytes 6, 7
-// zero). All sweep tables index with at most 8 distinct entries of 8 bytes or a 33-word array, so
-// a warp's random lookups never conflict in a shared-memory bank.
-//   cnt[v]  4 at byte v (v = 0..5), zero for v = 6, 7: one arm of value v
-//   nbw[v]  44 at byte v (v = 0..5), zero for v = 6, 7 (7 marks an arm with eta = 0)
-//   tv[i]   2*(T_i >> 16) + ((T_i & 0xffff) != 0) - 1 for the threshold T_i of entry
-//           i = 11*dN_hb + (h_new - h_old) + 17
+// zero). The sweep tables index with at most 8 distinct entries of 8 bytes or a 33-word array, so
+// a warp's random lookups never conflict in a shared-memory bank, except dcnt (36 live entries).
+//   cnt[v]   4 at byte v (v = 0..5), zero for v = 6, 7: one arm of value v
+//   nbw[v]   44 at byte v (v = 0..5), zero for v = 6, 7 (7 marks an arm with eta = 0)
+//   dcnt[i]  cnt[i >> 3] - cnt[i & 7] per 32-bit word (wrapping): the histogram change of an arm
+//            going from value i & 7 to value i >> 3, one lookup and two adds where cnt takes two
+//            lookups and four adds (the 8-cell sweep: L=256 step 205.8 -> 202.2 us; the kernels
+//            at the 64-register bound spill with it and keep cnt)
+//   tv[i]    2*(T_i >> 16) + ((T_i & 0xffff) != 0) - 1 for the threshold T_i of entry
+//            i = 11*dN_hb + (h_new - h_old) + 17
 struct SweepTables {
   uint2 cnt[8];
   uint2 nbw[8];
+  uint2 dcnt[64];
   uint32_t tv[33];
   EtaTables et;
 };
@@ -795,6 +800,10 @@ __device__ __forceinline__ void fill_sweep_tables(const ReplicaDesc& R, SweepTab
     wt->cnt[lane] = count_bytes(lane, 4u);
     wt->nbw[lane] = count_bytes(lane, 44u);
   }
+  for (uint32_t i = lane; i < 64; i += 32) {
+    const uint2 n = count_bytes(i >> 3, 4u), o = count_bytes(i & 7u, 4u);
+    wt->dcnt[i] = make_uint2(n.x - o.x, n.y - o.y);
+  }
 }
 
 __device__ __forceinline__ const SweepTables* warp_sweep_tables(const ReplicaDesc& R, SweepTables* all) {
@@ -817,6 +826,10 @@ __device__ __forceinline__ void fill_block_sweep_tables(const ReplicaDesc& R, Sw
     t->cnt[i] = count_bytes((uint32_t)i, 4u);
     t->nbw[i] = count_bytes((uint32_t)i, 44u);
   }
+  if (i < 64) {
+    const uint2 n = count_bytes((uint32_t)i >> 3, 4u), o = count_bytes((uint32_t)i & 7u, 4u);
+    t->dcnt[i] = make_uint2(n.x - o.x, n.y - o.y);
+  }
 }
 
 // Metropolis update of the six arms of one cell, arms in order 0..5 (GW:1964-2007 energy change,
@@ -833,7 +846,7 @@ __device__ __forceinline__ void fill_block_sweep_tables(const ReplicaDesc& R, Sw
 // decides every arm from the full 32-bit uniforms. A proposal equal to the old
 // value lands on entry 17 (dN = 0), which always accepts and changes nothing.
 // kCount: dacc also receives the cell's count changes, packed as 65536 dN_hb + dN_sigma.
-template <bool kCount, bool kFold>
+template <bool kCount, bool kFold, bool kDelta>
 __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbe, const U4& rr,
                                                 uint32_t c0, uint32_t t, const ReplicaDesc& R, const SweepTables* wt,
                                                 int32_t& dacc) {
@@ -872,12 +885,22 @@ __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbe, const 
     const uint32_t hu = (a & 1) ? (word >> 16) : (word & 0xffffu);
     const int d = (int)(tv - 2u * hu);
     tprod *= (uint32_t)d;
-    const uint2 cn = wt->cnt[sn - 0x7770u], co = wt->cnt[o];
-    const uint32_t dw = (sn - 0x7770u - o) << (3 * a);
-    asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %3, 1;\n\t@p add.u32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;"
-        "\n\t@p sub.u32 %1, %1, %6;\n\t@p add.u32 %2, %2, %7;\n\t@p sub.u32 %2, %2, %8;\n\t}"
-        : "+r"(w), "+r"(hx), "+r"(hy)
-        : "r"(d), "r"(dw), "r"(cn.x), "r"(co.x), "r"(cn.y), "r"(co.y));
+    const uint32_t nv = sn - 0x7770u;
+    const uint32_t dw = (nv - o) << (3 * a);
+    if (kDelta) {
+      // one lookup of the histogram change of the pair (new, old)
+      const uint2 dc = wt->dcnt[8 * nv + o];
+      asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %3, 1;\n\t@p add.u32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;"
+          "\n\t@p add.u32 %2, %2, %6;\n\t}"
+          : "+r"(w), "+r"(hx), "+r"(hy)
+          : "r"(d), "r"(dw), "r"(dc.x), "r"(dc.y));
+    } else {
+      const uint2 cn = wt->cnt[nv], co = wt->cnt[o];
+      asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %3, 1;\n\t@p add.u32 %0, %0, %4;\n\t@p add.u32 %1, %1, %5;"
+          "\n\t@p sub.u32 %1, %1, %6;\n\t@p add.u32 %2, %2, %7;\n\t@p sub.u32 %2, %2, %8;\n\t}"
+          : "+r"(w), "+r"(hx), "+r"(hy)
+          : "r"(d), "r"(dw), "r"(cn.x), "r"(co.x), "r"(cn.y), "r"(co.y));
+    }
   }
   if (tprod == 0u || reject) {
     const uint32_t ue = reject ? sweep_proposal_retry(c0, t, R.replica, R.key0, R.key1) : u;
@@ -911,7 +934,7 @@ struct SweepMinBlocks {
 // colour-1 cells count all bonds (delta of the facing sigmas times the bond's eta, twice), and
 // each colour-1 cell adds the sigma pairs of itself and of the colour-0 cell with the same word
 // index (the x-neighbour the segment loads anyway).
-template <int V, bool kMeasure, bool kCount = false, bool kFold = false>
+template <int V, bool kMeasure, bool kCount = false, bool kFold = false, bool kDelta = false>
 __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepTables* wt, uint32_t q, int colour,
                                               uint32_t t, uint32_t& hb2, uint32_t& ns, int32_t* dacc = nullptr) {
   int hc, y, z;
@@ -942,7 +965,7 @@ __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepT
     const uint32_t c0 = cbase + 2u * k;
     const U4 rr = philox_rk(c0, t, kStSweep, R.replica, rk);
     int32_t dummy = 0;
-    out[k] = update_cell<kCount, kFold>(out[k], nbe[k], rr, c0, t, R, wt, kCount ? *dacc : dummy);
+    out[k] = update_cell<kCount, kFold, kDelta>(out[k], nbe[k], rr, c0, t, R, wt, kCount ? *dacc : dummy);
   }
   VecLoad<V>::st(own_ptr, out);
   if (kMeasure) {
@@ -970,7 +993,7 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const 
   pdl_wait();
   uint32_t hb2 = 0, ns = 0;
   int32_t dacc = 0;
-  sweep_segment<V, false, kCount, true>(R, &s_tab, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
+  sweep_segment<V, false, kCount, true, V == 8 && !kCount>(R, &s_tab, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
                                   (from_ctr ? st[r].ctr[0] : st[r].cur[0]) + (uint32_t)jsweep, hb2, ns, &dacc);
   if (kCount) {
     const int ds = (int)(int16_t)(dacc & 0xffff);  // |dN_sigma| per thread <= 8 cells x 30
