@@ -622,11 +622,41 @@ def run_engine(args):
     resident = N * args.steps / (e0.elapsed_time(e1) * 1e6)
 
     # end to end through the C ABI with host buffers: upload a host configuration, then per step
-    # one run call and one observables read (device -> host), finally download the lattice
+    # one run call and one observables read (device -> host), finally download the lattice. The
+    # headline uses the reference's own host arrays (s and active_bond, one byte per arm each:
+    # what GW:1135-1137 copies to the device and GW:1298 copies back).
+    lat2 = Lattice(Params(L=L, T=T_BENCH, P=P_BENCH, seed=SEED + 7 + rank, start=1, replica=rank, device=local))
+    host_s, host_ab = lat.get_arms()
+    out_arms = (np.zeros_like(host_s), np.zeros_like(host_ab))  # a caller's reusable result buffers
+    lat2.set_arms(host_s, host_ab)
+    for _ in range(max(3, args.warmup)):
+        lat2.run(1, 1, 0)
+        lat2.observables()
+    lat2.get_arms(out=out_arms)
+    dist.barrier()
+    t0 = time.perf_counter()
+    lat2.set_arms(host_s, host_ab)
+    ta = time.perf_counter()
+    for _ in range(args.steps):
+        lat2.run(1, 1, 0)
+        lat2.observables()
+    tb = time.perf_counter()
+    lat2.get_arms(out=out_arms)
+    t1 = time.perf_counter()
+    arm_bytes = 12 * N  # s and active_bond, 6N bytes each
+    e2e = {"value": round(world * N * args.steps / (dist.max(t1 - t0) * 1e9), 4), "unit": "site-updates/ns",
+           "h2d_bytes_per_step": int(round(arm_bytes / args.steps)),
+           "d2h_bytes_per_step": int(round(arm_bytes / args.steps)) + 32,
+           "upload_ms": round(1e3 * (ta - t0), 3), "steps_ms": round(1e3 * (tb - ta), 3),
+           "download_ms": round(1e3 * (t1 - tb), 3),
+           "note": "per step: cvf_run_steps(1 step) + cvf_observables (measurement, 32 B D2H, sync); "
+                   "lattice upload (cvf_set_arms: the caller's s and active_bond arrays, 201 MB, read and "
+                   "packed by the GPU in host memory) and download (cvf_get_arms: unpacked by the GPU into "
+                   "the caller's arrays) amortised over the K steps"}
+    # the same sequence through the config.out order (cells12: twelve int32 per cell)
     host_cfg = lat.get_config()
     out_buf = np.empty_like(host_cfg)
     out_buf.fill(0)  # a caller's reusable result buffer
-    lat2 = Lattice(Params(L=L, T=T_BENCH, P=P_BENCH, seed=SEED + 7 + rank, start=1, replica=rank, device=local))
     # one untimed pass of the same sequence: the first GPU access to a host page (here the
     # result buffer's) sets up its translation, a one-time cost of a reused buffer
     lat2.set_config(host_cfg)
@@ -646,7 +676,7 @@ def run_engine(args):
     t1 = time.perf_counter()
     e2e_s = dist.max(t1 - t0)
     cells12_bytes = 12 * 4 * N  # what crosses the host link each way: the caller's int32 cells12 array
-    e2e = {"value": round(world * N * args.steps / (e2e_s * 1e9), 4), "unit": "site-updates/ns",
+    e2e_cells12 = {"value": round(world * N * args.steps / (e2e_s * 1e9), 4), "unit": "site-updates/ns",
            "h2d_bytes_per_step": int(round(cells12_bytes / args.steps)),
            "d2h_bytes_per_step": int(round(cells12_bytes / args.steps)) + 32,
            "upload_ms": round(1e3 * (ta - t0), 3), "steps_ms": round(1e3 * (tb - ta), 3),
@@ -693,23 +723,22 @@ def run_engine(args):
     lat2.samples()
     dist.barrier()
     t0 = time.perf_counter()
-    lat2.set_config(host_cfg)
+    lat2.set_arms(host_s, host_ab)
     lat2.clear_samples()
     ta = time.perf_counter()
     lat2.run_sampled(args.steps, 1, 0, 1)
     smp = lat2.samples()
     tb = time.perf_counter()
-    out_cfg = lat2.get_config(out=out_buf)
+    lat2.get_arms(out=out_arms)
     t1 = time.perf_counter()
     e2e_sampled = {"value": round(world * N * args.steps / (dist.max(t1 - t0) * 1e9), 4),
                    "unit": "site-updates/ns", "records": int(len(smp)),
                    "upload_ms": round(1e3 * (ta - t0), 3), "steps_ms": round(1e3 * (tb - ta), 3),
                    "download_ms": round(1e3 * (t1 - tb), 3),
-                   "note": "cvf_set_config, cvf_run_sampled(K steps, a record after every step), "
-                           "cvf_get_samples, cvf_get_config"}
-    del out_cfg
+                   "note": "cvf_set_arms, cvf_run_sampled(K steps, a record after every step), "
+                           "cvf_get_samples, cvf_get_arms"}
 
-    extras = {"e2e_sampled": e2e_sampled, "e2e_packed": e2e_packed}
+    extras = {"e2e_cells12": e2e_cells12, "e2e_sampled": e2e_sampled, "e2e_packed": e2e_packed}
     if rank == 0 and world == 1 and not args.no_extras:
         extras["batched"] = bench_batch64(max(10, min(args.steps, 50)), args.warmup, local, flush)
         extras["swendsen_wang"] = bench_sw(max(10, min(args.steps, 30)), args.warmup, local, flush)

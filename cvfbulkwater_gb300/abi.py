@@ -98,6 +98,8 @@ def lib():
         "cvf_num_replicas": (I, [P]),
         "cvf_set_config": (I, [P, I, P, LL]),
         "cvf_get_config": (I, [P, I, P, LL]),
+        "cvf_set_arms": (I, [P, I, P, P, LL]),
+        "cvf_get_arms": (I, [P, I, P, P, LL]),
         "cvf_set_distances": (I, [P, I, P, P, I]),
         "cvf_get_distances": (I, [P, I, P, P, I, C.POINTER(I)]),
         "cvf_run_steps": (I, [P, I, I, I]),

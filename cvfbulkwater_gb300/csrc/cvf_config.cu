@@ -142,6 +142,125 @@ __global__ void k_pack_cubes(const uint8_t* __restrict__ eta6, uint32_t L, uint3
 
 static inline unsigned grid_of(unsigned long long n) { return (unsigned)((n + kThreads - 1) / kThreads); }
 
+// The reference's own host arrays (GW:1135-1137, GW:1298): s[arm*N + cell] and
+// active_bond[arm*N + cell], one byte each, 12 bytes per cell. One thread per G consecutive cells
+// reads (or writes) G bytes of each of the twelve arm rows at once: G = 16 (16-byte accesses, a
+// warp covers 512 contiguous bytes of every row) when both arrays are 16-byte aligned and N is a
+// multiple of 16, else G = 4 (4-byte accesses when 4-byte aligned, else single bytes).
+template <int G, bool kWide>
+struct ArmRow;
+template <>
+struct ArmRow<16, true> {
+  static __device__ __forceinline__ void ld(const uint8_t* p, uint32_t q, uint32_t* v) {
+    const uint4 t = reinterpret_cast<const uint4*>(p)[q];
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  }
+  static __device__ __forceinline__ void st(uint8_t* p, uint32_t q, const uint32_t* v) {
+    reinterpret_cast<uint4*>(p)[q] = make_uint4(v[0], v[1], v[2], v[3]);
+  }
+};
+template <>
+struct ArmRow<4, true> {
+  static __device__ __forceinline__ void ld(const uint8_t* p, uint32_t q, uint32_t* v) {
+    v[0] = reinterpret_cast<const uint32_t*>(p)[q];
+  }
+  static __device__ __forceinline__ void st(uint8_t* p, uint32_t q, const uint32_t* v) {
+    reinterpret_cast<uint32_t*>(p)[q] = v[0];
+  }
+};
+template <>
+struct ArmRow<4, false> {
+  static __device__ __forceinline__ void ld(const uint8_t* p, uint32_t q, uint32_t* v) {
+    v[0] = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[0] |= (uint32_t)p[4 * q + k] << (8 * k);
+  }
+  static __device__ __forceinline__ void st(uint8_t* p, uint32_t q, const uint32_t* v) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) p[4 * q + k] = (uint8_t)(v[0] >> (8 * k));
+  }
+};
+
+template <int G, bool kWide>
+__global__ void __launch_bounds__(kThreads) k_pack_arms(const uint8_t* __restrict__ s, const uint8_t* __restrict__ ab,
+                                                        uint32_t L, uint32_t H, int lgL, uint32_t N,
+                                                        uint32_t* __restrict__ cells0, uint32_t* __restrict__ cells1,
+                                                        uint8_t* __restrict__ eta6, unsigned long long* bad) {
+  constexpr int W = G / 4;  // 32-bit words per row segment
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x, c0 = G * q;
+  if (c0 >= N) return;
+  uint32_t sv[6][W], ev[6][W];
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    ArmRow<G, kWide>::ld(s + (size_t)a * N, q, sv[a]);
+    ArmRow<G, kWide>::ld(ab + (size_t)a * N, q, ev[a]);
+  }
+#pragma unroll
+  for (int k = 0; k < G; ++k) {
+    uint32_t w = 0, e = 0;
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+      const uint32_t sg = (sv[a][k >> 2] >> (8 * (k & 3))) & 0xffu, et = (ev[a][k >> 2] >> (8 * (k & 3))) & 0xffu;
+      ok = ok && sg <= 5u && et <= 1u;
+      w |= (sg & 7u) << (3 * a);
+      e |= (et & 1u) << a;
+    }
+    const uint32_t c = c0 + k;
+    if (!ok) {
+      atomicMin(bad, (unsigned long long)c);
+      continue;
+    }
+    uint32_t x, y, z;
+    cell_xyz(c, L, lgL, x, y, z);
+    ((x + y + z) & 1u ? cells1 : cells0)[(x >> 1) + H * (y + L * z)] = w;
+    eta6[c] = (uint8_t)e;
+  }
+}
+
+// The reverse: sigma from the colour-split words, eta from the two cubes of each cell.
+template <int G, bool kWide>
+__global__ void __launch_bounds__(kThreads) k_unpack_arms(const uint32_t* __restrict__ cells0,
+                                                          const uint32_t* __restrict__ cells1,
+                                                          const uint8_t* __restrict__ ce, const uint8_t* __restrict__ co,
+                                                          uint32_t L, uint32_t H, int lgL, uint32_t N,
+                                                          uint8_t* __restrict__ s, uint8_t* __restrict__ ab) {
+  constexpr int W = G / 4;
+  __shared__ uint8_t s_tab[72];
+  if (threadIdx.x < 72) s_tab[threadIdx.x] = (uint8_t)cube_eta_bits(threadIdx.x >> 3, threadIdx.x & 7);
+  __syncthreads();
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x, c0 = G * q;
+  if (c0 >= N) return;
+  uint32_t sv[6][W], ev[6][W];
+#pragma unroll
+  for (int a = 0; a < 6; ++a)
+#pragma unroll
+    for (int i = 0; i < W; ++i) sv[a][i] = ev[a][i] = 0;
+#pragma unroll
+  for (int k = 0; k < G; ++k) {
+    uint32_t x, y, z;
+    cell_xyz(c0 + k, L, lgL, x, y, z);
+    const uint32_t w = ((x + y + z) & 1u ? cells1 : cells0)[(x >> 1) + H * (y + L * z)];
+    const uint32_t xo = (x & 1u) ? x : (x == 0 ? L - 1 : x - 1);
+    const uint32_t yo = (y & 1u) ? y : (y == 0 ? L - 1 : y - 1);
+    const uint32_t zo = (z & 1u) ? z : (z == 0 ? L - 1 : z - 1);
+    const uint32_t p = (x & 1u) | ((y & 1u) << 1) | ((z & 1u) << 2);
+    const uint32_t se = ce[(x >> 1) + H * ((y >> 1) + H * (z >> 1))];
+    const uint32_t so = co[(xo >> 1) + H * ((yo >> 1) + H * (zo >> 1))];
+    const uint32_t eta = (uint32_t)s_tab[se * 8 + p] | (uint32_t)s_tab[so * 8 + (p ^ 7u)];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+      sv[a][k >> 2] |= ((w >> (3 * a)) & 7u) << (8 * (k & 3));
+      ev[a][k >> 2] |= ((eta >> a) & 1u) << (8 * (k & 3));
+    }
+  }
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    ArmRow<G, kWide>::st(s + (size_t)a * N, q, sv[a]);
+    ArmRow<G, kWide>::st(ab + (size_t)a * N, q, ev[a]);
+  }
+}
+
 // Validation of a packed state (cvf_set_packed) already copied to the device: words words[0..nw)
 // must hold six sigma fields in 0..5 and zero bits 18..31, bytes cubes[0..ncb) cube states 0..8.
 // The smallest offending index goes to *bad (words first, then cube bytes at nw + i).
@@ -174,6 +293,33 @@ cudaError_t launch_pack_config(const ReplicaDesc& R, const int* c12, uint32_t* c
   if (vec) k_pack_cells<true><<<grid_of(N), kCfgCells, 0, s>>>(c12, L, H, R.lgL, N, cells0, cells1, eta6, bad);
   else k_pack_cells<false><<<grid_of(N), kCfgCells, 0, s>>>(c12, L, H, R.lgL, N, cells0, cells1, eta6, bad);
   k_pack_cubes<<<grid_of(2ull * H * H * H), kThreads, 0, s>>>(eta6, L, H, ce, co);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pack_arms(const ReplicaDesc& R, const uint8_t* sg, const uint8_t* ab, uint32_t* cells0,
+                             uint32_t* cells1, uint8_t* eta6, uint8_t* ce, uint8_t* co, unsigned long long* bad,
+                             cudaStream_t s) {
+  const uint32_t L = (uint32_t)R.L, H = (uint32_t)R.H, N = L * L * L;  // N is a multiple of 8
+  const uintptr_t al = (uintptr_t)sg | (uintptr_t)ab;
+  if ((al & 15u) == 0 && N % 16 == 0)
+    k_pack_arms<16, true><<<grid_of(N / 16), kThreads, 0, s>>>(sg, ab, L, H, R.lgL, N, cells0, cells1, eta6, bad);
+  else if ((al & 3u) == 0)
+    k_pack_arms<4, true><<<grid_of(N / 4), kThreads, 0, s>>>(sg, ab, L, H, R.lgL, N, cells0, cells1, eta6, bad);
+  else
+    k_pack_arms<4, false><<<grid_of(N / 4), kThreads, 0, s>>>(sg, ab, L, H, R.lgL, N, cells0, cells1, eta6, bad);
+  k_pack_cubes<<<grid_of(2ull * H * H * H), kThreads, 0, s>>>(eta6, L, H, ce, co);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_arms(const ReplicaDesc& R, uint8_t* sg, uint8_t* ab, cudaStream_t s) {
+  const uint32_t L = (uint32_t)R.L, H = (uint32_t)R.H, N = L * L * L;
+  const uintptr_t al = (uintptr_t)sg | (uintptr_t)ab;
+  if ((al & 15u) == 0 && N % 16 == 0)
+    k_unpack_arms<16, true><<<grid_of(N / 16), kThreads, 0, s>>>(R.cells[0], R.cells[1], R.cubes[0], R.cubes[1], L, H, R.lgL, N, sg, ab);
+  else if ((al & 3u) == 0)
+    k_unpack_arms<4, true><<<grid_of(N / 4), kThreads, 0, s>>>(R.cells[0], R.cells[1], R.cubes[0], R.cubes[1], L, H, R.lgL, N, sg, ab);
+  else
+    k_unpack_arms<4, false><<<grid_of(N / 4), kThreads, 0, s>>>(R.cells[0], R.cells[1], R.cubes[0], R.cubes[1], L, H, R.lgL, N, sg, ab);
   return cudaGetLastError();
 }
 

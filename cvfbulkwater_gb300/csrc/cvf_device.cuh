@@ -252,6 +252,12 @@ cudaError_t launch_pack_config(const ReplicaDesc& R, const int* c12, uint32_t* c
 // 16-byte aligned array in host memory (pageable-memory access); cudaErrorInvalidValue if the
 // array is not aligned.
 cudaError_t launch_unpack_config(const ReplicaDesc& R, int* c12, cudaStream_t s);
+// The same from / to the reference's host arrays s[arm*N + cell] and active_bond[arm*N + cell]
+// (one byte each) where they lie in host memory; *bad as for launch_pack_config.
+cudaError_t launch_pack_arms(const ReplicaDesc& R, const uint8_t* s, const uint8_t* active_bond, uint32_t* cells0,
+                             uint32_t* cells1, uint8_t* eta6, uint8_t* ce, uint8_t* co, unsigned long long* bad,
+                             cudaStream_t st);
+cudaError_t launch_unpack_arms(const ReplicaDesc& R, uint8_t* s, uint8_t* active_bond, cudaStream_t st);
 // Checks a packed state on the device (sigma fields in 0..5 with bits 18..31 zero in the nw
 // words, cube states 0..8 in the ncb bytes); *bad must start at nw + ncb and receives the smallest
 // offending index (cube byte i at nw + i).

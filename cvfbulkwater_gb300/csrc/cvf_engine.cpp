@@ -853,6 +853,80 @@ int cvf_get_config(cvf_handle* h, int r, int* c12, long long n_cells) {
   return 0;
 }
 
+// The reference's host arrays s[arm*N + cell] and active_bond[arm*N + cell] (GW:1135-1137 copies
+// them to the device, GW:1298 copies s back): checked and packed on the GPU where they lie in host
+// memory, or through the cells12 path.
+static std::string arms_value_error(const uint8_t* sg, const uint8_t* ab, long long N, long long c) {
+  for (int a = 0; a < 6; ++a) {
+    const int v = sg[a * N + c], e = ab[a * N + c];
+    if (v > 5) return "Unexpected value for spin (" + std::to_string(v) + ") appeared in cell " + std::to_string(c);
+    if (e > 1) return "Unexpected value for active_bond (" + std::to_string(e) + ") appeared in cell " + std::to_string(c);
+  }
+  return "invalid cell " + std::to_string(c);
+}
+
+int cvf_set_arms(cvf_handle* h, int r, const unsigned char* sg, const unsigned char* ab, long long n_sites) {
+  if (int rc = check_rep(h, r)) return rc;
+  ReplicaHost& R = h->reps[r];
+  if (!sg || !ab || n_sites != 6 * R.N) return fail(CVF_EINVAL, "s and active_bond must hold 6 N bytes each");
+  if (h->io_mode != 1 || h->nhb_mode) {
+    std::vector<int> c12((size_t)R.N * 12);
+    for (long long c = 0; c < R.N; ++c)
+      for (int a = 0; a < 6; ++a) {
+        if (sg[a * R.N + c] > 5 || ab[a * R.N + c] > 1) return fail(CVF_ECONFIG, arms_value_error(sg, ab, R.N, c));
+        c12[(size_t)c * 12 + a] = sg[a * R.N + c];
+        c12[(size_t)c * 12 + 6 + a] = ab[a * R.N + c];
+      }
+    return cvf_set_config(h, r, c12.data(), R.N);
+  }
+  h->count_valid = false;
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  if (int rc = ensure_io_scratch(h, R)) return rc;
+  const size_t half = (size_t)(R.N / 2), nc = (size_t)R.H * R.H * R.H;
+  uint32_t* d0 = (uint32_t*)h->io_scratch;
+  uint32_t* d1 = d0 + half;
+  uint8_t* eta6 = (uint8_t*)(d1 + half);
+  uint8_t* dce = eta6 + R.N;
+  uint8_t* dco = dce + nc;
+  unsigned long long bad = (unsigned long long)R.N;
+  CK(cudaMemcpyAsync(h->io_bad, &bad, sizeof(bad), cudaMemcpyHostToDevice, h->stream));
+  CK(launch_pack_arms(R.desc, sg, ab, d0, d1, eta6, dce, dco, h->io_bad, h->stream));
+  CK(cudaMemcpyAsync(&bad, h->io_bad, sizeof(bad), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  if (bad < (unsigned long long)R.N) return fail(CVF_ECONFIG, arms_value_error(sg, ab, R.N, (long long)bad));
+  CK(cudaMemcpyAsync(R.desc.cells[0], d0, half * 4, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(R.desc.cells[1], d1, half * 4, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(R.desc.cubes[0], dce, nc, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(R.desc.cubes[1], dco, nc, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int cvf_get_arms(cvf_handle* h, int r, unsigned char* sg, unsigned char* ab, long long n_sites) {
+  if (int rc = check_rep(h, r)) return rc;
+  ReplicaHost& R = h->reps[r];
+  if (!sg || !ab || n_sites != 6 * R.N) return fail(CVF_EINVAL, "s and active_bond must hold 6 N bytes each");
+  if (h->io_mode != 1 || h->nhb_mode) {
+    std::vector<int> c12((size_t)R.N * 12);
+    if (int rc = cvf_get_config(h, r, c12.data(), R.N)) return rc;
+    for (long long c = 0; c < R.N; ++c)
+      for (int a = 0; a < 6; ++a) {
+        sg[a * R.N + c] = (unsigned char)c12[(size_t)c * 12 + a];
+        ab[a * R.N + c] = (unsigned char)c12[(size_t)c * 12 + 6 + a];
+      }
+    return 0;
+  }
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  // the GPU writes the caller's arrays in place, into pages host threads have made present first
+  touch_pages(sg, (size_t)(6 * R.N));
+  touch_pages(ab, (size_t)(6 * R.N));
+  CK(launch_unpack_arms(R.desc, sg, ab, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
 // Packed state of one replica: the colour-0 words, the colour-1 words, the even-origin cube
 // states, the odd-origin cube states, exactly as the replica holds them on the device.
 static long long packed_bytes(const ReplicaHost& R) { return 4 * R.N + 2LL * R.H * R.H * R.H; }

@@ -89,6 +89,23 @@ class Lattice:
         check(lib().cvf_get_config(self._h, r, _ptr(a), self.N(r)))
         return a
 
+    def set_arms(self, s: np.ndarray, active_bond: np.ndarray, r: int = 0):
+        """The reference's host arrays s[arm*N + cell] and active_bond[arm*N + cell] (uint8)."""
+        a = np.ascontiguousarray(s, dtype=np.uint8).reshape(-1)
+        b = np.ascontiguousarray(active_bond, dtype=np.uint8).reshape(-1)
+        check(lib().cvf_set_arms(self._h, r, _ptr(a), _ptr(b), a.size))
+
+    def get_arms(self, r: int = 0, out=None):
+        """(s, active_bond) of replica r as uint8 arrays of 6N bytes (arm-major); pass `out`, a pair
+        of such arrays, to reuse buffers."""
+        n = 6 * self.N(r)
+        a, b = (np.empty(n, dtype=np.uint8), np.empty(n, dtype=np.uint8)) if out is None else out
+        for x in (a, b):
+            if x.dtype != np.uint8 or x.size != n or not x.flags.c_contiguous:
+                raise ValueError("out must hold two C-contiguous uint8 arrays of 6 N bytes")
+        check(lib().cvf_get_arms(self._h, r, _ptr(a), _ptr(b), n))
+        return a, b
+
     def packed_size(self, r: int = 0) -> int:
         n = C.c_longlong()
         check(lib().cvf_packed_size(self._h, r, C.byref(n)))

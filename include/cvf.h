@@ -111,6 +111,15 @@ int cvf_num_replicas(const cvf_handle* h);
 int cvf_set_config(cvf_handle* h, int replica, const int* cells12, long long n_cells);
 /* Replaces the config.out writer GW:1296-1305. */
 int cvf_get_config(cvf_handle* h, int replica, int* cells12, long long n_cells);
+/* The reference's own host arrays: s[arm*N + cell] (sigma 0..5) and active_bond[arm*N + cell]
+ * (eta 0/1), one byte each, 6N bytes per array (replaces the cudaMemcpy of s and active_bond to
+ * dev_s / dev_active_bond, GW:1135-1137, and of dev_s back to s, GW:1298). Same checks and
+ * cube-state inference as cvf_set_config (CVF_ECONFIG names the first bad cell; the lattice is
+ * then unchanged); cvf_get_arms writes eta as the cubes give it. 12 bytes per cell cross the
+ * host link instead of the 48 of cells12. */
+int cvf_set_arms(cvf_handle* h, int replica, const unsigned char* s, const unsigned char* active_bond,
+                 long long n_sites);
+int cvf_get_arms(cvf_handle* h, int replica, unsigned char* s, unsigned char* active_bond, long long n_sites);
 
 /* Packed state of a replica, for checkpoint and resume without the text format: the engine's own
  * device layout, 4 N + 2 (L/2)^3 bytes (about 4.25 bytes per cell against the 48 of cells12):
