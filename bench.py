@@ -87,16 +87,27 @@ class Clocks:
         self.gpu = gpu
         self.proc = None
         self.path = None
+        self.skip = 0
 
     def start(self):
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        # the sampler takes a moment to start: wait (at most 3 s) for its first line, so that the
+        # timed region that follows is sampled from its start
+        t0 = time.time()
+        while time.time() - t0 < 3.0 and self.proc.poll() is None:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.01)
+        with open(self.path) as f:
+            self.skip = sum(1 for _ in f)  # lines written before the timed region
 
     def stop(self):
         if not self.proc:
@@ -116,6 +127,8 @@ class Clocks:
             except ValueError:
                 continue
         os.unlink(self.path)
+        if len(rows) > self.skip:
+            rows = rows[self.skip:]  # the samples taken while the timed region ran
         if not rows:
             return None
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
