@@ -76,8 +76,63 @@ class Dist:
             self.td.destroy_process_group()
 
 
+class NvmlClocks:
+    """Reads SM clocks and clock-event reasons through NVML (libnvidia-ml, read-only queries) from
+    a thread every 2 ms while the timed region runs; None when NVML cannot be loaded."""
+
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown", 0x4: "sw_power_cap"}
+
+    def __init__(self, gpu: int):
+        import ctypes as C
+        import threading
+        self.C, self.threading = C, threading
+        self.lib = C.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = C.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(gpu), C.byref(self.h)) != 0:
+            raise OSError("no NVML handle")
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.rows, self.stop_flag, self.thread = [], False, None
+
+    def _sample(self):
+        C = self.C
+        mhz, mx, rs = C.c_uint(), C.c_uint(), C.c_ulonglong()
+        while not self.stop_flag:
+            if (self.lib.nvmlDeviceGetClockInfo(self.h, 1, C.byref(mhz)) == 0 and
+                    self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, C.byref(mx)) == 0 and
+                    self.reasons_fn(self.h, C.byref(rs)) == 0):
+                self.rows.append((mhz.value, mx.value, rs.value))
+            time.sleep(0.002)
+
+    def start(self):
+        self.thread = self.threading.Thread(target=self._sample, daemon=True)
+        self.thread.start()
+
+    def stop(self):
+        self.stop_flag = True
+        self.thread.join(timeout=5)
+        try:
+            self.lib.nvmlShutdown()
+        except Exception:
+            pass
+        if not self.rows:
+            return None
+        reasons = sorted({n for _, _, r in self.rows for b, n in self.REASONS.items() if r & b})
+        return {"sm_mhz": float(np.median([r[0] for r in self.rows])), "sm_max_mhz": float(max(r[1] for r in self.rows)),
+                "reasons": reasons, "samples": len(self.rows), "source": "NVML, every 2 ms"}
+
+
 class Clocks:
-    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+    """Samples SM clocks and throttle reasons while the timed region runs: through NVML when the
+    library loads, else with nvidia-smi."""
+
+    def __new__(cls, gpu: int):
+        try:
+            return NvmlClocks(gpu)
+        except (OSError, AttributeError):
+            return super().__new__(cls)
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
