@@ -9,10 +9,10 @@
                         CVF_ThermodynamicAnalysis/*.c, compiled as they are with gcc (tools()).
 
 Run where the reference checkout exists: its path is the argument, else the environment variable
-CVF_REFERENCE_DIR, else the checkout's location in the build container (DEFAULT_CHECKOUT, the one
-place the repository names it). Where none exists (the GPU box) every call returns None or {}
-and the tests that need these builds skip. Nothing from the reference is copied into the repository; the output stays in the
-git-ignored oracle/_ref/.
+CVF_REFERENCE_DIR (__graft_entry__.build() passes it). Without a checkout every call returns what
+an earlier build left in oracle/_ref/ (None or {} where nothing was built, as on the GPU machine), and
+the tests that need these builds skip. Nothing from the reference is copied into the repository;
+the output stays in the git-ignored oracle/_ref/.
 """
 from __future__ import annotations
 
@@ -21,12 +21,11 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_CHECKOUT = "/root/reference"
 
 
 def checkout(ref: str | None = None) -> str | None:
-    """The reference checkout to build from, or None where there is none."""
-    for cand in (ref, os.environ.get("CVF_REFERENCE_DIR"), DEFAULT_CHECKOUT):
+    """The reference checkout to build from (the argument, else CVF_REFERENCE_DIR), or None."""
+    for cand in (ref, os.environ.get("CVF_REFERENCE_DIR")):
         if cand and os.path.isdir(os.path.join(cand, "SOURCE")):
             return cand
     return None
@@ -37,7 +36,7 @@ LIB = os.path.join(OUT, "libref_correlator.so")
 def build(ref: str | None = None, force: bool = False):
     ref = checkout(ref)
     if ref is None:
-        return None
+        return LIB if os.path.exists(LIB) else None
     src = os.path.join(ref, "SOURCE", "gpu_water3D.cu")
     if not os.path.exists(src):
         return None
@@ -68,7 +67,8 @@ def tools(ref: str | None = None):
     gcc -O2 (empty where the checkout is absent)."""
     ref = checkout(ref)
     if ref is None:
-        return {}
+        built = {name: os.path.join(OUT, name) for name in TOOLS}
+        return built if all(os.path.exists(p) for p in built.values()) else {}
     src_dir = os.path.join(ref, "CVF_ThermodynamicAnalysis")
     out = {}
     for name in TOOLS:
