@@ -88,3 +88,18 @@ def test_arms_nhb_mode(engine_lib, oracle_mod):
     ora.step(1, 0)
     assert np.array_equal(eng.get_arms()[0], _to_arms(ora.get_config())[0])
     eng.close()
+
+
+def test_arms_batch_replica_and_sizes(engine_lib, oracle_mod):
+    """A batch replica takes its own arrays; a wrong size is CVF_EINVAL."""
+    specs = [(8, 0.7), (12, 0.6)]
+    eng = Lattice([Params(L=L, T=T, P=0.45, seed=600 + i, start=1, replica=i) for i, (L, T) in enumerate(specs)])
+    ora = oracle_mod.Oracle(12, 0.6, 0.45, 601, 6.0, 1, 0)
+    s, ab = _to_arms(ora.get_config())
+    eng.set_arms(s, ab, r=1)
+    assert np.array_equal(eng.get_config(1), ora.get_config())
+    got = eng.get_arms(1)
+    assert np.array_equal(got[0], s) and np.array_equal(got[1], ab)
+    assert abi.lib().cvf_set_arms(eng._h, 1, s.ctypes.data, ab.ctypes.data, s.size - 1) == -1
+    assert abi.lib().cvf_get_arms(eng._h, 0, s.ctypes.data, ab.ctypes.data, s.size) == -1  # replica 0 is L=8
+    eng.close()
