@@ -315,7 +315,18 @@ def bench_batch64(steps, warmup, local, flush, verify=4):
             "batched_site_updates_per_ns": round(cells * steps / (t_batch * 1e6), 4),
             "plain_site_updates_per_ns": round(cells * steps / (t_plain * 1e6), 4),
             "speedup": round(t_plain / t_batch, 2), "identical_chains_checked": verify, "identical": same,
-            "l2": "256 MB write before every timed step in both arms"}
+            "l2": "256 MB write before every timed step in both arms", "occupancy": batch_occupancy()}
+
+
+def batch_occupancy():
+    """SM occupancy of the batch's kernels (achieved and theoretical warps per SM, waves) from the
+    committed ncu summary of the same workload; None where the summary is absent."""
+    p = os.path.join(ROOT, "profiles", "batch64_occupancy.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return dict(d["summary"], source="profiles/batch64_occupancy.json")
 
 
 def sample_columns(lat, smp, r=0):

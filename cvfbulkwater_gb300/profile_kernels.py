@@ -7,7 +7,9 @@ and then --launches profiled repetitions of the chosen kind: a single kernel kin
 cvf_profile_launch (sweep = 2 launches per repetition), or whole steps (kind "step": cube +
 volume + sweep; kind "step_sw": cube + volume + one Swendsen-Wang step; kind "step_wolff": cube +
 volume + one Wolff step; --correlation adds
-the multi-tau correlator's histogram and update to every step).
+the multi-tau correlator's histogram and update to every step). Kind "batch64" runs the steps of
+the 64-replica batch (L drawn from {16,24,32,48,64} with seed 20261203, the 8x8 grid T 0.55..0.95
+x P 0..0.60, disordered starts, seeds 44648604 + replica) with the 4-cell sweep tile.
 Prints the mean time per repetition measured with CUDA events on the engine's stream. Kind
 "c2c" times the configuration transfers against plain copies over the host link, kind
 "h2d_scan" the 2-D reweighting search.
@@ -20,7 +22,21 @@ import ctypes as C
 KINDS = {"sweep": 0, "cube": 1, "volume": 2, "measure": 3}
 ANALYSIS = ("h2d_scan", "c2c")
 # full MC steps: (Metropolis sweeps, cluster steps); step_wolff's cluster steps are Wolff steps
-STEPS = {"step": (1, 0), "step_sw": (0, 1), "step_wolff": (0, 1)}
+STEPS = {"step": (1, 0), "step_sw": (0, 1), "step_wolff": (0, 1), "batch64": (1, 0)}
+
+
+def batch64_params():
+    """The 64-replica batch: L drawn from {16,24,32,48,64}, T on 8 points of [0.55, 0.95], P on 8
+    points of [0, 0.60], disordered starts."""
+    import numpy as np
+
+    from .engine import Params
+    rng = np.random.default_rng(20261203)
+    Ls = rng.choice([16, 24, 32, 48, 64], size=64)
+    Ts = np.linspace(0.55, 0.95, 8)
+    Ps = np.linspace(0.0, 0.60, 8)
+    return [Params(L=int(Ls[i]), T=float(Ts[i % 8]), P=float(Ps[i // 8]), seed=44648604 + i, start=0, replica=i)
+            for i in range(64)]
 
 
 def main():
@@ -49,7 +65,11 @@ def main():
         return h2d_scan(a)
     if a.kind == "c2c":
         return c2c(a)
-    lat = Lattice(Params(L=a.L, T=a.T, P=a.P, seed=44648604, start=a.start, flag_chessboard=0 if a.nhb else 1))
+    if a.kind == "batch64":
+        lat = Lattice(batch64_params())
+        lat.set_sweep_tile(4)
+    else:
+        lat = Lattice(Params(L=a.L, T=a.T, P=a.P, seed=44648604, start=a.start, flag_chessboard=0 if a.nhb else 1))
     if a.mode is not None:
         lat.launch_mode = a.mode
     if a.correlation:
