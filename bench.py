@@ -509,9 +509,11 @@ def independent_run_check(runs, pts, N, reweighted, nb=20):
     return out
 
 
-def bench_plain_l16(steps, warmup, local, flush):
+def bench_plain_l16(steps, warmup, local, flush, cpu=True):
     """Plain small run: L=16, disordered start, T=0.815, P=0.45, 1 sweep + volume + cube per step.
-    Launch-latency bound, so the per-step time inside a 32-step graph replay is reported too."""
+    Launch-latency bound, so the per-step time inside a 32-step graph replay is reported too. With
+    cpu, the oracle's steps/s on one host core over the first 2000 steps of the same chain, and
+    whether its lattice after them equals the engine's."""
     import torch
     from cvfbulkwater_gb300.engine import Lattice, Params
     lat = Lattice(Params(L=16, T=0.815, P=0.45, seed=SEED, start=0, device=local))
@@ -541,13 +543,29 @@ def bench_plain_l16(steps, warmup, local, flush):
     def mean_err(x):
         b = x[: len(x) // 20 * 20].reshape(20, -1).mean(1)
         return [round(float(x.mean()), 6), round(float(b.std(ddof=1) / np.sqrt(20)), 6)]
-    return {"workload": "L=16 disordered start, T=0.815, P=0.45, 1 cube + 1 volume move + 1 sweep per step",
-            "steps_per_s": round(steps / (ms / 1e3), 1), "site_updates_per_ns": round(4096 * steps / (ms * 1e6), 4),
-            "graph_replay_us_per_step": round(replay_us, 3),
-            "sampled_run": {"steps": 11000, "records": int(len(smp)), "wall_s": round(wall, 3),
-                            "per_cell_mean_and_20_block_error": {
-                                "E": mean_err(e / 4096), "V": mean_err(v / 4096), "rho": mean_err(4096 / v),
-                                "N_hb": mean_err(nhb / 4096)}}}
+    out = {"workload": "L=16 disordered start, T=0.815, P=0.45, 1 cube + 1 volume move + 1 sweep per step",
+           "steps_per_s": round(steps / (ms / 1e3), 1), "site_updates_per_ns": round(4096 * steps / (ms * 1e6), 4),
+           "graph_replay_us_per_step": round(replay_us, 3),
+           "sampled_run": {"steps": 11000, "records": int(len(smp)), "wall_s": round(wall, 3),
+                           "per_cell_mean_and_20_block_error": {
+                               "E": mean_err(e / 4096), "V": mean_err(v / 4096), "rho": mean_err(4096 / v),
+                               "N_hb": mean_err(nhb / 4096)}}}
+    if cpu:
+        from oracle import oracle as O
+        n = 2000
+        lat = Lattice(Params(L=16, T=0.815, P=0.45, seed=SEED, start=0, device=local))
+        lat.run(n, 1, 0)
+        o = O.Oracle(16, 0.815, 0.45, SEED, 6.0, 0, 0)
+        t0 = time.perf_counter()
+        for _ in range(n):
+            o.step(1, 0)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"steps_per_s": round(n / dt, 1), "site_updates_per_ns": round(4096 * n / (dt * 1e9), 6),
+                               "cores": 1, "kind": "port", "sample": f"the first {n} steps of the same chain",
+                               "identical_lattice": bool(np.array_equal(lat.get_config(), o.get_config()))}
+        lat.close()
+        o.close()
+    return out
 
 
 def bench_sw(steps, warmup, local, flush):
@@ -705,6 +723,7 @@ def run_engine(args):
     # headline uses the reference's own host arrays (s and active_bond, one byte per arm each:
     # what GW:1135-1137 copies to the device and GW:1298 copies back).
     lat2 = Lattice(Params(L=L, T=T_BENCH, P=P_BENCH, seed=SEED + 7 + rank, start=1, replica=rank, device=local))
+    lat2.set_sweep_tile(tile)  # tuned once like the handle above (a fresh handle starts at 4 cells)
     host_s, host_ab = lat.get_arms()
     out_arms = (np.zeros_like(host_s), np.zeros_like(host_ab))  # a caller's reusable result buffers
     lat2.set_arms(host_s, host_ab)
@@ -728,7 +747,7 @@ def run_engine(args):
            "d2h_bytes_per_step": int(round(arm_bytes / args.steps)) + 32,
            "upload_ms": round(1e3 * (ta - t0), 3), "steps_ms": round(1e3 * (tb - ta), 3),
            "download_ms": round(1e3 * (t1 - tb), 3),
-           "note": "per step: cvf_run_steps(1 step) + cvf_observables (measurement, 32 B D2H, sync); "
+           "note": "per step: cvf_run_steps(1 step, measured on its colour-1 sweep) + cvf_observables (the record, 32 B D2H, sync); "
                    "lattice upload (cvf_set_arms: the caller's s and active_bond arrays, 201 MB, read and "
                    "packed by the GPU in host memory) and download (cvf_get_arms: unpacked by the GPU into "
                    "the caller's arrays) amortised over the K steps"}
@@ -760,7 +779,7 @@ def run_engine(args):
            "d2h_bytes_per_step": int(round(cells12_bytes / args.steps)) + 32,
            "upload_ms": round(1e3 * (ta - t0), 3), "steps_ms": round(1e3 * (tb - ta), 3),
            "download_ms": round(1e3 * (t1 - tb), 3),
-           "note": "per step: cvf_run_steps(1 step) + cvf_observables (measurement, 32 B D2H, sync); "
+           "note": "per step: cvf_run_steps(1 step, measured on its colour-1 sweep) + cvf_observables (the record, 32 B D2H, sync); "
                    "lattice upload (cvf_set_config: the caller's 805 MB cells12 array read and packed "
                    "by the GPU in host memory, io_mode 1) and download (cvf_get_config: unpacked by the "
                    "GPU into the caller's array) amortised over the K steps"}
@@ -822,7 +841,8 @@ def run_engine(args):
         extras["batched"] = bench_batch64(max(10, min(args.steps, 50)), args.warmup, local, flush)
         extras["swendsen_wang"] = bench_sw(max(10, min(args.steps, 30)), args.warmup, local, flush)
         extras["wolff"] = bench_wolff(local)
-        extras["plain_l16"] = bench_plain_l16(max(10, min(args.steps, 50)), args.warmup, local, flush)
+        extras["plain_l16"] = bench_plain_l16(max(10, min(args.steps, 50)), args.warmup, local, flush,
+                                              cpu=not args.no_cpu_baseline)
         extras["differentiation"] = bench_differentiation(local)
         if not args.no_cpu_baseline:
             extras["cpu_baseline_1thread"] = cpu_baseline_oracle(steps_cap=1, budget_s=10.0, threads=1)

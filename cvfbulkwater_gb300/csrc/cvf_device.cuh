@@ -94,10 +94,6 @@ struct ReplicaState {
   CStatsRec* cstats;    // device cluster-statistics stream
   SampleRec last;
   CStatsRec last_cstats;
-  // Running counts for cvf_observables: the counts of the last full measurement plus the
-  // changes the counting kernels added since (two's complement in slot block % 32)
-  long long base_hb2, base_ns;
-  unsigned long long dlt_slot[2][32];
   // Wolff cluster steps: the poke counter (the random streams of poke P) and the last step's
   // pokes, summed cluster sizes and largest cluster
   unsigned long long wpoke;
@@ -167,9 +163,6 @@ struct BatchDev {
   int* blk_site4;       // one thread per 4 arm sites
   int* blk_cell4;       // one thread per 4 cell words
   int nblk_sweep, nblk_cube, nblk_cubev, nblk_cell, nblk_site, nblk_site4, nblk_cell4;
-  int vec_count;        // tile of the counting sweep: vec, at most 4 (8 would spill registers)
-  int* blk_sweep_count; // its block prefix table
-  int nblk_sweep_count;
   int max_L;            // largest edge among the replicas
   int pdl;              // launch the step's kernels as programmatic dependents (launch_pdl)
   GridSync* gsync;      // device barrier state of the persistent step kernel
@@ -194,24 +187,18 @@ void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do
                        int zero_slots = 0);
 // Cube moves of all replicas (do_cubes) and, in extra blocks of the same launch, their volume
 // moves (do_volume): the two moves are independent, so the volume move hides under the cubes.
-// count: the counting variants also add the changes of N_hb and N_sigma they make to the
-// replicas' running counts (dlt_slot).
 // soff >= 0: the step is step soff of a chunk whose kernels take their counters as offsets from
 // ctr (no k_step_begin; launch_chunk_end after the chunk); soff < 0: the counters of cur.
-void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, bool count = false,
-                        int soff = -1);
+void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, int soff = -1);
 void launch_chunk_end(const BatchDev& b, int steps, int nmet, int ncl, int do_volume, cudaStream_t s);
 void launch_volume_chain(const BatchDev& b, int steps, cudaStream_t s);
 cudaError_t launch_chunk_cluster(const BatchDev& b, int steps, int nmet, cudaStream_t s);
 // jsweep: the sweep's offset from cur[0], or with from_ctr from ctr[0] (step i, sweep j of a chunk:
 // i * nmet + j).
-void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, bool count = false, int from_ctr = 0);
-// The running counts into every replica's last record (with its r_cell and volume; appended to
-// the sample stream when record is set), and the re-basing after a full measurement (base =
-// last record, changes zeroed).
-void launch_count_read(const BatchDev& b, cudaStream_t s, int record, SampleRec* host_out = nullptr,
-                       int host_r = -1);
-void launch_count_rebase(const BatchDev& b, cudaStream_t s);
+void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, int from_ctr = 0);
+// Replica host_r's last record with its current r_cell and volume into host_out (mapped
+// page-locked host memory).
+void launch_last_read(const BatchDev& b, cudaStream_t s, SampleRec* host_out, int host_r);
 void launch_measure(const BatchDev& b, int record, cudaStream_t s);
 // Colour-1 sweep jsweep fused with the measurement of the step (slots zeroed by the step's
 // launch_step_begin), and the summation of the slots into the replica's record.

@@ -81,11 +81,10 @@ struct cvf_handle {
   // Flag_chessboard = 0 for every replica: the nhb<=4 compatibility mode (no cube moves, bond
   // counts per cell, per-arm sweep launches, greedy bond count in the measurement)
   bool nhb_mode = false;
-  // Running counts for cvf_observables: a run right after cvf_observables uses the counting
-  // kernels, which add the changes of N_hb and N_sigma they make to the counts of the last full
-  // measurement; while every step since then counted, cvf_observables reads those counts
-  // instead of measuring the lattice again.
-  bool count_valid = false;
+  // Every replica's last record (st.last) holds the measurement of its current cells:
+  // cvf_observables then reads it instead of measuring the lattice. A Metropolis-only run that
+  // follows cvf_observables measures its last step, so the read after it finds it there.
+  bool last_valid = false;
   bool obs_since_run = false;
   cudaGraphExec_t nhb_read = nullptr;  // Flag_chessboard = 0: the read's 3L + 1 launches, captured once
   struct Group {
@@ -182,9 +181,8 @@ static int build_tables(cvf_handle* h, int force_vec = 0) {
 // Block prefix tables of replicas [r0, r1) (a new device allocation) into b.
 static int fill_tables(cvf_handle* h, int r0, int r1, int vec, BatchDev& b) {
   const int n = r1 - r0;
-  const int vec_count = vec < 4 ? vec : 4;
-  std::vector<int> ts(n + 1), tc(n + 1), tcv(n + 1), tl(n + 1), tsi(n + 1), ts4(n + 1), tl4(n + 1), tsc(n + 1);
-  ts[0] = tc[0] = tcv[0] = tl[0] = tsi[0] = ts4[0] = tl4[0] = tsc[0] = 0;
+  std::vector<int> ts(n + 1), tc(n + 1), tcv(n + 1), tl(n + 1), tsi(n + 1), ts4(n + 1), tl4(n + 1);
+  ts[0] = tc[0] = tcv[0] = tl[0] = tsi[0] = ts4[0] = tl4[0] = 0;
   auto blocks = [](long long threads) { return (int)((threads + kThreads - 1) / kThreads); };
   for (int i = 0; i < n; ++i) {
     const auto& r = h->reps[r0 + i];
@@ -196,10 +194,9 @@ static int fill_tables(cvf_handle* h, int r0, int r1, int vec, BatchDev& b) {
     tsi[i + 1] = tsi[i] + blocks(6 * r.N);
     ts4[i + 1] = ts4[i] + blocks(6 * r.N / 4);
     tl4[i + 1] = tl4[i] + blocks(r.N / 4);
-    tsc[i + 1] = tsc[i] + blocks((H / vec_count) * L * L);
   }
   int* d;
-  if (int rc = dev_alloc(h, (void**)&d, sizeof(int) * 8 * (n + 1))) return rc;
+  if (int rc = dev_alloc(h, (void**)&d, sizeof(int) * 7 * (n + 1))) return rc;
   std::vector<int> all;
   all.insert(all.end(), ts.begin(), ts.end());
   all.insert(all.end(), tc.begin(), tc.end());
@@ -208,7 +205,6 @@ static int fill_tables(cvf_handle* h, int r0, int r1, int vec, BatchDev& b) {
   all.insert(all.end(), ts4.begin(), ts4.end());
   all.insert(all.end(), tcv.begin(), tcv.end());
   all.insert(all.end(), tl4.begin(), tl4.end());
-  all.insert(all.end(), tsc.begin(), tsc.end());
   CK(cudaMemcpy(d, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
   b.blk_sweep = d;
   b.blk_cube = d + (n + 1);
@@ -217,9 +213,6 @@ static int fill_tables(cvf_handle* h, int r0, int r1, int vec, BatchDev& b) {
   b.blk_site4 = d + 4 * (n + 1);
   b.blk_cubev = d + 5 * (n + 1);
   b.blk_cell4 = d + 6 * (n + 1);
-  b.blk_sweep_count = d + 7 * (n + 1);
-  b.vec_count = vec_count;
-  b.nblk_sweep_count = tsc[n];
   b.nblk_cell4 = tl4[n];
   b.nblk_cubev = tcv[n];
   b.nblk_site4 = ts4[n];
@@ -344,12 +337,12 @@ static void launch_cluster_step(const BatchDev& b, int jsw, cudaStream_t s, int 
 
 // volume: the step's volume move in the cube kernel (false when a side branch runs the chunk's
 // volume moves).
-static void enqueue_step(cvf_handle* h, int nmet, int ncl, bool count = false, bool volume = true) {
+static void enqueue_step(cvf_handle* h, int nmet, int ncl, bool volume = true) {
   launch_step_begin(h->b, nmet, ncl, 1, volume ? 1 : 0, h->stream);
-  launch_cube_volume(h->b, 1, volume ? 1 : 0, h->stream, count);
+  launch_cube_volume(h->b, 1, volume ? 1 : 0, h->stream);
   for (int j = 0; j < nmet; ++j) {
-    launch_sweep(h->b, 0, j, h->stream, count);
-    launch_sweep(h->b, 1, j, h->stream, count);
+    launch_sweep(h->b, 0, j, h->stream);
+    launch_sweep(h->b, 1, j, h->stream);
   }
   for (int j = 0; j < ncl; ++j) launch_cluster_step(h->b, j, h->stream);
 }
@@ -357,18 +350,19 @@ static void enqueue_step(cvf_handle* h, int nmet, int ncl, bool count = false, b
 // Step i of a chunk without records: the kernels take their counters as offsets from ctr (cube
 // ctr[1] + i, volume ctr[2] + i, sweep j ctr[0] + i*nmet + j, SW step j ctr[3] + i*ncl + j), and
 // one launch_chunk_end after the chunk advances the counters, instead of one k_step_begin per step.
-static void enqueue_step_at(const BatchDev& b, cudaStream_t s, int nmet, int ncl, bool count, bool volume, int i) {
-  launch_cube_volume(b, 1, volume ? 1 : 0, s, count, i);
+static void enqueue_step_at(const BatchDev& b, cudaStream_t s, int nmet, int ncl, bool volume, int i) {
+  launch_cube_volume(b, 1, volume ? 1 : 0, s, i);
   for (int j = 0; j < nmet; ++j) {
-    launch_sweep(b, 0, i * nmet + j, s, count, 1);
-    launch_sweep(b, 1, i * nmet + j, s, count, 1);
+    launch_sweep(b, 0, i * nmet + j, s, 1);
+    launch_sweep(b, 1, i * nmet + j, s, 1);
   }
   for (int j = 0; j < ncl; ++j) launch_cluster_step(b, i * ncl + j, s, 1);
 }
 
 // A Metropolis-only step followed by a recorded measurement: the measurement rides on the last
-// colour-1 sweep (slots zeroed by the step's begin kernel), then the slots are summed.
-static void enqueue_recorded_metropolis_step(cvf_handle* h, int nmet) {
+// colour-1 sweep (slots zeroed by the step's begin kernel), then the slots are summed into the
+// last record (appended to the sample stream when keep is set).
+static void enqueue_recorded_metropolis_step(cvf_handle* h, int nmet, int keep = 1) {
   launch_step_begin(h->b, nmet, 0, 1, 1, h->stream, 1);
   launch_cube_volume(h->b, 1, 1, h->stream);
   for (int j = 0; j < nmet; ++j) {
@@ -376,12 +370,13 @@ static void enqueue_recorded_metropolis_step(cvf_handle* h, int nmet) {
     if (j + 1 < nmet) launch_sweep(h->b, 1, j, h->stream);
     else launch_sweep_measure(h->b, j, h->stream);
   }
-  launch_measure_end(h->b, 1, h->stream);
+  launch_measure_end(h->b, keep, h->stream);
 }
 
 // One Metropolis-only step of the replicas of view b on stream s, with the recorded measurement
-// when record is set and the correlator step when corr is set.
-static void enqueue_metropolis_on(const BatchDev& b, cudaStream_t s, int nmet, bool record, bool corr) {
+// when record is set (appended to the sample stream when keep is set) and the correlator step
+// when corr is set.
+static void enqueue_metropolis_on(const BatchDev& b, cudaStream_t s, int nmet, bool record, bool corr, int keep = 1) {
   if (record && nmet > 0) {
     launch_step_begin(b, nmet, 0, 1, 1, s, 1);
     launch_cube_volume(b, 1, 1, s);
@@ -390,7 +385,7 @@ static void enqueue_metropolis_on(const BatchDev& b, cudaStream_t s, int nmet, b
       if (j + 1 < nmet) launch_sweep(b, 1, j, s);
       else launch_sweep_measure(b, j, s);
     }
-    launch_measure_end(b, 1, s);
+    launch_measure_end(b, keep, s);
   } else {
     launch_step_begin(b, nmet, 0, 1, 1, s);
     launch_cube_volume(b, 1, 1, s);
@@ -398,7 +393,7 @@ static void enqueue_metropolis_on(const BatchDev& b, cudaStream_t s, int nmet, b
       launch_sweep(b, 0, j, s);
       launch_sweep(b, 1, j, s);
     }
-    if (record) launch_measure(b, 1, s);
+    if (record) launch_measure(b, keep, s);
   }
   if (corr) launch_corr_step(b, s);
 }
@@ -414,21 +409,20 @@ static void enqueue_cstats(cvf_handle* h, int record) {
 
 // Graph of `steps` MC steps; when record is set, step i is followed by a recorded measurement (and
 // cluster statistics when ncl > 0) for every i with i % rec_every == 0 (rec_every = 0: the first
-// step only), so one graph can hold several intervals of a sampled run.
-// count: plain steps with the counting kernels (ungrouped per-phase capture; with record, the
-// records are read from the running counts).
+// step only), so one graph can hold several intervals of a sampled run. record = 2: the
+// measurement of Metropolis-only steps is kept as the replicas' last record only (no sample).
 static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cudaGraphExec_t* out,
-                     bool count = false, int rec_every = 0) {
+                     int rec_every = 0) {
   if (!record) rec_every = 0;
   const auto rec_at = [&](int i) { return record && (rec_every > 0 ? i % rec_every == 0 : i == 0); };
-  auto key = std::make_tuple(steps, nmet, ncl, record | (count ? 2 : 0) | (rec_every << 2));
+  auto key = std::make_tuple(steps, nmet, ncl, record | (rec_every << 2));
   auto it = h->graphs.find(key);
   if (it != h->graphs.end()) {
     *out = it->second;
     return 0;
   }
   cudaGraph_t g;
-  if (h->launch_mode == 1 && ncl == 0 && !h->corr_on && !h->nhb_mode && !count) {
+  if (h->launch_mode == 1 && ncl == 0 && !h->corr_on && !h->nhb_mode && record != 2) {
     // one persistent launch; a driver that cannot capture a cooperative launch leaves the
     // handle on the per-phase kernels
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -449,17 +443,17 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     cudaGetLastError();
     h->launch_mode = 0;
   }
-  if (ncl == 0 && group_count(h) > 1 && !h->nhb_mode && !count) {
+  if (ncl == 0 && group_count(h) > 1 && !h->nhb_mode) {
     if (int rc = build_groups(h)) return rc;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     CK(cudaEventRecord(h->fork, h->stream));
     for (auto& gr : h->groups) CK(cudaStreamWaitEvent(gr.s, h->fork, 0));
     for (auto& gr : h->groups) {
       if (record) {
-        for (int i = 0; i < steps; ++i) enqueue_metropolis_on(gr.b, gr.s, nmet, rec_at(i), h->corr_on);
+        for (int i = 0; i < steps; ++i) enqueue_metropolis_on(gr.b, gr.s, nmet, rec_at(i), h->corr_on, record == 1);
       } else {
         for (int i = 0; i < steps; ++i) {
-          enqueue_step_at(gr.b, gr.s, nmet, 0, false, true, i);
+          enqueue_step_at(gr.b, gr.s, nmet, 0, true, i);
           if (h->corr_on) launch_corr_step(gr.b, gr.s);
         }
         launch_chunk_end(gr.b, steps, nmet, 0, 1, gr.s);
@@ -515,28 +509,24 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
   int max_cells = 0;
   for (const auto& r : h->reps) max_cells = std::max(max_cells, (int)r.N);
   bool clustered = false;
-  if (side && !count && ncl == 0 && nmet > 0 && !h->corr_on && max_cells <= (1 << 14)) {
+  if (side && ncl == 0 && nmet > 0 && !h->corr_on && max_cells <= (1 << 14)) {
     clustered = launch_chunk_cluster(h->b, steps, nmet, h->stream) == cudaSuccess;
     if (!clustered) cudaGetLastError();
   }
   // chunks without records take their counters as offsets (one end kernel per chunk)
   const bool offsets = !record && !h->nhb_mode && !clustered && steps > 0;
   for (int i = 0; i < steps && offsets; ++i) {
-    enqueue_step_at(h->b, h->stream, nmet, ncl, count, !side, i);
+    enqueue_step_at(h->b, h->stream, nmet, ncl, !side, i);
     if (h->corr_on) launch_corr_step(h->b, h->stream);
   }
   if (offsets) launch_chunk_end(h->b, steps, nmet, ncl, side ? 0 : 1, h->stream);
   for (int i = 0; i < steps && !h->nhb_mode && !clustered && !offsets; ++i) {
     if (side) {
-      enqueue_step(h, nmet, ncl, count, false);
-    } else if (count) {
-      // the record of a counting step is the running counts
-      enqueue_step(h, nmet, ncl, true);
-      if (rec_at(i)) launch_count_read(h->b, h->stream, 1);
+      enqueue_step(h, nmet, ncl, false);
     } else if (rec_at(i) && ncl == 0 && nmet > 0) {
-      enqueue_recorded_metropolis_step(h, nmet);
+      enqueue_recorded_metropolis_step(h, nmet, record == 1);
     } else {
-      enqueue_step(h, nmet, ncl, count);
+      enqueue_step(h, nmet, ncl);
       if (rec_at(i)) {
         launch_measure(h->b, 1, h->stream);
         if (ncl > 0 && !h->b.wolff) enqueue_cstats(h, 1);
@@ -760,7 +750,7 @@ int cvf_num_replicas(const cvf_handle* h) { return h ? (int)h->reps.size() : 0; 
 
 int cvf_set_config(cvf_handle* h, int r, const int* c12, long long n_cells) {
   if (int rc = check_rep(h, r)) return rc;
-  h->count_valid = false;
+  h->last_valid = false;
   ReplicaHost& R = h->reps[r];
   if (!c12 || n_cells != R.N) return fail(CVF_EINVAL, "cells12 must hold 12 ints for each of the N cells");
   CK(cudaSetDevice(h->device));
@@ -879,7 +869,7 @@ int cvf_set_arms(cvf_handle* h, int r, const unsigned char* sg, const unsigned c
       }
     return cvf_set_config(h, r, c12.data(), R.N);
   }
-  h->count_valid = false;
+  h->last_valid = false;
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
   if (int rc = ensure_io_scratch(h, R)) return rc;
@@ -959,7 +949,7 @@ int cvf_set_packed(cvf_handle* h, int r, const void* buf, long long bytes) {
   if (h->nhb_mode) return fail(CVF_EINVAL, "the packed state holds cube states: Flag_chessboard = 1 only");
   ReplicaHost& R = h->reps[r];
   if (!buf || bytes != packed_bytes(R)) return fail(CVF_EINVAL, "packed buffer must hold 4 N + 2 (L/2)^3 bytes");
-  h->count_valid = false;
+  h->last_valid = false;
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
   // copied and checked in scratch first: the lattice changes only when every value is valid
@@ -1019,54 +1009,55 @@ int cvf_get_distances(const cvf_handle* h, int r, float* dist, int* freq, int ca
 static int run_impl(cvf_handle* h, int n_steps, int nmet, int ncl, int interval) {
   if (!h) return fail(CVF_EINVAL, "null handle");
   if (n_steps < 0 || nmet < 0 || ncl < 0) return fail(CVF_EINVAL, "negative step counts");
-  const bool want_count = h->obs_since_run;
+  const bool want_last = h->obs_since_run;
   h->obs_since_run = false;
   CK(cudaSetDevice(h->device));
   if (ncl > 0) {
     if (int rc = h->b.wolff ? ensure_wolff(h) : ensure_sw(h)) return rc;
   }
   if (n_steps == 0) return 0;
+  h->last_valid = false;
   const int chunk_plain = 32;
   if (interval <= 0) {
-    // the counting kernels run where the per-phase capture of one group serves the handle
-    const bool count = want_count && h->count_valid && ncl == 0 && !h->nhb_mode && group_count(h) <= 1;
-    if (!count) h->count_valid = false;
-    int full = n_steps / chunk_plain, rem = n_steps % chunk_plain;
+    // a Metropolis-only run right after cvf_observables measures its last step (on the step's
+    // last colour-1 sweep), and the next cvf_observables reads that record
+    const bool last = want_last && ncl == 0 && nmet > 0 && !h->nhb_mode;
+    const int plain = last ? n_steps - 1 : n_steps;
+    int full = plain / chunk_plain, rem = plain % chunk_plain;
     cudaGraphExec_t g;
     if (full) {
-      if (int rc = get_graph(h, chunk_plain, nmet, ncl, 0, &g, count)) return rc;
+      if (int rc = get_graph(h, chunk_plain, nmet, ncl, 0, &g)) return rc;
       for (int i = 0; i < full; ++i) CK(cudaGraphLaunch(g, h->stream));
     }
     if (rem) {
-      if (int rc = get_graph(h, rem, nmet, ncl, 0, &g, count)) return rc;
+      if (int rc = get_graph(h, rem, nmet, ncl, 0, &g)) return rc;
       CK(cudaGraphLaunch(g, h->stream));
     }
-  } else {
-    // sampled runs record from running counts (one full measurement first when they are not
-    // current) wherever the plain per-phase capture serves the handle
-    const bool count = ncl == 0 && nmet > 0 && !h->nhb_mode && group_count(h) <= 1 && h->launch_mode == 0;
-    if (count && !h->count_valid) {
-      launch_measure(h->b, 0, h->stream);
-      launch_count_rebase(h->b, h->stream);
+    if (last) {
+      if (int rc = get_graph(h, 1, nmet, 0, 2, &g)) return rc;
+      CK(cudaGraphLaunch(g, h->stream));
+      h->last_valid = true;
     }
-    h->count_valid = count;
+  } else {
     // graphs of m intervals (about 32 steps) while enough steps remain, then single intervals,
     // then the remainder: each graph launch costs a few microseconds on the device
     const int m = interval >= chunk_plain ? 1 : chunk_plain / interval;
     int left = n_steps;
     cudaGraphExec_t g;
     if (m > 1 && left >= m * interval) {
-      if (int rc = get_graph(h, m * interval, nmet, ncl, 1, &g, count, interval)) return rc;
+      if (int rc = get_graph(h, m * interval, nmet, ncl, 1, &g, interval)) return rc;
       for (; left >= m * interval; left -= m * interval) CK(cudaGraphLaunch(g, h->stream));
     }
     if (left >= interval) {
-      if (int rc = get_graph(h, interval, nmet, ncl, 1, &g, count)) return rc;
+      if (int rc = get_graph(h, interval, nmet, ncl, 1, &g)) return rc;
       for (; left >= interval; left -= interval) CK(cudaGraphLaunch(g, h->stream));
     }
     if (left) {
-      if (int rc = get_graph(h, left, nmet, ncl, 1, &g, count)) return rc;
+      if (int rc = get_graph(h, left, nmet, ncl, 1, &g)) return rc;
       CK(cudaGraphLaunch(g, h->stream));
     }
+    // the run's last step was recorded when it sits on the interval grid
+    h->last_valid = !h->nhb_mode && (n_steps - 1) % interval == 0;
   }
   if (ncl > 0 && !h->b.wolff) h->sw_done = true;
   CK(cudaGetLastError());
@@ -1103,10 +1094,10 @@ int cvf_observables(cvf_handle* h, int r, cvf_obs* out) {
     }
   }
   bool landed = false;  // the record already written to rec_pin by the kernel
-  if (h->count_valid) {
-    // every step since the last measurement counted: the read kernel writes the record
-    // straight into the mapped page-locked buffer
-    launch_count_read(h->b, h->stream, 0, h->rec_dev, r);
+  if (h->last_valid) {
+    // the last step was measured: the read kernel writes its record straight into the mapped
+    // page-locked buffer
+    launch_last_read(h->b, h->stream, h->rec_dev, r);
     landed = true;
   } else if (h->nhb_mode) {
     if (!h->nhb_read) {
@@ -1124,8 +1115,7 @@ int cvf_observables(cvf_handle* h, int r, cvf_obs* out) {
     CK(cudaGraphLaunch(h->nhb_read, h->stream));
   } else {
     launch_measure(h->b, 0, h->stream);
-    launch_count_rebase(h->b, h->stream);
-    h->count_valid = true;
+    h->last_valid = true;
   }
   // only the 32-byte measurement record crosses to the host, into page-locked memory
   if (!landed)
@@ -1367,7 +1357,7 @@ static int restore_state(cvf_handle* h, const StateBackup& b) {
 
 int cvf_autotune(cvf_handle* h, int* vec_out) {
   if (!h) return fail(CVF_EINVAL, "null handle");
-  h->count_valid = false;
+  h->last_valid = false;
   if (h->nhb_mode) {  // the per-arm sweep of Flag_chessboard = 0 has no tile to choose
     if (vec_out) *vec_out = h->b.vec;
     return 0;
@@ -1467,7 +1457,7 @@ int cvf_autotune(cvf_handle* h, int* vec_out) {
     }
     drop_graphs(h);
     h->launch_mode = best_mode;
-    h->count_valid = false;
+    h->last_valid = false;
     if (int rc = restore_state(h, full)) return rc;
   }
   cudaEventDestroy(e0);
@@ -1511,7 +1501,7 @@ int cvf_get_stream(cvf_handle* h, void** stream) {
 
 int cvf_profile_launch(cvf_handle* h, int kind, int n) {
   if (!h || n < 0 || kind < 0 || kind > 3) return fail(CVF_EINVAL, "bad profile request");
-  h->count_valid = false;
+  h->last_valid = false;
   if (h->nhb_mode) return fail(CVF_EINVAL, "kernel profiling covers the Flag_chessboard = 1 kernels");
   CK(cudaSetDevice(h->device));
   for (int i = 0; i < n; ++i) {

@@ -414,7 +414,7 @@ __device__ __noinline__ bool cube_accept_exact(uint32_t gid, uint32_t t, uint32_
 // wrote earlier in the same launch.
 template <int VC>
 __device__ __forceinline__ void cube_move_v(const ReplicaDesc& R, const CubeTables* ct, const int* __restrict__ blk,
-                                            int r, int vb, uint32_t t, int& cdh) {
+                                            int r, int vb, uint32_t t) {
   const uint32_t L = R.L, H = R.H, cpr = H / VC;
   const int lb = vb - __ldg(blk + r);
   const uint32_t par = (uint32_t)lb & 1u;
@@ -507,7 +507,6 @@ __device__ __forceinline__ void cube_move_v(const ReplicaDesc& R, const CubeTabl
     if (((acc_mask >> k) & 1u) && nwk[k] != st[k]) {
       st[k] = nwk[k];
       changed = true;
-      cdh += dhk[k];
     }
   }
   if (changed) {
@@ -520,43 +519,16 @@ __device__ __forceinline__ void cube_move_v(const ReplicaDesc& R, const CubeTabl
   }
 }
 
-// cdh receives the change of N_hb the thread's accepted cube moves make.
 __device__ __forceinline__ void cube_move(const ReplicaDesc& R, const CubeTables* ct, const int* __restrict__ blk,
-                                          int r, int vb, uint32_t t, int& cdh) {
-  if (R.cvec == 4) cube_move_v<4>(R, ct, blk, r, vb, t, cdh);
-  else if (R.cvec == 2) cube_move_v<2>(R, ct, blk, r, vb, t, cdh);
-  else cube_move_v<1>(R, ct, blk, r, vb, t, cdh);
-}
-
-// Block sums of the threads' count changes (dn in N_hb units, ds in N_sigma units) added to one
-// of the replica's 32 running-count slots: one pair of atomics per block (per warp they queued
-// on the few cache lines of the slots). Every thread of the block calls it.
-__device__ __forceinline__ void count_accumulate_block(ReplicaState& S, int vb, int dn, int ds) {
-  __shared__ int s_cnt[2][kThreads / 32];
-  const int wn = __reduce_add_sync(0xffffffffu, dn), wsum = __reduce_add_sync(0xffffffffu, ds);
-  const int warp = (int)(threadIdx.x >> 5);
-  if ((threadIdx.x & 31) == 0) {
-    s_cnt[0][warp] = wn;
-    s_cnt[1][warp] = wsum;
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    const int nw = (int)(blockDim.x >> 5);
-    const int a = threadIdx.x < (unsigned)nw ? s_cnt[0][threadIdx.x] : 0;
-    const int b = threadIdx.x < (unsigned)nw ? s_cnt[1][threadIdx.x] : 0;
-    const int bn = __reduce_add_sync(0xffffffffu, a), bs = __reduce_add_sync(0xffffffffu, b);
-    if (threadIdx.x == 0 && (bn | bs)) {
-      const int slot = vb & 31;
-      atomicAdd(&S.dlt_slot[0][slot], (unsigned long long)(long long)bn);
-      atomicAdd(&S.dlt_slot[1][slot], (unsigned long long)(long long)bs);
-    }
-  }
+                                          int r, int vb, uint32_t t) {
+  if (R.cvec == 4) cube_move_v<4>(R, ct, blk, r, vb, t);
+  else if (R.cvec == 2) cube_move_v<2>(R, ct, blk, r, vb, t);
+  else cube_move_v<1>(R, ct, blk, r, vb, t);
 }
 
 // The volume move of replica b for the first nvol blocks b (one warp each: scheduled first, they
 // run beside the cube blocks), then the cube moves of every replica, both with the counters of the
 // current step.
-template <bool kCount>
 __global__ void __launch_bounds__(kThreads, 4) k_cube_volume(const ReplicaDesc* __restrict__ reps,
                                                           ReplicaState* __restrict__ st,
                                                           const int* __restrict__ blk, int nrep, int nvol,
@@ -577,9 +549,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_cube_volume(const ReplicaDesc* 
   fill_cube_tables(R, ct, threadIdx.x & 31);
   __syncwarp();
   pdl_wait();
-  int cdh = 0;
-  cube_move(R, ct, blk, r, vb, soff < 0 ? st[r].cur[1] : st[r].ctr[1] + (uint32_t)soff, cdh);
-  if (kCount) count_accumulate_block(st[r], vb, cdh, 0);
+  cube_move(R, ct, blk, r, vb, soff < 0 ? st[r].cur[1] : st[r].ctr[1] + (uint32_t)soff);
 }
 
 // ------------------------------------------------------------------ checkerboard sweep
@@ -707,16 +677,13 @@ __device__ __noinline__ uint32_t sweep_proposal_retry(uint32_t c0, uint32_t t, u
 }
 
 // Exact update of one cell with the full 32-bit uniforms (high halves from the sweep block,
-// low halves from the refinement block). Taken only when a 16-bit comparison tied.
-// Returns the new word in the low 32 bits and the packed count changes of the accepted arms,
-// 65536 dN_hb + dN_sigma, in the high 32 bits.
-__device__ __noinline__ unsigned long long sweep_cell_exact(uint32_t w, uint32_t nbe, uint32_t u,
-                                                            uint32_t a1, uint32_t a2, uint32_t a3, uint32_t c0,
-                                                            uint32_t t, const ReplicaDesc* R) {
+// low halves from the refinement block). Taken only when a 16-bit comparison tied. Returns the
+// new word.
+__device__ __noinline__ uint32_t sweep_cell_exact(uint32_t w, uint32_t nbe, uint32_t u, uint32_t a1, uint32_t a2,
+                                                  uint32_t a3, uint32_t c0, uint32_t t, const ReplicaDesc* R) {
   const U4 rf = philox(c0, t, kStSweepRefine, R->replica, R->key0, R->key1);
   uint32_t h = sigma_histogram(w);
   uint32_t f = u;
-  int32_t acc = 0;
   for (int a = 0; a < 6; ++a) {
     unsigned long long m = (unsigned long long)f * 6ull;
     const uint32_t n = (uint32_t)(m >> 32);
@@ -734,10 +701,9 @@ __device__ __noinline__ unsigned long long sweep_cell_exact(uint32_t w, uint32_t
     if (U < T) {
       w = (w & ~(7u << (3 * a))) | (n << (3 * a));
       h += (1u << (4 * n)) - (1u << (4 * o));
-      acc += dhb * 65536 + dns;
     }
   }
-  return ((unsigned long long)(uint32_t)acc << 32) | w;
+  return w;
 }
 
 // Byte select: byte i of the result is byte ((sel >> 4i) & 7) of the eight bytes {hi:lo}. Every
@@ -853,11 +819,9 @@ __device__ __forceinline__ void fill_block_sweep_tables(const ReplicaDesc& R, Sw
 // that wraps to zero without a tie only sends the cell through the exact path as well, which
 // decides every arm from the full 32-bit uniforms. A proposal equal to the old
 // value lands on entry 17 (dN = 0), which always accepts and changes nothing.
-// kCount: dacc also receives the cell's count changes, packed as 65536 dN_hb + dN_sigma.
-template <bool kCount, bool kFold, bool kDelta>
+template <bool kFold, bool kDelta>
 __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbe, const U4& rr,
-                                                uint32_t c0, uint32_t t, const ReplicaDesc& R, const SweepTables* wt,
-                                                int32_t& dacc) {
+                                                uint32_t c0, uint32_t t, const ReplicaDesc& R, const SweepTables* wt) {
   // a proposal word in the rejected range of the exact draw (p = 6e-7): with kFold it sends the
   // cell through the exact path, which draws the retry word, and the fast path's decisions are
   // discarded (one rare-path test per cell instead of two); otherwise the retry word is drawn
@@ -876,7 +840,6 @@ __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbe, const 
     hx += c.x;
     hy += c.y;
   }
-  const int s0 = kCount ? (int)__dp4a(hx, hx, __dp4a(hy, hy, 0u)) : 0;
   const char* tvb = reinterpret_cast<const char*>(wt->tv) + 68;
   uint32_t f = u, tprod = 1u;
 #pragma unroll
@@ -912,17 +875,7 @@ __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbe, const 
   }
   if (tprod == 0u || reject) {
     const uint32_t ue = reject ? sweep_proposal_retry(c0, t, R.replica, R.key0, R.key1) : u;
-    const unsigned long long x = sweep_cell_exact(w0, nbe, ue, rr.y, rr.z, rr.w, c0, t, &R);
-    w = (uint32_t)x;
-    if (kCount) dacc += (int32_t)(uint32_t)(x >> 32);
-  } else if (kCount) {
-    // the cell's count changes: N_hb from its arms equal to the facing neighbour value before
-    // and after (a field of 7 in nbe never matches), N_sigma from the sum of the squared
-    // histogram bytes b = 4h: the equal pairs of a cell are (sum h^2 - 6) / 2 = (sum b^2 / 16 - 6) / 2
-    const uint32_t x0 = w0 ^ nbe, x1 = w ^ nbe;
-    const int dhb = __popc(~(x1 | (x1 >> 1) | (x1 >> 2)) & 0x9249u) - __popc(~(x0 | (x0 >> 1) | (x0 >> 2)) & 0x9249u);
-    const int s1 = (int)__dp4a(hx, hx, __dp4a(hy, hy, 0u));
-    dacc += dhb * 65536 + (s1 - s0) / 32;
+    w = sweep_cell_exact(w0, nbe, ue, rr.y, rr.z, rr.w, c0, t, &R);
   }
   return w;
 }
@@ -942,9 +895,9 @@ struct SweepMinBlocks {
 // colour-1 cells count all bonds (delta of the facing sigmas times the bond's eta, twice), and
 // each colour-1 cell adds the sigma pairs of itself and of the colour-0 cell with the same word
 // index (the x-neighbour the segment loads anyway).
-template <int V, bool kMeasure, bool kCount = false, bool kFold = false, bool kDelta = false>
+template <int V, bool kMeasure, bool kFold = false, bool kDelta = false>
 __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepTables* wt, uint32_t q, int colour,
-                                              uint32_t t, uint32_t& hb2, uint32_t& ns, int32_t* dacc = nullptr) {
+                                              uint32_t t, uint32_t& hb2, uint32_t& ns) {
   int hc, y, z;
   if (!segment_of<V>(R, q, hc, y, z)) return;
   // nbe: the facing neighbour sigmas with 7 in the field of every arm whose eta is 0 -- all that
@@ -972,8 +925,7 @@ __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepT
   for (int k = 0; k < V; ++k) {
     const uint32_t c0 = cbase + 2u * k;
     const U4 rr = philox_rk(c0, t, kStSweep, R.replica, rk);
-    int32_t dummy = 0;
-    out[k] = update_cell<kCount, kFold, kDelta>(out[k], nbe[k], rr, c0, t, R, wt, kCount ? *dacc : dummy);
+    out[k] = update_cell<kFold, kDelta>(out[k], nbe[k], rr, c0, t, R, wt);
   }
   VecLoad<V>::st(own_ptr, out);
   if (kMeasure) {
@@ -987,7 +939,7 @@ __device__ __forceinline__ void sweep_segment(const ReplicaDesc& R, const SweepT
   }
 }
 
-template <int V, bool kCount>
+template <int V>
 __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const ReplicaDesc* __restrict__ reps,
                                                     ReplicaState* __restrict__ st,
                                                     const int* __restrict__ blk, int nrep, int colour, int jsweep,
@@ -1000,13 +952,8 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep(const 
   __syncthreads();
   pdl_wait();
   uint32_t hb2 = 0, ns = 0;
-  int32_t dacc = 0;
-  sweep_segment<V, false, kCount, true, V == 8 && !kCount>(R, &s_tab, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
-                                  (from_ctr ? st[r].ctr[0] : st[r].cur[0]) + (uint32_t)jsweep, hb2, ns, &dacc);
-  if (kCount) {
-    const int ds = (int)(int16_t)(dacc & 0xffff);  // |dN_sigma| per thread <= 8 cells x 30
-    count_accumulate_block(st[r], blockIdx.x, (dacc - ds) / 65536, ds);
-  }
+  sweep_segment<V, false, true, V == 8>(R, &s_tab, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, colour,
+                                        (from_ctr ? st[r].ctr[0] : st[r].cur[0]) + (uint32_t)jsweep, hb2, ns);
 }
 
 // A chunk of Metropolis-only steps of a small replica on one thread-block cluster of kClusterCtas
@@ -1049,18 +996,17 @@ __global__ void __launch_bounds__(kThreads) k_chunk_cluster(const ReplicaDesc* _
   uint32_t hb2 = 0, ns = 0;
   cluster_barrier();  // every block has read the counters before block 0 moves them
   for (int s = 0; s < steps; ++s) {
-    int cdh = 0;
     if (live)
       for (int vb = vb0 + (int)rank; vb < vb1; vb += kClusterCtas)
-        if (cube1) cube_move_v<1>(R, ct, blk_cube, r, vb, c1 + (uint32_t)s, cdh);
-        else cube_move(R, ct, blk_cube, r, vb, c1 + (uint32_t)s, cdh);
+        if (cube1) cube_move_v<1>(R, ct, blk_cube, r, vb, c1 + (uint32_t)s);
+        else cube_move(R, ct, blk_cube, r, vb, c1 + (uint32_t)s);
     cluster_barrier();
     for (int j = 0; j < nmet; ++j) {
       const uint32_t t = c0 + (uint32_t)(s * nmet + j);
       for (int colour = 0; colour < 2; ++colour) {
         if (live)
           for (uint32_t q = rank * kThreads + threadIdx.x; q < nseg; q += kClusterCtas * kThreads)
-            sweep_segment<V, false, false, true>(R, wt, q, colour, t, hb2, ns);
+            sweep_segment<V, false, true>(R, wt, q, colour, t, hb2, ns);
         cluster_barrier();
       }
     }
@@ -1219,8 +1165,7 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_run(BatchDev
           const int r = find_replica(b.blk_cubev, b.nrep, vb);
           StepTables* wt = s_tab + (threadIdx.x >> 5);
           ensure_tables(b.reps, r, wt, s_held[threadIdx.x >> 5]);
-          int cdh = 0;
-          cube_move(b.reps[r], &wt->cube, b.blk_cubev, r, vb, b.st[r].ctr[1] + (uint32_t)s, cdh);
+          cube_move(b.reps[r], &wt->cube, b.blk_cubev, r, vb, b.st[r].ctr[1] + (uint32_t)s);
         } else if (threadIdx.x < 32) {
           const int r = vb - b.nblk_cubev;
           ReplicaState& S = b.st[r];
@@ -1329,13 +1274,12 @@ void launch_measure_end(const BatchDev& b, int record, cudaStream_t s) {
   k_measure_end<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, record);
 }
 
-void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, bool count, int soff) {
+void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, int soff) {
   const int cube_blocks = do_cubes ? b.nblk_cubev : 0;
   const int vol_blocks = do_volume ? b.nrep : 0;
   if (cube_blocks + vol_blocks == 0) return;
   const dim3 grid((unsigned)(cube_blocks + vol_blocks));
-  if (count) launch_pdl(k_cube_volume<true>, grid, s, b.pdl, b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks, soff);
-  else launch_pdl(k_cube_volume<false>, grid, s, b.pdl, b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks, soff);
+  launch_pdl(k_cube_volume, grid, s, b.pdl, b.reps, b.st, b.blk_cubev, b.nrep, vol_blocks, soff);
 }
 
 void launch_chunk_end(const BatchDev& b, int steps, int nmet, int ncl, int do_volume, cudaStream_t s) {
@@ -1343,77 +1287,34 @@ void launch_chunk_end(const BatchDev& b, int steps, int nmet, int ncl, int do_vo
              ncl, do_volume);
 }
 
-// The counting sweep runs at most 4 cells per thread (its 8-cell tile spills registers under
-// the 3-blocks-per-SM bound and ran 6-13 us per recorded step slower at L=256).
-void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, bool count, int from_ctr) {
-  if (count) {
-    const int n = b.nblk_sweep_count;
-    const int* blk = b.blk_sweep_count;
-    const dim3 g((unsigned)n);
-    switch (b.vec_count) {
-      case 4: launch_pdl(k_sweep<4, true>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
-      case 2: launch_pdl(k_sweep<2, true>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
-      default: launch_pdl(k_sweep<1, true>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
-    }
-    return;
-  }
+void launch_sweep(const BatchDev& b, int colour, int jsweep, cudaStream_t s, int from_ctr) {
   const dim3 g((unsigned)b.nblk_sweep);
   const int* blk = b.blk_sweep;
   switch (b.vec) {
-    case 8: launch_pdl(k_sweep<8, false>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
-    case 4: launch_pdl(k_sweep<4, false>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
-    case 2: launch_pdl(k_sweep<2, false>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
-    default: launch_pdl(k_sweep<1, false>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
+    case 8: launch_pdl(k_sweep<8>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
+    case 4: launch_pdl(k_sweep<4>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
+    case 2: launch_pdl(k_sweep<2>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
+    default: launch_pdl(k_sweep<1>, g, s, b.pdl, b.reps, b.st, blk, b.nrep, colour, jsweep, from_ctr); break;
   }
 }
 
-// One warp per replica: the 32 slots of each count summed across the lanes (modulo 2^64, so in
-// any order), the record stored as the replica's last measurement (and appended to the sample
-// stream when record is set); replica host_r's record is also written to host_out, page-locked
-// host memory mapped for the device, when that is given.
-__global__ void k_count_read(ReplicaState* __restrict__ st, int nrep, int record, SampleRec* host_out, int host_r) {
+// Replica host_r's last measurement, with its current r_cell and volume (a state set since the
+// measurement changed them, not the cells), written to host_out: page-locked host memory mapped
+// for the device.
+__global__ void k_last_read(const ReplicaState* __restrict__ st, SampleRec* host_out, int host_r) {
   pdl_trigger();
-  const int r = blockIdx.x * (int)(blockDim.x >> 5) + (int)(threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
   pdl_wait();
-  if (r >= nrep) return;
-  ReplicaState& S = st[r];
-  unsigned long long dn = S.dlt_slot[0][lane], ds = S.dlt_slot[1][lane];
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    dn += __shfl_xor_sync(0xffffffffu, dn, off);
-    ds += __shfl_xor_sync(0xffffffffu, ds, off);
-  }
-  if (lane != 0) return;
-  SampleRec rec;
-  rec.n_hb2 = S.base_hb2 + 2 * (long long)dn;
-  rec.n_sigma = S.base_ns + (long long)ds;
+  if (threadIdx.x != 0) return;
+  const ReplicaState& S = st[host_r];
+  SampleRec rec = S.last;
   rec.r_cell = S.r_cell;
   rec.volume = S.volume;
-  S.last = rec;
-  if (record && S.samples && S.n_samples < S.cap_samples) S.samples[S.n_samples] = rec;
-  if (record) S.n_samples++;
-  if (host_out && r == host_r) {
-    *host_out = rec;
-    __threadfence_system();
-  }
+  *host_out = rec;
+  __threadfence_system();
 }
 
-__global__ void k_count_rebase(ReplicaState* __restrict__ st, int nrep) {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrep) return;
-  ReplicaState& S = st[r];
-  S.base_hb2 = S.last.n_hb2;
-  S.base_ns = S.last.n_sigma;
-  for (int i = 0; i < 32; ++i) S.dlt_slot[0][i] = S.dlt_slot[1][i] = 0ull;
-}
-
-void launch_count_read(const BatchDev& b, cudaStream_t s, int record, SampleRec* host_out, int host_r) {
-  launch_pdl(k_count_read, dim3((unsigned)((b.nrep + kThreads / 32 - 1) / (kThreads / 32))), s, b.pdl, b.st, b.nrep,
-             record, host_out, host_r);
-}
-void launch_count_rebase(const BatchDev& b, cudaStream_t s) {
-  k_count_rebase<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep);
+void launch_last_read(const BatchDev& b, cudaStream_t s, SampleRec* host_out, int host_r) {
+  launch_pdl(k_last_read, dim3(1u), s, b.pdl, b.st, host_out, host_r);
 }
 
 void launch_measure(const BatchDev& b, int record, cudaStream_t s) {

@@ -1,9 +1,9 @@
-"""Running counts of cvf_observables: after each run that follows cvf_observables the engine adds,
-inside the sweep and cube kernels, the changes of N_hb and N_sigma of every accepted move to the
-counts of the last full measurement, and cvf_observables reads those instead of measuring the
-lattice again. The counts must equal the oracle's full measurement after every step, through
-the rare exact (16-bit tie) path, and across the calls that end the counting (a run without a
-following read, sampled runs, cluster steps, new configurations)."""
+"""Reads of cvf_observables between runs: a Metropolis-only run that follows cvf_observables
+measures its last step on that step's colour-1 sweep, and the next cvf_observables reads that
+record instead of measuring the lattice again (as it does after a sampled run whose last step was
+recorded). The reads must equal the oracle's full measurement after every step, through the rare
+exact (16-bit tie) path, and across the calls that leave no current record (a run without a
+following read, sampled runs off the interval grid, cluster steps, new configurations)."""
 import numpy as np
 import pytest
 
@@ -30,7 +30,7 @@ def test_read_after_every_step(engine_lib, oracle_mod, L, T, start):
         eng.run(1, 1, 0)
         ora.step(1, 0)
         same_counts(eng, ora)
-    # a few steps between reads still count (the first run after a read uses the counting kernels)
+    # a few steps between reads (the run after a read measures only its last step)
     eng.run(7, 2, 0)
     for _ in range(7):
         ora.step(2, 0)
@@ -40,7 +40,7 @@ def test_read_after_every_step(engine_lib, oracle_mod, L, T, start):
 
 @pytest.mark.parametrize("L", [32, 48])
 def test_eight_cell_tile(engine_lib, oracle_mod, L):
-    # a handle on the 8-cell sweep tile counts with the 4-cell tile and its own block table
+    # a handle on the 8-cell sweep tile: its last step measured with the 8-cell measuring sweep
     eng, ora = pair(oracle_mod, L, 0.7, 0.45, 40 + L, 2)
     assert eng.set_sweep_tile(8) == 8
     for _ in range(12):
@@ -82,11 +82,20 @@ def test_mixed_calls(engine_lib, oracle_mod):
     for _ in range(5):
         run(1)
         same_counts(eng, ora)
-    eng.run_sampled(4, 1, 0, 2)
+    eng.run_sampled(4, 1, 0, 2)  # last step off the interval grid: the read measures in full
     for _ in range(4):
         ora.step(1, 0)
     same_counts(eng, ora)
-    run(3, 0, 1)  # Swendsen-Wang steps end the counting
+    eng.run_sampled(5, 1, 0, 2)  # last step recorded: the read takes its record
+    for _ in range(5):
+        ora.step(1, 0)
+    same_counts(eng, ora)
+    # a state set after the record: the read takes r_cell and volume from it
+    r_cell, vol, _, ctr = eng.state()
+    eng.set_state(r_cell * 1.001, vol * 1.001 ** 3, ctr)
+    ora.set_state(r_cell * 1.001, vol * 1.001 ** 3, ctr)
+    same_counts(eng, ora)
+    run(3, 0, 1)  # Swendsen-Wang steps leave no record: the next read measures in full
     same_counts(eng, ora)
     run(2)
     same_counts(eng, ora)
