@@ -259,6 +259,23 @@ void launch_cluster_stats_impl(const BatchDev& b, unsigned long long* blocktop, 
 // (pdl_wait) before it touches the state that kernel writes; what it does before the wait reads
 // only the descriptors and tables, which no kernel writes. Without a programmatic predecessor
 // the wait returns at once.
+// Bit 2 of every 3-bit field of x (18 bits) set where the field is not zero: adding 3 to the
+// field's low two bits carries into bit 2 unless they are zero (no carry leaves the field).
+__device__ __forceinline__ uint32_t nonzero_fields(uint32_t x) {
+  return (((x & 0x1b6dbu) + 0x1b6dbu) | x) & 0x24924u;
+}
+
+// sum_{a<b} delta(sigma_a, sigma_b) of one cell: with Z_k the number of arms a equal to arm
+// (a+k) mod 6, every unordered pair is counted by Z_k and Z_{6-k}, so the sum is
+// Z_1 + Z_2 + Z_3/2, and Z_3/2 counts arms 0..2 against 3..5. The rotations by 3k bits are
+// windows of the word repeated above itself (w * (1 + 2^18), 18 + 14 bits).
+__device__ __forceinline__ uint32_t sigma_pairs(uint32_t w) {
+  w &= 0x3ffffu;
+  const uint32_t ww = w * 0x40001u;
+  const uint32_t x1 = (w ^ (ww >> 3)) & 0x3ffffu, x2 = (w ^ (ww >> 6)) & 0x3ffffu, x3 = (w ^ (ww >> 9)) & 0x1ffu;
+  return 15u - (uint32_t)(__popc(nonzero_fields(x1)) + __popc(nonzero_fields(x2)) + __popc(nonzero_fields(x3)));
+}
+
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 

@@ -643,21 +643,6 @@ __device__ __forceinline__ uint32_t neighbour_sigmas(uint32_t xp, uint32_t xm, u
   return (up >> 3) | (dn << 3);
 }
 
-// Number of zero 3-bit fields among the six fields of x.
-__device__ __forceinline__ uint32_t zero_fields(uint32_t x) {
-  return 6u - (uint32_t)__popc((x | (x >> 1) | (x >> 2)) & 0x9249u);
-}
-
-// sum_{a<b} delta(sigma_a, sigma_b) of one cell: with Z_k the number of arms a equal to arm
-// (a+k) mod 6, every unordered pair is counted by Z_k and Z_{6-k}, so the sum is Z_1 + Z_2 + Z_3/2.
-__device__ __forceinline__ uint32_t sigma_pairs(uint32_t w) {
-  w &= 0x3ffffu;
-  const uint32_t r1 = ((w >> 3) | (w << 15)) & 0x3ffffu;
-  const uint32_t r2 = ((w >> 6) | (w << 12)) & 0x3ffffu;
-  const uint32_t r3 = ((w >> 9) | (w << 9)) & 0x3ffffu;
-  return zero_fields(w ^ r1) + zero_fields(w ^ r2) + (zero_fields(w ^ r3) >> 1);
-}
-
 __device__ __forceinline__ uint32_t sigma_histogram(uint32_t w) {
   uint32_t h = 0;
 #pragma unroll
@@ -1035,7 +1020,7 @@ __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep_measur
   fill_block_sweep_tables(R, &s_tab);
   __syncthreads();
   uint32_t hb2 = 0, ns = 0;
-  sweep_segment<V, true>(R, &s_tab, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, 1,
+  sweep_segment<V, true, true, V == 8>(R, &s_tab, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, 1,
                          st[r].cur[0] + (uint32_t)jsweep, hb2, ns);
   measure_accumulate(st[r], blockIdx.x, hb2, ns, s_acc);
 }

@@ -163,18 +163,6 @@ __global__ void k_nhb_begin(ReplicaState* __restrict__ st, int nrep) {
   }
 }
 
-// sum_{a<b} delta(sigma_a, sigma_b) of one cell (rotations by 1, 2, 3 arms).
-__device__ __forceinline__ uint32_t zero_fields6(uint32_t x) {
-  return 6u - (uint32_t)__popc((x | (x >> 1) | (x >> 2)) & 0x9249u);
-}
-__device__ __forceinline__ uint32_t pairs6(uint32_t w) {
-  w &= 0x3ffffu;
-  const uint32_t r1 = ((w >> 3) | (w << 15)) & 0x3ffffu;
-  const uint32_t r2 = ((w >> 6) | (w << 12)) & 0x3ffffu;
-  const uint32_t r3 = ((w >> 9) | (w << 9)) & 0x3ffffu;
-  return zero_fields6(w ^ r1) + zero_fields6(w ^ r2) + (zero_fields6(w ^ r3) >> 1);
-}
-
 // Per cell: which of its six arms agree with the arm they face (eta plays no part,
 // GW:2064-2099), stored as the matched forward bonds (bits 0..2: x+, y+, z+) and a mark (bit 3)
 // when 5 or more agree; the matched forward bonds and the sigma pairs summed per block into slot
@@ -201,7 +189,7 @@ __global__ void k_nhb_mark(const ReplicaDesc* __restrict__ reps, ReplicaState* _
     fwd = __popc(bits);
     R.sat[c] = (uint8_t)(bits | (uint32_t)(m >= 5) << 3);
     R.cnt[c] = 0;
-    ns = pairs6(w);
+    ns = sigma_pairs(w);
   }
   if (threadIdx.x < 2) s_acc[threadIdx.x] = 0;
   __syncthreads();
