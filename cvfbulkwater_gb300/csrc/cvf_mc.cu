@@ -585,6 +585,25 @@ struct CellBlock {
   uint32_t* own_ptr;
   int x0, y, z, s;
 
+  static __device__ __forceinline__ void ld_bytes(const uint8_t* a, uint32_t* b) {
+    if (V == 8) {
+      const uint2 t = *reinterpret_cast<const uint2*>(a);
+      b[0] = t.x;
+      b[1] = t.y;
+    } else if (V == 4) {
+      b[0] = *reinterpret_cast<const uint32_t*>(a);
+    } else if (V == 2) {
+      b[0] = *reinterpret_cast<const uint16_t*>(a);
+    } else {
+      b[0] = *a;
+    }
+  }
+  static __device__ __forceinline__ uint32_t byte_of(const uint32_t* b, int k) {
+    return (b[k >> 2] >> (8 * (k & 3))) & 0xffu;
+  }
+
+  // The segment's words, the other colour's words around them and the eta masks of its cells
+  // (s_eta: cube state x vertex offset -> mask).
   __device__ __forceinline__ void load(const ReplicaDesc& R, int colour, int hc, int y_, int z_,
                                        const uint8_t* s_eta) {
     const int L = R.L, H = R.H;
@@ -617,17 +636,22 @@ struct CellBlock {
         xp[k] = k + 1 < V ? mid[k + 1] : extra;
       }
     }
-    // eta from the even cube (x>>1, y>>1, z>>1) and the odd cube containing the cell
+    // eta from the even cube (x>>1, y>>1, z>>1) and the odd cube containing the cell: cell k
+    // lies in even cube h0 + k and odd cube h0 + k (s = 1) or h0 + k - 1 (s = 0)
     const int yo = (y & 1) ? y : ym1, zo = (z & 1) ? z : zm1;
     const uint32_t erow = (uint32_t)H * ((uint32_t)(y >> 1) + (uint32_t)H * (z >> 1));
     const uint32_t orow = (uint32_t)H * ((uint32_t)(yo >> 1) + (uint32_t)H * (zo >> 1));
     const int p = s | ((y & 1) << 1) | ((z & 1) << 2);
+    // the states of the V even cubes over the segment and of the V odd cubes from its start (one
+    // V-byte load each: rows and segments start at multiples of V), and the odd cube before it
+    uint32_t ce[(V + 3) / 4], co[(V + 3) / 4];
+    ld_bytes(R.cubes[0] + erow + h0, ce);
+    ld_bytes(R.cubes[1] + orow + h0, co);
+    const uint32_t co_prev = R.cubes[1][orow + (h0 == 0 ? H - 1 : h0 - 1)];
 #pragma unroll
     for (int k = 0; k < V; ++k) {
-      int ae = h0 + k;
-      int ao = s ? ae : (ae == 0 ? H - 1 : ae - 1);
-      uint32_t se = R.cubes[0][erow + ae];
-      uint32_t so = R.cubes[1][orow + ao];
+      const uint32_t se = byte_of(ce, k);
+      const uint32_t so = s ? byte_of(co, k) : (k == 0 ? co_prev : byte_of(co, k - 1));
       eta[k] = (uint32_t)s_eta[se * 8 + p] | (uint32_t)s_eta[so * 8 + (p ^ 7)];
     }
   }
