@@ -856,26 +856,30 @@ __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbe, const 
     const unsigned long long m = (unsigned long long)f * 6ull + (0x7770ull << 32);
     const uint32_t sn = (uint32_t)(m >> 32);
     f = (uint32_t)m;
-    const uint32_t o = (w0 >> (3 * a)) & 7u;
+    const uint32_t osel = ((w0 >> (3 * a)) & 7u) | 0x7770u;  // the old value's selector
     const uint2 e = wt->nbw[(nbe >> (3 * a)) & 7u];
     const uint32_t gx = hx + e.x, gy = hy + e.y;
-    const int off = (int)(prmt(gx, gy, sn) - prmt(gx, gy, o | 0x7770u));
+    const int off = (int)(prmt(gx, gy, sn) - prmt(gx, gy, osel));
     const uint32_t tv = *reinterpret_cast<const uint32_t*>(tvb + off);
     const uint32_t word = a < 2 ? rr.y : (a < 4 ? rr.z : rr.w);
     const uint32_t hu = (a & 1) ? (word >> 16) : (word & 0xffffu);
     const int d = (int)(tv - 2u * hu);
     tprod *= (uint32_t)d;
-    const uint32_t nv = sn - 0x7770u;
-    const uint32_t dv = nv - o;  // the word changes by dv << 3a: one predicated multiply-add
-    if (kDelta) {
-      // one lookup of the histogram change of the pair (new, old)
-      const uint2 dc = wt->dcnt[8 * nv + o];
+    const uint32_t dv = sn - osel;  // new - old: the word changes by dv << 3a (one predicated multiply-add)
+    if (a == 5) {
+      // the histogram is not read after the last arm
+      asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %1, 1;\n\t@p mad.lo.u32 %0, %2, %3, %0;\n\t}"
+          : "+r"(w)
+          : "r"(d), "r"(dv), "r"(1u << (3 * a)));
+    } else if (kDelta) {
+      // one lookup of the histogram change of the pair (new, old): entry 8 * new + old
+      const uint2 dc = wt->dcnt[8u * sn + osel - 9u * 0x7770u];
       asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %3, 1;\n\t@p mad.lo.u32 %0, %4, %7, %0;\n\t@p add.u32 %1, %1, %5;"
           "\n\t@p add.u32 %2, %2, %6;\n\t}"
           : "+r"(w), "+r"(hx), "+r"(hy)
           : "r"(d), "r"(dv), "r"(dc.x), "r"(dc.y), "r"(1u << (3 * a)));
     } else {
-      const uint2 cn = wt->cnt[nv], co = wt->cnt[o];
+      const uint2 cn = wt->cnt[sn - 0x7770u], co = wt->cnt[osel - 0x7770u];
       asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %3, 1;\n\t@p mad.lo.u32 %0, %4, %9, %0;\n\t@p add.u32 %1, %1, %5;"
           "\n\t@p sub.u32 %1, %1, %6;\n\t@p add.u32 %2, %2, %7;\n\t@p sub.u32 %2, %2, %8;\n\t}"
           : "+r"(w), "+r"(hx), "+r"(hy)
