@@ -828,6 +828,8 @@ __device__ __forceinline__ void fill_block_sweep_tables(const ReplicaDesc& R, Sw
 // that wraps to zero without a tie only sends the cell through the exact path as well, which
 // decides every arm from the full 32-bit uniforms. A proposal equal to the old
 // value lands on entry 17 (dN = 0), which always accepts and changes nothing.
+// An accepted arm adds (new - old) << 3a to the word (the difference of the two selectors) and
+// its histogram change to h, except after the last arm, whose histogram nothing reads.
 template <bool kFold, bool kDelta>
 __device__ __forceinline__ uint32_t update_cell(uint32_t w, uint32_t nbe, const U4& rr,
                                                 uint32_t c0, uint32_t t, const ReplicaDesc& R, const SweepTables* wt) {
