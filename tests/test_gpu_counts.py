@@ -120,3 +120,34 @@ def test_batch_reads(engine_lib, oracle_mod):
         for i, o in enumerate(oras):
             same_counts(eng, o, i)
     eng.close()
+
+
+def test_reads_in_persistent_mode(engine_lib, oracle_mod):
+    # plain steps in the persistent kernel, the measured last step in the per-phase kernels
+    eng, ora = pair(oracle_mod, 12, 0.7, 0.45, 21)
+    eng.launch_mode = 1
+    same_counts(eng, ora)
+    for n in (1, 3, 2, 1):
+        eng.run(n, 2, 0)
+        for _ in range(n):
+            ora.step(2, 0)
+        same_counts(eng, ora)
+    assert np.array_equal(eng.get_config(), ora.get_config())
+    eng.close()
+
+
+def test_grouped_batch_reads(engine_lib, oracle_mod):
+    # eight replicas run as replica groups on parallel graph branches; the measured last step too
+    specs = [(8 + 4 * (i % 3), 0.5 + 0.05 * i) for i in range(8)]
+    eng = Lattice([Params(L=L, T=T, P=0.45, seed=60 + i, start=0, replica=i) for i, (L, T) in enumerate(specs)])
+    oras = [oracle_mod.Oracle(L, T, 0.45, 60 + i, 6.0, i, 0) for i, (L, T) in enumerate(specs)]
+    for i, o in enumerate(oras):
+        same_counts(eng, o, i)
+    for n in (1, 2, 1):
+        eng.run(n, 1, 0)
+        for o in oras:
+            for _ in range(n):
+                o.step(1, 0)
+        for i, o in enumerate(oras):
+            same_counts(eng, o, i)
+    eng.close()
