@@ -203,7 +203,7 @@ void launch_measure(const BatchDev& b, int record, cudaStream_t s);
 // Colour-1 sweep jsweep fused with the measurement of the step (slots zeroed by the step's
 // launch_step_begin), and the summation of the slots into the replica's record.
 void launch_sweep_measure(const BatchDev& b, int jsweep, cudaStream_t s);
-void launch_measure_end(const BatchDev& b, int record, cudaStream_t s);
+void launch_measure_end(const BatchDev& b, int record, cudaStream_t s, SampleRec* host_out = nullptr);
 // Persistent cooperative launch of nsteps Metropolis steps (cube + volume move, nmet sweeps) of
 // every replica, with a recorded measurement after every step s with s % interval == 0 when
 // interval > 0. Same lattice, counters and samples as the per-phase kernels.

@@ -61,8 +61,10 @@ struct cvf_handle {
   // cooperative launch per graph.
   int launch_mode = 0;
   void* staging = nullptr;  // pinned host buffer for configuration transfers (lazily allocated)
-  SampleRec* rec_pin = nullptr;  // mapped page-locked landing place of the record cvf_observables reads
-  SampleRec* rec_dev = nullptr;  // its device address
+  SampleRec* rec_pin = nullptr;  // mapped page-locked landing place of the records cvf_observables
+  SampleRec* rec_dev = nullptr;  // reads (one per replica), and its device address
+  // the measured last step of the last run wrote every replica's record into rec_pin
+  bool host_rec_valid = false;
   size_t staging_bytes = 0;
   // cvf_set_config / cvf_get_config: 1 = kernels read and pack, or unpack and write, the
   // caller's array in host memory (the GPU accesses pageable memory through the host page
@@ -337,6 +339,21 @@ static void launch_cluster_step(const BatchDev& b, int jsw, cudaStream_t s, int 
 
 // volume: the step's volume move in the cube kernel (false when a side branch runs the chunk's
 // volume moves).
+// The mapped page-locked records of cvf_observables (one per replica), allocated once.
+static int ensure_rec(cvf_handle* h) {
+  if (h->rec_pin) return 0;
+  const size_t bytes = h->reps.size() * sizeof(SampleRec);
+  cudaError_t e = cudaHostAlloc((void**)&h->rec_pin, bytes, cudaHostAllocMapped);
+  if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&h->rec_dev, h->rec_pin, 0);
+  if (e != cudaSuccess) {
+    if (h->rec_pin) cudaFreeHost(h->rec_pin);
+    h->rec_pin = nullptr;
+    h->rec_dev = nullptr;
+    return fail(CVF_ENOMEM, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
+  }
+  return 0;
+}
+
 static void enqueue_step(cvf_handle* h, int nmet, int ncl, bool volume = true) {
   launch_step_begin(h->b, nmet, ncl, 1, volume ? 1 : 0, h->stream);
   launch_cube_volume(h->b, 1, volume ? 1 : 0, h->stream);
@@ -361,8 +378,9 @@ static void enqueue_step_at(const BatchDev& b, cudaStream_t s, int nmet, int ncl
 
 // A Metropolis-only step followed by a recorded measurement: the measurement rides on the last
 // colour-1 sweep (slots zeroed by the step's begin kernel), then the slots are summed into the
-// last record (appended to the sample stream when keep is set).
-static void enqueue_recorded_metropolis_step(cvf_handle* h, int nmet, int keep = 1) {
+// last record (appended to the sample stream when keep is set; also written to host_out, mapped
+// page-locked memory with one record per replica, when that is given).
+static void enqueue_recorded_metropolis_step(cvf_handle* h, int nmet, int keep = 1, SampleRec* host_out = nullptr) {
   launch_step_begin(h->b, nmet, 0, 1, 1, h->stream, 1);
   launch_cube_volume(h->b, 1, 1, h->stream);
   for (int j = 0; j < nmet; ++j) {
@@ -370,7 +388,7 @@ static void enqueue_recorded_metropolis_step(cvf_handle* h, int nmet, int keep =
     if (j + 1 < nmet) launch_sweep(h->b, 1, j, h->stream);
     else launch_sweep_measure(h->b, j, h->stream);
   }
-  launch_measure_end(h->b, keep, h->stream);
+  launch_measure_end(h->b, keep, h->stream, host_out);
 }
 
 // One Metropolis-only step of the replicas of view b on stream s, with the recorded measurement
@@ -410,7 +428,8 @@ static void enqueue_cstats(cvf_handle* h, int record) {
 // Graph of `steps` MC steps; when record is set, step i is followed by a recorded measurement (and
 // cluster statistics when ncl > 0) for every i with i % rec_every == 0 (rec_every = 0: the first
 // step only), so one graph can hold several intervals of a sampled run. record = 2: the
-// measurement of Metropolis-only steps is kept as the replicas' last record only (no sample).
+// measurement of Metropolis-only steps is kept as the replicas' last record only (no sample)
+// and, outside replica groups, also written to the mapped records that cvf_observables reads.
 static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cudaGraphExec_t* out,
                      int rec_every = 0) {
   if (!record) rec_every = 0;
@@ -421,6 +440,8 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     *out = it->second;
     return 0;
   }
+  if (record == 2)
+    if (int rc = ensure_rec(h)) return rc;  // the graph holds the records' device address
   cudaGraph_t g;
   if (h->launch_mode == 1 && ncl == 0 && !h->corr_on && !h->nhb_mode && record != 2) {
     // one persistent launch; a driver that cannot capture a cooperative launch leaves the
@@ -524,7 +545,7 @@ static int get_graph(cvf_handle* h, int steps, int nmet, int ncl, int record, cu
     if (side) {
       enqueue_step(h, nmet, ncl, false);
     } else if (rec_at(i) && ncl == 0 && nmet > 0) {
-      enqueue_recorded_metropolis_step(h, nmet, record == 1);
+      enqueue_recorded_metropolis_step(h, nmet, record == 1, record == 2 ? h->rec_dev : nullptr);
     } else {
       enqueue_step(h, nmet, ncl);
       if (rec_at(i)) {
@@ -751,6 +772,7 @@ int cvf_num_replicas(const cvf_handle* h) { return h ? (int)h->reps.size() : 0; 
 int cvf_set_config(cvf_handle* h, int r, const int* c12, long long n_cells) {
   if (int rc = check_rep(h, r)) return rc;
   h->last_valid = false;
+  h->host_rec_valid = false;
   ReplicaHost& R = h->reps[r];
   if (!c12 || n_cells != R.N) return fail(CVF_EINVAL, "cells12 must hold 12 ints for each of the N cells");
   CK(cudaSetDevice(h->device));
@@ -870,6 +892,7 @@ int cvf_set_arms(cvf_handle* h, int r, const unsigned char* sg, const unsigned c
     return cvf_set_config(h, r, c12.data(), R.N);
   }
   h->last_valid = false;
+  h->host_rec_valid = false;
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
   if (int rc = ensure_io_scratch(h, R)) return rc;
@@ -950,6 +973,7 @@ int cvf_set_packed(cvf_handle* h, int r, const void* buf, long long bytes) {
   ReplicaHost& R = h->reps[r];
   if (!buf || bytes != packed_bytes(R)) return fail(CVF_EINVAL, "packed buffer must hold 4 N + 2 (L/2)^3 bytes");
   h->last_valid = false;
+  h->host_rec_valid = false;
   CK(cudaSetDevice(h->device));
   CK(cudaStreamSynchronize(h->stream));
   // copied and checked in scratch first: the lattice changes only when every value is valid
@@ -1017,6 +1041,7 @@ static int run_impl(cvf_handle* h, int n_steps, int nmet, int ncl, int interval)
   }
   if (n_steps == 0) return 0;
   h->last_valid = false;
+  h->host_rec_valid = false;
   const int chunk_plain = 32;
   if (interval <= 0) {
     // a Metropolis-only run right after cvf_observables measures its last step (on the step's
@@ -1037,6 +1062,7 @@ static int run_impl(cvf_handle* h, int n_steps, int nmet, int ncl, int interval)
       if (int rc = get_graph(h, 1, nmet, 0, 2, &g)) return rc;
       CK(cudaGraphLaunch(g, h->stream));
       h->last_valid = true;
+      h->host_rec_valid = group_count(h) <= 1;  // the per-phase capture writes the mapped records
     }
   } else {
     // graphs of m intervals (about 32 steps) while enough steps remain, then single intervals,
@@ -1084,20 +1110,15 @@ int cvf_observables(cvf_handle* h, int r, cvf_obs* out) {
   if (!out) return fail(CVF_EINVAL, "null out");
   CK(cudaSetDevice(h->device));
   h->obs_since_run = true;
-  if (!h->rec_pin) {
-    cudaError_t e = cudaHostAlloc((void**)&h->rec_pin, sizeof(SampleRec), cudaHostAllocMapped);
-    if (e == cudaSuccess) e = cudaHostGetDevicePointer((void**)&h->rec_dev, h->rec_pin, 0);
-    if (e != cudaSuccess) {
-      if (h->rec_pin) cudaFreeHost(h->rec_pin);
-      h->rec_pin = nullptr;
-      return fail(CVF_ENOMEM, std::string("cudaHostAlloc: ") + cudaGetErrorString(e));
-    }
-  }
-  bool landed = false;  // the record already written to rec_pin by the kernel
-  if (h->last_valid) {
-    // the last step was measured: the read kernel writes its record straight into the mapped
-    // page-locked buffer
-    launch_last_read(h->b, h->stream, h->rec_dev, r);
+  if (int rc = ensure_rec(h)) return rc;
+  bool landed = false;  // the record already written to rec_pin[r] by a kernel
+  if (h->last_valid && h->host_rec_valid) {
+    // the run's measured last step wrote every replica's record into the mapped buffer
+    landed = true;
+  } else if (h->last_valid) {
+    // the record is current: the read kernel writes it, with the replica's current r_cell and
+    // volume, straight into the mapped page-locked buffer
+    launch_last_read(h->b, h->stream, h->rec_dev + r, r);
     landed = true;
   } else if (h->nhb_mode) {
     if (!h->nhb_read) {
@@ -1119,10 +1140,10 @@ int cvf_observables(cvf_handle* h, int r, cvf_obs* out) {
   }
   // only the 32-byte measurement record crosses to the host, into page-locked memory
   if (!landed)
-    CK(cudaMemcpyAsync(h->rec_pin, (char*)(h->b.st + r) + offsetof(ReplicaState, last), sizeof(SampleRec),
+    CK(cudaMemcpyAsync(h->rec_pin + r, (char*)(h->b.st + r) + offsetof(ReplicaState, last), sizeof(SampleRec),
                        cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  const SampleRec last = *h->rec_pin;
+  const SampleRec last = h->rec_pin[r];
   const ReplicaHost& R = h->reps[r];
   fill_obs(out, last.n_hb2, last.n_sigma, last.r_cell, last.volume,
            host_evdw(last.r_cell, R.dist, R.freq, R.p.R_cutoff), R.N, R.p.P);
@@ -1299,6 +1320,7 @@ int cvf_set_state(cvf_handle* h, int r, const cvf_state* in) {
   s.e_vdw = host_evdw(in->r_cell, R.dist, R.freq, R.p.R_cutoff);
   for (int i = 0; i < 4; ++i) s.ctr[i] = in->counters[i];
   CK(cudaMemcpy(h->b.st + r, &s, sizeof(ReplicaState), cudaMemcpyHostToDevice));
+  h->host_rec_valid = false;  // the mapped records hold the old r_cell and volume
   return 0;
 }
 
@@ -1358,6 +1380,7 @@ static int restore_state(cvf_handle* h, const StateBackup& b) {
 int cvf_autotune(cvf_handle* h, int* vec_out) {
   if (!h) return fail(CVF_EINVAL, "null handle");
   h->last_valid = false;
+  h->host_rec_valid = false;
   if (h->nhb_mode) {  // the per-arm sweep of Flag_chessboard = 0 has no tile to choose
     if (vec_out) *vec_out = h->b.vec;
     return 0;
@@ -1458,6 +1481,7 @@ int cvf_autotune(cvf_handle* h, int* vec_out) {
     drop_graphs(h);
     h->launch_mode = best_mode;
     h->last_valid = false;
+    h->host_rec_valid = false;
     if (int rc = restore_state(h, full)) return rc;
   }
   cudaEventDestroy(e0);
@@ -1502,6 +1526,7 @@ int cvf_get_stream(cvf_handle* h, void** stream) {
 int cvf_profile_launch(cvf_handle* h, int kind, int n) {
   if (!h || n < 0 || kind < 0 || kind > 3) return fail(CVF_EINVAL, "bad profile request");
   h->last_valid = false;
+  h->host_rec_valid = false;
   if (h->nhb_mode) return fail(CVF_EINVAL, "kernel profiling covers the Flag_chessboard = 1 kernels");
   CK(cudaSetDevice(h->device));
   for (int i = 0; i < n; ++i) {

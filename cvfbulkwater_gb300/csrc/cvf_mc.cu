@@ -1100,9 +1100,16 @@ __global__ void k_measure_begin(ReplicaState* __restrict__ st, int nrep) {
   if (r < nrep) measure_zero(st[r]);
 }
 
-__global__ void k_measure_end(ReplicaState* __restrict__ st, int nrep, int record) {
+// host_out (mapped page-locked host memory, one record per replica) also receives the records.
+__global__ void k_measure_end(ReplicaState* __restrict__ st, int nrep, int record, SampleRec* host_out) {
   int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < nrep) measure_finish(st[r], record);
+  if (r < nrep) {
+    measure_finish(st[r], record);
+    if (host_out) {
+      host_out[r] = st[r].last;
+      __threadfence_system();
+    }
+  }
 }
 
 // ------------------------------------------------------------------ persistent step kernel
@@ -1285,8 +1292,8 @@ void launch_sweep_measure(const BatchDev& b, int jsweep, cudaStream_t s) {
   }
 }
 
-void launch_measure_end(const BatchDev& b, int record, cudaStream_t s) {
-  k_measure_end<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, record);
+void launch_measure_end(const BatchDev& b, int record, cudaStream_t s, SampleRec* host_out) {
+  k_measure_end<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, record, host_out);
 }
 
 void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, int soff) {
@@ -1340,7 +1347,7 @@ void launch_measure(const BatchDev& b, int record, cudaStream_t s) {
     case 2: k_measure<2><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep); break;
     default: k_measure<1><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep); break;
   }
-  k_measure_end<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, record);
+  k_measure_end<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, record, nullptr);
 }
 
 template <int V>
