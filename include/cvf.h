@@ -153,7 +153,9 @@ int cvf_batch_run(cvf_handle* h, int n_steps, int n_metropolis, int n_cluster);
 int cvf_run_sampled(cvf_handle* h, int n_steps, int n_metropolis, int n_cluster, int interval);
 int cvf_synchronize(cvf_handle* h);
 
-/* Replaces measure() GW:2014-2160 for the current configuration. */
+/* Replaces measure() GW:2014-2160 for the current configuration. A Metropolis-only
+ * cvf_run_steps that follows a cvf_observables call measures its last step on the way, so the
+ * next call reads that record (synchronising with the stream) instead of measuring again. */
 int cvf_observables(cvf_handle* h, int replica, cvf_obs* out);
 /* Replaces print_cluster_statistics() GW:2677-2721 for the current labels. Before any SW step
  * the labels are all zero (one cluster of 6N sites), as in the reference's cluster.out. */
