@@ -1043,12 +1043,14 @@ template <int V>
 __global__ void __launch_bounds__(kThreads, SweepMinBlocks<V>::v) k_sweep_measure(
     const ReplicaDesc* __restrict__ reps, ReplicaState* __restrict__ st, const int* __restrict__ blk, int nrep,
     int jsweep) {
+  pdl_trigger();
   __shared__ SweepTables s_tab;
   __shared__ unsigned long long s_acc[2];
   const int r = find_replica(blk, nrep, blockIdx.x);
   const ReplicaDesc& R = reps[r];
   fill_block_sweep_tables(R, &s_tab);
   __syncthreads();
+  pdl_wait();
   uint32_t hb2 = 0, ns = 0;
   sweep_segment<V, true, true, V == 8>(R, &s_tab, (uint32_t)(blockIdx.x - blk[r]) * blockDim.x + threadIdx.x, 1,
                          st[r].cur[0] + (uint32_t)jsweep, hb2, ns);
@@ -1102,6 +1104,8 @@ __global__ void k_measure_begin(ReplicaState* __restrict__ st, int nrep) {
 
 // host_out (mapped page-locked host memory, one record per replica) also receives the records.
 __global__ void k_measure_end(ReplicaState* __restrict__ st, int nrep, int record, SampleRec* host_out) {
+  pdl_trigger();
+  pdl_wait();
   int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r < nrep) {
     measure_finish(st[r], record);
@@ -1284,16 +1288,17 @@ void launch_step_begin(const BatchDev& b, int nmet, int ncl, int do_cube, int do
 }
 
 void launch_sweep_measure(const BatchDev& b, int jsweep, cudaStream_t s) {
+  const dim3 g((unsigned)b.nblk_sweep);
   switch (b.vec) {
-    case 8: k_sweep_measure<8><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, jsweep); break;
-    case 4: k_sweep_measure<4><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, jsweep); break;
-    case 2: k_sweep_measure<2><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, jsweep); break;
-    default: k_sweep_measure<1><<<b.nblk_sweep, kThreads, 0, s>>>(b.reps, b.st, b.blk_sweep, b.nrep, jsweep); break;
+    case 8: launch_pdl(k_sweep_measure<8>, g, s, b.pdl, b.reps, b.st, b.blk_sweep, b.nrep, jsweep); break;
+    case 4: launch_pdl(k_sweep_measure<4>, g, s, b.pdl, b.reps, b.st, b.blk_sweep, b.nrep, jsweep); break;
+    case 2: launch_pdl(k_sweep_measure<2>, g, s, b.pdl, b.reps, b.st, b.blk_sweep, b.nrep, jsweep); break;
+    default: launch_pdl(k_sweep_measure<1>, g, s, b.pdl, b.reps, b.st, b.blk_sweep, b.nrep, jsweep); break;
   }
 }
 
 void launch_measure_end(const BatchDev& b, int record, cudaStream_t s, SampleRec* host_out) {
-  k_measure_end<<<grid1(b.nrep), kThreads, 0, s>>>(b.st, b.nrep, record, host_out);
+  launch_pdl(k_measure_end, grid1(b.nrep), s, b.pdl, b.st, b.nrep, record, host_out);
 }
 
 void launch_cube_volume(const BatchDev& b, int do_cubes, int do_volume, cudaStream_t s, int soff) {
