@@ -252,6 +252,14 @@ def cpu_baseline_oracle(steps_cap=3, budget_s=30.0, threads=None):
                       f"OpenMP threads ({dt:.1f} s)"}
 
 
+def warm_steps(lat, n, nmet=1, ncl=0):
+    """n (at least 3) untimed steps as the timed loops make them, one run call per step, so the
+    one-step graph is built and warm before the timed region."""
+    for _ in range(max(3, n)):
+        lat.run(1, nmet, ncl)
+    lat.synchronize()
+
+
 def timed_steps(lat, steps, flush, nmet=1, ncl=0):
     """Device time (ms) of `steps` MC steps of a handle, each bracketed by CUDA events on the
     handle's stream with a 256 MB L2 flush before it."""
@@ -291,15 +299,13 @@ def bench_batch64(steps, warmup, local, flush, verify=4):
     batch = Lattice(params)
     tile = batch.autotune()
     tuned = batch.tuning()
-    batch.run(warmup, 1, 0)
-    batch.synchronize()
+    warm_steps(batch, warmup)
     t_batch = timed_steps(batch, steps, flush)
     t_plain = 0.0
     same = True
     for i, p in enumerate(params):
         h = Lattice(p)
-        h.run(warmup, 1, 0)
-        h.synchronize()
+        warm_steps(h, warmup)
         t_plain += timed_steps(h, steps, flush)
         if i < verify:
             same = same and bool(np.array_equal(h.get_config(), batch.get_config(i)))
@@ -517,8 +523,7 @@ def bench_plain_l16(steps, warmup, local, flush, cpu=True):
     import torch
     from cvfbulkwater_gb300.engine import Lattice, Params
     lat = Lattice(Params(L=16, T=0.815, P=0.45, seed=SEED, start=0, device=local))
-    lat.run(warmup, 1, 0)
-    lat.synchronize()
+    warm_steps(lat, warmup)
     ms = timed_steps(lat, steps, flush)
     stream = torch.cuda.ExternalStream(lat.stream_ptr())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -576,8 +581,7 @@ def bench_sw(steps, warmup, local, flush):
     for L in (64, 128):
         for T in (0.60, 0.75):
             lat = Lattice(Params(L=L, T=T, P=0.45, seed=SEED, start=0, device=local))
-            lat.run(warmup, 0, 1)
-            lat.synchronize()
+            warm_steps(lat, warmup, nmet=0, ncl=1)
             ms = timed_steps(lat, steps, flush, nmet=0, ncl=1)
             cs = lat.cluster_stats()
             out.append({"L": L, "T": T, "sw_steps_per_s": round(steps / (ms / 1e3), 1),
@@ -682,8 +686,7 @@ def run_engine(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
 
     tile = lat.set_sweep_tile(args.tile) if args.tile else lat.autotune()
-    lat.run(args.warmup, 1, 0)
-    lat.synchronize()
+    warm_steps(lat, args.warmup)
     # roofline of the dominant kernel (the sweep), two launches per profiled sweep
     nprof = max(4, min(args.steps, 50))
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nprof)]
